@@ -1,0 +1,403 @@
+"""Benchmark: steady MG-PCG solves per second on the 800 x 800 x 10 stack.
+
+Workload (a "step"): one steady solve from T = 0 to ||r|| / ||P|| < 1e-10 of
+the 800 x 800 x 10 two-tier stack (25 W per Si tier + a seeded 3 W, 1 mm
+hotspot), with the FP32 V-cycle inside FP64 flexible PCG, the operator and
+multigrid hierarchy resident in HBM (built once, outside the timed region, as
+in a power-map sweep). Inputs are larger than L2 (the fine level alone moves
+~1.7 GB per iteration), so no L2 flush is needed between steps.
+
+Reported beside it, on the same GPU: the plain FP64 MG-PCG (FP64 V-cycle)
+solves/s, max|dT| between the two, the end-to-end rate through the C ABI
+with the power map copied in and the temperatures copied out every step, the
+per-kernel roofline of the dominant kernel, and the CPU oracle (a C
+restatement of the reference CPU solver) timed on this machine's host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cuda-thermal_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "steady solves/s + % HBM roofline: FP32-MG & batched vs FP64 MG-PCG, <=5e-4 K"
+N_GRID = 800
+TOL = 1e-10
+MAXIT = 1000
+SEED = 2
+FALLBACK_HBM_GBS = 6800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    td.all_reduce(t, op=td.ReduceOp.SUM)
+    return float(t.item())
+
+
+def timed_solves(ct, solver, k, world):
+    """k steady solves, timed with CUDA events on the solver's stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(solver.stream())
+    stats = []
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k):
+        solver.set_x_zero()
+        solver.set_rhs_steady()
+        stats.append(solver.solve(TOL, MAXIT))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    return ms, stats
+
+
+def cpu_oracle_rate(m, threads, solves_per_thread=1, mg_double=False, flexible=False):
+    """The CPU oracle (reference default build arithmetic) on `threads` host
+    threads, each solving its own copy of the workload; returns solves/s and
+    the seconds the timed phase took."""
+    import oracle
+    solvers = [oracle.Solver(m, "multigrid", mg_double=mg_double, flexible=flexible)
+               for _ in range(threads)]
+    go = threading.Barrier(threads + 1)
+    iters = [0] * threads
+
+    def work(k):
+        s = solvers[k]
+        go.wait()
+        for _ in range(solves_per_thread):
+            s.set_x_zero()
+            s.set_rhs_steady()
+            iters[k] = s.solve(TOL, MAXIT)[0]
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    for t in th:
+        t.start()
+    go.wait()
+    t0 = time.perf_counter()
+    for t in th:
+        t.join()
+    sec = time.perf_counter() - t0
+    del solvers
+    return threads * solves_per_thread / sec, sec, iters[0]
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """Reference arm: the reference CPU solver's arithmetic (the C oracle, a
+    restatement of src/pcg3d_cpu.cpp in its default float-V-cycle build) on
+    every host thread, each thread solving its own copy of the workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+    import workloads
+    oracle.build()
+    m = workloads.steady_hotspot(N_GRID, seed=SEED)
+    threads = host_threads()
+    for _ in range(args.warmup):
+        cpu_oracle_rate(m, threads)
+    rates, secs = [], []
+    for _ in range(args.steps):
+        r, s, it = cpu_oracle_rate(m, threads)
+        rates.append(r)
+        secs.append(s)
+    total = sum(secs)
+    value = threads * args.steps / total
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"steady solve {N_GRID}x{N_GRID}x10, tol {TOL:g}",
+                   "iters": it, "cpu_threads": threads},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"{threads} threads x 1 steady {N_GRID}x{N_GRID}x10 solve per step"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def traffic_from_profiles(kernel_name):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/*.md), when one lists it."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for f in sorted(os.listdir(pdir)):
+        if not f.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(pdir, f)):
+            if line.startswith("traffic_per_launch") and kernel_name in line:
+                try:
+                    return float(line.split("=")[1].split()[0])
+                except Exception:
+                    pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    import cthermal as ct
+    import workloads
+
+    rank, world, local = dist_setup(args.gpus)
+    ct.lib()
+    hbm_peak, peak_kind = peaks()
+    m = workloads.steady_hotspot(N_GRID, seed=SEED)
+    ncells = m.ncells()
+
+    s32 = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX)
+    s64 = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP64)
+    for _ in range(args.warmup):
+        for s in (s32, s64):
+            s.set_x_zero()
+            s.set_rhs_steady()
+            s.solve(TOL, MAXIT)
+
+    # ---- headline: FP32 V-cycle in flexible FP64 PCG, device-resident -----
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms32, st32 = timed_solves(ct, s32, args.steps, world)
+    clk = clocks.stop()
+    T32 = s32.get_x()
+    ms32 = max_over_ranks(ms32, world)
+    value = sum_over_ranks(args.steps, world) / (ms32 / 1e3)
+
+    # ---- plain FP64 MG-PCG on the same GPU ---------------------------------
+    k64 = max(3, args.steps // 2)
+    ms64, st64 = timed_solves(ct, s64, k64, world)
+    T64 = s64.get_x()
+    ms64 = max_over_ranks(ms64, world)
+    value64 = sum_over_ranks(k64, world) / (ms64 / 1e3)
+    max_dT = float(np.abs(T32 - T64).max())
+
+    # ---- end to end through the C ABI: host P in, host T out -------------
+    P_host = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
+    T_host = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
+    P_np, T_np = P_host.numpy(), T_host.numpy()
+    P_np[:] = m.P
+    stream = torch.cuda.ExternalStream(s32.stream())
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        s32.set_power(P_np)
+        s32.set_x_zero()
+        s32.set_rhs_steady()
+        s32.solve(TOL, MAXIT)
+        s32.get_x(T_np)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall_e2e = time.perf_counter() - t0
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1), world)
+    e2e_value = sum_over_ranks(args.steps, world) / (ms_e2e / 1e3)
+    e2e_same_bits = bool(np.array_equal(T_np, T32))
+
+    # ---- roofline: per-kernel CUDA-event times of one solve ------------------
+    s32.set_x_zero()
+    s32.set_rhs_steady()
+    _, rows = s32.profile_solve(TOL, MAXIT)
+    rows.sort(key=lambda r: -r["total_ms"])
+    tot_ms = sum(r["total_ms"] for r in rows)
+    top = rows[0]
+    achieved = top["bytes"] / top["launches"] / (top["total_ms"] / top["launches"] / 1e3) / 1e9
+    traffic = traffic_from_profiles(top["name"])
+    alg_bytes_solve = sum(r["bytes"] for r in rows)
+    iters = st32[-1].iters
+    nlev = s32.num_levels()
+    body_kernels = 4 + 5 * (nlev - 1) + 1
+    launches_per_solve = 1 + iters * body_kernels
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = host_threads()
+        rate, sec, it = cpu_oracle_rate(m, threads)
+        cpu = {"value": rate, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"{threads} threads x 1 steady {N_GRID}x{N_GRID}x10 solve "
+                         f"({sec:.1f} s, {it} iterations, float V-cycle as the reference default)"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32", "data": "synthetic",
+            "config": {"workload": f"steady solve {N_GRID}x{N_GRID}x10 two-tier stack, seeded "
+                                   f"3 W hotspot, tol {TOL:g}, FP32 V-cycle in FP64 flexible PCG",
+                       "cells": ncells, "levels": nlev, "iters": iters,
+                       "l2": "inputs larger than L2 (fine level ~1.7 GB moved per iteration)",
+                       "parallelism": f"replicas x{world}"},
+            "fp64_mg_pcg": {"value": value64, "unit": "solves/s", "iters": st64[-1].iters,
+                            "ms_per_solve": ms64 / k64},
+            "speedup_vs_fp64": value / value64,
+            "max_dT_K": max_dT,
+            "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved,
+                         "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "peak_kind": peak_kind, "traffic": traffic,
+                         "alg_bytes_per_launch": top["bytes"] / top["launches"],
+                         "launch_ms": top["total_ms"] / top["launches"],
+                         "share": top["total_ms"] / tot_ms,
+                         "solve_frac": alg_bytes_solve / (ms32 / args.steps / 1e3) / 1e9 / hbm_peak},
+            "kernels": [{"name": r["name"], "launches": r["launches"],
+                         "ms": round(r["total_ms"], 4),
+                         "GBs": round(r["bytes"] / (r["total_ms"] / 1e3) / 1e9, 1)}
+                        for r in rows[:12]],
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": ncells * 8,
+                    "d2h_bytes_per_step": ncells * 8, "wall_s": wall_e2e,
+                    "same_bits_as_device_run": e2e_same_bits},
+            "gpu_launches": launches_per_solve * args.steps,
+            "clocks": clk,
+        }
+        if cpu:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out), flush=True)
+    s32.close()
+    s64.close()
+    if world > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

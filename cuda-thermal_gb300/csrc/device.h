@@ -1,0 +1,86 @@
+// device.h - data layout and control structures shared by the kernels and the
+// host orchestration.
+//
+// Layout in HBM. Every vector and every operator array of every multigrid
+// level, the finest included, uses the colour-split layout: each row j of a
+// z-plane stores its red columns ((i + j) even) first and its black columns
+// after them, hx = ceil(nx / 2) slots each, so column (i, j) sits at
+//     scol(i, j) = (2 j + ((i + j) & 1)) * hx + i / 2
+// and cell (i, j, l) at l * plane + scol(i, j), plane = ny * 2 * hx. A
+// red-black sweep then reads and writes one contiguous half-row per colour,
+// and its lateral neighbours are the other half of the same and adjacent rows.
+// The outer PCG vectors share this layout, so the fine level's operator is
+// stored once and the V-cycle reads the PCG residual with no permutation.
+// Padding slots (odd nx: one per row and colour parity) hold zero in every
+// vector and are never read as neighbours.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace ct {
+
+constexpr int NT = 256;  // threads per block of every solver kernel
+
+struct Geo {
+    int nx, ny, nz, hx;
+    unsigned plane;  // slots per z-plane: ny * 2 * hx
+};
+
+__host__ __device__ inline Geo geo_of(int nx, int ny, int nz) {
+    Geo g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.hx = (nx + 1) / 2;
+    g.plane = (unsigned)ny * 2u * (unsigned)g.hx;
+    return g;
+}
+
+__host__ __device__ inline unsigned scol(const Geo& g, int i, int j) {
+    return (unsigned)(2 * j + ((i + j) & 1)) * (unsigned)g.hx + (unsigned)(i >> 1);
+}
+
+// Reduction slots: each reducing kernel owns one, with its own ticket counter
+// and two rows of per-block partial sums.
+enum Slot { SL_INIT = 0, SL_APPLY, SL_UPDATE, SL_DOT, SL_AUX, NSLOT };
+
+// Per-solver control block in device memory. The kernels keep every scalar
+// of the iteration here (alpha, beta and the dot products never visit the
+// host), and the last block of each reduction finishes it in a fixed order,
+// so results are reproducible run to run.
+struct Ctl {
+    // set by the host before a solve
+    double tol;
+    int maxit;
+    int pad0;
+    // scalars of the iteration
+    double inv_dt;
+    double bb, rr, rz, pAp, zAp, alpha, beta, relres;
+    double aux0, aux1, aux2;  // results of the auxiliary reductions
+    int iter;                 // completed iterations
+    int body;                 // loop bodies entered (bounds the graph loop)
+    int done;                 // stop flag: every kernel of the loop body exits early
+    int converged;
+    int breakdown;
+    int bb_zero;
+    unsigned ticket[NSLOT];
+};
+
+// Graph while-loop handle: kernels that decide the loop's fate set it.
+struct Cond {
+    cudaGraphConditionalHandle h;
+    int use;
+};
+
+// One multigrid level as the kernels see it (split layout). T = float or
+// double: the V-cycle precision. Faces and capacities are always float.
+template <class T>
+struct LevelView {
+    Geo g;
+    const float *gE, *gN, *gU, *gB, *cap;
+    T *fcp, *finv;
+    T *x, *b;
+};
+
+}  // namespace ct

@@ -1,0 +1,606 @@
+// k_outer.cu - FP64 outer-PCG kernels, setup and bookkeeping kernels.
+//
+// The outer iteration is FP64 (residual, iterate updates, dot products,
+// alpha, beta), as in the reference (src/pcg3d_gpu.cu:134-264). Its stencil
+// kernels walk one column per thread through the z-planes, so the vertical
+// neighbours and the face below come from registers and every z-plane access
+// of a warp is one contiguous run of the split layout.
+#include <cmath>
+
+#include "kernels.h"
+#include "reduce.cuh"
+
+namespace ct {
+
+namespace {
+
+// Column of the split-layout slot s: (i, j), colour c and half-row index t.
+struct Col {
+    int i, j;
+    unsigned s, sw, se, ss, sn;
+    bool valid;
+};
+
+__device__ __forceinline__ Col col_of_slot(const Geo& g, unsigned s) {
+    Col c;
+    const unsigned row2 = 2u * (unsigned)g.hx;
+    const int j = (int)(s / row2);
+    const unsigned rem = s - (unsigned)j * row2;
+    const int colour = rem >= (unsigned)g.hx ? 1 : 0;
+    const int t = (int)rem - colour * g.hx;
+    const int i = 2 * t + ((j + colour) & 1);
+    const int oc = colour ^ 1;
+    const unsigned row_o = (unsigned)(2 * j + oc) * (unsigned)g.hx;
+    c.i = i;
+    c.j = j;
+    c.s = s;
+    c.sw = row_o + (unsigned)((i - 1) >> 1);
+    c.se = row_o + (unsigned)((i + 1) >> 1);
+    c.ss = (unsigned)(2 * j - 2 + oc) * (unsigned)g.hx + (unsigned)t;
+    c.sn = (unsigned)(2 * j + 2 + oc) * (unsigned)g.hx + (unsigned)t;
+    c.valid = i < g.nx;
+    return c;
+}
+
+// Walks one column through the planes computing a = (A + C/dt) v with the
+// stored diagonal (op_apply_diag, src/operator3d.h:100-106), and hands each
+// plane's (l, index, v, a) to f.
+template <class F>
+__device__ __forceinline__ void apply_column(const OpView& o, const double* __restrict__ diag,
+                                             const double* __restrict__ v, const Col& c, F&& f) {
+    const Geo& g = o.g;
+    double v_c = v[c.s], v_b = 0.0;
+    float gu_b = 0.0f;
+    for (int l = 0; l < g.nz; ++l) {
+        const unsigned base = (unsigned)l * g.plane;
+        const unsigned id = base + c.s;
+        const bool up = l < g.nz - 1;
+        const double v_a = up ? v[id + g.plane] : 0.0;
+        const float gu = o.gU[id];
+        double off = 0.0;
+        if (c.i > 0) off += (double)o.gE[base + c.sw] * v[base + c.sw];
+        if (c.i < g.nx - 1) off += (double)o.gE[id] * v[base + c.se];
+        if (c.j > 0) off += (double)o.gN[base + c.ss] * v[base + c.ss];
+        if (c.j < g.ny - 1) off += (double)o.gN[id] * v[base + c.sn];
+        if (l > 0) off += (double)gu_b * v_b;
+        if (up) off += (double)gu * v_a;
+        f(l, id, v_c, diag[id] * v_c - off);
+        v_b = v_c;
+        v_c = v_a;
+        gu_b = gu;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(NT)
+    k_residual(OpView o, const double* __restrict__ diag, const double* __restrict__ b,
+               const double* __restrict__ x, double* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
+               double* part, int maxb, Cond cond) {
+    const Geo& g = o.g;
+    double rr = 0.0, bb = 0.0;
+    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) {
+            for (int l = 0; l < g.nz; ++l) {
+                r[(unsigned)l * g.plane + s] = 0.0;
+                if (b0) b0[(unsigned)l * g.plane + s] = T(0);
+            }
+            continue;
+        }
+        apply_column(o, diag, x, c, [&](int, unsigned id, double, double ax) {
+            const double bi = b[id];
+            const double ri = bi - ax;
+            r[id] = ri;
+            if (b0) b0[id] = (T)ri;
+            rr += ri * ri;
+            bb += bi * bi;
+        });
+    }
+    block_sum2(rr, bb);
+    if (publish2(rr, bb, part, maxb, &ctl->ticket[SL_INIT])) {
+        double RR, BB;
+        gather2(part, maxb, &ctl->ticket[SL_INIT], RR, BB);
+        if (threadIdx.x == 0) {
+            ctl->rr = RR;
+            ctl->bb = BB;
+            if (BB == 0.0) {  // no heat in: x = 0 (src/pcg3d_cpu.cpp:146)
+                ctl->bb_zero = 1;
+                ctl->converged = 1;
+                ctl->relres = 0.0;
+                stop_loop(ctl, cond);
+            } else {
+                const double rel = sqrt(RR / BB);
+                ctl->relres = rel;
+                if (rel < ctl->tol) {
+                    ctl->converged = 1;
+                    stop_loop(ctl, cond);
+                } else if (!isfinite(rel)) {
+                    ctl->breakdown = 1;
+                    stop_loop(ctl, cond);
+                } else if (ctl->maxit <= 0) {
+                    stop_loop(ctl, cond);
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NT)
+    k_apply(OpView o, const double* __restrict__ diag, const double* __restrict__ p,
+            double* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const Geo& g = o.g;
+    double pap = 0.0, unused = 0.0;
+    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) {
+            for (int l = 0; l < g.nz; ++l) Ap[(unsigned)l * g.plane + s] = 0.0;
+            continue;
+        }
+        apply_column(o, diag, p, c, [&](int, unsigned id, double pc, double a) {
+            Ap[id] = a;
+            pap += pc * a;
+        });
+    }
+    block_sum2(pap, unused);
+    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
+        double PAP, U;
+        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
+        if (threadIdx.x == 0) {
+            ctl->pAp = PAP;
+            if (!(PAP > 0.0) || !isfinite(PAP)) {  // A is SPD: p.Ap > 0 unless p = 0
+                ctl->breakdown = 1;
+                ctl->alpha = 0.0;
+                stop_loop(ctl, cond);
+            } else {
+                ctl->alpha = ctl->rz / PAP;
+            }
+        }
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void store2(T* b0, unsigned k, double a, double b);
+template <>
+__device__ __forceinline__ void store2<float>(float* b0, unsigned k, double a, double b) {
+    reinterpret_cast<float2*>(b0)[k] = make_float2((float)a, (float)b);
+}
+template <>
+__device__ __forceinline__ void store2<double>(double* b0, unsigned k, double a, double b) {
+    reinterpret_cast<double2*>(b0)[k] = make_double2(a, b);
+}
+
+// n2 = n / 2 pairs (n, the slots of all planes, is even).
+template <class T, bool MG>
+__global__ void __launch_bounds__(NT)
+    k_update(unsigned n2, const double* __restrict__ p, const double* __restrict__ Ap,
+             double* __restrict__ x, double* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
+             double* part, int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const double alpha = ctl->alpha;
+    const double2* p2 = reinterpret_cast<const double2*>(p);
+    const double2* a2 = reinterpret_cast<const double2*>(Ap);
+    double2* x2 = reinterpret_cast<double2*>(x);
+    double2* r2 = reinterpret_cast<double2*>(r);
+    double rr = 0.0, unused = 0.0;
+    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
+        const double2 pv = p2[k], av = a2[k];
+        double2 xv = x2[k], rv = r2[k];
+        xv.x += alpha * pv.x;
+        xv.y += alpha * pv.y;
+        rv.x -= alpha * av.x;
+        rv.y -= alpha * av.y;
+        x2[k] = xv;
+        r2[k] = rv;
+        if (MG) store2<T>(b0, k, rv.x, rv.y);
+        rr += rv.x * rv.x;
+        rr += rv.y * rv.y;
+    }
+    block_sum2(rr, unused);
+    if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
+        double RR, U;
+        gather2(part, maxb, &ctl->ticket[SL_UPDATE], RR, U);
+        if (threadIdx.x == 0) {
+            ctl->rr = RR;
+            ctl->iter += 1;
+            const double rel = sqrt(RR / ctl->bb);
+            ctl->relres = rel;
+            if (rel < ctl->tol) {
+                ctl->converged = 1;
+                stop_loop(ctl, cond);
+            } else if (!isfinite(rel)) {
+                ctl->breakdown = 1;
+                stop_loop(ctl, cond);
+            } else if (ctl->iter >= ctl->maxit) {
+                stop_loop(ctl, cond);
+            }
+        }
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void load2(const T* z, unsigned k, double& a, double& b);
+template <>
+__device__ __forceinline__ void load2<float>(const float* z, unsigned k, double& a, double& b) {
+    const float2 v = reinterpret_cast<const float2*>(z)[k];
+    a = (double)v.x;
+    b = (double)v.y;
+}
+template <>
+__device__ __forceinline__ void load2<double>(const double* z, unsigned k, double& a, double& b) {
+    const double2 v = reinterpret_cast<const double2*>(z)[k];
+    a = v.x;
+    b = v.y;
+}
+
+// z = the V-cycle result (T) or, with JAC, r * invd.
+template <class T, bool JAC>
+__device__ __forceinline__ void z_pair(const T* z, const double2* r2, const double2* d2, unsigned k,
+                                       double& za, double& zb) {
+    if (JAC) {
+        const double2 rv = r2[k], dv = d2[k];
+        za = rv.x * dv.x;
+        zb = rv.y * dv.y;
+    } else {
+        load2<T>(z, k, za, zb);
+    }
+}
+
+template <class T, bool JAC, bool FLEX>
+__global__ void __launch_bounds__(NT)
+    k_dot(unsigned n2, const double* __restrict__ r, const T* __restrict__ z,
+          const double* __restrict__ invd, const double* __restrict__ Ap, Ctl* ctl, double* part,
+          int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const double2* r2 = reinterpret_cast<const double2*>(r);
+    const double2* d2 = reinterpret_cast<const double2*>(invd);
+    const double2* a2 = reinterpret_cast<const double2*>(Ap);
+    double rz = 0.0, zap = 0.0;
+    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
+        double za, zb;
+        z_pair<T, JAC>(z, r2, d2, k, za, zb);
+        const double2 rv = r2[k];
+        rz += rv.x * za;
+        rz += rv.y * zb;
+        if (FLEX) {
+            const double2 av = a2[k];
+            zap += za * av.x;
+            zap += zb * av.y;
+        }
+    }
+    block_sum2(rz, zap);
+    if (publish2(rz, zap, part, maxb, &ctl->ticket[SL_DOT])) {
+        double RZ, ZAP;
+        gather2(part, maxb, &ctl->ticket[SL_DOT], RZ, ZAP);
+        if (threadIdx.x == 0) {
+            if (ctl->iter > 0) {
+                // Fletcher-Reeves (src/pcg3d_cpu.cpp:179) or flexible
+                // Polak-Ribiere: z_new.(r_new - r_old) / (z_old . r_old)
+                // = -(z_new . Ap) / (p . Ap).
+                ctl->beta = FLEX ? -ZAP / ctl->pAp : RZ / ctl->rz;
+            } else {
+                ctl->beta = 0.0;
+            }
+            ctl->rz = RZ;
+            ctl->zAp = ZAP;
+            if (!isfinite(RZ) || !isfinite(ctl->beta)) {
+                ctl->breakdown = 1;
+                stop_loop(ctl, cond);
+            }
+        }
+    }
+}
+
+template <class T, bool JAC>
+__global__ void __launch_bounds__(NT)
+    k_update_p(unsigned n2, const T* __restrict__ z, const double* __restrict__ r,
+               const double* __restrict__ invd, double* __restrict__ p, const Ctl* ctl, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const double beta = ctl->beta;
+    const bool first = ctl->iter == 0;
+    const double2* r2 = reinterpret_cast<const double2*>(r);
+    const double2* d2 = reinterpret_cast<const double2*>(invd);
+    double2* p2 = reinterpret_cast<double2*>(p);
+    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
+        double za, zb;
+        z_pair<T, JAC>(z, r2, d2, k, za, zb);
+        if (first) {
+            p2[k] = make_double2(za, zb);
+        } else {
+            const double2 pv = p2[k];
+            p2[k] = make_double2(za + beta * pv.x, zb + beta * pv.y);
+        }
+    }
+}
+
+// ---- setup and bookkeeping ------------------------------------------------
+
+__global__ void k_to_split_f(Geo g, int planes, const float* __restrict__ in,
+                             float* __restrict__ out) {
+    const size_t nxy = (size_t)g.nx * g.ny;
+    const size_t n = nxy * (size_t)planes;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(c / nxy);
+        const size_t rem = c - (size_t)l * nxy;
+        const int j = (int)(rem / g.nx), i = (int)(rem - (size_t)j * g.nx);
+        out[(size_t)l * g.plane + scol(g, i, j)] = in[c];
+    }
+}
+
+__global__ void k_to_split_d(Geo g, const double* __restrict__ in, double* __restrict__ out) {
+    const size_t nxy = (size_t)g.nx * g.ny;
+    const size_t n = nxy * (size_t)g.nz;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(c / nxy);
+        const size_t rem = c - (size_t)l * nxy;
+        const int j = (int)(rem / g.nx), i = (int)(rem - (size_t)j * g.nx);
+        out[(size_t)l * g.plane + scol(g, i, j)] = in[c];
+    }
+}
+
+__global__ void k_to_natural_d(Geo g, const double* __restrict__ in, double* __restrict__ out) {
+    const size_t nxy = (size_t)g.nx * g.ny;
+    const size_t n = nxy * (size_t)g.nz;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(c / nxy);
+        const size_t rem = c - (size_t)l * nxy;
+        const int j = (int)(rem / g.nx), i = (int)(rem - (size_t)j * g.nx);
+        out[c] = in[(size_t)l * g.plane + scol(g, i, j)];
+    }
+}
+
+// op_diag (src/operator3d.h:80-88) in double with every rounding explicit
+// (no contraction), so the diagonal equals the CPU's bit for bit.
+__global__ void k_diag(OpView o, double inv_dt, double* __restrict__ diag,
+                       double* __restrict__ invd) {
+    const Geo& g = o.g;
+    const size_t ncol = (size_t)g.nx * g.ny;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < ncol;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(q / g.nx), i = (int)(q - (size_t)j * g.nx);
+        const unsigned s = scol(g, i, j);
+        for (int l = 0; l < g.nz; ++l) {
+            const unsigned base = (unsigned)l * g.plane, id = base + s;
+            double d = 0.0;
+            if (i > 0) d = __dadd_rn(d, (double)o.gE[base + scol(g, i - 1, j)]);
+            if (i < g.nx - 1) d = __dadd_rn(d, (double)o.gE[id]);
+            if (j > 0) d = __dadd_rn(d, (double)o.gN[base + scol(g, i, j - 1)]);
+            if (j < g.ny - 1) d = __dadd_rn(d, (double)o.gN[id]);
+            d = __dadd_rn(d, (double)o.gU[id]);
+            d = __dadd_rn(d, l > 0 ? (double)o.gU[id - g.plane] : (double)o.gB[s]);
+            d = __dadd_rn(d, __dmul_rn((double)o.cap[id], inv_dt));
+            diag[id] = d;
+            if (invd) invd[id] = __drcp_rn(d);
+        }
+    }
+}
+
+__global__ void k_rhs_transient(unsigned n, const float* __restrict__ cap, double inv_dt,
+                                const double* __restrict__ P, const double* __restrict__ x,
+                                double* __restrict__ b, double* __restrict__ xold) {
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const double xv = x[k];
+        // b = P + C/dt x, rounded as the reference rounds it (src/pcg3d_cpu.cpp:64)
+        b[k] = __dadd_rn(P[k], __dmul_rn(__dmul_rn((double)cap[k], inv_dt), xv));
+        xold[k] = xv;
+    }
+}
+
+// true_relres (src/pcg3d_cpu.cpp:207-220): the steady residual P - A x with
+// the diagonal rebuilt from the faces, in FP64.
+__global__ void __launch_bounds__(NT)
+    k_true_residual(OpView o, const double* __restrict__ P, const double* __restrict__ x, Ctl* ctl,
+                    double* part, int maxb) {
+    const Geo& g = o.g;
+    double rr = 0.0, bb = 0.0;
+    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) continue;
+        double x_c = x[c.s], x_b = 0.0;
+        float gu_b = 0.0f;
+        for (int l = 0; l < g.nz; ++l) {
+            const unsigned base = (unsigned)l * g.plane, id = base + c.s;
+            const bool up = l < g.nz - 1;
+            const double x_a = up ? x[id + g.plane] : 0.0;
+            const float gu = o.gU[id];
+            double d = 0.0, off = 0.0;
+            if (c.i > 0) {
+                d += (double)o.gE[base + c.sw];
+                off += (double)o.gE[base + c.sw] * x[base + c.sw];
+            }
+            if (c.i < g.nx - 1) {
+                d += (double)o.gE[id];
+                off += (double)o.gE[id] * x[base + c.se];
+            }
+            if (c.j > 0) {
+                d += (double)o.gN[base + c.ss];
+                off += (double)o.gN[base + c.ss] * x[base + c.ss];
+            }
+            if (c.j < g.ny - 1) {
+                d += (double)o.gN[id];
+                off += (double)o.gN[id] * x[base + c.sn];
+            }
+            d += (double)gu;
+            d += l > 0 ? (double)gu_b : (double)o.gB[c.s];
+            if (l > 0) off += (double)gu_b * x_b;
+            if (up) off += (double)gu * x_a;
+            const double res = P[id] - (d * x_c - off);
+            rr += res * res;
+            bb += P[id] * P[id];
+            x_b = x_c;
+            x_c = x_a;
+            gu_b = gu;
+        }
+    }
+    block_sum2(rr, bb);
+    if (publish2(rr, bb, part, maxb, &ctl->ticket[SL_AUX])) {
+        double RR, BB;
+        gather2(part, maxb, &ctl->ticket[SL_AUX], RR, BB);
+        if (threadIdx.x == 0) {
+            ctl->aux0 = RR;
+            ctl->aux1 = BB;
+        }
+    }
+}
+
+// T_max, heat_out and sum C (x - xold) (src/stack3d.h:252-273).
+__global__ void __launch_bounds__(NT)
+    k_step_record(OpView o, const double* __restrict__ x, const double* __restrict__ xold,
+                  Ctl* ctl, double* part, int maxb) {
+    const Geo& g = o.g;
+    double tmax = -INFINITY, qout = 0.0, qst = 0.0;
+    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) continue;
+        for (int l = 0; l < g.nz; ++l) {
+            const unsigned id = (unsigned)l * g.plane + s;
+            const double xv = x[id];
+            tmax = fmax(tmax, xv);
+            qst += (double)o.cap[id] * (xv - xold[id]);
+        }
+        const unsigned top = (unsigned)(g.nz - 1) * g.plane + s;
+        qout += (double)o.gU[top] * x[top];
+        qout += (double)o.gB[s] * x[s];
+    }
+    // block max of tmax (fixed tree), then the two sums
+    __shared__ double sm[NT / 32];
+    double m = tmax;
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < NT / 32 ? sm[threadIdx.x] : -INFINITY;
+        for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+    }
+    block_sum2(qout, qst);
+    if (threadIdx.x == 0) part[2 * maxb + blockIdx.x] = m;
+    if (publish2(qout, qst, part, maxb, &ctl->ticket[SL_AUX])) {
+        double QO, QS;
+        __threadfence();
+        double mm = -INFINITY;
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += NT) mm = fmax(mm, __ldcg(part + 2 * maxb + k));
+        for (int off = 16; off > 0; off >>= 1) mm = fmax(mm, __shfl_down_sync(0xffffffffu, mm, off));
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mm;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            mm = threadIdx.x < NT / 32 ? sm[threadIdx.x] : -INFINITY;
+            for (int off = 16; off > 0; off >>= 1) mm = fmax(mm, __shfl_down_sync(0xffffffffu, mm, off));
+        }
+        gather2(part, maxb, &ctl->ticket[SL_AUX], QO, QS);
+        if (threadIdx.x == 0) {
+            ctl->aux0 = mm;
+            ctl->aux1 = QO;
+            ctl->aux2 = QS;
+        }
+    }
+}
+
+unsigned grid_for(size_t n, int threads = NT) {
+    size_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 65535u * 16u) b = 65535u * 16u;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+void launch_residual(cudaStream_t st, MgType mt, const OpView& o, const double* diag,
+                     const double* b, const double* x, double* r, void* b0, Ctl* ctl,
+                     const Red& red, Cond cond) {
+    if (mt == MG_F64)
+        k_residual<double><<<red.blocks, NT, 0, st>>>(o, diag, b, x, r, (double*)b0, ctl, red.part,
+                                                      red.maxb, cond);
+    else
+        k_residual<float><<<red.blocks, NT, 0, st>>>(o, diag, b, x, r,
+                                                     mt == MG_F32 ? (float*)b0 : nullptr, ctl,
+                                                     red.part, red.maxb, cond);
+}
+
+void launch_apply(cudaStream_t st, const OpView& o, const double* diag, const double* p,
+                  double* Ap, Ctl* ctl, const Red& red, Cond cond) {
+    k_apply<<<red.blocks, NT, 0, st>>>(o, diag, p, Ap, ctl, red.part, red.maxb, cond);
+}
+
+void launch_update(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap,
+                   double* x, double* r, void* b0, Ctl* ctl, const Red& red, Cond cond) {
+    const unsigned n2 = n / 2;
+    if (mt == MG_F32)
+        k_update<float, true><<<red.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (float*)b0, ctl, red.part,
+                                                         red.maxb, cond);
+    else if (mt == MG_F64)
+        k_update<double, true><<<red.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (double*)b0, ctl,
+                                                          red.part, red.maxb, cond);
+    else
+        k_update<float, false><<<red.blocks, NT, 0, st>>>(n2, p, Ap, x, r, nullptr, ctl, red.part,
+                                                          red.maxb, cond);
+}
+
+void launch_dot(cudaStream_t st, MgType mt, bool flexible, unsigned n, const double* r,
+                const void* z, const double* invd, const double* Ap, Ctl* ctl, const Red& red,
+                Cond cond) {
+    const unsigned n2 = n / 2;
+    if (mt == MG_NONE)
+        k_dot<float, true, false><<<red.blocks, NT, 0, st>>>(n2, r, nullptr, invd, Ap, ctl,
+                                                             red.part, red.maxb, cond);
+    else if (mt == MG_F32 && flexible)
+        k_dot<float, false, true><<<red.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap, ctl,
+                                                             red.part, red.maxb, cond);
+    else if (mt == MG_F32)
+        k_dot<float, false, false><<<red.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap,
+                                                              ctl, red.part, red.maxb, cond);
+    else if (flexible)
+        k_dot<double, false, true><<<red.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
+                                                              ctl, red.part, red.maxb, cond);
+    else
+        k_dot<double, false, false><<<red.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
+                                                               ctl, red.part, red.maxb, cond);
+}
+
+void launch_update_p(cudaStream_t st, MgType mt, unsigned n, const void* z, const double* r,
+                     const double* invd, double* p, Ctl* ctl, Cond cond) {
+    const unsigned n2 = n / 2;
+    const unsigned grid = grid_for(n2);
+    if (mt == MG_NONE)
+        k_update_p<float, true><<<grid, NT, 0, st>>>(n2, nullptr, r, invd, p, ctl, cond);
+    else if (mt == MG_F32)
+        k_update_p<float, false><<<grid, NT, 0, st>>>(n2, (const float*)z, r, invd, p, ctl, cond);
+    else
+        k_update_p<double, false><<<grid, NT, 0, st>>>(n2, (const double*)z, r, invd, p, ctl, cond);
+}
+
+void launch_to_split_f(cudaStream_t st, const Geo& g, int planes, const float* nat, float* split) {
+    k_to_split_f<<<grid_for((size_t)g.nx * g.ny * planes), NT, 0, st>>>(g, planes, nat, split);
+}
+
+void launch_to_split_d(cudaStream_t st, const Geo& g, const double* nat, double* split) {
+    k_to_split_d<<<grid_for((size_t)g.nx * g.ny * g.nz), NT, 0, st>>>(g, nat, split);
+}
+
+void launch_to_natural_d(cudaStream_t st, const Geo& g, const double* split, double* nat) {
+    k_to_natural_d<<<grid_for((size_t)g.nx * g.ny * g.nz), NT, 0, st>>>(g, split, nat);
+}
+
+void launch_diag(cudaStream_t st, const OpView& o, double inv_dt, double* diag, double* invd) {
+    k_diag<<<grid_for((size_t)o.g.nx * o.g.ny), NT, 0, st>>>(o, inv_dt, diag, invd);
+}
+
+void launch_rhs_transient(cudaStream_t st, unsigned n, const float* cap, double inv_dt,
+                          const double* P, const double* x, double* b, double* xold) {
+    k_rhs_transient<<<grid_for(n), NT, 0, st>>>(n, cap, inv_dt, P, x, b, xold);
+}
+
+void launch_true_residual(cudaStream_t st, const OpView& o, const double* P, const double* x,
+                          Ctl* ctl, const Red& red) {
+    k_true_residual<<<red.blocks, NT, 0, st>>>(o, P, x, ctl, red.part, red.maxb);
+}
+
+void launch_step_record(cudaStream_t st, const OpView& o, const double* x, const double* xold,
+                        Ctl* ctl, const Red& red) {
+    k_step_record<<<red.blocks, NT, 0, st>>>(o, x, xold, ctl, red.part, red.maxb);
+}
+
+}  // namespace ct

@@ -1,0 +1,88 @@
+// reduce.cuh - deterministic grid reductions for the solver kernels.
+//
+// Each reducing kernel sums two doubles per thread, then per block (a fixed
+// warp-shuffle tree), writes the block's pair to its slot's partials and takes
+// a ticket. The block that takes the last ticket adds the partials in block
+// order with the same fixed tree and finishes the iteration's scalar work
+// (alpha, beta, the convergence test). No floating-point atomics, so the same
+// inputs give the same bits on every run and in graph or direct launches.
+#pragma once
+#include "device.h"
+
+namespace ct {
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum of (a, b); the result is valid in thread 0.
+__device__ __forceinline__ void block_sum2(double& a, double& b) {
+    __shared__ double sa[NT / 32], sb[NT / 32];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sa[w] = a;
+        sb[w] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        a = lane < NT / 32 ? sa[lane] : 0.0;
+        b = lane < NT / 32 ? sb[lane] : 0.0;
+        a = warp_sum(a);
+        b = warp_sum(b);
+    }
+}
+
+// Publishes the block's sums (valid in thread 0) and returns, in every
+// thread, whether this block arrived last.
+__device__ __forceinline__ bool publish2(double a, double b, double* part, int maxb,
+                                         unsigned* ticket) {
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = a;
+        part[maxb + blockIdx.x] = b;
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        last = (t == gridDim.x - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    return last != 0;
+}
+
+// In the last block: the grid totals, valid in thread 0. Resets the ticket.
+__device__ __forceinline__ void gather2(const double* part, int maxb, unsigned* ticket, double& A,
+                                        double& B) {
+    __threadfence();
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += NT) {
+        a += __ldcg(part + k);
+        b += __ldcg(part + maxb + k);
+    }
+    block_sum2(a, b);
+    if (threadIdx.x == 0) {
+        A = a;
+        B = b;
+        *ticket = 0u;
+    }
+}
+
+// Stops the solve: marks it done and, inside a graph loop, ends the loop
+// after the current body. Called by one thread.
+__device__ __forceinline__ void stop_loop(Ctl* c, const Cond& cond) {
+    c->done = 1;
+    if (cond.use) cudaGraphSetConditional(cond.h, 0u);
+}
+
+// Entry test of every loop-body kernel: once the solve is done, the rest of
+// the body is a no-op, and (inside a graph loop) the loop is told to end.
+__device__ __forceinline__ bool loop_done(const Ctl* c, const Cond& cond) {
+    if (*(volatile const int*)&c->done) {
+        if (cond.use && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond.h, 0u);
+        return true;
+    }
+    return false;
+}
+
+}  // namespace ct

@@ -1,0 +1,833 @@
+// solver.cu - the solver object behind ct_solver_* (GpuPcg, src/pcg3d.h:115-163).
+//
+// Memory: one device allocation per solver (an arena), carved into the fine
+// operator, the FP64 PCG vectors, every multigrid level and the reduction
+// scratch, all in the split layout (device.h), zeroed once so padding slots
+// stay zero. One CUDA stream per solver.
+//
+// Control flow of a solve: the host writes tol / maxit into the control block
+// and launches ONE CUDA graph: the start residual, then a conditional WHILE
+// node whose body is one PCG iteration rotated so that it ends with the
+// convergence test,
+//     V-cycle(r) -> z;  beta;  p = z + beta p;  Ap, alpha;  x, r update, test
+// The kernel that finishes the test clears the loop condition, and once the
+// solve is done every later kernel of the body returns at entry. alpha, beta
+// and the dot products never leave the device; the host reads the control
+// block once at the end. Where conditional nodes are unavailable the same two
+// parts are replayed as plain graphs with a host check every few iterations,
+// and with ct_use_graphs(0) every kernel is launched directly with a host
+// check per iteration, as the reference does (src/pcg3d_gpu.cu:672-680).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "cthermal.h"
+#include "kernels.h"
+#include "status.h"
+
+namespace ct {
+
+namespace {
+
+bool g_use_graphs = true;
+std::mutex g_setup_mu;
+ct_setup_times g_last_setup{};
+
+using clk = std::chrono::steady_clock;
+double ms_since(clk::time_point t) {
+    return std::chrono::duration<double, std::milli>(clk::now() - t).count();
+}
+
+#define CT_CK(call)                                                                              \
+    do {                                                                                         \
+        const cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                                   \
+            return ct::fail(e_ == cudaErrorMemoryAllocation ? CT_OUT_OF_MEMORY : CT_CUDA_ERROR,  \
+                            "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+// Bump allocator over one device allocation, 256-byte aligned.
+struct Arena {
+    size_t used = 0;
+    size_t take(size_t bytes) {
+        const size_t off = used;
+        used += (bytes + 255) & ~size_t(255);
+        return off;
+    }
+};
+
+// Host-side record of one multigrid level.
+struct Level {
+    Geo g;
+    size_t o_gE, o_gN, o_gU, o_gB, o_cap, o_fcp, o_finv, o_x, o_b, o_dx, o_dy;
+    std::vector<double> dx, dy;  // cell widths (m), for the coarsening
+};
+
+// mg_coarse_widths (src/mg3d.h:250-256).
+std::vector<double> coarse_widths(const std::vector<double>& f) {
+    std::vector<double> c;
+    const int n = (int)f.size();
+    for (int I = 0; I < (n + 1) / 2; ++I) c.push_back(f[2 * I] + (2 * I + 1 < n ? f[2 * I + 1] : 0.0));
+    return c;
+}
+
+struct ProfEntry {
+    std::string name;
+    double bytes;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+class Solver {
+  public:
+    ct_precond pc = CT_MULTIGRID;
+    ct_precision prec = CT_MG_FP32_FLEX;
+    MgType mt = MG_F32;
+    bool flex = true;
+    size_t tsize = 4;  // bytes per V-cycle value
+    Geo g0{};
+    unsigned n = 0;      // slots of all planes (split layout, with padding)
+    size_t ncells = 0;   // nx * ny * nz
+    double dx = 0, dy = 0;
+    int sms = 0;
+    cudaStream_t st = nullptr;
+    char* base = nullptr;
+    size_t bytes = 0;
+    // fine operator and PCG vectors (split layout)
+    float *gE = nullptr, *gN = nullptr, *gU = nullptr, *gB = nullptr, *cap = nullptr;
+    double *P = nullptr, *x = nullptr, *b = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr;
+    double *diag = nullptr, *invd = nullptr, *xold = nullptr, *nat = nullptr, *part = nullptr;
+    Ctl* ctl = nullptr;
+    Ctl* h_ctl = nullptr;  // pinned mirror
+    std::vector<Level> lv;
+    int maxb = 0;
+    double inv_dt = 0;
+    bool use_graphs = true;
+    bool have_cond = false;
+    cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr;
+    ct_setup_times times{};
+    // per-kernel timing (ct_profile_solve)
+    bool prof = false;
+    std::vector<ProfEntry> prof_log;
+
+    ~Solver() {
+        if (st) cudaStreamSynchronize(st);
+        for (cudaGraphExec_t g : {gx_solve, gx_init, gx_body})
+            if (g) cudaGraphExecDestroy(g);
+        if (base) cudaFree(base);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    template <class T>
+    T* at(size_t off) const { return reinterpret_cast<T*>(base + off); }
+
+    OpView op() const { return OpView{g0, gE, gN, gU, gB, cap}; }
+
+    template <class T>
+    LevelView<T> view(size_t k) const {
+        const Level& L = lv[k];
+        LevelView<T> v;
+        v.g = L.g;
+        v.gE = at<float>(L.o_gE);
+        v.gN = at<float>(L.o_gN);
+        v.gU = at<float>(L.o_gU);
+        v.gB = at<float>(L.o_gB);
+        v.cap = at<float>(L.o_cap);
+        v.fcp = at<T>(L.o_fcp);
+        v.finv = at<T>(L.o_finv);
+        v.x = at<T>(L.o_x);
+        v.b = at<T>(L.o_b);
+        return v;
+    }
+
+    Red red(int blocks_wanted, Slot sl) const {
+        Red rd;
+        rd.part = part + (size_t)sl * 4 * maxb;
+        rd.maxb = maxb;
+        rd.blocks = std::max(1, std::min(blocks_wanted, maxb));
+        return rd;
+    }
+    Red red_cols(Slot sl) const { return red((int)((g0.plane + NT - 1) / NT), sl); }
+    Red red_vec(Slot sl) const { return red((int)((n / 2 + NT - 1) / NT), sl); }
+
+    ct_status create(const ct_model* m, ct_precond pc_, ct_precision prec_);
+    ct_status set_dt(double dt);
+    ct_status solve(double tol, int maxit, ct_stats* out);
+    ct_status record_graphs();
+
+    // Enqueues one kernel launch; in profiling mode brackets it with events.
+    template <class F>
+    void enq(const char* name, double nbytes, F&& launch) {
+        if (!prof) {
+            launch();
+            return;
+        }
+        ProfEntry e{name, nbytes, nullptr, nullptr};
+        cudaEventCreate(&e.a);
+        cudaEventCreate(&e.b);
+        cudaEventRecord(e.a, st);
+        launch();
+        cudaEventRecord(e.b, st);
+        prof_log.push_back(e);
+    }
+
+    void enqueue_init(Cond cond);
+    void enqueue_body(Cond cond);
+    template <class T>
+    void vcycle(size_t k, Cond cond);
+};
+
+// ---- setup ---------------------------------------------------------------
+
+ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) {
+    if (!m) return fail(CT_BAD_ARG, "ct_solver_create: null model");
+    if (m->nx < 1 || m->ny < 1 || m->nz < 1 || m->nz > CT_MAXZ)
+        return fail(CT_BAD_ARG, "ct_solver_create: bad size %d x %d x %d (nz must be 1..%d)", m->nx,
+                    m->ny, m->nz, CT_MAXZ);
+    if (!m->gE || !m->gN || !m->gU || !m->gB || !m->cap)
+        return fail(CT_NOT_FINALIZED, "Model3D used before finalize()");
+    if (!m->P) return fail(CT_BAD_ARG, "ct_solver_create: null power map");
+    if (!(m->dx > 0) || !(m->dy > 0)) return fail(CT_BAD_ARG, "ct_solver_create: dx, dy must be > 0");
+    if (pc_ != CT_JACOBI && pc_ != CT_MULTIGRID) return fail(CT_BAD_ARG, "bad preconditioner");
+    if (prec_ != CT_MG_FP64 && prec_ != CT_MG_FP32 && prec_ != CT_MG_FP32_FLEX)
+        return fail(CT_BAD_ARG, "bad precision");
+    pc = pc_;
+    prec = prec_;
+    mt = pc == CT_JACOBI ? MG_NONE : (prec == CT_MG_FP64 ? MG_F64 : MG_F32);
+    flex = pc == CT_MULTIGRID && prec == CT_MG_FP32_FLEX;
+    tsize = mt == MG_F64 ? 8 : 4;
+    g0 = geo_of(m->nx, m->ny, m->nz);
+    const double slots = (double)g0.plane * g0.nz;
+    if (slots > 2.0e9) return fail(CT_BAD_ARG, "model too large for one solver (%.0f cells)", slots);
+    n = g0.plane * (unsigned)g0.nz;
+    ncells = (size_t)m->nx * m->ny * m->nz;
+    dx = m->dx;
+    dy = m->dy;
+    use_graphs = g_use_graphs;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CT_NO_DEVICE, "no CUDA device");
+    }
+    int dev = 0;
+    CT_CK(cudaGetDevice(&dev));
+    CT_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    maxb = std::max(1, sms * (2048 / NT));
+
+    auto t0 = clk::now();
+    CT_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CT_CK(cudaMallocHost(&h_ctl, sizeof(Ctl)));
+    std::memset(h_ctl, 0, sizeof(Ctl));
+
+    // Level sizes (src/mg3d.h:271-293) and the arena layout.
+    Arena ar;
+    const size_t o_gE = ar.take(n * 4), o_gN = ar.take(n * 4), o_gU = ar.take(n * 4);
+    const size_t o_cap = ar.take(n * 4), o_gB = ar.take((size_t)g0.plane * 4);
+    size_t o_vec[8];
+    for (size_t& o : o_vec) o = ar.take((size_t)n * 8);
+    const size_t o_invd = pc == CT_JACOBI ? ar.take((size_t)n * 8) : 0;
+    const size_t o_nat = ar.take(ncells * 8);
+    const size_t o_part = ar.take((size_t)NSLOT * 4 * maxb * 8);
+    const size_t o_ctl = ar.take(sizeof(Ctl));
+    if (pc == CT_MULTIGRID) {
+        Level L;
+        L.g = g0;
+        L.dx.assign(m->nx, m->dx);
+        L.dy.assign(m->ny, m->dy);
+        while (true) {
+            const size_t ln = (size_t)L.g.plane * L.g.nz;
+            if (lv.empty()) {  // level 0 shares the fine operator
+                L.o_gE = o_gE;
+                L.o_gN = o_gN;
+                L.o_gU = o_gU;
+                L.o_cap = o_cap;
+                L.o_gB = o_gB;
+            } else {
+                L.o_gE = ar.take(ln * 4);
+                L.o_gN = ar.take(ln * 4);
+                L.o_gU = ar.take(ln * 4);
+                L.o_cap = ar.take(ln * 4);
+                L.o_gB = ar.take((size_t)L.g.plane * 4);
+            }
+            L.o_fcp = ar.take(ln * tsize);
+            L.o_finv = ar.take(ln * tsize);
+            L.o_x = ar.take(ln * tsize);
+            L.o_b = ar.take(ln * tsize);
+            L.o_dx = ar.take(L.dx.size() * 8);
+            L.o_dy = ar.take(L.dy.size() * 8);
+            lv.push_back(L);
+            if (L.g.nx == 1 && L.g.ny == 1) break;
+            Level C;
+            C.g = geo_of((L.g.nx + 1) / 2, (L.g.ny + 1) / 2, L.g.nz);
+            C.dx = coarse_widths(L.dx);
+            C.dy = coarse_widths(L.dy);
+            L = C;
+        }
+    }
+    bytes = ar.used;
+    {
+        const cudaError_t e = cudaMalloc(&base, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            base = nullptr;
+            return fail(CT_OUT_OF_MEMORY, "cudaMalloc of %.1f MB failed: %s", bytes / 1e6,
+                        cudaGetErrorString(e));
+        }
+    }
+    CT_CK(cudaMemsetAsync(base, 0, bytes, st));
+    gE = at<float>(o_gE);
+    gN = at<float>(o_gN);
+    gU = at<float>(o_gU);
+    cap = at<float>(o_cap);
+    gB = at<float>(o_gB);
+    P = at<double>(o_vec[0]);
+    x = at<double>(o_vec[1]);
+    b = at<double>(o_vec[2]);
+    r = at<double>(o_vec[3]);
+    p = at<double>(o_vec[4]);
+    Ap = at<double>(o_vec[5]);
+    diag = at<double>(o_vec[6]);
+    xold = at<double>(o_vec[7]);
+    invd = pc == CT_JACOBI ? at<double>(o_invd) : nullptr;
+    nat = at<double>(o_nat);
+    part = at<double>(o_part);
+    ctl = at<Ctl>(o_ctl);
+    CT_CK(cudaStreamSynchronize(st));
+    times.alloc_ms = ms_since(t0);
+
+    // Upload the fine operator and P through the natural staging buffer.
+    t0 = clk::now();
+    float* natf = reinterpret_cast<float*>(nat);
+    const float* src[4] = {m->gE, m->gN, m->gU, m->cap};
+    float* dst[4] = {gE, gN, gU, cap};
+    for (int a = 0; a < 4; ++a) {
+        CT_CK(cudaMemcpyAsync(natf, src[a], ncells * 4, cudaMemcpyHostToDevice, st));
+        launch_to_split_f(st, g0, g0.nz, natf, dst[a]);
+    }
+    CT_CK(cudaMemcpyAsync(natf, m->gB, (size_t)m->nx * m->ny * 4, cudaMemcpyHostToDevice, st));
+    launch_to_split_f(st, g0, 1, natf, gB);
+    CT_CK(cudaMemcpyAsync(nat, m->P, ncells * 8, cudaMemcpyHostToDevice, st));
+    launch_to_split_d(st, g0, nat, P);
+    for (Level& L : lv) {
+        CT_CK(cudaMemcpyAsync(base + L.o_dx, L.dx.data(), L.dx.size() * 8, cudaMemcpyHostToDevice, st));
+        CT_CK(cudaMemcpyAsync(base + L.o_dy, L.dy.data(), L.dy.size() * 8, cudaMemcpyHostToDevice, st));
+    }
+    CT_CK(cudaGetLastError());
+    CT_CK(cudaStreamSynchronize(st));
+    times.upload_ms = ms_since(t0);
+
+    // Coarse levels, built on the device from the next finer one.
+    t0 = clk::now();
+    for (size_t k = 1; k < lv.size(); ++k) {
+        const Level& F = lv[k - 1];
+        const Level& C = lv[k];
+        launch_coarsen(st, F.g, at<float>(F.o_gE), at<float>(F.o_gN), at<float>(F.o_gU),
+                       at<float>(F.o_gB), at<float>(F.o_cap), at<double>(F.o_dx),
+                       at<double>(F.o_dy), C.g, at<double>(C.o_dx), at<double>(C.o_dy),
+                       at<float>(C.o_gE), at<float>(C.o_gN), at<float>(C.o_gU), at<float>(C.o_gB),
+                       at<float>(C.o_cap));
+    }
+    CT_CK(cudaGetLastError());
+    CT_CK(cudaStreamSynchronize(st));
+    times.levels_ms = ms_since(t0);
+
+    t0 = clk::now();
+    ct_status s = set_dt(0.0);
+    if (s != CT_OK) return s;
+    CT_CK(cudaStreamSynchronize(st));
+    times.factor_ms = ms_since(t0);
+
+    t0 = clk::now();
+    if (use_graphs) {
+        s = record_graphs();
+        if (s != CT_OK) return s;
+    }
+    CT_CK(cudaStreamSynchronize(st));
+    times.graphs_ms = ms_since(t0);
+    {
+        std::lock_guard<std::mutex> lk(g_setup_mu);
+        g_last_setup = times;
+    }
+    return CT_OK;
+}
+
+ct_status Solver::set_dt(double dt) {
+    if (!(dt >= 0) || !std::isfinite(dt)) return fail(CT_BAD_ARG, "ct_set_dt: dt must be >= 0");
+    inv_dt = dt > 0 ? 1.0 / dt : 0.0;
+    launch_diag(st, op(), inv_dt, diag, invd);
+    if (mt == MG_F32)
+        for (size_t k = 0; k < lv.size(); ++k) launch_factor<float>(st, view<float>(k), (float)inv_dt);
+    else if (mt == MG_F64)
+        for (size_t k = 0; k < lv.size(); ++k) launch_factor<double>(st, view<double>(k), inv_dt);
+    CT_CK(cudaGetLastError());
+    return CT_OK;
+}
+
+// ---- one PCG iteration ----------------------------------------------------
+
+template <class T>
+void Solver::vcycle(size_t k, Cond cond) {
+    const LevelView<T> L = view<T>(k);
+    const double cells = (double)L.g.nx * L.g.ny * L.g.nz;
+    const double t = (double)sizeof(T);
+    const std::string lvl = "_l" + std::to_string(k);
+    // algorithmic bytes: each array touched once per kernel
+    const double b_zero = cells / 2 * (4 * t + 4);
+    const double b_sweep = cells / 2 * (4 * t + 12) + cells / 2 * (t + 8);
+    if (k + 1 == lv.size()) {
+        enq(("mg_sweep0" + lvl).c_str(), b_zero,
+            [&] { launch_sweep<T>(st, L, 0, true, nullptr, ctl, cond); });
+        return;
+    }
+    const LevelView<T> C = view<T>(k + 1);
+    enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { launch_sweep<T>(st, L, 0, true, nullptr, ctl, cond); });
+    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(st, L, 1, false, nullptr, ctl, cond); });
+    enq(("mg_restrict" + lvl).c_str(), cells * (2 * t + 16) + cells / 4 * t,
+        [&] { launch_restrict<T>(st, L, C, ctl, cond); });
+    vcycle<T>(k + 1, cond);
+    enq(("mg_sweep" + lvl).c_str(), b_sweep + cells / 4 * t,
+        [&] { launch_sweep<T>(st, L, 1, false, &C, ctl, cond); });
+    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(st, L, 0, false, nullptr, ctl, cond); });
+}
+
+void Solver::enqueue_init(Cond cond) {
+    void* b0 = mt == MG_NONE ? nullptr : (void*)(base + lv[0].o_b);
+    enq("pcg_residual", (double)ncells * (36 + 8 + 8 + tsize), [&] {
+        launch_residual(st, mt, op(), diag, b, x, r, b0, ctl, red_cols(SL_INIT), cond);
+    });
+}
+
+void Solver::enqueue_body(Cond cond) {
+    const double N = (double)ncells;
+    const void* z = nullptr;
+    if (mt == MG_F32) {
+        vcycle<float>(0, cond);
+        z = base + lv[0].o_x;
+    } else if (mt == MG_F64) {
+        vcycle<double>(0, cond);
+        z = base + lv[0].o_x;
+    }
+    const double zb = mt == MG_NONE ? 16.0 : (double)tsize;
+    enq("pcg_dot", N * (8 + zb + (flex ? 8 : 0)),
+        [&] { launch_dot(st, mt, flex, n, r, z, invd, Ap, ctl, red_vec(SL_DOT), cond); });
+    enq("pcg_update_p", N * (zb + 16), [&] { launch_update_p(st, mt, n, z, r, invd, p, ctl, cond); });
+    enq("pcg_apply", N * 36, [&] { launch_apply(st, op(), diag, p, Ap, ctl, red_cols(SL_APPLY), cond); });
+    void* b0 = mt == MG_NONE ? nullptr : (void*)(base + lv[0].o_b);
+    enq("pcg_update_xr", N * (48 + (mt == MG_NONE ? 0 : tsize)),
+        [&] { launch_update(st, mt, n, p, Ap, x, r, b0, ctl, red_vec(SL_UPDATE), cond); });
+}
+
+ct_status Solver::record_graphs() {
+    // Preferred: init + WHILE(body) as one graph.
+    cudaGraph_t graph = nullptr;
+    CT_CK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h{};
+    bool ok = cudaGraphConditionalHandleCreate(&h, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+        const Cond cond{h, 1};
+        ok = cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            enqueue_init(cond);
+            cudaStreamCaptureStatus cs;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t ndeps = 0;
+            cudaGraph_t cg = nullptr;
+            ok = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &ndeps) == cudaSuccess;
+            cudaGraphNode_t cnode = nullptr;
+            cudaGraph_t body = nullptr;
+            if (ok) {
+                cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+                cp.conditional.handle = h;
+                cp.conditional.type = cudaGraphCondTypeWhile;
+                cp.conditional.size = 1;
+                ok = cudaGraphAddNode(&cnode, cg, deps, nullptr, ndeps, &cp) == cudaSuccess;
+                if (ok) body = cp.conditional.phGraph_out[0];
+            }
+            if (ok)
+                ok = cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1,
+                                                         cudaStreamSetCaptureDependencies) == cudaSuccess;
+            cudaGraph_t outg = nullptr;
+            const bool ended = cudaStreamEndCapture(st, &outg) == cudaSuccess;
+            ok = ok && ended;
+            if (ok) {
+                ok = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+                if (ok) {
+                    enqueue_body(cond);
+                    cudaGraph_t bg = nullptr;
+                    ok = cudaStreamEndCapture(st, &bg) == cudaSuccess;
+                }
+            }
+            if (ok) ok = cudaGraphInstantiate(&gx_solve, graph, 0) == cudaSuccess;
+        }
+    }
+    cudaGraphDestroy(graph);
+    if (ok) {
+        have_cond = true;
+        return CT_OK;
+    }
+    cudaGetLastError();  // clear the failed attempt
+    if (gx_solve) {
+        cudaGraphExecDestroy(gx_solve);
+        gx_solve = nullptr;
+    }
+    // Fallback: the two parts as plain graphs, polled by the host.
+    const Cond none{0, 0};
+    for (int part_i = 0; part_i < 2; ++part_i) {
+        cudaGraph_t g = nullptr;
+        CT_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        if (part_i == 0)
+            enqueue_init(none);
+        else
+            enqueue_body(none);
+        CT_CK(cudaStreamEndCapture(st, &g));
+        const cudaError_t e = cudaGraphInstantiate(part_i == 0 ? &gx_init : &gx_body, g, 0);
+        cudaGraphDestroy(g);
+        CT_CK(e);
+    }
+    have_cond = false;
+    return CT_OK;
+}
+
+ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
+    if (!(tol >= 0)) return fail(CT_BAD_ARG, "ct_solve: tol must be >= 0");
+    if (maxit > 100000000) return fail(CT_BAD_ARG, "ct_solve: maxit above 1e8");
+    Ctl c;
+    std::memset(&c, 0, sizeof c);
+    c.tol = tol;
+    c.maxit = maxit;
+    c.inv_dt = inv_dt;
+    *h_ctl = c;
+    CT_CK(cudaMemcpyAsync(ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    const Cond none{0, 0};
+    if (prof) {
+        enqueue_init(none);
+        for (int it = 0; it <= maxit; ++it) {
+            CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+            CT_CK(cudaStreamSynchronize(st));
+            if (h_ctl->done) break;
+            enqueue_body(none);
+        }
+    } else if (have_cond) {
+        CT_CK(cudaGraphLaunch(gx_solve, st));
+    } else if (gx_init) {
+        CT_CK(cudaGraphLaunch(gx_init, st));
+        int launched = 0;
+        int k = 2;
+        while (true) {
+            CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+            CT_CK(cudaStreamSynchronize(st));
+            if (h_ctl->done || launched > maxit) break;
+            for (int q = 0; q < k; ++q) CT_CK(cudaGraphLaunch(gx_body, st));
+            launched += k;
+            k = std::min(k * 2, 8);
+        }
+    } else {
+        enqueue_init(none);
+        for (int it = 0; it <= maxit; ++it) {
+            CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+            CT_CK(cudaStreamSynchronize(st));
+            if (h_ctl->done) break;
+            enqueue_body(none);
+        }
+    }
+    CT_CK(cudaGetLastError());
+    CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CT_CK(cudaStreamSynchronize(st));
+    if (h_ctl->bb_zero) {  // no heat in: x = 0 (src/pcg3d_cpu.cpp:146)
+        CT_CK(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
+        CT_CK(cudaStreamSynchronize(st));
+    }
+    ct_stats s;
+    s.iters = h_ctl->iter;
+    s.relres = h_ctl->relres;
+    s.converged = h_ctl->converged;
+    s.breakdown = h_ctl->breakdown;
+    if (out) *out = s;
+    if (s.breakdown) return fail(CT_BREAKDOWN, "PCG breakdown after %d iterations (p.Ap = %g)", s.iters, h_ctl->pAp);
+    if (!s.converged) return fail(CT_NOT_CONVERGED, "not converged after %d iterations (relres %g)", s.iters, s.relres);
+    return CT_OK;
+}
+
+}  // namespace ct
+
+// ---- C ABI ----------------------------------------------------------------
+
+struct ct_solver {
+    ct::Solver impl;
+};
+
+using ct::fail;
+
+#define CT_SOLVER_OK(s) \
+    if (!(s)) return fail(CT_BAD_ARG, "%s: null solver", __func__)
+
+#define CT_CUDA(call)                                                                         \
+    do {                                                                                      \
+        const cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(CT_CUDA_ERROR, "%s: %s", #call, cudaGetErrorString(e_));              \
+    } while (0)
+
+namespace {
+// Copies a split-layout level array to the host in the natural layout.
+template <class S, class D>
+ct_status level_to_host(ct::Solver& v, const ct::Geo& g, size_t off, int planes, D* out) {
+    std::vector<S> tmp((size_t)g.plane * planes);
+    CT_CUDA(cudaMemcpyAsync(tmp.data(), v.base + off, tmp.size() * sizeof(S), cudaMemcpyDeviceToHost, v.st));
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    for (int l = 0; l < planes; ++l)
+        for (int j = 0; j < g.ny; ++j)
+            for (int i = 0; i < g.nx; ++i)
+                out[((size_t)l * g.ny + j) * g.nx + i] = (D)tmp[(size_t)l * g.plane + ct::scol(g, i, j)];
+    return CT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+void ct_use_graphs(int on) { ct::g_use_graphs = on != 0; }
+
+ct_status ct_last_setup(ct_setup_times* out) {
+    if (!out) return fail(CT_BAD_ARG, "ct_last_setup: null");
+    std::lock_guard<std::mutex> lk(ct::g_setup_mu);
+    *out = ct::g_last_setup;
+    return CT_OK;
+}
+
+ct_status ct_solver_create(const ct_model* m, ct_precond pc, ct_precision prec, ct_solver** out) {
+    if (!out) return fail(CT_BAD_ARG, "ct_solver_create: null output");
+    *out = nullptr;
+    ct_solver* s = new (std::nothrow) ct_solver();
+    if (!s) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
+    const ct_status st = s->impl.create(m, pc, prec);
+    if (st != CT_OK) {
+        delete s;
+        return st;
+    }
+    *out = s;
+    return CT_OK;
+}
+
+ct_status ct_solver_destroy(ct_solver* s) {
+    delete s;
+    return CT_OK;
+}
+
+ct_status ct_set_dt(ct_solver* s, double dt) {
+    CT_SOLVER_OK(s);
+    return s->impl.set_dt(dt);
+}
+
+ct_status ct_set_x_zero(ct_solver* s) {
+    CT_SOLVER_OK(s);
+    CT_CUDA(cudaMemsetAsync(s->impl.x, 0, (size_t)s->impl.n * 8, s->impl.st));
+    return CT_OK;
+}
+
+ct_status ct_set_x(ct_solver* s, const double* T) {
+    CT_SOLVER_OK(s);
+    if (!T) return fail(CT_BAD_ARG, "ct_set_x: null");
+    ct::Solver& v = s->impl;
+    CT_CUDA(cudaMemcpyAsync(v.nat, T, v.ncells * 8, cudaMemcpyHostToDevice, v.st));
+    ct::launch_to_split_d(v.st, v.g0, v.nat, v.x);
+    CT_CUDA(cudaGetLastError());
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    return CT_OK;
+}
+
+ct_status ct_set_rhs_steady(ct_solver* s) {
+    CT_SOLVER_OK(s);
+    CT_CUDA(cudaMemcpyAsync(s->impl.b, s->impl.P, (size_t)s->impl.n * 8, cudaMemcpyDeviceToDevice,
+                            s->impl.st));
+    return CT_OK;
+}
+
+ct_status ct_set_rhs_transient(ct_solver* s) {
+    CT_SOLVER_OK(s);
+    ct::Solver& v = s->impl;
+    ct::launch_rhs_transient(v.st, v.n, v.cap, v.inv_dt, v.P, v.x, v.b, v.xold);
+    CT_CUDA(cudaGetLastError());
+    return CT_OK;
+}
+
+ct_status ct_set_power(ct_solver* s, const double* P) {
+    CT_SOLVER_OK(s);
+    if (!P) return fail(CT_BAD_ARG, "ct_set_power: null");
+    ct::Solver& v = s->impl;
+    CT_CUDA(cudaMemcpyAsync(v.nat, P, v.ncells * 8, cudaMemcpyHostToDevice, v.st));
+    ct::launch_to_split_d(v.st, v.g0, v.nat, v.P);
+    CT_CUDA(cudaGetLastError());
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    return CT_OK;
+}
+
+ct_status ct_set_power_device(ct_solver* s, const double* P_dev) {
+    CT_SOLVER_OK(s);
+    if (!P_dev) return fail(CT_BAD_ARG, "ct_set_power_device: null");
+    ct::Solver& v = s->impl;
+    ct::launch_to_split_d(v.st, v.g0, P_dev, v.P);
+    CT_CUDA(cudaGetLastError());
+    return CT_OK;
+}
+
+ct_status ct_solve(ct_solver* s, double tol, int maxit, ct_stats* st) {
+    CT_SOLVER_OK(s);
+    return s->impl.solve(tol, maxit, st);
+}
+
+ct_status ct_get_x(ct_solver* s, double* T) {
+    CT_SOLVER_OK(s);
+    if (!T) return fail(CT_BAD_ARG, "ct_get_x: null");
+    ct::Solver& v = s->impl;
+    ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
+    CT_CUDA(cudaGetLastError());
+    CT_CUDA(cudaMemcpyAsync(T, v.nat, v.ncells * 8, cudaMemcpyDeviceToHost, v.st));
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    return CT_OK;
+}
+
+ct_status ct_device_x(ct_solver* s, const double** T_dev) {
+    CT_SOLVER_OK(s);
+    if (!T_dev) return fail(CT_BAD_ARG, "ct_device_x: null");
+    ct::Solver& v = s->impl;
+    ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
+    CT_CUDA(cudaGetLastError());
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    *T_dev = v.nat;
+    return CT_OK;
+}
+
+ct_status ct_solver_setup_times(const ct_solver* s, ct_setup_times* out) {
+    CT_SOLVER_OK(s);
+    if (!out) return fail(CT_BAD_ARG, "ct_solver_setup_times: null");
+    *out = s->impl.times;
+    return CT_OK;
+}
+
+ct_status ct_solver_stream(const ct_solver* s, void** stream) {
+    CT_SOLVER_OK(s);
+    if (!stream) return fail(CT_BAD_ARG, "ct_solver_stream: null");
+    *stream = (void*)s->impl.st;
+    return CT_OK;
+}
+
+ct_status ct_true_relres(ct_solver* s, double* out) {
+    CT_SOLVER_OK(s);
+    if (!out) return fail(CT_BAD_ARG, "ct_true_relres: null");
+    ct::Solver& v = s->impl;
+    ct::launch_true_residual(v.st, v.op(), v.P, v.x, v.ctl, v.red_cols(ct::SL_AUX));
+    CT_CUDA(cudaGetLastError());
+    CT_CUDA(cudaMemcpyAsync(v.h_ctl, v.ctl, sizeof(ct::Ctl), cudaMemcpyDeviceToHost, v.st));
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    *out = std::sqrt(v.h_ctl->aux0 / v.h_ctl->aux1);
+    return CT_OK;
+}
+
+ct_status ct_solver_step_record(ct_solver* s, double dt, ct_step_record* out) {
+    CT_SOLVER_OK(s);
+    if (!out || !(dt > 0)) return fail(CT_BAD_ARG, "ct_solver_step_record: null output or dt <= 0");
+    ct::Solver& v = s->impl;
+    ct::launch_step_record(v.st, v.op(), v.x, v.xold, v.ctl, v.red_cols(ct::SL_AUX));
+    CT_CUDA(cudaGetLastError());
+    CT_CUDA(cudaMemcpyAsync(v.h_ctl, v.ctl, sizeof(ct::Ctl), cudaMemcpyDeviceToHost, v.st));
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    out->T_max = v.h_ctl->aux0;
+    out->q_out = v.h_ctl->aux1;
+    out->q_stored = v.h_ctl->aux2 / dt;
+    return CT_OK;
+}
+
+ct_status ct_num_levels(const ct_solver* s, int* nlev) {
+    CT_SOLVER_OK(s);
+    if (!nlev) return fail(CT_BAD_ARG, "ct_num_levels: null");
+    *nlev = (int)s->impl.lv.size();
+    return CT_OK;
+}
+
+ct_status ct_level_dims(const ct_solver* s, int k, int* nx, int* ny, int* nz) {
+    CT_SOLVER_OK(s);
+    if (k < 0 || k >= (int)s->impl.lv.size() || !nx || !ny || !nz)
+        return fail(CT_BAD_ARG, "ct_level_dims: bad level %d", k);
+    const ct::Geo& g = s->impl.lv[(size_t)k].g;
+    *nx = g.nx;
+    *ny = g.ny;
+    *nz = g.nz;
+    return CT_OK;
+}
+
+
+ct_status ct_level_operator(ct_solver* s, int k, float* gE, float* gN, float* gU, float* gB,
+                            float* cap) {
+    CT_SOLVER_OK(s);
+    ct::Solver& v = s->impl;
+    if (k < 0 || k >= (int)v.lv.size() || !gE || !gN || !gU || !gB || !cap)
+        return fail(CT_BAD_ARG, "ct_level_operator: bad level %d or null array", k);
+    const ct::Level& L = v.lv[(size_t)k];
+    ct_status r;
+    if ((r = level_to_host<float>(v, L.g, L.o_gE, L.g.nz, gE)) != CT_OK) return r;
+    if ((r = level_to_host<float>(v, L.g, L.o_gN, L.g.nz, gN)) != CT_OK) return r;
+    if ((r = level_to_host<float>(v, L.g, L.o_gU, L.g.nz, gU)) != CT_OK) return r;
+    if ((r = level_to_host<float>(v, L.g, L.o_gB, 1, gB)) != CT_OK) return r;
+    return level_to_host<float>(v, L.g, L.o_cap, L.g.nz, cap);
+}
+
+ct_status ct_level_factors(ct_solver* s, int k, double* fcp, double* finv) {
+    CT_SOLVER_OK(s);
+    ct::Solver& v = s->impl;
+    if (k < 0 || k >= (int)v.lv.size() || !fcp || !finv)
+        return fail(CT_BAD_ARG, "ct_level_factors: bad level %d or null array", k);
+    const ct::Level& L = v.lv[(size_t)k];
+    ct_status r;
+    if (v.mt == ct::MG_F64) {
+        if ((r = level_to_host<double>(v, L.g, L.o_fcp, L.g.nz, fcp)) != CT_OK) return r;
+        return level_to_host<double>(v, L.g, L.o_finv, L.g.nz, finv);
+    }
+    if ((r = level_to_host<float>(v, L.g, L.o_fcp, L.g.nz, fcp)) != CT_OK) return r;
+    return level_to_host<float>(v, L.g, L.o_finv, L.g.nz, finv);
+}
+
+ct_status ct_profile_solve(ct_solver* s, double tol, int maxit, ct_stats* st, ct_kernel_time* out,
+                           int max, int* nout) {
+    CT_SOLVER_OK(s);
+    if (!out || !nout || max <= 0) return fail(CT_BAD_ARG, "ct_profile_solve: bad output");
+    ct::Solver& v = s->impl;
+    v.prof = true;
+    v.prof_log.clear();
+    const ct_status rs = v.solve(tol, maxit, st);
+    v.prof = false;
+    cudaStreamSynchronize(v.st);
+    std::vector<ct_kernel_time> agg;
+    for (const ct::ProfEntry& e : v.prof_log) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e.a, e.b);
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+        auto it = std::find_if(agg.begin(), agg.end(), [&](const ct_kernel_time& k) { return e.name == k.name; });
+        if (it == agg.end()) {
+            ct_kernel_time k;
+            std::memset(&k, 0, sizeof k);
+            std::snprintf(k.name, sizeof k.name, "%s", e.name.c_str());
+            agg.push_back(k);
+            it = agg.end() - 1;
+        }
+        it->launches += 1;
+        it->total_ms += ms;
+        it->bytes += e.bytes;
+    }
+    v.prof_log.clear();
+    *nout = std::min((int)agg.size(), max);
+    for (int k = 0; k < *nout; ++k) out[k] = agg[(size_t)k];
+    return rs;
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+/* cthermal.h - C ABI of libcthermal, a GB300 (sm_103a) solver for the steady
+ * and backward-Euler heat equation of a layered 3D chip stack: matrix-free
+ * PCG preconditioned by one geometric x-y semi-coarsening multigrid V-cycle
+ * with a red-black vertical-column (tridiagonal) line smoother, on the 7-point
+ * harmonic-mean conductance operator with a heat-sink boundary.
+ *
+ * This is the drop-in boundary for cuda-thermal's solver layer. Each entry
+ * point names the reference interface it replaces (file:line in cuda-thermal).
+ * Plain C: pointers, sizes and status codes, no C++ or framework types.
+ *
+ * Conventions
+ *  - Every call returns a ct_status; nothing calls exit(). ct_last_error()
+ *    gives the message of the last failure on the calling thread.
+ *  - Arrays are in the reference's natural layout: cell (i, j, l) at
+ *    (l * ny + j) * nx + i (src/stack3d.h:73). Temperatures are rises above
+ *    ambient (K), powers in W, conductances in W/K, capacities in J/K.
+ *  - A solver owns its device memory and one CUDA stream. The model arrays are
+ *    copied at creation, so the caller may free them afterwards. A solver is
+ *    not thread-safe; distinct solvers may be used from distinct threads.
+ */
+#ifndef CTHERMAL_H
+#define CTHERMAL_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CT_MAXZ 64 /* most z-planes a model may have (src/stack3d.h:34) */
+
+typedef enum ct_status {
+    CT_OK = 0,
+    CT_NOT_CONVERGED = 1, /* maxit reached (PcgStats.converged = false) */
+    CT_BREAKDOWN = 2,     /* p.Ap <= 0 or a NaN/Inf in the recurrence */
+    CT_CUDA_ERROR = 3,
+    CT_TIMEOUT = 4,       /* a bounded device wait ran out */
+    CT_BAD_ARG = 5,
+    CT_NOT_FINALIZED = 6, /* model arrays missing (finalize() not called) */
+    CT_NO_DEVICE = 7,
+    CT_OUT_OF_MEMORY = 8,
+    CT_IO_ERROR = 9
+} ct_status;
+
+/* Precond (src/pcg3d.h:54). */
+typedef enum ct_precond { CT_JACOBI = 0, CT_MULTIGRID = 1 } ct_precond;
+
+/* Precision of the V-cycle and form of beta. The outer PCG (residual, iterate
+ * updates, dot products, alpha, beta) is FP64 in every mode.
+ *  CT_MG_FP64      V-cycle in double, beta = rz_new / rz: the reference built
+ *                  with -DMG_DOUBLE (src/pcg3d.h:30-34), the plain FP64 method.
+ *  CT_MG_FP32      V-cycle in float, same beta: the reference's default build.
+ *  CT_MG_FP32_FLEX V-cycle in float inside flexible PCG, beta =
+ *                  -(z_new . Ap) / (p . Ap) (Polak-Ribiere form). */
+typedef enum ct_precision { CT_MG_FP64 = 0, CT_MG_FP32 = 1, CT_MG_FP32_FLEX = 2 } ct_precision;
+
+/* A finalized Model3D's arrays (src/stack3d.h:45-79): gE, gN, gU, cap have
+ * nx*ny*nz entries, gB nx*ny, P nx*ny*nz. dx, dy (m) are the lateral cell
+ * sizes, which the multigrid coarsening needs (src/mg3d.h:259-265). */
+typedef struct ct_model {
+    int nx, ny, nz;
+    double dx, dy;
+    const float* gE;
+    const float* gN;
+    const float* gU;
+    const float* gB;
+    const float* cap;
+    const double* P;
+} ct_model;
+
+/* PcgStats (src/pcg3d.h:45-49), plus the breakdown flag. */
+typedef struct ct_stats {
+    int iters;
+    double relres; /* ||r|| / ||b|| from the PCG recurrence */
+    int converged;
+    int breakdown;
+} ct_stats;
+
+/* GpuSetupTimes (src/pcg3d.h:102-108), in ms. */
+typedef struct ct_setup_times {
+    double alloc_ms, upload_ms, levels_ms, factor_ms, graphs_ms;
+} ct_setup_times;
+
+/* One backward Euler step's bookkeeping (StepRecord, src/transient3d.h:29-35),
+ * computed on the device from the current x and the x that
+ * ct_set_rhs_transient saw. */
+typedef struct ct_step_record {
+    double T_max;    /* hottest cell (K above ambient) */
+    double q_out;    /* heat leaving through top and bottom (W), heat_out */
+    double q_stored; /* sum C (T_new - T_old) / dt (W), heat_stored */
+} ct_step_record;
+
+typedef struct ct_solver ct_solver;
+
+/* ---- library ------------------------------------------------------------ */
+const char* ct_version(void);
+const char* ct_status_string(ct_status s);
+const char* ct_last_error(void);
+/* gpu_use_graphs (src/pcg3d_gpu.cu:84-85): solvers created afterwards replay
+ * each solve as one CUDA graph (on, the default) or launch every kernel
+ * directly with a host check per iteration (off). */
+void ct_use_graphs(int on);
+/* gpu_last_setup (src/pcg3d_gpu.cu:87-88): setup times of the last solver
+ * created on any thread. */
+ct_status ct_last_setup(ct_setup_times* out);
+
+/* ---- single solver: GpuPcg (src/pcg3d.h:115-163) ------------------------- */
+/* GpuPcg::GpuPcg (src/pcg3d_gpu.cu:346-493): uploads the model, builds the
+ * multigrid levels on the device, factors for dt = 0, records the graphs. */
+ct_status ct_solver_create(const ct_model* m, ct_precond pc, ct_precision prec, ct_solver** out);
+/* GpuPcg::~GpuPcg (src/pcg3d_gpu.cu:495-509). */
+ct_status ct_solver_destroy(ct_solver* s);
+/* GpuPcg::set_dt (src/pcg3d_gpu.cu:511-524): 0 = steady state. */
+ct_status ct_set_dt(ct_solver* s, double dt);
+/* GpuPcg::set_x_zero (src/pcg3d_gpu.cu:526). */
+ct_status ct_set_x_zero(ct_solver* s);
+/* No reference counterpart beyond get_x: loads x (natural layout, host),
+ * e.g. to warm-start or resume a transient. */
+ct_status ct_set_x(ct_solver* s, const double* T);
+/* GpuPcg::set_rhs_steady (src/pcg3d_gpu.cu:528-530): b = P. */
+ct_status ct_set_rhs_steady(ct_solver* s);
+/* GpuPcg::set_rhs_transient (src/pcg3d_gpu.cu:532-536): b = P + C/dt x. */
+ct_status ct_set_rhs_transient(ct_solver* s);
+/* GpuPcg::set_power (src/pcg3d_gpu.cu:538-546): P from host memory. */
+ct_status ct_set_power(ct_solver* s, const double* P);
+/* Same, from device memory (natural layout). */
+ct_status ct_set_power_device(ct_solver* s, const double* P_dev);
+/* GpuPcg::solve (src/pcg3d_gpu.cu:640-682): PCG from the current x until
+ * ||r|| / ||b|| < tol or maxit. Blocks until done. Returns CT_OK,
+ * CT_NOT_CONVERGED or CT_BREAKDOWN, with the statistics in *st. */
+ct_status ct_solve(ct_solver* s, double tol, int maxit, ct_stats* st);
+/* GpuPcg::get_x (src/pcg3d_gpu.cu:548-552): x to host memory. */
+ct_status ct_get_x(ct_solver* s, double* T);
+/* GpuPcg::device_x (src/pcg3d.h:130): device pointer to x in the natural
+ * layout, valid until the next call on this solver. */
+ct_status ct_device_x(ct_solver* s, const double** T_dev);
+/* GpuPcg::setup_ (src/pcg3d_gpu.cu:369-492) of this solver. */
+ct_status ct_solver_setup_times(const ct_solver* s, ct_setup_times* out);
+/* The solver's CUDA stream (cudaStream_t), for callers that time or order
+ * work around it. */
+ct_status ct_solver_stream(const ct_solver* s, void** stream);
+/* true_relres (src/pcg3d_cpu.cpp:207-220) of the current x, recomputed from
+ * scratch in FP64 on the device: ||P - A x|| / ||P|| (steady operator). */
+ct_status ct_true_relres(ct_solver* s, double* out);
+/* T_max, heat_out and heat_stored (src/stack3d.h:252-273, as used by
+ * run_transient, src/transient3d.h:72-80) on the device, for the step of
+ * length dt that the last ct_set_rhs_transient started. */
+ct_status ct_solver_step_record(ct_solver* s, double dt, ct_step_record* out);
+/* Multigrid hierarchy: number of levels, and level k's size. */
+ct_status ct_num_levels(const ct_solver* s, int* n);
+ct_status ct_level_dims(const ct_solver* s, int k, int* nx, int* ny, int* nz);
+/* Level k's operator (natural layout, host arrays as in MgLevelHost,
+ * src/mg3d.h:200-204) as built on the device. gB has nx*ny entries. */
+ct_status ct_level_operator(ct_solver* s, int k, float* gE, float* gN, float* gU, float* gB,
+                            float* cap);
+/* Level k's column factors for the current dt, widened to double. */
+ct_status ct_level_factors(ct_solver* s, int k, double* fcp, double* finv);
+
+/* ---- per-kernel timing --------------------------------------------------- */
+typedef struct ct_kernel_time {
+    char name[32];     /* kernel family, e.g. "mg_sweep_l0" */
+    int launches;
+    double total_ms;   /* sum of CUDA-event durations on the solver's stream */
+    double bytes;      /* algorithmic bytes, summed over the launches */
+} ct_kernel_time;
+/* Runs one solve like ct_solve, but launches every kernel directly with a
+ * CUDA event pair around each launch; fills up to max entries of out, one per
+ * kernel family, and *n with the count. */
+ct_status ct_profile_solve(ct_solver* s, double tol, int maxit, ct_stats* st,
+                           ct_kernel_time* out, int max, int* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CTHERMAL_H */

@@ -1,0 +1,230 @@
+"""GPU solver parity against the C oracle (itself pinned bit-for-bit to the
+reference CPU solver), through the C ABI.
+
+Tolerances (written here, used below):
+  * plain FP64 MG-PCG and the reference-default FP32 V-cycle vs the oracle of
+    the same arithmetic: max|dT| <= 1e-7 * Tmax; iteration counts within 1.
+  * FP32 V-cycle inside flexible PCG vs the FP64 oracle: max|dT| <= 5e-4 K
+    (the stated bound) and, in practice, <= 1e-7 * Tmax.
+  * Jacobi (tol 1e-6) vs the oracle's Jacobi: max|dT| / Tmax <= 1e-6, the
+    reference's own GPU-vs-CPU bound (src/main3d.cu:41).
+  * true residual ||P - A T|| / ||P|| (FP64, recomputed by the oracle) <= 1e-9
+    for solves to 1e-10.
+Setup is checked bit for bit: level sizes, every coarse operator array and
+every column factor.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import build_spec_model
+
+pytestmark = pytest.mark.gpu
+
+DT_BOUND_K = 5e-4
+CASES = ["hotspot64", "blocks_tsv_17x13", "blocks_tsv_40x24", "tiny3x5", "column1x1", "row1x9",
+         "tsv_layer64", "base3dice_50"]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def gpu_solve(ct, m, tol, pc, prec):
+    with ct.GpuPcg(m, pc, prec) as s:
+        s.set_x_zero()
+        s.set_rhs_steady()
+        st = s.solve(tol, 50000)
+        return st, s.get_x()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_mg_matches_oracle(ct, orc, golden, name):
+    m = build_spec_model(ct, golden["cases"][name]["spec"])
+    ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
+    st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, ct.Precision.MG_FP64)
+    assert st.converged and not st.breakdown
+    assert abs(st.iters - ref.iters) <= 1
+    tmax = np.abs(ref.T).max()
+    assert np.abs(T - ref.T).max() <= 1e-7 * tmax
+    assert orc.true_relres(m, T) <= 1e-9
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp32_mg_matches_oracle(ct, orc, golden, name):
+    m = build_spec_model(ct, golden["cases"][name]["spec"])
+    ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=False)
+    st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, ct.Precision.MG_FP32)
+    assert st.converged
+    assert abs(st.iters - ref.iters) <= 1
+    assert np.abs(T - ref.T).max() <= 1e-7 * np.abs(ref.T).max()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp32_flexible_within_bound_of_fp64(ct, orc, golden, name):
+    m = build_spec_model(ct, golden["cases"][name]["spec"])
+    ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
+    st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX)
+    assert st.converged
+    dT = np.abs(T - ref.T).max()
+    assert dT <= DT_BOUND_K
+    assert dT <= 1e-7 * np.abs(ref.T).max()
+    assert orc.true_relres(m, T) <= 1e-9
+    # same iterates as the oracle's flexible variant
+    refx = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=False, flexible=True)
+    assert abs(st.iters - refx.iters) <= 1
+
+
+@pytest.mark.parametrize("name", ["hotspot64", "blocks_tsv_17x13", "tiny3x5", "row1x9"])
+def test_jacobi_matches_oracle(ct, orc, golden, name):
+    m = build_spec_model(ct, golden["cases"][name]["spec"])
+    ref = orc.solve_steady(m, 1e-6, 50000, "jacobi", mg_double=True)
+    st, T = gpu_solve(ct, m, 1e-6, ct.Precond.Jacobi, ct.Precision.MG_FP64)
+    assert st.converged
+    assert abs(st.iters - ref.iters) <= 2
+    assert np.abs(T - ref.T).max() / np.abs(ref.T).max() <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["hotspot64", "blocks_tsv_17x13", "blocks_tsv_40x24", "tiny3x5",
+                                  "row1x9", "column1x1"])
+def test_levels_and_factors_bitwise(ct, orc, golden, name):
+    rec = golden["cases"][name]
+    m = build_spec_model(ct, rec["spec"])
+    for prec, mgd in ((ct.Precision.MG_FP64, True), (ct.Precision.MG_FP32, False)):
+        o = orc.Solver(m, "multigrid", mg_double=mgd)
+        with ct.GpuPcg(m, ct.Precond.Multigrid, prec) as s:
+            assert s.num_levels() == len(rec["levels"])
+            for dt in (0.0, 1e-4):
+                s.set_dt(dt)
+                o.set_dt(dt)
+                for k, L in enumerate(rec["levels"]):
+                    nx, ny, nz = s.level_dims(k)
+                    assert (nx, ny, nz) == (L["nx"], L["ny"], m.nz)
+                    op = s.level_operator(k)
+                    for a in ("gE", "gN", "gU", "gB", "cap"):
+                        assert sha(op[a]) == L["sha"][a], (k, a)
+                    fcp, finv = s.level_factors(k)
+                    ofcp, ofinv = o.level_factors(k)
+                    np.testing.assert_array_equal(fcp, ofcp)
+                    np.testing.assert_array_equal(finv, ofinv)
+
+
+def test_graphs_match_direct_launches_bitwise(ct, golden):
+    """verify 4 (src/main3d.cu:212-222), tightened: graph replay and direct
+    launches give the same bits through a transient where 1/dt changes."""
+    m = build_spec_model(ct, golden["cases"]["blocks_tsv_40x24"]["spec"])
+    o = ct.TransientOptions(t_end=0.02, growth=1.2, precision=ct.Precision.MG_FP32_FLEX)
+    a = ct.run_transient(m, o)
+    ct.gpu_use_graphs(False)
+    try:
+        b = ct.run_transient(m, o)
+    finally:
+        ct.gpu_use_graphs(True)
+    assert a.total_iters == b.total_iters
+    np.testing.assert_array_equal(a.T, b.T)
+
+
+@pytest.mark.parametrize("prec,mgd", [("MG_FP64", True), ("MG_FP32", False)])
+def test_transient_matches_oracle(ct, orc, golden, prec, mgd):
+    spec = dict(golden["cases"]["hotspot64"]["spec"])
+    spec["nx"] = spec["ny"] = 32
+    m = build_spec_model(ct, spec)
+    o = ct.TransientOptions(dt0=1e-5, growth=1.2, dt_max=0.05, t_end=0.02, tol=1e-9,
+                            precision=getattr(ct.Precision, prec))
+    g = ct.run_transient(m, o)
+    r = orc.run_transient(m, "multigrid", mg_double=mgd, dt0=1e-5, growth=1.2, dt_max=0.05,
+                          t_end=0.02, tol=1e-9)
+    assert len(g.steps) == len(r.steps)
+    P = ct.total_power(m)
+    for k, s in enumerate(g.steps):
+        t, dt, it, tmax, qo, qs = r.steps[k]
+        assert s.t == t and s.dt == dt
+        assert abs(s.iters - it) <= 1
+        assert abs(s.T_max - tmax) <= 1e-7 * tmax
+        assert abs(s.q_out + s.q_stored - P) / P < 1e-6  # energy balance per step
+    assert np.abs(g.T - r.T).max() <= 1e-7 * np.abs(r.T).max()
+
+
+def test_device_records_match_host_records(ct, golden):
+    spec = dict(golden["cases"]["hotspot64"]["spec"])
+    spec["nx"] = spec["ny"] = 24
+    m = build_spec_model(ct, spec)
+    o = ct.TransientOptions(t_end=0.005, growth=1.3)
+    a = ct.run_transient(m, o, device_records=True)
+    b = ct.run_transient(m, o, device_records=False)
+    for x, y in zip(a.steps, b.steps):
+        assert x.iters == y.iters
+        assert x.T_max == y.T_max
+        assert abs(x.q_out - y.q_out) <= 1e-12 * abs(y.q_out)
+        assert abs(x.q_stored - y.q_stored) <= 1e-9 * max(1.0, abs(y.q_stored))
+
+
+def test_true_relres_on_device(ct, orc, golden):
+    m = build_spec_model(ct, golden["cases"]["blocks_tsv_40x24"]["spec"])
+    with ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX) as s:
+        s.set_x_zero()
+        s.set_rhs_steady()
+        s.solve(1e-6, 100)
+        T = s.get_x()
+        dev = s.true_relres()
+    host = orc.true_relres(m, T)
+    assert abs(dev - host) <= 1e-6 * host
+
+
+def test_zero_power_gives_zero(ct):
+    m = ct.default_model(16, 16)
+    ct.finalize(m)
+    with ct.GpuPcg(m) as s:
+        s.set_x(np.ones(m.ncells()))
+        s.set_rhs_steady()
+        st = s.solve(1e-10, 100)
+        assert st.converged and st.iters == 0
+        assert np.all(s.get_x() == 0)
+
+
+def test_power_roundtrip_and_warm_start(ct, orc):
+    import workloads
+    m = workloads.steady_hotspot(48, seed=7)
+    ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
+    with ct.GpuPcg(m) as s:
+        s.set_x_zero()
+        s.set_rhs_steady()
+        s.solve(1e-10, 100)
+        # a second solve from the converged state takes no iteration
+        s.set_rhs_steady()
+        st = s.solve(1e-10, 100)
+        assert st.iters == 0 and st.converged
+        # new power map: twice the power -> twice the temperature rise
+        s.set_power(2 * m.P)
+        s.set_rhs_steady()
+        st = s.solve(1e-10, 100)
+        assert st.converged
+        T2 = s.get_x()
+    assert np.abs(T2 - 2 * ref.T).max() <= 1e-7 * np.abs(ref.T).max()
+
+
+def test_singular_stack_reports_status_not_hang(ct):
+    """No heat sink and an adiabatic bottom: A is singular and P is not in its
+    range. The solve must end with a status (not converged or breakdown)."""
+    m = ct.build_model(ct.default_stack(), 12, 12, 10e-3, 10e-3, 0.0, 0.0)
+    ct.add_uniform_power(m, 0, 1.0)
+    ct.finalize(m)
+    with ct.GpuPcg(m) as s:
+        s.set_x_zero()
+        s.set_rhs_steady()
+        st = s.solve(1e-12, 200)
+        assert not st.converged
+        assert st.iters <= 200
+
+
+def test_nan_power_is_breakdown(ct):
+    m = ct.default_model(8, 8)
+    ct.add_uniform_power(m, 0, 1.0)
+    ct.finalize(m)
+    m.P[5] = np.nan
+    with ct.GpuPcg(m) as s:
+        s.set_x_zero()
+        s.set_rhs_steady()
+        st = s.solve(1e-10, 50)
+        assert st.breakdown and not st.converged
