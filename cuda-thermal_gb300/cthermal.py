@@ -109,6 +109,7 @@ def _signatures():
         "ct_level_operator": (i, [vp, i, vp, vp, vp, vp, vp]),
         "ct_level_factors": (i, [vp, i, vp, vp]),
         "ct_profile_solve": (i, [vp, d, i, C.POINTER(CtStats), C.POINTER(CtKernelTime), i, ip]),
+        "ct_true_relres_noalloc": (i, [C.POINTER(CtModel), vp, vp, vp]),
         "ct_model_planes": (i, [lp, i, ip, vp, vp]),
         "ct_model_finalize": (i, [gp, lp, vp, vp, d, d, d, d, vp, vp, vp, vp, vp, vp]),
         "ct_model_add_power_block": (i, [gp, lp, vp, i, d, d, d, d, d, vp]),

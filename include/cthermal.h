@@ -156,6 +156,30 @@ ct_status ct_level_operator(ct_solver* s, int k, float* gE, float* gN, float* gU
 /* Level k's column factors for the current dt, widened to double. */
 ct_status ct_level_factors(ct_solver* s, int k, double* fcp, double* finv);
 
+/* ---- allocation-free residual check -------------------------------------- */
+/* No counterpart in the reference. The steady true residual
+ * ||P - A T|| / ||P|| of a temperature field, like ct_true_relres, for
+ * callers that may not allocate device memory: a per-frame loop that must
+ * not stall the GPU (cudaMalloc can synchronise the device), or a host
+ * framework that holds the device memory in its own pool and hands out
+ * buffers but no allocator. It takes caller-owned DEVICE arrays and allocates
+ * nothing: m_dev->gE, gN, gU, gB and P, and T_dev, are device pointers in the
+ * natural layout (cap is not read), and the ratio is written to out_dev[0]
+ * (device memory) on `stream` (a cudaStream_t, or NULL for the default
+ * stream); the call does not synchronise.
+ * Its scratch is a fixed CT_NOALLOC_SCRATCH_BYTES array in the library's
+ * device memory, held on every GPU that loads the library until exit, which
+ * limits a model to CT_NOALLOC_MAX_COLUMNS columns (nx * ny); larger models
+ * get CT_BAD_ARG. The first call on each device looks up that array's device
+ * address (cudaGetSymbolAddress, no allocation), so make the first call on a
+ * device before any stream capture. All calls share the one scratch array:
+ * calls whose work can overlap on the GPU (other streams, other threads)
+ * race on it and must be serialised by the caller. */
+#define CT_NOALLOC_SCRATCH_BYTES 131072
+#define CT_NOALLOC_MAX_COLUMNS 2096640
+ct_status ct_true_relres_noalloc(const ct_model* m_dev, const double* T_dev, double* out_dev,
+                                 void* stream);
+
 /* ---- per-kernel timing --------------------------------------------------- */
 typedef struct ct_kernel_time {
     char name[32];     /* kernel family, e.g. "mg_sweep_l0" */
