@@ -58,12 +58,16 @@ struct Ctl {
     double inv_dt;
     double bb, rr, rz, pAp, zAp, alpha, beta, relres;
     double aux0, aux1, aux2;  // results of the auxiliary reductions
+    double stop;              // relres at which the current loop ends (double-word mode: phase 1)
+    float2 alpha_w, beta_w;   // alpha, beta as float pairs (double-word mode)
     int iter;                 // completed iterations
     int body;                 // loop bodies entered (bounds the graph loop)
     int done;                 // stop flag: every kernel of the loop body exits early
     int converged;
     int breakdown;
     int bb_zero;
+    int phase_end;  // double-word mode: phase 1 done, residual replacement next
+    int x_zero;     // set by the host: x = 0 at the start of this solve (r = b)
     unsigned ticket[NSLOT];
 };
 

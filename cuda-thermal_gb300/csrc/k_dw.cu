@@ -1,0 +1,521 @@
+// k_dw.cu - the outer PCG on the FP32 pipes: double-word (float-pair)
+// arithmetic for CT_MG_FP32_FLEX_DW.
+//
+// On GB300 an FP64 instruction issues at ~1/70 of the FP32 rate (and float <->
+// double conversions at the FP64 rate), so the FP64 outer kernels of the
+// reference's algorithm are bound by the FP64 pipe, not by HBM. Here x, r, p,
+// Ap and the diagonal are stored as float pairs (hi, lo) - the same 8 bytes
+// per value as a double - and combined with error-free transformations
+// (TwoSum, Fast2Sum, FMA-based TwoProd; Joldes, Muller and Popescu, "Tight
+// and rigorous error bounds for basic building blocks of double-word
+// arithmetic", 2017), which carry ~48 significant bits. Dot products are
+// accumulated in double words per thread and in FP64 per block; alpha and beta
+// stay FP64 scalars on the device.
+//
+// The recurrence residual of a 48-bit iteration drifts from the true residual
+// by ~2^-48 times the operator's cancellation (up to ~1e4 here), which would
+// leave ||P - A T|| / ||P|| near 1e-10 on large grids. So the solve recomputes
+// r = b - A x once in FP64 (k_residual_x, "residual replacement") when the
+// recurrence first passes a threshold (1e-5 by default); the drift after that
+// is five orders of magnitude smaller, and the true FP64 residual meets tol.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+
+#include "kernels.h"
+#include "reduce.cuh"
+
+namespace ct {
+
+namespace {
+
+// ---- double-word arithmetic ------------------------------------------------
+// A value is float2 v = (hi, lo) with v = hi + lo and |lo| <= ulp(hi) / 2.
+
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+    const float s = a + b;
+    const float bp = s - a;
+    const float ap = s - bp;
+    return make_float2(s, (a - ap) + (b - bp));
+}
+
+// |a| >= |b| (or a = 0).
+__device__ __forceinline__ float2 fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+
+__device__ __forceinline__ float2 dw_add(float2 a, float2 b) {
+    const float2 s = two_sum(a.x, b.x);
+    return fast_two_sum(s.x, s.y + (a.y + b.y));
+}
+
+__device__ __forceinline__ float2 dw_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ float2 dw_mul_f(float2 a, float b) {
+    const float p = a.x * b;
+    float e = fmaf(a.x, b, -p);
+    e = fmaf(a.y, b, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ float2 dw_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ float2 dw_of(double d) {
+    const float h = __double2float_rn(d);
+    return make_float2(h, __double2float_rn(d - (double)h));
+}
+
+__device__ __forceinline__ double dw_d(float2 a) { return (double)a.x + (double)a.y; }
+
+// ---- column walk (split layout), as in k_outer.cu ----------------------------
+struct Col {
+    int i, j;
+    unsigned s, sw, se, ss, sn;
+    bool valid;
+};
+
+__device__ __forceinline__ Col col_of_slot(const Geo& g, unsigned s) {
+    Col c;
+    const unsigned row2 = 2u * (unsigned)g.hx;
+    const int j = (int)(s / row2);
+    const unsigned rem = s - (unsigned)j * row2;
+    const int colour = rem >= (unsigned)g.hx ? 1 : 0;
+    const int t = (int)rem - colour * g.hx;
+    const int i = 2 * t + ((j + colour) & 1);
+    const int oc = colour ^ 1;
+    const unsigned row_o = (unsigned)(2 * j + oc) * (unsigned)g.hx;
+    c.i = i;
+    c.j = j;
+    c.s = s;
+    c.sw = row_o + (unsigned)((i - 1) >> 1);
+    c.se = row_o + (unsigned)((i + 1) >> 1);
+    c.ss = (unsigned)(2 * j - 2 + oc) * (unsigned)g.hx + (unsigned)t;
+    c.sn = (unsigned)(2 * j + 2 + oc) * (unsigned)g.hx + (unsigned)t;
+    c.valid = i < g.nx;
+    return c;
+}
+
+// ---- FP64 residual from a double-word x: start and replacement -------------
+
+// r = b - (A + C/dt) x in FP64 with x = hi + lo, the stored FP64 diagonal;
+// stores r as a double word and b0 = r (float, the V-cycle's input). `start`:
+// the first residual of a solve (sets ||b||^2 and the start test); otherwise
+// the residual replacement (phase 2 begins, or the solve ends if already
+// converged).
+__global__ void __launch_bounds__(NT)
+    k_residual_x(OpView o, const double* __restrict__ diag, const double* __restrict__ b,
+                 const float2* __restrict__ x, float2* __restrict__ r, float* __restrict__ b0,
+                 int start, Ctl* ctl, double* part, int maxb, Cond cond) {
+    if (!start && *(volatile const int*)&ctl->done) {  // converged or stopped in phase 1
+        if (cond.use && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond.h, 0u);
+        return;
+    }
+    const Geo& g = o.g;
+    double rr = 0.0, bb = 0.0;
+    // A solve that starts from x = 0 (every steady solve) has r = b exactly.
+    const bool zero = start && ctl->x_zero;
+    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) {
+            for (int l = 0; l < g.nz; ++l) {
+                r[(unsigned)l * g.plane + s] = make_float2(0.0f, 0.0f);
+                b0[(unsigned)l * g.plane + s] = 0.0f;
+            }
+            continue;
+        }
+        if (zero) {
+            for (int l = 0; l < g.nz; ++l) {
+                const unsigned id = (unsigned)l * g.plane + c.s;
+                const double bi = b[id];
+                const float2 rw = dw_of(bi);
+                r[id] = rw;
+                b0[id] = rw.x;
+                bb += bi * bi;
+            }
+            continue;
+        }
+        double x_c = dw_d(x[c.s]), x_b = 0.0;
+        float gu_b = 0.0f;
+        for (int l = 0; l < g.nz; ++l) {
+            const unsigned base = (unsigned)l * g.plane, id = base + c.s;
+            const bool up = l < g.nz - 1;
+            const double x_a = up ? dw_d(x[id + g.plane]) : 0.0;
+            const float gu = o.gU[id];
+            double off = 0.0;
+            if (c.i > 0) off += (double)o.gE[base + c.sw] * dw_d(x[base + c.sw]);
+            if (c.i < g.nx - 1) off += (double)o.gE[id] * dw_d(x[base + c.se]);
+            if (c.j > 0) off += (double)o.gN[base + c.ss] * dw_d(x[base + c.ss]);
+            if (c.j < g.ny - 1) off += (double)o.gN[id] * dw_d(x[base + c.sn]);
+            if (l > 0) off += (double)gu_b * x_b;
+            if (up) off += (double)gu * x_a;
+            const double bi = b[id];
+            const double ri = bi - (diag[id] * x_c - off);
+            const float2 rw = dw_of(ri);
+            r[id] = rw;
+            b0[id] = rw.x;
+            rr += ri * ri;
+            bb += bi * bi;
+            x_b = x_c;
+            x_c = x_a;
+            gu_b = gu;
+        }
+    }
+    if (zero) rr = bb;
+    block_sum2(rr, bb);
+    if (publish2(rr, bb, part, maxb, &ctl->ticket[SL_INIT])) {
+        double RR, BB;
+        gather2(part, maxb, &ctl->ticket[SL_INIT], RR, BB);
+        if (threadIdx.x == 0) {
+            ctl->rr = RR;
+            if (start) {
+                ctl->bb = BB;
+                if (BB == 0.0) {
+                    ctl->bb_zero = 1;
+                    ctl->converged = 1;
+                    ctl->relres = 0.0;
+                    stop_loop(ctl, cond);
+                    return;
+                }
+            }
+            const double rel = sqrt(RR / ctl->bb);
+            ctl->relres = rel;
+            ctl->phase_end = 0;
+            if (!start) ctl->stop = ctl->tol;  // phase 2 runs to tol
+            if (rel < ctl->tol) {
+                ctl->converged = 1;
+                stop_loop(ctl, cond);
+            } else if (!isfinite(rel)) {
+                ctl->breakdown = 1;
+                stop_loop(ctl, cond);
+            } else if (ctl->iter >= ctl->maxit) {
+                stop_loop(ctl, cond);
+            }
+        }
+    }
+}
+
+// ---- the iteration ------------------------------------------------------------
+
+// Ap = d p - sum G p_nbr, p.Ap, alpha.
+__global__ void __launch_bounds__(NT)
+    k_apply_dw(OpView o, const float2* __restrict__ dgw, const float2* __restrict__ p,
+               float2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const Geo& g = o.g;
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) {
+            for (int l = 0; l < g.nz; ++l) Ap[(unsigned)l * g.plane + s] = make_float2(0.0f, 0.0f);
+            continue;
+        }
+        float2 p_c = p[c.s], p_b = make_float2(0.0f, 0.0f);
+        float gu_b = 0.0f;
+        for (int l = 0; l < g.nz; ++l) {
+            const unsigned base = (unsigned)l * g.plane, id = base + c.s;
+            const bool up = l < g.nz - 1;
+            const float2 p_a = up ? p[id + g.plane] : make_float2(0.0f, 0.0f);
+            const float gu = o.gU[id];
+            float2 off = make_float2(0.0f, 0.0f);
+            if (c.i > 0) off = dw_add(off, dw_mul_f(p[base + c.sw], o.gE[base + c.sw]));
+            if (c.i < g.nx - 1) off = dw_add(off, dw_mul_f(p[base + c.se], o.gE[id]));
+            if (c.j > 0) off = dw_add(off, dw_mul_f(p[base + c.ss], o.gN[base + c.ss]));
+            if (c.j < g.ny - 1) off = dw_add(off, dw_mul_f(p[base + c.sn], o.gN[id]));
+            if (l > 0) off = dw_add(off, dw_mul_f(p_b, gu_b));
+            if (up) off = dw_add(off, dw_mul_f(p_a, gu));
+            const float2 a = dw_add(dw_mul(dgw[id], p_c), dw_neg(off));
+            Ap[id] = a;
+            acc = dw_add(acc, dw_mul(p_c, a));
+            p_b = p_c;
+            p_c = p_a;
+            gu_b = gu;
+        }
+    }
+    double pap = dw_d(acc), unused = 0.0;
+    block_sum2(pap, unused);
+    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
+        double PAP, U;
+        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
+        if (threadIdx.x == 0) {
+            ctl->pAp = PAP;
+            if (!(PAP > 0.0) || !isfinite(PAP)) {
+                ctl->breakdown = 1;
+                ctl->alpha = 0.0;
+                stop_loop(ctl, cond);
+            } else {
+                ctl->alpha = ctl->rz / PAP;
+                ctl->alpha_w = dw_of(ctl->alpha);
+            }
+        }
+    }
+}
+
+// Same as k_apply_dw, one cell per loop step instead of one column: the steps
+// are independent (no value carried from plane to plane), so consecutive
+// cells' loads overlap; vertical neighbours come from L1/L2.
+__global__ void __launch_bounds__(NT)
+    k_apply_dw_cells(OpView o, const float2* __restrict__ dgw, const float2* __restrict__ p,
+                     float2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const Geo& g = o.g;
+    const unsigned n = g.plane * (unsigned)g.nz;
+    float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll 2
+    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
+        const unsigned l = k / g.plane;
+        const unsigned s = k - l * g.plane;
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) {
+            Ap[k] = make_float2(0.0f, 0.0f);
+            continue;
+        }
+        const unsigned base = l * g.plane;
+        float2 off = make_float2(0.0f, 0.0f);
+        if (c.i > 0) off = dw_add(off, dw_mul_f(p[base + c.sw], o.gE[base + c.sw]));
+        if (c.i < g.nx - 1) off = dw_add(off, dw_mul_f(p[base + c.se], o.gE[k]));
+        if (c.j > 0) off = dw_add(off, dw_mul_f(p[base + c.ss], o.gN[base + c.ss]));
+        if (c.j < g.ny - 1) off = dw_add(off, dw_mul_f(p[base + c.sn], o.gN[k]));
+        if (l > 0) off = dw_add(off, dw_mul_f(p[k - g.plane], o.gU[k - g.plane]));
+        if ((int)l < g.nz - 1) off = dw_add(off, dw_mul_f(p[k + g.plane], o.gU[k]));
+        const float2 pc = p[k];
+        const float2 a = dw_add(dw_mul(dgw[k], pc), dw_neg(off));
+        Ap[k] = a;
+        acc = dw_add(acc, dw_mul(pc, a));
+    }
+    double pap = dw_d(acc), unused = 0.0;
+    block_sum2(pap, unused);
+    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
+        double PAP, U;
+        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
+        if (threadIdx.x == 0) {
+            ctl->pAp = PAP;
+            if (!(PAP > 0.0) || !isfinite(PAP)) {
+                ctl->breakdown = 1;
+                ctl->alpha = 0.0;
+                stop_loop(ctl, cond);
+            } else {
+                ctl->alpha = ctl->rz / PAP;
+                ctl->alpha_w = dw_of(ctl->alpha);
+            }
+        }
+    }
+}
+
+// x += alpha p, r -= alpha Ap, b0 = r (hi word), ||r||^2, convergence test.
+// Two values per thread and step (float4 = two double words).
+__global__ void __launch_bounds__(NT)
+    k_update_dw(unsigned n2, const float4* __restrict__ p, const float4* __restrict__ Ap,
+                float4* __restrict__ x, float4* __restrict__ r, float2* __restrict__ b0, Ctl* ctl,
+                double* part, int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const float2 a = ctl->alpha_w;
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
+        const float4 pv = p[k], av = Ap[k];
+        float4 xv = x[k], rv = r[k];
+        const float2 x0 = dw_add(make_float2(xv.x, xv.y), dw_mul(a, make_float2(pv.x, pv.y)));
+        const float2 x1 = dw_add(make_float2(xv.z, xv.w), dw_mul(a, make_float2(pv.z, pv.w)));
+        const float2 r0 = dw_add(make_float2(rv.x, rv.y), dw_neg(dw_mul(a, make_float2(av.x, av.y))));
+        const float2 r1 = dw_add(make_float2(rv.z, rv.w), dw_neg(dw_mul(a, make_float2(av.z, av.w))));
+        x[k] = make_float4(x0.x, x0.y, x1.x, x1.y);
+        r[k] = make_float4(r0.x, r0.y, r1.x, r1.y);
+        b0[k] = make_float2(r0.x, r1.x);
+        acc = dw_add(acc, dw_mul(r0, r0));
+        acc = dw_add(acc, dw_mul(r1, r1));
+    }
+    double rr = dw_d(acc), unused = 0.0;
+    block_sum2(rr, unused);
+    if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
+        double RR, U;
+        gather2(part, maxb, &ctl->ticket[SL_UPDATE], RR, U);
+        if (threadIdx.x == 0) {
+            ctl->rr = RR;
+            ctl->iter += 1;
+            const double rel = sqrt(RR / ctl->bb);
+            ctl->relres = rel;
+            if (rel < ctl->tol) {
+                ctl->converged = 1;
+                stop_loop(ctl, cond);
+            } else if (!isfinite(rel)) {
+                ctl->breakdown = 1;
+                stop_loop(ctl, cond);
+            } else if (ctl->iter >= ctl->maxit) {
+                stop_loop(ctl, cond);
+            } else if (rel < ctl->stop) {
+                // end of phase 1: the next step is the FP64 residual replacement
+                ctl->phase_end = 1;
+                if (cond.use) cudaGraphSetConditional(cond.h, 0u);
+            }
+        }
+    }
+}
+
+// rz = r.z and z.Ap (flexible beta); beta.
+__global__ void __launch_bounds__(NT)
+    k_dot_dw(unsigned n2, const float4* __restrict__ r, const float2* __restrict__ z,
+             const float4* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    float2 rz = make_float2(0.0f, 0.0f), zap = make_float2(0.0f, 0.0f);
+    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
+        const float4 rv = r[k], av = Ap[k];
+        const float2 zv = z[k];
+        rz = dw_add(rz, dw_mul_f(make_float2(rv.x, rv.y), zv.x));
+        rz = dw_add(rz, dw_mul_f(make_float2(rv.z, rv.w), zv.y));
+        zap = dw_add(zap, dw_mul_f(make_float2(av.x, av.y), zv.x));
+        zap = dw_add(zap, dw_mul_f(make_float2(av.z, av.w), zv.y));
+    }
+    double RZ0 = dw_d(rz), ZAP0 = dw_d(zap);
+    block_sum2(RZ0, ZAP0);
+    if (publish2(RZ0, ZAP0, part, maxb, &ctl->ticket[SL_DOT])) {
+        double RZ, ZAP;
+        gather2(part, maxb, &ctl->ticket[SL_DOT], RZ, ZAP);
+        if (threadIdx.x == 0) {
+            ctl->beta = ctl->iter > 0 ? -ZAP / ctl->pAp : 0.0;
+            ctl->beta_w = dw_of(ctl->beta);
+            ctl->rz = RZ;
+            ctl->zAp = ZAP;
+            if (!isfinite(RZ) || !isfinite(ctl->beta)) {
+                ctl->breakdown = 1;
+                stop_loop(ctl, cond);
+            }
+        }
+    }
+}
+
+// p = z + beta p (p = z on the first iteration).
+__global__ void __launch_bounds__(NT)
+    k_update_p_dw(unsigned n2, const float2* __restrict__ z, float4* __restrict__ p, const Ctl* ctl,
+                  Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const float2 beta = ctl->beta_w;
+    const bool first = ctl->iter == 0;
+    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
+        const float2 zv = z[k];
+        if (first) {
+            p[k] = make_float4(zv.x, 0.0f, zv.y, 0.0f);
+        } else {
+            const float4 pv = p[k];
+            const float2 p0 = dw_add(dw_mul(beta, make_float2(pv.x, pv.y)), make_float2(zv.x, 0.0f));
+            const float2 p1 = dw_add(dw_mul(beta, make_float2(pv.z, pv.w)), make_float2(zv.y, 0.0f));
+            p[k] = make_float4(p0.x, p0.y, p1.x, p1.y);
+        }
+    }
+}
+
+// ---- conversions at the boundary -------------------------------------------
+
+// FP64 diagonal -> double word.
+__global__ void k_to_dw(unsigned n, const double* __restrict__ in, float2* __restrict__ out) {
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        out[k] = dw_of(in[k]);
+}
+
+// split double word -> natural double.
+__global__ void k_dw_to_natural(Geo g, const float2* __restrict__ in, double* __restrict__ out) {
+    const size_t nxy = (size_t)g.nx * g.ny;
+    const size_t n = nxy * (size_t)g.nz;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(c / nxy);
+        const size_t rem = c - (size_t)l * nxy;
+        const int j = (int)(rem / g.nx), i = (int)(rem - (size_t)j * g.nx);
+        out[c] = dw_d(in[(size_t)l * g.plane + scol(g, i, j)]);
+    }
+}
+
+// natural double -> split double word.
+__global__ void k_natural_to_dw(Geo g, const double* __restrict__ in, float2* __restrict__ out) {
+    const size_t nxy = (size_t)g.nx * g.ny;
+    const size_t n = nxy * (size_t)g.nz;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(c / nxy);
+        const size_t rem = c - (size_t)l * nxy;
+        const int j = (int)(rem / g.nx), i = (int)(rem - (size_t)j * g.nx);
+        out[(size_t)l * g.plane + scol(g, i, j)] = dw_of(in[c]);
+    }
+}
+
+// split double word -> split double (for the FP64 bookkeeping kernels).
+__global__ void k_dw_to_d(unsigned n, const float2* __restrict__ in, double* __restrict__ out) {
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        out[k] = dw_d(in[k]);
+}
+
+unsigned blocks_of(size_t n) {
+    size_t b = (n + NT - 1) / NT;
+    if (b < 1) b = 1;
+    if (b > 65535u * 16u) b = 65535u * 16u;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+void launch_residual_x(cudaStream_t st, const OpView& o, const double* diag, const double* b,
+                       const float2* x, float2* r, float* b0, bool start, Ctl* ctl,
+                       const Red& red, Cond cond) {
+    static const int wb = wave_blocks(k_residual_x, 1 << 30);
+    k_residual_x<<<std::min(red.blocks, wb), NT, 0, st>>>(o, diag, b, x, r, b0, start ? 1 : 0, ctl, red.part,
+                                            red.maxb, cond);
+}
+
+void launch_apply_dw(cudaStream_t st, const OpView& o, const float2* dgw, const float2* p,
+                     float2* Ap, Ctl* ctl, const Red& red, Cond cond) {
+    static const bool cells = [] {
+        const char* e = std::getenv("CT_APPLY_COLUMNS");
+        return !(e && e[0] == '1');
+    }();
+    if (cells) {
+        static const int wb = wave_blocks(k_apply_dw_cells, 1 << 30);
+        k_apply_dw_cells<<<std::min(red.maxb, wb), NT, 0, st>>>(o, dgw, p, Ap, ctl, red.part,
+                                                               red.maxb, cond);
+        return;
+    }
+    static const int wb = wave_blocks(k_apply_dw, 1 << 30);
+    k_apply_dw<<<std::min(red.blocks, wb), NT, 0, st>>>(o, dgw, p, Ap, ctl, red.part, red.maxb, cond);
+}
+
+void launch_update_dw(cudaStream_t st, unsigned n, const float2* p, const float2* Ap, float2* x,
+                      float2* r, float* b0, Ctl* ctl, const Red& red, Cond cond) {
+    static const int wb = wave_blocks(k_update_dw, 1 << 30);
+    k_update_dw<<<std::min(red.blocks, wb), NT, 0, st>>>(n / 2, (const float4*)p, (const float4*)Ap, (float4*)x,
+                                           (float4*)r, (float2*)b0, ctl, red.part, red.maxb, cond);
+}
+
+void launch_dot_dw(cudaStream_t st, unsigned n, const float2* r, const float* z, const float2* Ap,
+                   Ctl* ctl, const Red& red, Cond cond) {
+    static const int wb = wave_blocks(k_dot_dw, 1 << 30);
+    k_dot_dw<<<std::min(red.blocks, wb), NT, 0, st>>>(n / 2, (const float4*)r, (const float2*)z,
+                                        (const float4*)Ap, ctl, red.part, red.maxb, cond);
+}
+
+void launch_update_p_dw(cudaStream_t st, unsigned n, const float* z, float2* p, Ctl* ctl,
+                        Cond cond) {
+    static const int wb = wave_blocks(k_update_p_dw, 1 << 30);
+    k_update_p_dw<<<std::min((int)blocks_of(n / 2), wb), NT, 0, st>>>(n / 2, (const float2*)z, (float4*)p, ctl, cond);
+}
+
+void launch_to_dw(cudaStream_t st, unsigned n, const double* in, float2* out) {
+    k_to_dw<<<blocks_of(n), NT, 0, st>>>(n, in, out);
+}
+
+void launch_dw_to_natural(cudaStream_t st, const Geo& g, const float2* split, double* nat) {
+    k_dw_to_natural<<<blocks_of((size_t)g.nx * g.ny * g.nz), NT, 0, st>>>(g, split, nat);
+}
+
+void launch_natural_to_dw(cudaStream_t st, const Geo& g, const double* nat, float2* split) {
+    k_natural_to_dw<<<blocks_of((size_t)g.nx * g.ny * g.nz), NT, 0, st>>>(g, nat, split);
+}
+
+void launch_dw_to_d(cudaStream_t st, unsigned n, const float2* in, double* out) {
+    k_dw_to_d<<<blocks_of(n), NT, 0, st>>>(n, in, out);
+}
+
+}  // namespace ct

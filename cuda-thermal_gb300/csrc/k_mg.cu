@@ -14,8 +14,12 @@
 //    the fly, and the red sweep after it overwrites the red cells.
 // The arithmetic of each line solve, restriction and factorisation follows the
 // reference functions named beside them.
+#include <cooperative_groups.h>
+
 #include "kernels.h"
 #include "reduce.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace ct {
 
@@ -158,184 +162,329 @@ __device__ __forceinline__ Nbr neighbours(const Geo& g, const Geo& cg, int i, in
     return n;
 }
 
+// Loads of values that other blocks of the same kernel may have written
+// (x and b inside the cluster tail kernel) go to L2 (CG = true); everything
+// else may use the L1 path.
+template <bool CG, class T>
+__device__ __forceinline__ T ldm(const T* p) {
+    if (CG) return __ldcg(p);
+    return *p;
+}
+
 // Lateral neighbour sum of op_lat_sum (src/operator3d.h:62-78) at plane l:
 // west, east, south, north; with PRO each neighbour value carries its
 // parent's coarse correction.
-template <class T, bool PRO>
+template <class T, bool PRO, bool CG>
 __device__ __forceinline__ T lat_sum(const LevelView<T>& L, const LevelView<T>& C, const Nbr& n,
                                      int l) {
     const unsigned base = (unsigned)l * L.g.plane;
     const unsigned cbase = PRO ? (unsigned)l * C.g.plane : 0u;
     T s = 0;
     if (n.w) {
-        T xv = L.x[base + n.sw];
-        if (PRO) xv = xv + C.x[cbase + n.pw];
+        T xv = ldm<CG>(L.x + base + n.sw);
+        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.pw);
         s += (T)L.gE[base + n.sw] * xv;
     }
     if (n.e) {
-        T xv = L.x[base + n.se];
-        if (PRO) xv = xv + C.x[cbase + n.pe];
+        T xv = ldm<CG>(L.x + base + n.se);
+        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.pe);
         s += (T)L.gE[base + n.s] * xv;
     }
     if (n.so) {
-        T xv = L.x[base + n.ss];
-        if (PRO) xv = xv + C.x[cbase + n.ps];
+        T xv = ldm<CG>(L.x + base + n.ss);
+        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.ps);
         s += (T)L.gN[base + n.ss] * xv;
     }
     if (n.no) {
-        T xv = L.x[base + n.sn];
-        if (PRO) xv = xv + C.x[cbase + n.pn];
+        T xv = ldm<CG>(L.x + base + n.sn);
+        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.pn);
         s += (T)L.gN[base + n.s] * xv;
     }
     return s;
 }
 
-// Red-black sweep with the column held in registers (nz <= MZ).
-template <class T, int MZ, bool ZERO, bool PRO>
-__global__ void __launch_bounds__(NT)
-    k_sweep_reg(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
-    if (loop_done(ctl, cond)) return;
+// Line solve of the q-th column of colour `color` (mg_line_solve,
+// src/mg3d.h:179-196). With MZ > 0 (nz <= MZ) the column stays in registers:
+// every plane's right-hand side (b plus the lateral sum) is gathered first,
+// all loads independent of one another, then the Thomas recurrence runs on
+// registers and x is written once. MZ = 0 is the general path for deep
+// columns, with forward values going through x as in the reference.
+template <class T, int MZ, bool ZERO, bool PRO, bool CG>
+__device__ __forceinline__ void sweep_column(const LevelView<T>& L, const LevelView<T>& C,
+                                             int color, unsigned q) {
     const Geo& g = L.g;
-    const unsigned q = blockIdx.x * NT + threadIdx.x;
-    if (q >= (unsigned)g.ny * (unsigned)g.hx) return;
     const int j = (int)(q / (unsigned)g.hx), t = (int)(q - (unsigned)j * g.hx);
     const int i = 2 * t + ((j + color) & 1);
     if (i >= g.nx) return;
     const Nbr n = neighbours<PRO>(g, C.g, i, j, t, color);
-    T v[MZ];
-    T prev = 0;
-    float gu_b = 0.0f;
+    if constexpr (MZ > 0) {
+        // Gather: every operand of every plane, all loads independent, so the
+        // whole column costs about one memory latency.
+        T v[MZ], fi[MZ], fc[MZ];
+        float gu[MZ];
 #pragma unroll
-    for (int l = 0; l < MZ; ++l) {
-        if (l < g.nz) {
+        for (int l = 0; l < MZ; ++l) {
+            if (l < g.nz) {
+                const unsigned id = (unsigned)l * g.plane + n.s;
+                T rhs = ldm<CG>(L.b + id);
+                if (!ZERO) rhs = rhs + lat_sum<T, PRO, CG>(L, C, n, l);
+                v[l] = rhs;
+                fi[l] = L.finv[id];
+                fc[l] = L.fcp[id];
+                gu[l] = L.gU[id];
+            }
+        }
+        // Thomas recurrence on registers.
+        T prev = 0;
+#pragma unroll
+        for (int l = 0; l < MZ; ++l) {
+            if (l < g.nz) {
+                const T lower = l > 0 ? -(T)gu[l - 1] : T(0);
+                prev = (v[l] - lower * prev) * fi[l];
+                v[l] = prev;
+            }
+        }
+#pragma unroll
+        for (int l = MZ - 2; l >= 0; --l)
+            if (l < g.nz - 1) v[l] -= fc[l] * v[l + 1];
+#pragma unroll
+        for (int l = 0; l < MZ; ++l)
+            if (l < g.nz) L.x[(unsigned)l * g.plane + n.s] = v[l];
+    } else {
+        T prev = 0;
+        float gu_b = 0.0f;
+        for (int l = 0; l < g.nz; ++l) {
             const unsigned id = (unsigned)l * g.plane + n.s;
-            T rhs = L.b[id];
-            if (!ZERO) rhs = rhs + lat_sum<T, PRO>(L, C, n, l);
+            T rhs = ldm<CG>(L.b + id);
+            if (!ZERO) rhs = rhs + lat_sum<T, PRO, CG>(L, C, n, l);
             const T lower = l > 0 ? -(T)gu_b : T(0);
             prev = (rhs - lower * prev) * L.finv[id];
-            v[l] = prev;
+            L.x[id] = prev;
             gu_b = L.gU[id];
         }
+        for (int l = g.nz - 2; l >= 0; --l) {
+            const unsigned id = (unsigned)l * g.plane + n.s;
+            prev = ldm<CG>(L.x + id) - L.fcp[id] * prev;
+            L.x[id] = prev;
+        }
     }
-#pragma unroll
-    for (int l = MZ - 2; l >= 0; --l)
-        if (l < g.nz - 1) v[l] -= L.fcp[(unsigned)l * g.plane + n.s] * v[l + 1];
-#pragma unroll
-    for (int l = 0; l < MZ; ++l)
-        if (l < g.nz) L.x[(unsigned)l * g.plane + n.s] = v[l];
 }
 
-// Same for deep columns: forward values go through x, as in the reference.
-template <class T, bool ZERO, bool PRO>
+// (b - (A + C/dt) x) at fine cell (i, j, l), in op_apply's order
+// (src/operator3d.h:108-112): diagonal (lateral faces, up, down or ambient,
+// C/dt) times x, minus the six neighbour terms.
+template <class T, bool CG>
+__device__ __forceinline__ T residual_at(const LevelView<T>& F, T inv_dt, int i, int j, int l) {
+    const Geo& fg = F.g;
+    const Nbr n = neighbours<false>(fg, fg, i, j, i >> 1, (i + j) & 1);
+    const unsigned base = (unsigned)l * fg.plane, id = base + n.s;
+    const bool up = l < fg.nz - 1;
+    const T xc = ldm<CG>(F.x + id);
+    T d = 0, off = 0;
+    if (n.w) {
+        const T ge = (T)F.gE[base + n.sw];
+        d += ge;
+        off += ge * ldm<CG>(F.x + base + n.sw);
+    }
+    if (n.e) {
+        const T ge = (T)F.gE[id];
+        d += ge;
+        off += ge * ldm<CG>(F.x + base + n.se);
+    }
+    if (n.so) {
+        const T gn = (T)F.gN[base + n.ss];
+        d += gn;
+        off += gn * ldm<CG>(F.x + base + n.ss);
+    }
+    if (n.no) {
+        const T gn = (T)F.gN[id];
+        d += gn;
+        off += gn * ldm<CG>(F.x + base + n.sn);
+    }
+    const float gu = F.gU[id];
+    d += (T)gu;
+    d += l > 0 ? (T)F.gU[id - fg.plane] : (T)F.gB[n.s];
+    d += (T)F.cap[id] * inv_dt;
+    if (l > 0) off += (T)F.gU[id - fg.plane] * ldm<CG>(F.x + id - fg.plane);
+    if (up) off += (T)gu * ldm<CG>(F.x + id + fg.plane);
+    return ldm<CG>(F.b + id) - (d * xc - off);
+}
+
+// Restriction (src/pcg3d_cpu.cpp:87-100) of coarse cell (I, J, l), q = J cnx + I:
+// the sum over the (up to 4) children, j then i, of the fine residual.
+template <class T, bool CG>
+__device__ __forceinline__ void restrict_cell(const LevelView<T>& F, const LevelView<T>& C,
+                                              T inv_dt, unsigned q, int l) {
+    const Geo& fg = F.g;
+    const Geo& cg = C.g;
+    const int J = (int)(q / (unsigned)cg.nx), I = (int)(q - (unsigned)J * cg.nx);
+    const int i1 = min(2 * I + 2, fg.nx), j1 = min(2 * J + 2, fg.ny);
+    T sum = 0;
+    for (int j = 2 * J; j < j1; ++j)
+        for (int i = 2 * I; i < i1; ++i) sum += residual_at<T, CG>(F, inv_dt, i, j, l);
+    C.b[(unsigned)l * cg.plane + scol(cg, I, J)] = sum;
+}
+
+template <class T, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(NT)
-    k_sweep_mem(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
+    k_sweep(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
     if (loop_done(ctl, cond)) return;
-    const Geo& g = L.g;
     const unsigned q = blockIdx.x * NT + threadIdx.x;
-    if (q >= (unsigned)g.ny * (unsigned)g.hx) return;
-    const int j = (int)(q / (unsigned)g.hx), t = (int)(q - (unsigned)j * g.hx);
-    const int i = 2 * t + ((j + color) & 1);
-    if (i >= g.nx) return;
-    const Nbr n = neighbours<PRO>(g, C.g, i, j, t, color);
-    T prev = 0;
-    float gu_b = 0.0f;
-    for (int l = 0; l < g.nz; ++l) {
-        const unsigned id = (unsigned)l * g.plane + n.s;
-        T rhs = L.b[id];
-        if (!ZERO) rhs = rhs + lat_sum<T, PRO>(L, C, n, l);
-        const T lower = l > 0 ? -(T)gu_b : T(0);
-        prev = (rhs - lower * prev) * L.finv[id];
-        L.x[id] = prev;
-        gu_b = L.gU[id];
-    }
-    for (int l = g.nz - 2; l >= 0; --l) {
-        const unsigned id = (unsigned)l * g.plane + n.s;
-        prev = L.x[id] - L.fcp[id] * prev;
-        L.x[id] = prev;
-    }
+    if (q >= (unsigned)L.g.ny * (unsigned)L.g.hx) return;
+    sweep_column<T, MZ, ZERO, PRO, false>(L, C, color, q);
 }
 
-// Restriction (src/pcg3d_cpu.cpp:87-100): coarse b(I, J, l) = sum over the
-// (up to 4) children, j then i, of b - (A + C/dt) x, the operator applied
-// with op_apply's order (src/operator3d.h:108-112). One thread per coarse
-// column; each child keeps its x at l-1, l and the face below in registers.
+// One thread per coarse cell: blockIdx.y is the plane.
 template <class T>
 __global__ void __launch_bounds__(NT)
     k_restrict(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
     if (loop_done(ctl, cond)) return;
-    const Geo& fg = F.g;
-    const Geo& cg = C.g;
     const unsigned q = blockIdx.x * NT + threadIdx.x;
-    if (q >= (unsigned)cg.nx * (unsigned)cg.ny) return;
-    const int J = (int)(q / (unsigned)cg.nx), I = (int)(q - (unsigned)J * cg.nx);
+    if (q >= (unsigned)C.g.nx * (unsigned)C.g.ny) return;
+    restrict_cell<T, false>(F, C, (T)ctl->inv_dt, q, (int)blockIdx.y);
+}
+
+// The V-cycle below level k0 (all levels from k0 to the single column) in ONE
+// launch of one thread-block cluster: the phases (sweeps, restrictions, the
+// coarsest solve, prolongation-sweeps back up) are separated by cluster
+// barriers instead of kernel boundaries. Values written by other blocks of
+// the cluster (x, b) are read from L2. Every block runs the same phase
+// sequence, so all of them reach every barrier.
+template <class T, int MZ>
+__global__ void __launch_bounds__(kTailThreads, 1)
+    k_vtail(TailLevels<T> tl, const Ctl* ctl, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned tid = cl.block_rank() * kTailThreads + threadIdx.x;
+    const unsigned nth = cl.num_blocks() * kTailThreads;
     const T inv_dt = (T)ctl->inv_dt;
-    int ci[4], cj[4];
-    int nc = 0;
-    for (int j = 2 * J; j < min(2 * J + 2, fg.ny); ++j)
-        for (int i = 2 * I; i < min(2 * I + 2, fg.nx); ++i) {
-            ci[nc] = i;
-            cj[nc] = j;
-            ++nc;
+    const int last = tl.n - 1;
+    for (int k = 0; k < last; ++k) {
+        const LevelView<T>& L = tl.L[k];
+        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true>(L, L, 0, q);
+        cl.sync();
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true>(L, L, 1, q);
+        cl.sync();
+        const LevelView<T>& C = tl.L[k + 1];
+        const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
+        const unsigned work = ccols * (unsigned)C.g.nz;
+        for (unsigned w = tid; w < work; w += nth) {
+            const int l = (int)(w / ccols);
+            restrict_cell<T, true>(L, C, inv_dt, w - (unsigned)l * ccols, l);
         }
-    Nbr nb[4];
-    T xc[4], xb[4];
-    float gub[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        if (k < nc) {
-            const int colour = (ci[k] + cj[k]) & 1;
-            nb[k] = neighbours<false>(fg, cg, ci[k], cj[k], ci[k] >> 1, colour);
-            xc[k] = F.x[nb[k].s];
-            xb[k] = 0;
-            gub[k] = 0.0f;
-        }
+        cl.sync();
     }
-    const unsigned cs = scol(cg, I, J);
-    for (int l = 0; l < fg.nz; ++l) {
-        const unsigned base = (unsigned)l * fg.plane;
-        const bool up = l < fg.nz - 1;
-        T sum = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (k < nc) {
-                const Nbr& n = nb[k];
-                const unsigned id = base + n.s;
-                const T xa = up ? F.x[id + fg.plane] : T(0);
-                const float gu = F.gU[id];
-                T d = 0, off = 0;
-                if (n.w) {
-                    const T ge = (T)F.gE[base + n.sw];
-                    d += ge;
-                    off += ge * F.x[base + n.sw];
-                }
-                if (n.e) {
-                    const T ge = (T)F.gE[id];
-                    d += ge;
-                    off += ge * F.x[base + n.se];
-                }
-                if (n.so) {
-                    const T gn = (T)F.gN[base + n.ss];
-                    d += gn;
-                    off += gn * F.x[base + n.ss];
-                }
-                if (n.no) {
-                    const T gn = (T)F.gN[id];
-                    d += gn;
-                    off += gn * F.x[base + n.sn];
-                }
-                d += (T)gu;
-                d += l > 0 ? (T)gub[k] : (T)F.gB[n.s];
-                d += (T)F.cap[id] * inv_dt;
-                if (l > 0) off += (T)gub[k] * xb[k];
-                if (up) off += (T)gu * xa;
-                sum += F.b[id] - (d * xc[k] - off);
-                xb[k] = xc[k];
-                xc[k] = xa;
-                gub[k] = gu;
+    {
+        const LevelView<T>& L = tl.L[last];
+        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true>(L, L, 0, q);
+        cl.sync();
+    }
+    for (int k = last - 1; k >= 0; --k) {
+        const LevelView<T>& L = tl.L[k];
+        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
+        for (unsigned q = tid; q < ncol; q += nth)
+            sweep_column<T, MZ, false, true, true>(L, tl.L[k + 1], 1, q);
+        cl.sync();
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true>(L, L, 0, q);
+        cl.sync();
+    }
+}
+
+// The bottom of the V-cycle (levels k0 .. single column) in ONE block, with
+// every one of those levels held in shared memory: operator, factors, x and b
+// are copied in (the levels are a few tens of KB), the phases run with block
+// barriers, and level k0's x goes back out for the prolongation above it.
+// Same line-solve and restriction code as the grid-wide kernels, pointed at
+// shared memory.
+template <class T, int MZ>
+__global__ void __launch_bounds__(kSmallThreads, 1)
+    k_vsmall(TailLevels<T> tl, const Ctl* ctl, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ TailLevels<T> sl;  // views of the same levels, in shared memory
+    if (threadIdx.x == 0) sl.n = tl.n;
+    {
+        unsigned char* q = smem;
+        auto take = [&](size_t bytes) {
+            unsigned char* r = q;
+            q += (bytes + 15) & ~size_t(15);
+            return r;
+        };
+        for (int k = 0; k < tl.n; ++k) {
+            const LevelView<T>& G = tl.L[k];
+            LevelView<T> S;
+            const unsigned ln = G.g.plane * (unsigned)G.g.nz;
+            S.g = G.g;
+            float* gE = (float*)take(ln * 4);
+            float* gN = (float*)take(ln * 4);
+            float* gU = (float*)take(ln * 4);
+            float* cap = (float*)take(ln * 4);
+            float* gB = (float*)take(G.g.plane * 4);
+            T* fcp = (T*)take(ln * sizeof(T));
+            T* finv = (T*)take(ln * sizeof(T));
+            T* x = (T*)take(ln * sizeof(T));
+            T* b = (T*)take(ln * sizeof(T));
+            for (unsigned i = threadIdx.x; i < ln; i += kSmallThreads) {
+                gE[i] = G.gE[i];
+                gN[i] = G.gN[i];
+                gU[i] = G.gU[i];
+                cap[i] = G.cap[i];
+                fcp[i] = G.fcp[i];
+                finv[i] = G.finv[i];
+                if (k == 0) b[i] = G.b[i];
             }
+            for (unsigned i = threadIdx.x; i < G.g.plane; i += kSmallThreads) gB[i] = G.gB[i];
+            S.gE = gE;
+            S.gN = gN;
+            S.gU = gU;
+            S.cap = cap;
+            S.gB = gB;
+            S.fcp = fcp;
+            S.finv = finv;
+            S.x = x;
+            S.b = b;
+            if (threadIdx.x == 0) sl.L[k] = S;
         }
-        C.b[(unsigned)l * cg.plane + cs] = sum;
     }
+    __syncthreads();
+    const unsigned tid = threadIdx.x, nth = kSmallThreads;
+    const T inv_dt = (T)ctl->inv_dt;
+    const int last = sl.n - 1;
+    for (int k = 0; k < last; ++k) {
+        const LevelView<T>& L = sl.L[k];
+        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
+        __syncthreads();
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 1, q);
+        __syncthreads();
+        const LevelView<T>& C = sl.L[k + 1];
+        const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
+        const unsigned work = ccols * (unsigned)C.g.nz;
+        for (unsigned w = tid; w < work; w += nth) {
+            const int l = (int)(w / ccols);
+            restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
+        }
+        __syncthreads();
+    }
+    {
+        const LevelView<T>& L = sl.L[last];
+        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
+        __syncthreads();
+    }
+    for (int k = last - 1; k >= 0; --k) {
+        const LevelView<T>& L = sl.L[k];
+        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
+        for (unsigned q = tid; q < ncol; q += nth)
+            sweep_column<T, MZ, false, true, false>(L, sl.L[k + 1], 1, q);
+        __syncthreads();
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 0, q);
+        __syncthreads();
+    }
+    const unsigned ln0 = sl.L[0].g.plane * (unsigned)sl.L[0].g.nz;
+    for (unsigned i = tid; i < ln0; i += nth) tl.L[0].x[i] = sl.L[0].x[i];
 }
 
 unsigned blocks_for(unsigned n) { return n == 0 ? 1u : (n + NT - 1) / NT; }
@@ -362,33 +511,95 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
     const unsigned grid = blocks_for((unsigned)L.g.ny * (unsigned)L.g.hx);
     const LevelView<T> C = coarse ? *coarse : L;
     const int nz = L.g.nz;
-#define CT_SWEEP(MZ)                                                                        \
-    do {                                                                                    \
-        if (zero_x)                                                                         \
-            k_sweep_reg<T, MZ, true, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);   \
-        else if (coarse)                                                                    \
-            k_sweep_reg<T, MZ, false, true><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);   \
-        else                                                                                \
-            k_sweep_reg<T, MZ, false, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);  \
+#define CT_SWEEP(MZ)                                                                    \
+    do {                                                                                \
+        if (zero_x)                                                                     \
+            k_sweep<T, MZ, true, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);   \
+        else if (coarse)                                                                \
+            k_sweep<T, MZ, false, true><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);   \
+        else                                                                            \
+            k_sweep<T, MZ, false, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);  \
     } while (0)
-    if (nz <= 16) {
+    if (nz <= 8)
+        CT_SWEEP(8);
+    else if (nz <= 12)
+        CT_SWEEP(12);
+    else if (nz <= 16)
         CT_SWEEP(16);
-    } else if (nz <= 32) {
+    else if (nz <= 32)
         CT_SWEEP(32);
-    } else if (zero_x) {
-        k_sweep_mem<T, true, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);
-    } else if (coarse) {
-        k_sweep_mem<T, false, true><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);
-    } else {
-        k_sweep_mem<T, false, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);
-    }
+    else
+        CT_SWEEP(0);
 #undef CT_SWEEP
 }
 
 template <class T>
 void launch_restrict(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,
                      Cond cond) {
-    k_restrict<T><<<blocks_for((unsigned)C.g.nx * C.g.ny), NT, 0, st>>>(F, C, ctl, cond);
+    const dim3 grid(blocks_for((unsigned)C.g.nx * C.g.ny), (unsigned)C.g.nz);
+    k_restrict<T><<<grid, NT, 0, st>>>(F, C, ctl, cond);
+}
+
+template <class T>
+int tail_cluster_size() {
+    // Largest cluster this GPU can co-schedule for the tail kernel (16 needs
+    // the non-portable opt-in; 8 is portable).
+    static int cached = 0;
+    if (cached) return cached;
+    int best = 1;
+    for (int cs : {16, 8, 4, 2}) {
+        auto k = k_vtail<T, 12>;
+        if (cs > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(kTailThreads);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k, &cfg) == cudaSuccess && nclusters > 0) {
+            best = cs;
+            break;
+        }
+        cudaGetLastError();
+    }
+    cached = best;
+    return best;
+}
+
+template <class T>
+cudaError_t launch_vtail(cudaStream_t st, const TailLevels<T>& tl, int cluster, const Ctl* ctl,
+                         Cond cond) {
+    int mz = 0;
+    for (int k = 0; k < tl.n; ++k) mz = tl.L[k].g.nz;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(kTailThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    auto pick = [&](auto kern) {
+        if (cluster > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        return cudaLaunchKernelEx(&cfg, kern, tl, ctl, cond);
+    };
+    if (mz <= 8) return pick(k_vtail<T, 8>);
+    if (mz <= 12) return pick(k_vtail<T, 12>);
+    if (mz <= 16) return pick(k_vtail<T, 16>);
+    if (mz <= 32) return pick(k_vtail<T, 32>);
+    if (cluster > 8) cudaFuncSetAttribute(k_vtail<T, 0>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return cudaLaunchKernelEx(&cfg, k_vtail<T, 0>, tl, ctl, cond);
 }
 
 template void launch_factor<float>(cudaStream_t, const LevelView<float>&, float);
@@ -401,5 +612,51 @@ template void launch_restrict<float>(cudaStream_t, const LevelView<float>&,
                                      const LevelView<float>&, const Ctl*, Cond);
 template void launch_restrict<double>(cudaStream_t, const LevelView<double>&,
                                       const LevelView<double>&, const Ctl*, Cond);
+template int tail_cluster_size<float>();
+template int tail_cluster_size<double>();
+template cudaError_t launch_vtail<float>(cudaStream_t, const TailLevels<float>&, int, const Ctl*,
+                                         Cond);
+template cudaError_t launch_vtail<double>(cudaStream_t, const TailLevels<double>&, int, const Ctl*,
+                                          Cond);
+
+template <class T>
+size_t small_smem_bytes(const TailLevels<T>& tl) {
+    size_t b = 0;
+    auto take = [&](size_t bytes) { b += (bytes + 15) & ~size_t(15); };
+    for (int k = 0; k < tl.n; ++k) {
+        const size_t ln = (size_t)tl.L[k].g.plane * tl.L[k].g.nz;
+        for (int a = 0; a < 4; ++a) take(ln * 4);
+        take((size_t)tl.L[k].g.plane * 4);
+        for (int a = 0; a < 4; ++a) take(ln * sizeof(T));
+    }
+    return b;
+}
+
+template <class T>
+cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, const Ctl* ctl, Cond cond) {
+    const size_t smem = small_smem_bytes(tl);
+    int mz = 0;
+    for (int k = 0; k < tl.n; ++k) mz = tl.L[k].g.nz;
+    auto go = [&](auto kern) {
+        // Every k_vsmall instantiation needs its own opt-in to more than 48 KB
+        // of dynamic shared memory; set it on every launch (host-side only).
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSmallSmemMax);
+        if (e != cudaSuccess) return e;
+        kern<<<1, kSmallThreads, smem, st>>>(tl, ctl, cond);
+        return cudaGetLastError();
+    };
+    if (mz <= 8) return go(k_vsmall<T, 8>);
+    if (mz <= 12) return go(k_vsmall<T, 12>);
+    if (mz <= 16) return go(k_vsmall<T, 16>);
+    if (mz <= 32) return go(k_vsmall<T, 32>);
+    return go(k_vsmall<T, 0>);
+}
+
+template size_t small_smem_bytes<float>(const TailLevels<float>&);
+template size_t small_smem_bytes<double>(const TailLevels<double>&);
+template cudaError_t launch_vsmall<float>(cudaStream_t, const TailLevels<float>&, const Ctl*, Cond);
+template cudaError_t launch_vsmall<double>(cudaStream_t, const TailLevels<double>&, const Ctl*,
+                                           Cond);
 
 }  // namespace ct

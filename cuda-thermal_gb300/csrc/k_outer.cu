@@ -5,6 +5,7 @@
 // kernels walk one column per thread through the z-planes, so the vertical
 // neighbours and the face below come from registers and every z-plane access
 // of a warp is one contiguous run of the split layout.
+#include <algorithm>
 #include <cmath>
 
 #include "kernels.h"
@@ -511,31 +512,37 @@ unsigned grid_for(size_t n, int threads = NT) {
 void launch_residual(cudaStream_t st, MgType mt, const OpView& o, const double* diag,
                      const double* b, const double* x, double* r, void* b0, Ctl* ctl,
                      const Red& red, Cond cond) {
+    static const int wb = wave_blocks(k_residual<float>, 1 << 30);
+    const int nb = std::min(red.blocks, wb);
     if (mt == MG_F64)
-        k_residual<double><<<red.blocks, NT, 0, st>>>(o, diag, b, x, r, (double*)b0, ctl, red.part,
-                                                      red.maxb, cond);
+        k_residual<double><<<nb, NT, 0, st>>>(o, diag, b, x, r, (double*)b0, ctl, red.part,
+                                              red.maxb, cond);
     else
-        k_residual<float><<<red.blocks, NT, 0, st>>>(o, diag, b, x, r,
+        k_residual<float><<<nb, NT, 0, st>>>(o, diag, b, x, r,
                                                      mt == MG_F32 ? (float*)b0 : nullptr, ctl,
                                                      red.part, red.maxb, cond);
 }
 
 void launch_apply(cudaStream_t st, const OpView& o, const double* diag, const double* p,
                   double* Ap, Ctl* ctl, const Red& red, Cond cond) {
-    k_apply<<<red.blocks, NT, 0, st>>>(o, diag, p, Ap, ctl, red.part, red.maxb, cond);
+    static const int wb = wave_blocks(k_apply, 1 << 30);
+    k_apply<<<std::min(red.blocks, wb), NT, 0, st>>>(o, diag, p, Ap, ctl, red.part, red.maxb, cond);
 }
 
 void launch_update(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap,
                    double* x, double* r, void* b0, Ctl* ctl, const Red& red, Cond cond) {
     const unsigned n2 = n / 2;
+    static const int wb = wave_blocks(k_update<double, true>, 1 << 30);
+    Red rb = red;
+    rb.blocks = std::min(red.blocks, wb);
     if (mt == MG_F32)
-        k_update<float, true><<<red.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (float*)b0, ctl, red.part,
+        k_update<float, true><<<rb.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (float*)b0, ctl, red.part,
                                                          red.maxb, cond);
     else if (mt == MG_F64)
-        k_update<double, true><<<red.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (double*)b0, ctl,
+        k_update<double, true><<<rb.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (double*)b0, ctl,
                                                           red.part, red.maxb, cond);
     else
-        k_update<float, false><<<red.blocks, NT, 0, st>>>(n2, p, Ap, x, r, nullptr, ctl, red.part,
+        k_update<float, false><<<rb.blocks, NT, 0, st>>>(n2, p, Ap, x, r, nullptr, ctl, red.part,
                                                           red.maxb, cond);
 }
 
@@ -543,27 +550,31 @@ void launch_dot(cudaStream_t st, MgType mt, bool flexible, unsigned n, const dou
                 const void* z, const double* invd, const double* Ap, Ctl* ctl, const Red& red,
                 Cond cond) {
     const unsigned n2 = n / 2;
+    static const int wb = wave_blocks(k_dot<double, false, true>, 1 << 30);
+    Red rb = red;
+    rb.blocks = std::min(red.blocks, wb);
     if (mt == MG_NONE)
-        k_dot<float, true, false><<<red.blocks, NT, 0, st>>>(n2, r, nullptr, invd, Ap, ctl,
+        k_dot<float, true, false><<<rb.blocks, NT, 0, st>>>(n2, r, nullptr, invd, Ap, ctl,
                                                              red.part, red.maxb, cond);
     else if (mt == MG_F32 && flexible)
-        k_dot<float, false, true><<<red.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap, ctl,
+        k_dot<float, false, true><<<rb.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap, ctl,
                                                              red.part, red.maxb, cond);
     else if (mt == MG_F32)
-        k_dot<float, false, false><<<red.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap,
+        k_dot<float, false, false><<<rb.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap,
                                                               ctl, red.part, red.maxb, cond);
     else if (flexible)
-        k_dot<double, false, true><<<red.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
+        k_dot<double, false, true><<<rb.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
                                                               ctl, red.part, red.maxb, cond);
     else
-        k_dot<double, false, false><<<red.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
+        k_dot<double, false, false><<<rb.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
                                                                ctl, red.part, red.maxb, cond);
 }
 
 void launch_update_p(cudaStream_t st, MgType mt, unsigned n, const void* z, const double* r,
                      const double* invd, double* p, Ctl* ctl, Cond cond) {
     const unsigned n2 = n / 2;
-    const unsigned grid = grid_for(n2);
+    static const int wb = wave_blocks(k_update_p<double, false>, 1 << 30);
+    const unsigned grid = std::min(grid_for(n2), (unsigned)wb);
     if (mt == MG_NONE)
         k_update_p<float, true><<<grid, NT, 0, st>>>(n2, nullptr, r, invd, p, ctl, cond);
     else if (mt == MG_F32)

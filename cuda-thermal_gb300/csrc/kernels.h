@@ -23,6 +23,27 @@ struct Red {
 
 enum MgType { MG_NONE = 0, MG_F32 = 1, MG_F64 = 2 };
 
+// Grid for a grid-stride kernel: one full wave, SMs x resident blocks of
+// this kernel (from the occupancy calculator), capped at `cap` blocks.
+template <class K>
+inline int wave_blocks(K kernel, int cap) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, NT, 0) != cudaSuccess ||
+        per_sm <= 0) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const int b = sms * per_sm;
+    return b < cap ? b : cap;
+}
+
 // ---- outer PCG (FP64), k_outer.cu ----------------------------------------
 // r = b - (A + C/dt) x, b0 = r in the V-cycle precision; rr, bb; start test.
 void launch_residual(cudaStream_t st, MgType mt, const OpView& o, const double* diag,
@@ -59,6 +80,25 @@ void launch_true_residual(cudaStream_t st, const OpView& o, const double* P, con
 void launch_step_record(cudaStream_t st, const OpView& o, const double* x, const double* xold,
                         Ctl* ctl, const Red& red);
 
+// ---- double-word outer PCG (FP32 pipes), k_dw.cu -----------------------------
+// r = b - A x in FP64 from the double-word x; start of a solve, or the residual
+// replacement that begins phase 2.
+void launch_residual_x(cudaStream_t st, const OpView& o, const double* diag, const double* b,
+                       const float2* x, float2* r, float* b0, bool start, Ctl* ctl,
+                       const Red& red, Cond cond);
+void launch_apply_dw(cudaStream_t st, const OpView& o, const float2* dgw, const float2* p,
+                     float2* Ap, Ctl* ctl, const Red& red, Cond cond);
+void launch_update_dw(cudaStream_t st, unsigned n, const float2* p, const float2* Ap, float2* x,
+                      float2* r, float* b0, Ctl* ctl, const Red& red, Cond cond);
+void launch_dot_dw(cudaStream_t st, unsigned n, const float2* r, const float* z, const float2* Ap,
+                   Ctl* ctl, const Red& red, Cond cond);
+void launch_update_p_dw(cudaStream_t st, unsigned n, const float* z, float2* p, Ctl* ctl,
+                        Cond cond);
+void launch_to_dw(cudaStream_t st, unsigned n, const double* in, float2* out);
+void launch_dw_to_natural(cudaStream_t st, const Geo& g, const float2* split, double* nat);
+void launch_natural_to_dw(cudaStream_t st, const Geo& g, const double* nat, float2* split);
+void launch_dw_to_d(cudaStream_t st, unsigned n, const float2* in, double* out);
+
 // ---- multigrid, k_mg.cu ---------------------------------------------------
 // Coarse level from the fine one (mg_coarse_cell arithmetic, split layouts).
 void launch_coarsen(cudaStream_t st, const Geo& fg, const float* fgE, const float* fgN,
@@ -79,5 +119,27 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
 template <class T>
 void launch_restrict(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,
                      Cond cond);
+
+// The levels below a threshold, run by one thread-block cluster in one launch.
+constexpr int kMaxTail = 24;
+constexpr int kTailThreads = 512;
+template <class T>
+struct TailLevels {
+    int n;  // levels in L, the finest of them first, the single column last
+    LevelView<T> L[kMaxTail];
+};
+template <class T>
+int tail_cluster_size();
+// The smallest levels (those whose arrays together fit kSmallSmemMax bytes),
+// run by one block out of shared memory.
+constexpr int kSmallThreads = 256;
+constexpr int kSmallSmemMax = 200 * 1024;
+template <class T>
+size_t small_smem_bytes(const TailLevels<T>& tl);
+template <class T>
+cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, const Ctl* ctl, Cond cond);
+template <class T>
+cudaError_t launch_vtail(cudaStream_t st, const TailLevels<T>& tl, int cluster, const Ctl* ctl,
+                         Cond cond);
 
 }  // namespace ct

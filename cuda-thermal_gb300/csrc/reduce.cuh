@@ -75,10 +75,11 @@ __device__ __forceinline__ void stop_loop(Ctl* c, const Cond& cond) {
     if (cond.use) cudaGraphSetConditional(cond.h, 0u);
 }
 
-// Entry test of every loop-body kernel: once the solve is done, the rest of
-// the body is a no-op, and (inside a graph loop) the loop is told to end.
+// Entry test of every loop-body kernel: once the solve is done (or, in the
+// double-word mode, once its first phase is), the rest of the body is a
+// no-op, and (inside a graph loop) the loop is told to end.
 __device__ __forceinline__ bool loop_done(const Ctl* c, const Cond& cond) {
-    if (*(volatile const int*)&c->done) {
+    if (*(volatile const int*)&c->done || *(volatile const int*)&c->phase_end) {
         if (cond.use && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond.h, 0u);
         return true;
     }

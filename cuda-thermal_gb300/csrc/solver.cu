@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -90,6 +91,10 @@ class Solver {
     ct_precision prec = CT_MG_FP32_FLEX;
     MgType mt = MG_F32;
     bool flex = true;
+    bool dw = false;       // double-word outer iteration (CT_MG_FP32_FLEX_DW)
+    bool x_zero = true;    // x is known to be 0 (set_x_zero since the last solve)
+    cudaError_t launch_error = cudaSuccess;  // first failed launch of a shaped (cluster/smem) kernel
+    double rr_thr = 1e-5;  // relres of the FP64 residual replacement (dw)
     size_t tsize = 4;  // bytes per V-cycle value
     Geo g0{};
     unsigned n = 0;      // slots of all planes (split layout, with padding)
@@ -97,12 +102,15 @@ class Solver {
     double dx = 0, dy = 0;
     int sms = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t st_body = nullptr;  // captures the graph loops' bodies
+    cudaStream_t cs = nullptr;       // stream the enqueue_* functions launch on
     char* base = nullptr;
     size_t bytes = 0;
     // fine operator and PCG vectors (split layout)
     float *gE = nullptr, *gN = nullptr, *gU = nullptr, *gB = nullptr, *cap = nullptr;
     double *P = nullptr, *x = nullptr, *b = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr;
     double *diag = nullptr, *invd = nullptr, *xold = nullptr, *nat = nullptr, *part = nullptr;
+    float2* dgw = nullptr;  // double-word diagonal (dw)
     Ctl* ctl = nullptr;
     Ctl* h_ctl = nullptr;  // pinned mirror
     std::vector<Level> lv;
@@ -110,7 +118,10 @@ class Solver {
     double inv_dt = 0;
     bool use_graphs = true;
     bool have_cond = false;
-    cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr;
+    size_t tail_k0 = 0;    // levels from tail_k0 down run in one cluster launch
+    size_t small_k0 = 0;   // levels from small_k0 down run in one block from shared memory
+    int tail_cluster = 1;  // CTAs in that cluster
+    cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
     ct_setup_times times{};
     // per-kernel timing (ct_profile_solve)
     bool prof = false;
@@ -118,10 +129,11 @@ class Solver {
 
     ~Solver() {
         if (st) cudaStreamSynchronize(st);
-        for (cudaGraphExec_t g : {gx_solve, gx_init, gx_body})
+        for (cudaGraphExec_t g : {gx_solve, gx_init, gx_body, gx_replace})
             if (g) cudaGraphExecDestroy(g);
         if (base) cudaFree(base);
         if (h_ctl) cudaFreeHost(h_ctl);
+        if (st_body) cudaStreamDestroy(st_body);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -172,14 +184,26 @@ class Solver {
         ProfEntry e{name, nbytes, nullptr, nullptr};
         cudaEventCreate(&e.a);
         cudaEventCreate(&e.b);
-        cudaEventRecord(e.a, st);
+        cudaEventRecord(e.a, cs);
         launch();
-        cudaEventRecord(e.b, st);
+        cudaEventRecord(e.b, cs);
         prof_log.push_back(e);
     }
 
     void enqueue_init(Cond cond);
     void enqueue_body(Cond cond);
+    void enqueue_replace(Cond cond);
+    // The double-word views of x, r, p, Ap (same storage as the FP64 vectors).
+    float2* xw() const { return reinterpret_cast<float2*>(x); }
+    float2* rw() const { return reinterpret_cast<float2*>(r); }
+    float2* pw() const { return reinterpret_cast<float2*>(p); }
+    float2* Apw() const { return reinterpret_cast<float2*>(Ap); }
+    // x as split-layout FP64 in `out` (out may be x itself outside dw mode).
+    const double* x_as_double(double* scratch) const {
+        if (!dw) return x;
+        launch_dw_to_d(st, n, xw(), scratch);
+        return scratch;
+    }
     template <class T>
     void vcycle(size_t k, Cond cond);
 };
@@ -196,12 +220,15 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     if (!m->P) return fail(CT_BAD_ARG, "ct_solver_create: null power map");
     if (!(m->dx > 0) || !(m->dy > 0)) return fail(CT_BAD_ARG, "ct_solver_create: dx, dy must be > 0");
     if (pc_ != CT_JACOBI && pc_ != CT_MULTIGRID) return fail(CT_BAD_ARG, "bad preconditioner");
-    if (prec_ != CT_MG_FP64 && prec_ != CT_MG_FP32 && prec_ != CT_MG_FP32_FLEX)
+    if (prec_ != CT_MG_FP64 && prec_ != CT_MG_FP32 && prec_ != CT_MG_FP32_FLEX &&
+        prec_ != CT_MG_FP32_FLEX_DW)
         return fail(CT_BAD_ARG, "bad precision");
     pc = pc_;
     prec = prec_;
     mt = pc == CT_JACOBI ? MG_NONE : (prec == CT_MG_FP64 ? MG_F64 : MG_F32);
-    flex = pc == CT_MULTIGRID && prec == CT_MG_FP32_FLEX;
+    flex = pc == CT_MULTIGRID && (prec == CT_MG_FP32_FLEX || prec == CT_MG_FP32_FLEX_DW);
+    dw = pc == CT_MULTIGRID && prec == CT_MG_FP32_FLEX_DW;
+    if (const char* e = std::getenv("CT_RR_THRESHOLD")) rr_thr = std::atof(e);
     tsize = mt == MG_F64 ? 8 : 4;
     g0 = geo_of(m->nx, m->ny, m->nz);
     const double slots = (double)g0.plane * g0.nz;
@@ -224,6 +251,8 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
 
     auto t0 = clk::now();
     CT_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CT_CK(cudaStreamCreateWithFlags(&st_body, cudaStreamNonBlocking));
+    cs = st;
     CT_CK(cudaMallocHost(&h_ctl, sizeof(Ctl)));
     std::memset(h_ctl, 0, sizeof(Ctl));
 
@@ -234,6 +263,7 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     size_t o_vec[8];
     for (size_t& o : o_vec) o = ar.take((size_t)n * 8);
     const size_t o_invd = pc == CT_JACOBI ? ar.take((size_t)n * 8) : 0;
+    const size_t o_dgw = dw ? ar.take((size_t)n * 8) : 0;
     const size_t o_nat = ar.take(ncells * 8);
     const size_t o_part = ar.take((size_t)NSLOT * 4 * maxb * 8);
     const size_t o_ctl = ar.take(sizeof(Ctl));
@@ -272,6 +302,34 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
             L = C;
         }
     }
+    // Levels with at most tail_cols columns run inside one thread-block
+    // cluster launch (k_vtail); CT_TAIL_COLS overrides the default.
+    {
+        long tail_cols = 0;
+        if (const char* e = std::getenv("CT_TAIL_COLS")) tail_cols = std::atol(e);
+        tail_k0 = lv.size();
+        for (size_t k = 0; k < lv.size(); ++k)
+            if ((long)lv[k].g.nx * lv[k].g.ny <= tail_cols) {
+                tail_k0 = k;
+                break;
+            }
+        if (lv.size() - tail_k0 > (size_t)kMaxTail) tail_k0 = lv.size() - kMaxTail;
+        if (tail_k0 < lv.size())
+            tail_cluster = mt == MG_F64 ? tail_cluster_size<double>() : tail_cluster_size<float>();
+        // The smallest levels whose arrays fit one block's shared memory.
+        small_k0 = lv.size();
+        long small_max = kSmallSmemMax;
+        if (const char* e = std::getenv("CT_SMALL_BYTES")) small_max = std::atol(e);
+        size_t acc = 0;
+        for (size_t k = lv.size(); k-- > 0;) {
+            const size_t ln = (size_t)lv[k].g.plane * lv[k].g.nz;
+            acc += 4 * ((ln * 4 + 15) & ~size_t(15)) + ((lv[k].g.plane * 4 + 15) & ~size_t(15)) +
+                   4 * ((ln * tsize + 15) & ~size_t(15));
+            if ((long)acc > small_max || lv.size() - k > (size_t)kMaxTail) break;
+            small_k0 = k;
+        }
+        if (small_k0 < tail_k0) tail_k0 = lv.size();  // the shared-memory kernel covers it
+    }
     bytes = ar.used;
     {
         const cudaError_t e = cudaMalloc(&base, bytes);
@@ -297,6 +355,7 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     diag = at<double>(o_vec[6]);
     xold = at<double>(o_vec[7]);
     invd = pc == CT_JACOBI ? at<double>(o_invd) : nullptr;
+    dgw = dw ? at<float2>(o_dgw) : nullptr;
     nat = at<double>(o_nat);
     part = at<double>(o_part);
     ctl = at<Ctl>(o_ctl);
@@ -363,6 +422,7 @@ ct_status Solver::set_dt(double dt) {
     if (!(dt >= 0) || !std::isfinite(dt)) return fail(CT_BAD_ARG, "ct_set_dt: dt must be >= 0");
     inv_dt = dt > 0 ? 1.0 / dt : 0.0;
     launch_diag(st, op(), inv_dt, diag, invd);
+    if (dw) launch_to_dw(st, n, diag, dgw);
     if (mt == MG_F32)
         for (size_t k = 0; k < lv.size(); ++k) launch_factor<float>(st, view<float>(k), (float)inv_dt);
     else if (mt == MG_F64)
@@ -375,6 +435,34 @@ ct_status Solver::set_dt(double dt) {
 
 template <class T>
 void Solver::vcycle(size_t k, Cond cond) {
+    if (k == small_k0) {
+        TailLevels<T> tl;
+        tl.n = (int)(lv.size() - k);
+        double b = 0;
+        for (int q = 0; q < tl.n; ++q) {
+            tl.L[q] = view<T>(k + q);
+            const Geo& g = tl.L[q].g;
+            b += (double)g.nx * g.ny * g.nz * (4 * sizeof(T) + 4 + 2 * sizeof(T) + 16);
+        }
+        enq(("mg_small_l" + std::to_string(k)).c_str(), b, [&] {
+            const cudaError_t e = launch_vsmall<T>(cs, tl, ctl, cond);
+            if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
+        });
+        return;
+    }
+    if (k == tail_k0) {
+        TailLevels<T> tl;
+        tl.n = (int)(lv.size() - k);
+        double b = 0;
+        for (int q = 0; q < tl.n; ++q) {
+            tl.L[q] = view<T>(k + q);
+            const Geo& g = tl.L[q].g;
+            b += (double)g.nx * g.ny * g.nz * (4 * sizeof(T) + 4 + 2 * sizeof(T) + 16);
+        }
+        enq(("mg_tail_l" + std::to_string(k) + "_c" + std::to_string(tail_cluster)).c_str(), b,
+            [&] { launch_vtail<T>(cs, tl, tail_cluster, ctl, cond); });
+        return;
+    }
     const LevelView<T> L = view<T>(k);
     const double cells = (double)L.g.nx * L.g.ny * L.g.nz;
     const double t = (double)sizeof(T);
@@ -384,30 +472,58 @@ void Solver::vcycle(size_t k, Cond cond) {
     const double b_sweep = cells / 2 * (4 * t + 12) + cells / 2 * (t + 8);
     if (k + 1 == lv.size()) {
         enq(("mg_sweep0" + lvl).c_str(), b_zero,
-            [&] { launch_sweep<T>(st, L, 0, true, nullptr, ctl, cond); });
+            [&] { launch_sweep<T>(cs, L, 0, true, nullptr, ctl, cond); });
         return;
     }
     const LevelView<T> C = view<T>(k + 1);
-    enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { launch_sweep<T>(st, L, 0, true, nullptr, ctl, cond); });
-    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(st, L, 1, false, nullptr, ctl, cond); });
+    enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { launch_sweep<T>(cs, L, 0, true, nullptr, ctl, cond); });
+    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(cs, L, 1, false, nullptr, ctl, cond); });
     enq(("mg_restrict" + lvl).c_str(), cells * (2 * t + 16) + cells / 4 * t,
-        [&] { launch_restrict<T>(st, L, C, ctl, cond); });
+        [&] { launch_restrict<T>(cs, L, C, ctl, cond); });
     vcycle<T>(k + 1, cond);
     enq(("mg_sweep" + lvl).c_str(), b_sweep + cells / 4 * t,
-        [&] { launch_sweep<T>(st, L, 1, false, &C, ctl, cond); });
-    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(st, L, 0, false, nullptr, ctl, cond); });
+        [&] { launch_sweep<T>(cs, L, 1, false, &C, ctl, cond); });
+    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(cs, L, 0, false, nullptr, ctl, cond); });
 }
 
 void Solver::enqueue_init(Cond cond) {
     void* b0 = mt == MG_NONE ? nullptr : (void*)(base + lv[0].o_b);
+    if (dw) {
+        enq("pcg_residual_fp64", (double)ncells * (36 + 8 + 8 + 4), [&] {
+            launch_residual_x(cs, op(), diag, b, xw(), rw(), (float*)b0, true, ctl,
+                              red_cols(SL_INIT), cond);
+        });
+        return;
+    }
     enq("pcg_residual", (double)ncells * (36 + 8 + 8 + tsize), [&] {
-        launch_residual(st, mt, op(), diag, b, x, r, b0, ctl, red_cols(SL_INIT), cond);
+        launch_residual(cs, mt, op(), diag, b, x, r, b0, ctl, red_cols(SL_INIT), cond);
+    });
+}
+
+void Solver::enqueue_replace(Cond cond) {
+    float* b0 = at<float>(lv[0].o_b);
+    enq("pcg_residual_fp64", (double)ncells * (36 + 8 + 8 + 4), [&] {
+        launch_residual_x(cs, op(), diag, b, xw(), rw(), b0, false, ctl, red_cols(SL_INIT), cond);
     });
 }
 
 void Solver::enqueue_body(Cond cond) {
     const double N = (double)ncells;
     const void* z = nullptr;
+    if (dw) {
+        vcycle<float>(0, cond);
+        const float* zf = at<float>(lv[0].o_x);
+        float* b0 = at<float>(lv[0].o_b);
+        enq("pcg_dot", N * (8 + 4 + 8),
+            [&] { launch_dot_dw(cs, n, rw(), zf, Apw(), ctl, red_vec(SL_DOT), cond); });
+        enq("pcg_update_p", N * (4 + 16), [&] { launch_update_p_dw(cs, n, zf, pw(), ctl, cond); });
+        enq("pcg_apply", N * 36,
+            [&] { launch_apply_dw(cs, op(), dgw, pw(), Apw(), ctl, red_cols(SL_APPLY), cond); });
+        enq("pcg_update_xr", N * (48 + 4), [&] {
+            launch_update_dw(cs, n, pw(), Apw(), xw(), rw(), b0, ctl, red_vec(SL_UPDATE), cond);
+        });
+        return;
+    }
     if (mt == MG_F32) {
         vcycle<float>(0, cond);
         z = base + lv[0].o_x;
@@ -417,80 +533,96 @@ void Solver::enqueue_body(Cond cond) {
     }
     const double zb = mt == MG_NONE ? 16.0 : (double)tsize;
     enq("pcg_dot", N * (8 + zb + (flex ? 8 : 0)),
-        [&] { launch_dot(st, mt, flex, n, r, z, invd, Ap, ctl, red_vec(SL_DOT), cond); });
-    enq("pcg_update_p", N * (zb + 16), [&] { launch_update_p(st, mt, n, z, r, invd, p, ctl, cond); });
-    enq("pcg_apply", N * 36, [&] { launch_apply(st, op(), diag, p, Ap, ctl, red_cols(SL_APPLY), cond); });
+        [&] { launch_dot(cs, mt, flex, n, r, z, invd, Ap, ctl, red_vec(SL_DOT), cond); });
+    enq("pcg_update_p", N * (zb + 16), [&] { launch_update_p(cs, mt, n, z, r, invd, p, ctl, cond); });
+    enq("pcg_apply", N * 36, [&] { launch_apply(cs, op(), diag, p, Ap, ctl, red_cols(SL_APPLY), cond); });
     void* b0 = mt == MG_NONE ? nullptr : (void*)(base + lv[0].o_b);
     enq("pcg_update_xr", N * (48 + (mt == MG_NONE ? 0 : tsize)),
-        [&] { launch_update(st, mt, n, p, Ap, x, r, b0, ctl, red_vec(SL_UPDATE), cond); });
+        [&] { launch_update(cs, mt, n, p, Ap, x, r, b0, ctl, red_vec(SL_UPDATE), cond); });
 }
 
 ct_status Solver::record_graphs() {
-    // Preferred: init + WHILE(body) as one graph.
+    launch_error = cudaSuccess;
+    // Preferred: one graph per solve: the start residual and a conditional
+    // WHILE loop over the iteration body (in the double-word mode: a first
+    // loop, the FP64 residual replacement, a second loop).
     cudaGraph_t graph = nullptr;
     CT_CK(cudaGraphCreate(&graph, 0));
-    cudaGraphConditionalHandle h{};
-    bool ok = cudaGraphConditionalHandleCreate(&h, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+    cudaGraphConditionalHandle h1{}, h2{};
+    bool ok = cudaGraphConditionalHandleCreate(&h1, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok && dw)
+        ok = cudaGraphConditionalHandleCreate(&h2, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+    // Adds a WHILE node after the captured work so far and captures its body.
+    auto add_while = [&](cudaGraphConditionalHandle h) -> bool {
+        cudaStreamCaptureStatus cst;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaGraph_t cg = nullptr;
+        if (cudaStreamGetCaptureInfo(st, &cst, nullptr, &cg, &deps, nullptr, &ndeps) != cudaSuccess)
+            return false;
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cnode = nullptr;
+        if (cudaGraphAddNode(&cnode, cg, deps, nullptr, ndeps, &cp) != cudaSuccess) return false;
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        if (cudaStreamBeginCaptureToGraph(st_body, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return false;
+        cs = st_body;
+        enqueue_body(Cond{h, 1});
+        cs = st;
+        cudaGraph_t bg = nullptr;
+        if (cudaStreamEndCapture(st_body, &bg) != cudaSuccess) return false;
+        return cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1,
+                                                   cudaStreamSetCaptureDependencies) == cudaSuccess;
+    };
     if (ok) {
-        const Cond cond{h, 1};
         ok = cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0,
                                            cudaStreamCaptureModeThreadLocal) == cudaSuccess;
         if (ok) {
-            enqueue_init(cond);
-            cudaStreamCaptureStatus cs;
-            const cudaGraphNode_t* deps = nullptr;
-            size_t ndeps = 0;
-            cudaGraph_t cg = nullptr;
-            ok = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &ndeps) == cudaSuccess;
-            cudaGraphNode_t cnode = nullptr;
-            cudaGraph_t body = nullptr;
-            if (ok) {
-                cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-                cp.conditional.handle = h;
-                cp.conditional.type = cudaGraphCondTypeWhile;
-                cp.conditional.size = 1;
-                ok = cudaGraphAddNode(&cnode, cg, deps, nullptr, ndeps, &cp) == cudaSuccess;
-                if (ok) body = cp.conditional.phGraph_out[0];
+            cs = st;
+            enqueue_init(Cond{h1, 1});
+            ok = add_while(h1);
+            if (ok && dw) {
+                enqueue_replace(Cond{h2, 1});
+                ok = add_while(h2);
             }
-            if (ok)
-                ok = cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1,
-                                                         cudaStreamSetCaptureDependencies) == cudaSuccess;
             cudaGraph_t outg = nullptr;
             const bool ended = cudaStreamEndCapture(st, &outg) == cudaSuccess;
-            ok = ok && ended;
-            if (ok) {
-                ok = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
-                                                   cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-                if (ok) {
-                    enqueue_body(cond);
-                    cudaGraph_t bg = nullptr;
-                    ok = cudaStreamEndCapture(st, &bg) == cudaSuccess;
-                }
-            }
+            ok = ok && ended && launch_error == cudaSuccess;
             if (ok) ok = cudaGraphInstantiate(&gx_solve, graph, 0) == cudaSuccess;
         }
     }
+    cs = st;
     cudaGraphDestroy(graph);
     if (ok) {
         have_cond = true;
         return CT_OK;
     }
     cudaGetLastError();  // clear the failed attempt
+    if (launch_error != cudaSuccess)
+        return fail(CT_CUDA_ERROR, "V-cycle kernel launch failed while recording: %s",
+                    cudaGetErrorString(launch_error));
     if (gx_solve) {
         cudaGraphExecDestroy(gx_solve);
         gx_solve = nullptr;
     }
-    // Fallback: the two parts as plain graphs, polled by the host.
+    // Fallback: the parts as plain graphs, polled by the host.
     const Cond none{0, 0};
-    for (int part_i = 0; part_i < 2; ++part_i) {
+    for (int part_i = 0; part_i < (dw ? 3 : 2); ++part_i) {
         cudaGraph_t g = nullptr;
         CT_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         if (part_i == 0)
             enqueue_init(none);
-        else
+        else if (part_i == 1)
             enqueue_body(none);
+        else
+            enqueue_replace(none);
         CT_CK(cudaStreamEndCapture(st, &g));
-        const cudaError_t e = cudaGraphInstantiate(part_i == 0 ? &gx_init : &gx_body, g, 0);
+        cudaGraphExec_t* dst = part_i == 0 ? &gx_init : (part_i == 1 ? &gx_body : &gx_replace);
+        const cudaError_t e = cudaGraphInstantiate(dst, g, 0);
         cudaGraphDestroy(g);
         CT_CK(e);
     }
@@ -506,38 +638,45 @@ ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
     c.tol = tol;
     c.maxit = maxit;
     c.inv_dt = inv_dt;
+    c.stop = dw ? std::max(tol, rr_thr) : tol;
+    c.x_zero = x_zero ? 1 : 0;
+    x_zero = false;
     *h_ctl = c;
     CT_CK(cudaMemcpyAsync(ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
     const Cond none{0, 0};
-    if (prof) {
-        enqueue_init(none);
-        for (int it = 0; it <= maxit; ++it) {
-            CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-            CT_CK(cudaStreamSynchronize(st));
-            if (h_ctl->done) break;
-            enqueue_body(none);
-        }
-    } else if (have_cond) {
+    cs = st;
+    if (have_cond && !prof) {
         CT_CK(cudaGraphLaunch(gx_solve, st));
-    } else if (gx_init) {
-        CT_CK(cudaGraphLaunch(gx_init, st));
-        int launched = 0;
-        int k = 2;
+    } else {
+        // Host-driven loop: direct launches (profiling, ct_use_graphs(0)) or
+        // the part graphs, with a host check after every body (direct) or
+        // after a few (graphs); the double-word mode's replacement step runs
+        // when the first phase ends.
+        const bool graphs = gx_init && !prof;
+        if (graphs)
+            CT_CK(cudaGraphLaunch(gx_init, st));
+        else
+            enqueue_init(none);
+        int launched = 0, k = graphs ? 2 : 1;
         while (true) {
             CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
             CT_CK(cudaStreamSynchronize(st));
-            if (h_ctl->done || launched > maxit) break;
-            for (int q = 0; q < k; ++q) CT_CK(cudaGraphLaunch(gx_body, st));
+            if (h_ctl->done || launched > maxit + 2) break;
+            if (h_ctl->phase_end) {
+                if (graphs)
+                    CT_CK(cudaGraphLaunch(gx_replace, st));
+                else
+                    enqueue_replace(none);
+                continue;
+            }
+            for (int q = 0; q < k; ++q) {
+                if (graphs)
+                    CT_CK(cudaGraphLaunch(gx_body, st));
+                else
+                    enqueue_body(none);
+            }
             launched += k;
-            k = std::min(k * 2, 8);
-        }
-    } else {
-        enqueue_init(none);
-        for (int it = 0; it <= maxit; ++it) {
-            CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-            CT_CK(cudaStreamSynchronize(st));
-            if (h_ctl->done) break;
-            enqueue_body(none);
+            if (graphs) k = std::min(k * 2, 8);
         }
     }
     CT_CK(cudaGetLastError());
@@ -630,6 +769,7 @@ ct_status ct_set_dt(ct_solver* s, double dt) {
 
 ct_status ct_set_x_zero(ct_solver* s) {
     CT_SOLVER_OK(s);
+    s->impl.x_zero = true;
     CT_CUDA(cudaMemsetAsync(s->impl.x, 0, (size_t)s->impl.n * 8, s->impl.st));
     return CT_OK;
 }
@@ -637,9 +777,13 @@ ct_status ct_set_x_zero(ct_solver* s) {
 ct_status ct_set_x(ct_solver* s, const double* T) {
     CT_SOLVER_OK(s);
     if (!T) return fail(CT_BAD_ARG, "ct_set_x: null");
+    s->impl.x_zero = false;
     ct::Solver& v = s->impl;
     CT_CUDA(cudaMemcpyAsync(v.nat, T, v.ncells * 8, cudaMemcpyHostToDevice, v.st));
-    ct::launch_to_split_d(v.st, v.g0, v.nat, v.x);
+    if (v.dw)
+        ct::launch_natural_to_dw(v.st, v.g0, v.nat, v.xw());
+    else
+        ct::launch_to_split_d(v.st, v.g0, v.nat, v.x);
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaStreamSynchronize(v.st));
     return CT_OK;
@@ -655,7 +799,8 @@ ct_status ct_set_rhs_steady(ct_solver* s) {
 ct_status ct_set_rhs_transient(ct_solver* s) {
     CT_SOLVER_OK(s);
     ct::Solver& v = s->impl;
-    ct::launch_rhs_transient(v.st, v.n, v.cap, v.inv_dt, v.P, v.x, v.b, v.xold);
+    const double* xd = v.x_as_double(v.xold);  // in place when the x_old copy is the conversion
+    ct::launch_rhs_transient(v.st, v.n, v.cap, v.inv_dt, v.P, xd, v.b, v.xold);
     CT_CUDA(cudaGetLastError());
     return CT_OK;
 }
@@ -689,7 +834,10 @@ ct_status ct_get_x(ct_solver* s, double* T) {
     CT_SOLVER_OK(s);
     if (!T) return fail(CT_BAD_ARG, "ct_get_x: null");
     ct::Solver& v = s->impl;
-    ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
+    if (v.dw)
+        ct::launch_dw_to_natural(v.st, v.g0, v.xw(), v.nat);
+    else
+        ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaMemcpyAsync(T, v.nat, v.ncells * 8, cudaMemcpyDeviceToHost, v.st));
     CT_CUDA(cudaStreamSynchronize(v.st));
@@ -700,7 +848,10 @@ ct_status ct_device_x(ct_solver* s, const double** T_dev) {
     CT_SOLVER_OK(s);
     if (!T_dev) return fail(CT_BAD_ARG, "ct_device_x: null");
     ct::Solver& v = s->impl;
-    ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
+    if (v.dw)
+        ct::launch_dw_to_natural(v.st, v.g0, v.xw(), v.nat);
+    else
+        ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaStreamSynchronize(v.st));
     *T_dev = v.nat;
@@ -725,7 +876,7 @@ ct_status ct_true_relres(ct_solver* s, double* out) {
     CT_SOLVER_OK(s);
     if (!out) return fail(CT_BAD_ARG, "ct_true_relres: null");
     ct::Solver& v = s->impl;
-    ct::launch_true_residual(v.st, v.op(), v.P, v.x, v.ctl, v.red_cols(ct::SL_AUX));
+    ct::launch_true_residual(v.st, v.op(), v.P, v.x_as_double(v.Ap), v.ctl, v.red_cols(ct::SL_AUX));
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaMemcpyAsync(v.h_ctl, v.ctl, sizeof(ct::Ctl), cudaMemcpyDeviceToHost, v.st));
     CT_CUDA(cudaStreamSynchronize(v.st));
@@ -737,7 +888,7 @@ ct_status ct_solver_step_record(ct_solver* s, double dt, ct_step_record* out) {
     CT_SOLVER_OK(s);
     if (!out || !(dt > 0)) return fail(CT_BAD_ARG, "ct_solver_step_record: null output or dt <= 0");
     ct::Solver& v = s->impl;
-    ct::launch_step_record(v.st, v.op(), v.x, v.xold, v.ctl, v.red_cols(ct::SL_AUX));
+    ct::launch_step_record(v.st, v.op(), v.x_as_double(v.Ap), v.xold, v.ctl, v.red_cols(ct::SL_AUX));
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaMemcpyAsync(v.h_ctl, v.ctl, sizeof(ct::Ctl), cudaMemcpyDeviceToHost, v.st));
     CT_CUDA(cudaStreamSynchronize(v.st));

@@ -348,6 +348,7 @@ class Precision(enum.IntEnum):
     MG_FP64 = 0       # plain FP64 MG-PCG (reference -DMG_DOUBLE)
     MG_FP32 = 1       # float V-cycle, Fletcher-Reeves beta (reference default)
     MG_FP32_FLEX = 2  # float V-cycle inside flexible PCG
+    MG_FP32_FLEX_DW = 3  # same, outer iteration in double-word arithmetic on FP32 pipes
 
 
 @dataclass

@@ -46,13 +46,25 @@ typedef enum ct_status {
 typedef enum ct_precond { CT_JACOBI = 0, CT_MULTIGRID = 1 } ct_precond;
 
 /* Precision of the V-cycle and form of beta. The outer PCG (residual, iterate
- * updates, dot products, alpha, beta) is FP64 in every mode.
+ * updates, dot products, alpha, beta) is FP64 in the first three modes.
  *  CT_MG_FP64      V-cycle in double, beta = rz_new / rz: the reference built
  *                  with -DMG_DOUBLE (src/pcg3d.h:30-34), the plain FP64 method.
  *  CT_MG_FP32      V-cycle in float, same beta: the reference's default build.
  *  CT_MG_FP32_FLEX V-cycle in float inside flexible PCG, beta =
- *                  -(z_new . Ap) / (p . Ap) (Polak-Ribiere form). */
-typedef enum ct_precision { CT_MG_FP64 = 0, CT_MG_FP32 = 1, CT_MG_FP32_FLEX = 2 } ct_precision;
+ *                  -(z_new . Ap) / (p . Ap) (Polak-Ribiere form).
+ *  CT_MG_FP32_FLEX_DW  as CT_MG_FP32_FLEX, but the outer iterate updates,
+ *                  operator apply and dot products run in double-word
+ *                  (float-pair, ~48-bit) arithmetic on the FP32 pipes, with
+ *                  the residual recomputed once in FP64 when ||r||/||b|| first
+ *                  drops below 1e-5 (residual replacement), so the FP64 true
+ *                  residual still meets tol. The FP64 residual, alpha, beta,
+ *                  dot-product totals and energy balance stay FP64. */
+typedef enum ct_precision {
+    CT_MG_FP64 = 0,
+    CT_MG_FP32 = 1,
+    CT_MG_FP32_FLEX = 2,
+    CT_MG_FP32_FLEX_DW = 3
+} ct_precision;
 
 /* A finalized Model3D's arrays (src/stack3d.h:45-79): gE, gN, gU, cap have
  * nx*ny*nz entries, gB nx*ny, P nx*ny*nz. dx, dy (m) are the lateral cell

@@ -67,6 +67,7 @@ def lib():
     L.oracle_solve.restype = C.c_int
     L.oracle_solve.argtypes = [vp, C.c_double, C.c_int, ip, dp]
     L.oracle_get_x.argtypes = [vp, _f64p]
+    L.oracle_set_outer_df.argtypes = [vp, C.c_int]
     L.oracle_num_levels.restype = C.c_int
     L.oracle_num_levels.argtypes = [vp]
     L.oracle_level_dims.argtypes = [vp, C.c_int, ip, ip, ip]
@@ -116,13 +117,15 @@ class Solver:
     "multigrid"; mg_double selects the -DMG_DOUBLE arithmetic; flexible the
     flexible (Polak-Ribiere) beta."""
 
-    def __init__(self, m, precond="multigrid", mg_double=True, flexible=False):
+    def __init__(self, m, precond="multigrid", mg_double=True, flexible=False, outer_df=False):
         self._m = _ModelRef(m)
         self.n = self._m.n
         self._h = lib().oracle_create(self._m.ref(), 1 if precond == "multigrid" else 0,
                                       int(bool(mg_double)), int(bool(flexible)))
         if not self._h:
             raise ValueError("oracle_create rejected the model")
+        if outer_df:
+            lib().oracle_set_outer_df(self._h, 1)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -182,9 +185,9 @@ class Solver:
 
 
 def solve_steady(m, tol=1e-10, maxit=50000, precond="multigrid", mg_double=True,
-                 flexible=False) -> SolveResult:
+                 flexible=False, outer_df=False) -> SolveResult:
     """cpu_pcg (src/pcg3d_cpu.cpp:187-205): steady solve from T = 0."""
-    s = Solver(m, precond, mg_double, flexible)
+    s = Solver(m, precond, mg_double, flexible, outer_df)
     s.set_x_zero()
     s.set_rhs_steady()
     it, rel, conv = s.solve(tol, maxit)

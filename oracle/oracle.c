@@ -40,6 +40,7 @@ typedef struct hlevel {
 struct oracle_solver {
     oracle_model m; /* fine operator (borrowed), P points at the copy below */
     int precond, mg_double, flexible;
+    int outer_df;   /* outer vectors and updates in double-float (see below) */
     size_t n;
     double inv_dt;
     double *P, *x, *b, *r, *z, *p, *Ap, *invd;
@@ -274,8 +275,157 @@ static double dot(const double* a, const double* b, size_t n) {
     return s;
 }
 
+
+/* ---- double-float outer iteration ------------------------------------------
+ * An extension for the GPU library's FP32-pipe outer mode, not in the
+ * reference: x, r, p, Ap and the diagonal are float pairs (hi + lo, about 48
+ * significant bits) combined with error-free transformations (TwoSum,
+ * Fast2Sum, FMA-based TwoProd, after Joldes, Muller and Popescu 2017), so that
+ * the outer iteration runs on FP32 units; dots and alpha, beta are double. */
+typedef struct dfl {
+    float h, l;
+} dfl;
+
+static inline dfl df_two_sum(float a, float b) {
+    const float s = a + b, bp = s - a, ap = s - bp;
+    const float t = (a - ap) + (b - bp);
+    dfl r = {s, t};
+    return r;
+}
+static inline dfl df_fast(float a, float b) {
+    const float s = a + b;
+    dfl r = {s, b - (s - a)};
+    return r;
+}
+static inline dfl df_of(double d) {
+    const float h = (float)d;
+    dfl r = {h, (float)(d - (double)h)};
+    return r;
+}
+static inline double df_d(dfl x) { return (double)x.h + (double)x.l; }
+static inline dfl df_add(dfl a, dfl b) {
+    const dfl s = df_two_sum(a.h, b.h);
+    return df_fast(s.h, s.l + (a.l + b.l));
+}
+static inline dfl df_neg(dfl a) {
+    dfl r = {-a.h, -a.l};
+    return r;
+}
+static inline dfl df_mul_f(dfl a, float b) {
+    const float p = a.h * b;
+    float e = fmaf(a.h, b, -p);
+    e = fmaf(a.l, b, e);
+    return df_fast(p, e);
+}
+static inline dfl df_mul(dfl a, dfl b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return df_fast(p, e);
+}
+
+void oracle_set_outer_df(oracle_solver* s, int on) { s->outer_df = on; }
+
+/* Ap = d p - sum of G p_nbr with the diagonal in double-float. */
+static void df_apply(const oracle_model* o, const dfl* dg, const dfl* p, dfl* Ap, double* pAp) {
+    const size_t sxy = (size_t)o->nx * o->ny;
+    double acc = 0;
+    for (int l = 0; l < o->nz; ++l)
+        for (int j = 0; j < o->ny; ++j)
+            for (int i = 0; i < o->nx; ++i) {
+                const size_t c = (size_t)l * sxy + (size_t)j * o->nx + i;
+                dfl off = {0.0f, 0.0f};
+                if (i > 0) off = df_add(off, df_mul_f(p[c - 1], o->gE[c - 1]));
+                if (i < o->nx - 1) off = df_add(off, df_mul_f(p[c + 1], o->gE[c]));
+                if (j > 0) off = df_add(off, df_mul_f(p[c - o->nx], o->gN[c - o->nx]));
+                if (j < o->ny - 1) off = df_add(off, df_mul_f(p[c + o->nx], o->gN[c]));
+                if (l > 0) off = df_add(off, df_mul_f(p[c - sxy], o->gU[c - sxy]));
+                if (l < o->nz - 1) off = df_add(off, df_mul_f(p[c + sxy], o->gU[c]));
+                Ap[c] = df_add(df_mul(dg[c], p[c]), df_neg(off));
+                acc += df_d(p[c]) * df_d(Ap[c]);
+            }
+    *pAp = acc;
+}
+
+/* PCG with the outer iteration in double-float; same recurrence as
+ * oracle_solve (flexible beta when s->flexible). */
+static int solve_df(oracle_solver* s, double tol, int maxit, int* iters, double* relres) {
+    const oracle_model* o = &s->m;
+    const size_t n = s->n;
+    for (int l = 0; l < o->nz; ++l)
+        for (int j = 0; j < o->ny; ++j)
+            for (int i = 0; i < o->nx; ++i) {
+                const size_t c = ((size_t)l * o->ny + j) * o->nx + i;
+                s->r[c] = s->b[c] - op_apply_d(o, s->x, i, j, l, s->inv_dt);
+            }
+    const double bb = dot(s->b, s->b, n);
+    double rr = dot(s->r, s->r, n);
+    *iters = 0;
+    *relres = 0;
+    if (bb == 0) {
+        oracle_set_x_zero(s);
+        return 1;
+    }
+    *relres = sqrt(rr / bb);
+    if (*relres < tol) return 1;
+    dfl* x = (dfl*)malloc(n * sizeof(dfl));
+    dfl* r = (dfl*)malloc(n * sizeof(dfl));
+    dfl* p = (dfl*)malloc(n * sizeof(dfl));
+    dfl* Ap = (dfl*)malloc(n * sizeof(dfl));
+    dfl* dg = (dfl*)malloc(n * sizeof(dfl));
+    for (int l = 0; l < o->nz; ++l)
+        for (int j = 0; j < o->ny; ++j)
+            for (int i = 0; i < o->nx; ++i) {
+                const size_t c = ((size_t)l * o->ny + j) * o->nx + i;
+                dg[c] = df_of(op_diag_d(o, i, j, l, s->inv_dt));
+            }
+    for (size_t c = 0; c < n; ++c) {
+        x[c] = df_of(s->x[c]);
+        r[c] = df_of(s->r[c]);
+    }
+    int converged = 0;
+    double rz = 0, pAp = 0;
+    for (int it = 1; it <= maxit; ++it) {
+        for (size_t c = 0; c < n; ++c) s->r[c] = r[c].h;  /* V-cycle input: float r */
+        precondition(s);                                    /* z in s->z */
+        double rz_new = 0, zAp = 0;
+        for (size_t c = 0; c < n; ++c) {
+            rz_new += df_d(r[c]) * s->z[c];
+            zAp += s->z[c] * df_d(Ap[c]);
+        }
+        if (it == 1) {
+            for (size_t c = 0; c < n; ++c) p[c] = df_of(s->z[c]);
+        } else {
+            const double beta = s->flexible ? -zAp / pAp : rz_new / rz;
+            const dfl bdf = df_of(beta);
+            for (size_t c = 0; c < n; ++c) p[c] = df_add(df_mul(bdf, p[c]), df_of(s->z[c]));
+        }
+        rz = rz_new;
+        df_apply(o, dg, p, Ap, &pAp);
+        const dfl a = df_of(rz / pAp);
+        rr = 0;
+        for (size_t c = 0; c < n; ++c) {
+            x[c] = df_add(x[c], df_mul(a, p[c]));
+            r[c] = df_add(r[c], df_neg(df_mul(a, Ap[c])));
+            const double rv = df_d(r[c]);
+            rr += rv * rv;
+        }
+        *iters = it;
+        *relres = sqrt(rr / bb);
+        if (*relres < tol) {
+            converged = 1;
+            break;
+        }
+    }
+    for (size_t c = 0; c < n; ++c) s->x[c] = df_d(x[c]);
+    free(x); free(r); free(p); free(Ap); free(dg);
+    return converged;
+}
+
 /* CpuPcg::solve (src/pcg3d_cpu.cpp:126-185). */
 int oracle_solve(oracle_solver* s, double tol, int maxit, int* iters, double* relres) {
+    if (s->outer_df) return solve_df(s, tol, maxit, iters, relres);
     const oracle_model* o = &s->m;
     const size_t n = s->n;
     for (int l = 0; l < o->nz; ++l)

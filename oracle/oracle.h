@@ -49,6 +49,10 @@ void oracle_set_power(oracle_solver* s, const double* P);
 /* Returns 1 when converged. iters / relres as the reference's PcgStats. */
 int oracle_solve(oracle_solver* s, double tol, int maxit, int* iters, double* relres);
 void oracle_get_x(const oracle_solver* s, double* T);
+/* Outer iteration in double-float (float pairs on FP32 arithmetic) instead of
+ * double: the arithmetic of the GPU library's FP32-pipe outer mode. Not in
+ * the reference. */
+void oracle_set_outer_df(oracle_solver* s, int on);
 
 /* Multigrid hierarchy (natural layout, as src/mg3d.h:259-295). */
 int oracle_num_levels(const oracle_solver* s);

@@ -61,11 +61,12 @@ def test_fp32_mg_matches_oracle(ct, orc, golden, name):
     assert np.abs(T - ref.T).max() <= 1e-7 * np.abs(ref.T).max()
 
 
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW"])
 @pytest.mark.parametrize("name", CASES)
-def test_fp32_flexible_within_bound_of_fp64(ct, orc, golden, name):
+def test_fp32_flexible_within_bound_of_fp64(ct, orc, golden, name, prec):
     m = build_spec_model(ct, golden["cases"][name]["spec"])
     ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
-    st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX)
+    st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, getattr(ct.Precision, prec))
     assert st.converged
     dT = np.abs(T - ref.T).max()
     assert dT <= DT_BOUND_K
@@ -110,11 +111,12 @@ def test_levels_and_factors_bitwise(ct, orc, golden, name):
                     np.testing.assert_array_equal(finv, ofinv)
 
 
-def test_graphs_match_direct_launches_bitwise(ct, golden):
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
+def test_graphs_match_direct_launches_bitwise(ct, golden, prec):
     """verify 4 (src/main3d.cu:212-222), tightened: graph replay and direct
     launches give the same bits through a transient where 1/dt changes."""
     m = build_spec_model(ct, golden["cases"]["blocks_tsv_40x24"]["spec"])
-    o = ct.TransientOptions(t_end=0.02, growth=1.2, precision=ct.Precision.MG_FP32_FLEX)
+    o = ct.TransientOptions(t_end=0.02, growth=1.2, precision=getattr(ct.Precision, prec))
     a = ct.run_transient(m, o)
     ct.gpu_use_graphs(False)
     try:
@@ -146,11 +148,12 @@ def test_transient_matches_oracle(ct, orc, golden, prec, mgd):
     assert np.abs(g.T - r.T).max() <= 1e-7 * np.abs(r.T).max()
 
 
-def test_device_records_match_host_records(ct, golden):
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW"])
+def test_device_records_match_host_records(ct, golden, prec):
     spec = dict(golden["cases"]["hotspot64"]["spec"])
     spec["nx"] = spec["ny"] = 24
     m = build_spec_model(ct, spec)
-    o = ct.TransientOptions(t_end=0.005, growth=1.3)
+    o = ct.TransientOptions(t_end=0.005, growth=1.3, precision=getattr(ct.Precision, prec))
     a = ct.run_transient(m, o, device_records=True)
     b = ct.run_transient(m, o, device_records=False)
     for x, y in zip(a.steps, b.steps):
@@ -160,9 +163,10 @@ def test_device_records_match_host_records(ct, golden):
         assert abs(x.q_stored - y.q_stored) <= 1e-9 * max(1.0, abs(y.q_stored))
 
 
-def test_true_relres_on_device(ct, orc, golden):
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW"])
+def test_true_relres_on_device(ct, orc, golden, prec):
     m = build_spec_model(ct, golden["cases"]["blocks_tsv_40x24"]["spec"])
-    with ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX) as s:
+    with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
         s.set_x_zero()
         s.set_rhs_steady()
         s.solve(1e-6, 100)
@@ -172,10 +176,11 @@ def test_true_relres_on_device(ct, orc, golden):
     assert abs(dev - host) <= 1e-6 * host
 
 
-def test_zero_power_gives_zero(ct):
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW"])
+def test_zero_power_gives_zero(ct, prec):
     m = ct.default_model(16, 16)
     ct.finalize(m)
-    with ct.GpuPcg(m) as s:
+    with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
         s.set_x(np.ones(m.ncells()))
         s.set_rhs_steady()
         st = s.solve(1e-10, 100)
@@ -183,11 +188,12 @@ def test_zero_power_gives_zero(ct):
         assert np.all(s.get_x() == 0)
 
 
-def test_power_roundtrip_and_warm_start(ct, orc):
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW"])
+def test_power_roundtrip_and_warm_start(ct, orc, prec):
     import workloads
     m = workloads.steady_hotspot(48, seed=7)
     ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
-    with ct.GpuPcg(m) as s:
+    with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
         s.set_x_zero()
         s.set_rhs_steady()
         s.solve(1e-10, 100)
@@ -218,13 +224,25 @@ def test_singular_stack_reports_status_not_hang(ct):
         assert st.iters <= 200
 
 
-def test_nan_power_is_breakdown(ct):
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
+def test_nan_power_is_breakdown(ct, prec):
     m = ct.default_model(8, 8)
     ct.add_uniform_power(m, 0, 1.0)
     ct.finalize(m)
     m.P[5] = np.nan
-    with ct.GpuPcg(m) as s:
+    with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
         s.set_x_zero()
         s.set_rhs_steady()
         st = s.solve(1e-10, 50)
         assert st.breakdown and not st.converged
+
+
+def test_dw_true_residual_meets_tol_on_larger_grid(ct, orc):
+    """The double-word mode's FP64 residual replacement: the FP64 true residual
+    of a 256 x 256 solve meets tol, as the plain FP64 solve's does."""
+    import workloads
+    m = workloads.steady_hotspot(256, seed=3)
+    for prec in (ct.Precision.MG_FP32_FLEX_DW, ct.Precision.MG_FP32_FLEX):
+        st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, prec)
+        assert st.converged
+        assert orc.true_relres(m, T) <= 1.5e-10
