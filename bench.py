@@ -2,14 +2,17 @@
 
 Workload (a "step"): one steady solve from T = 0 to ||r|| / ||P|| < 1e-10 of
 the 800 x 800 x 10 two-tier stack (25 W per Si tier + a seeded 3 W, 1 mm
-hotspot), with the FP32 V-cycle inside FP64 flexible PCG, the operator and
-multigrid hierarchy resident in HBM (built once, outside the timed region, as
-in a power-map sweep). Inputs are larger than L2 (the fine level alone moves
-~1.7 GB per iteration), so no L2 flush is needed between steps.
+hotspot), FP32 V-cycle inside flexible PCG whose outer iteration runs in
+double-word arithmetic on the FP32 pipes with one FP64 residual replacement
+(CT_MG_FP32_FLEX_DW), the operator and multigrid hierarchy resident in HBM
+(built once, outside the timed region, as in a power-map sweep). Inputs are
+larger than L2 (the fine level alone moves > 1 GB per iteration), so no L2
+flush is needed between steps.
 
-Reported beside it, on the same GPU: the plain FP64 MG-PCG (FP64 V-cycle)
-solves/s, max|dT| between the two, the end-to-end rate through the C ABI
-with the power map copied in and the temperatures copied out every step, the
+Reported beside it, on the same GPU: the FP32 V-cycle in FP64 flexible PCG
+(CT_MG_FP32_FLEX), the plain FP64 MG-PCG (FP64 V-cycle), max|dT| and the
+FP64 true residual of each, the end-to-end rate through the C ABI with the
+power map copied in and the temperatures copied out every step, the
 per-kernel roofline of the dominant kernel, and the CPU oracle (a C
 restatement of the reference CPU solver) timed on this machine's host cores.
 
@@ -284,30 +287,42 @@ def main():
     m = workloads.steady_hotspot(N_GRID, seed=SEED)
     ncells = m.ncells()
 
-    s32 = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX)
+    s32 = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX_DW)
+    sfx = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX)
     s64 = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP64)
     for _ in range(args.warmup):
-        for s in (s32, s64):
+        for s in (s32, sfx, s64):
             s.set_x_zero()
             s.set_rhs_steady()
             s.solve(TOL, MAXIT)
 
-    # ---- headline: FP32 V-cycle in flexible FP64 PCG, device-resident -----
+    # ---- headline: FP32 V-cycle, double-word flexible PCG, device-resident -
     clocks = ClockSampler(local)
     clocks.start()
     ms32, st32 = timed_solves(ct, s32, args.steps, world)
     clk = clocks.stop()
     T32 = s32.get_x()
+    true32 = s32.true_relres()
     ms32 = max_over_ranks(ms32, world)
     value = sum_over_ranks(args.steps, world) / (ms32 / 1e3)
+
+    # ---- FP32 V-cycle in FP64 flexible PCG -----------------------------------
+    kfx = max(3, args.steps // 2)
+    msfx, stfx = timed_solves(ct, sfx, kfx, world)
+    Tfx = sfx.get_x()
+    truefx = sfx.true_relres()
+    msfx = max_over_ranks(msfx, world)
+    valuefx = sum_over_ranks(kfx, world) / (msfx / 1e3)
 
     # ---- plain FP64 MG-PCG on the same GPU ---------------------------------
     k64 = max(3, args.steps // 2)
     ms64, st64 = timed_solves(ct, s64, k64, world)
     T64 = s64.get_x()
+    true64 = s64.true_relres()
     ms64 = max_over_ranks(ms64, world)
     value64 = sum_over_ranks(k64, world) / (ms64 / 1e3)
     max_dT = float(np.abs(T32 - T64).max())
+    max_dT_fx = float(np.abs(Tfx - T64).max())
 
     # ---- end to end through the C ABI: host P in, host T out -------------
     P_host = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
@@ -345,8 +360,7 @@ def main():
     alg_bytes_solve = sum(r["bytes"] for r in rows)
     iters = st32[-1].iters
     nlev = s32.num_levels()
-    body_kernels = 4 + 5 * (nlev - 1) + 1
-    launches_per_solve = 1 + iters * body_kernels
+    launches_per_solve = sum(r["launches"] for r in rows)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -363,14 +377,20 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64+f32", "data": "synthetic",
             "config": {"workload": f"steady solve {N_GRID}x{N_GRID}x10 two-tier stack, seeded "
-                                   f"3 W hotspot, tol {TOL:g}, FP32 V-cycle in FP64 flexible PCG",
+                                   f"3 W hotspot, tol {TOL:g}, FP32 V-cycle in flexible PCG, "
+                                   f"double-word outer on FP32 pipes + FP64 residual replacement",
+                       "precision": "CT_MG_FP32_FLEX_DW",
                        "cells": ncells, "levels": nlev, "iters": iters,
                        "l2": "inputs larger than L2 (fine level ~1.7 GB moved per iteration)",
                        "parallelism": f"replicas x{world}"},
             "fp64_mg_pcg": {"value": value64, "unit": "solves/s", "iters": st64[-1].iters,
-                            "ms_per_solve": ms64 / k64},
+                            "ms_per_solve": ms64 / k64, "true_relres": true64},
+            "fp32_mg_fp64_outer": {"value": valuefx, "unit": "solves/s", "iters": stfx[-1].iters,
+                                   "ms_per_solve": msfx / kfx, "true_relres": truefx,
+                                   "max_dT_K": max_dT_fx, "speedup_vs_fp64": valuefx / value64},
             "speedup_vs_fp64": value / value64,
             "max_dT_K": max_dT,
+            "true_relres": true32,
             "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved,
                          "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                          "peak_kind": peak_kind, "traffic": traffic,
@@ -392,6 +412,7 @@ def main():
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)
     s32.close()
+    sfx.close()
     s64.close()
     if world > 1:
         import torch.distributed as td

@@ -12,12 +12,17 @@
 // accumulated in double words per thread and in FP64 per block; alpha and beta
 // stay FP64 scalars on the device.
 //
-// The recurrence residual of a 48-bit iteration drifts from the true residual
-// by ~2^-48 times the operator's cancellation (up to ~1e4 here), which would
-// leave ||P - A T|| / ||P|| near 1e-10 on large grids. So the solve recomputes
-// r = b - A x once in FP64 (k_residual_x, "residual replacement") when the
-// recurrence first passes a threshold (1e-5 by default); the drift after that
-// is five orders of magnitude smaller, and the true FP64 residual meets tol.
+// Two limits of 48 bits, and how they are lifted:
+//  - the recurrence residual drifts from the true residual by ~2^-48 times the
+//    operator's cancellation (up to ~1e4 here). So the solve recomputes
+//    r = b - A x once in FP64 (k_residual_x, "residual replacement") when the
+//    recurrence first passes a threshold (1e-5 by default);
+//  - a 48-bit x cannot hold T (~50 K) finely enough for ||P - A T|| / ||P|| to
+//    reach 1e-10 where lateral conductances are large (the copper spreader).
+//    So x is an FP64 base xb plus a double-word correction xw: the iteration
+//    updates xw, and k_fold adds xw into xb (in FP64) before every FP64
+//    residual - at the start and at the replacement - after which xw only
+//    carries the small remaining correction.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -111,7 +116,7 @@ __device__ __forceinline__ Col col_of_slot(const Geo& g, unsigned s) {
 // converged).
 __global__ void __launch_bounds__(NT)
     k_residual_x(OpView o, const double* __restrict__ diag, const double* __restrict__ b,
-                 const float2* __restrict__ x, float2* __restrict__ r, float* __restrict__ b0,
+                 const double* __restrict__ x, float2* __restrict__ r, float* __restrict__ b0,
                  int start, Ctl* ctl, double* part, int maxb, Cond cond) {
     if (!start && *(volatile const int*)&ctl->done) {  // converged or stopped in phase 1
         if (cond.use && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond.h, 0u);
@@ -141,18 +146,18 @@ __global__ void __launch_bounds__(NT)
             }
             continue;
         }
-        double x_c = dw_d(x[c.s]), x_b = 0.0;
+        double x_c = x[c.s], x_b = 0.0;
         float gu_b = 0.0f;
         for (int l = 0; l < g.nz; ++l) {
             const unsigned base = (unsigned)l * g.plane, id = base + c.s;
             const bool up = l < g.nz - 1;
-            const double x_a = up ? dw_d(x[id + g.plane]) : 0.0;
+            const double x_a = up ? x[id + g.plane] : 0.0;
             const float gu = o.gU[id];
             double off = 0.0;
-            if (c.i > 0) off += (double)o.gE[base + c.sw] * dw_d(x[base + c.sw]);
-            if (c.i < g.nx - 1) off += (double)o.gE[id] * dw_d(x[base + c.se]);
-            if (c.j > 0) off += (double)o.gN[base + c.ss] * dw_d(x[base + c.ss]);
-            if (c.j < g.ny - 1) off += (double)o.gN[id] * dw_d(x[base + c.sn]);
+            if (c.i > 0) off += (double)o.gE[base + c.sw] * x[base + c.sw];
+            if (c.i < g.nx - 1) off += (double)o.gE[id] * x[base + c.se];
+            if (c.j > 0) off += (double)o.gN[base + c.ss] * x[base + c.ss];
+            if (c.j < g.ny - 1) off += (double)o.gN[id] * x[base + c.sn];
             if (l > 0) off += (double)gu_b * x_b;
             if (up) off += (double)gu * x_a;
             const double bi = b[id];
@@ -409,6 +414,24 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
+// xb += xw (in FP64), xw = 0: the double-word correction goes into the base.
+// Skipped (all blocks) once the solve is done; runs before the residual
+// replacement, which is what it serves.
+__global__ void k_fold(unsigned n2, double2* __restrict__ xb, float4* __restrict__ xw,
+                       const Ctl* ctl, int check_done) {
+    if (check_done && *(volatile const int*)&ctl->done) return;
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
+        const float4 w = xw[k];
+        if (w.x != 0.0f || w.z != 0.0f) {
+            double2 v = xb[k];
+            v.x += dw_d(make_float2(w.x, w.y));
+            v.y += dw_d(make_float2(w.z, w.w));
+            xb[k] = v;
+            xw[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
 // ---- conversions at the boundary -------------------------------------------
 
 // FP64 diagonal -> double word.
@@ -458,8 +481,15 @@ unsigned blocks_of(size_t n) {
 
 }  // namespace
 
+void launch_fold(cudaStream_t st, unsigned n, double* xb, float2* xw, const Ctl* ctl,
+                 bool check_done) {
+    static const int wb = wave_blocks(k_fold, 1 << 30);
+    k_fold<<<std::min((int)blocks_of(n / 2), wb), NT, 0, st>>>(n / 2, (double2*)xb, (float4*)xw, ctl,
+                                                               check_done ? 1 : 0);
+}
+
 void launch_residual_x(cudaStream_t st, const OpView& o, const double* diag, const double* b,
-                       const float2* x, float2* r, float* b0, bool start, Ctl* ctl,
+                       const double* x, float2* r, float* b0, bool start, Ctl* ctl,
                        const Red& red, Cond cond) {
     static const int wb = wave_blocks(k_residual_x, 1 << 30);
     k_residual_x<<<std::min(red.blocks, wb), NT, 0, st>>>(o, diag, b, x, r, b0, start ? 1 : 0, ctl, red.part,

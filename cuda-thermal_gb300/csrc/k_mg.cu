@@ -452,14 +452,18 @@ __global__ void __launch_bounds__(kSmallThreads, 1)
     const unsigned tid = threadIdx.x, nth = kSmallThreads;
     const T inv_dt = (T)ctl->inv_dt;
     const int last = sl.n - 1;
+    // Each phase works on register copies of the level views: the views live
+    // in shared memory, where the sweeps also store x through generic
+    // pointers, so reading them in place would reload every field after
+    // every store.
     for (int k = 0; k < last; ++k) {
-        const LevelView<T>& L = sl.L[k];
+        const LevelView<T> L = sl.L[k];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
         for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
         __syncthreads();
         for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 1, q);
         __syncthreads();
-        const LevelView<T>& C = sl.L[k + 1];
+        const LevelView<T> C = sl.L[k + 1];
         const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
         const unsigned work = ccols * (unsigned)C.g.nz;
         for (unsigned w = tid; w < work; w += nth) {
@@ -469,22 +473,24 @@ __global__ void __launch_bounds__(kSmallThreads, 1)
         __syncthreads();
     }
     {
-        const LevelView<T>& L = sl.L[last];
+        const LevelView<T> L = sl.L[last];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
         for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
         __syncthreads();
     }
     for (int k = last - 1; k >= 0; --k) {
-        const LevelView<T>& L = sl.L[k];
+        const LevelView<T> L = sl.L[k];
+        const LevelView<T> C = sl.L[k + 1];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth)
-            sweep_column<T, MZ, false, true, false>(L, sl.L[k + 1], 1, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false>(L, C, 1, q);
         __syncthreads();
         for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 0, q);
         __syncthreads();
     }
-    const unsigned ln0 = sl.L[0].g.plane * (unsigned)sl.L[0].g.nz;
-    for (unsigned i = tid; i < ln0; i += nth) tl.L[0].x[i] = sl.L[0].x[i];
+    const LevelView<T> S0 = sl.L[0];
+    const unsigned ln0 = S0.g.plane * (unsigned)S0.g.nz;
+    T* out = tl.L[0].x;
+    for (unsigned i = tid; i < ln0; i += nth) out[i] = S0.x[i];
 }
 
 unsigned blocks_for(unsigned n) { return n == 0 ? 1u : (n + NT - 1) / NT; }

@@ -84,8 +84,11 @@ void launch_step_record(cudaStream_t st, const OpView& o, const double* x, const
 // r = b - A x in FP64 from the double-word x; start of a solve, or the residual
 // replacement that begins phase 2.
 void launch_residual_x(cudaStream_t st, const OpView& o, const double* diag, const double* b,
-                       const float2* x, float2* r, float* b0, bool start, Ctl* ctl,
+                       const double* x, float2* r, float* b0, bool start, Ctl* ctl,
                        const Red& red, Cond cond);
+// xb += xw in FP64, xw = 0 (skipped once the solve is done when check_done).
+void launch_fold(cudaStream_t st, unsigned n, double* xb, float2* xw, const Ctl* ctl,
+                 bool check_done);
 void launch_apply_dw(cudaStream_t st, const OpView& o, const float2* dgw, const float2* p,
                      float2* Ap, Ctl* ctl, const Red& red, Cond cond);
 void launch_update_dw(cudaStream_t st, unsigned n, const float2* p, const float2* Ap, float2* x,

@@ -111,6 +111,7 @@ class Solver {
     double *P = nullptr, *x = nullptr, *b = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr;
     double *diag = nullptr, *invd = nullptr, *xold = nullptr, *nat = nullptr, *part = nullptr;
     float2* dgw = nullptr;  // double-word diagonal (dw)
+    float2* xwc = nullptr;  // double-word correction of x (dw); x is then its FP64 base
     Ctl* ctl = nullptr;
     Ctl* h_ctl = nullptr;  // pinned mirror
     std::vector<Level> lv;
@@ -194,15 +195,15 @@ class Solver {
     void enqueue_body(Cond cond);
     void enqueue_replace(Cond cond);
     // The double-word views of x, r, p, Ap (same storage as the FP64 vectors).
-    float2* xw() const { return reinterpret_cast<float2*>(x); }
+    float2* xw() const { return xwc; }
     float2* rw() const { return reinterpret_cast<float2*>(r); }
     float2* pw() const { return reinterpret_cast<float2*>(p); }
     float2* Apw() const { return reinterpret_cast<float2*>(Ap); }
-    // x as split-layout FP64 in `out` (out may be x itself outside dw mode).
-    const double* x_as_double(double* scratch) const {
-        if (!dw) return x;
-        launch_dw_to_d(st, n, xw(), scratch);
-        return scratch;
+    // x as split-layout FP64: in the double-word mode the correction is first
+    // folded into the FP64 base (which leaves x unchanged).
+    const double* x_as_double(double*) const {
+        if (dw) launch_fold(st, n, x, xwc, ctl, false);
+        return x;
     }
     template <class T>
     void vcycle(size_t k, Cond cond);
@@ -264,6 +265,7 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     for (size_t& o : o_vec) o = ar.take((size_t)n * 8);
     const size_t o_invd = pc == CT_JACOBI ? ar.take((size_t)n * 8) : 0;
     const size_t o_dgw = dw ? ar.take((size_t)n * 8) : 0;
+    const size_t o_xwc = dw ? ar.take((size_t)n * 8) : 0;
     const size_t o_nat = ar.take(ncells * 8);
     const size_t o_part = ar.take((size_t)NSLOT * 4 * maxb * 8);
     const size_t o_ctl = ar.take(sizeof(Ctl));
@@ -356,6 +358,7 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     xold = at<double>(o_vec[7]);
     invd = pc == CT_JACOBI ? at<double>(o_invd) : nullptr;
     dgw = dw ? at<float2>(o_dgw) : nullptr;
+    xwc = dw ? at<float2>(o_xwc) : nullptr;
     nat = at<double>(o_nat);
     part = at<double>(o_part);
     ctl = at<Ctl>(o_ctl);
@@ -489,8 +492,9 @@ void Solver::vcycle(size_t k, Cond cond) {
 void Solver::enqueue_init(Cond cond) {
     void* b0 = mt == MG_NONE ? nullptr : (void*)(base + lv[0].o_b);
     if (dw) {
+        enq("pcg_fold_x", (double)ncells * 32, [&] { launch_fold(cs, n, x, xwc, ctl, false); });
         enq("pcg_residual_fp64", (double)ncells * (36 + 8 + 8 + 4), [&] {
-            launch_residual_x(cs, op(), diag, b, xw(), rw(), (float*)b0, true, ctl,
+            launch_residual_x(cs, op(), diag, b, x, rw(), (float*)b0, true, ctl,
                               red_cols(SL_INIT), cond);
         });
         return;
@@ -502,8 +506,9 @@ void Solver::enqueue_init(Cond cond) {
 
 void Solver::enqueue_replace(Cond cond) {
     float* b0 = at<float>(lv[0].o_b);
+    enq("pcg_fold_x", (double)ncells * 32, [&] { launch_fold(cs, n, x, xwc, ctl, true); });
     enq("pcg_residual_fp64", (double)ncells * (36 + 8 + 8 + 4), [&] {
-        launch_residual_x(cs, op(), diag, b, xw(), rw(), b0, false, ctl, red_cols(SL_INIT), cond);
+        launch_residual_x(cs, op(), diag, b, x, rw(), b0, false, ctl, red_cols(SL_INIT), cond);
     });
 }
 
@@ -549,7 +554,11 @@ ct_status Solver::record_graphs() {
     cudaGraph_t graph = nullptr;
     CT_CK(cudaGraphCreate(&graph, 0));
     cudaGraphConditionalHandle h1{}, h2{};
-    bool ok = cudaGraphConditionalHandleCreate(&h1, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+    // CT_COND_GRAPHS=0 selects the plain part graphs (profilers cannot see
+    // inside conditional nodes).
+    const char* cg_env = std::getenv("CT_COND_GRAPHS");
+    bool ok = !(cg_env && cg_env[0] == '0') &&
+              cudaGraphConditionalHandleCreate(&h1, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
     if (ok && dw)
         ok = cudaGraphConditionalHandleCreate(&h2, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
     // Adds a WHILE node after the captured work so far and captures its body.
@@ -684,6 +693,7 @@ ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
     CT_CK(cudaStreamSynchronize(st));
     if (h_ctl->bb_zero) {  // no heat in: x = 0 (src/pcg3d_cpu.cpp:146)
         CT_CK(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
+        if (xwc) CT_CK(cudaMemsetAsync(xwc, 0, (size_t)n * 8, st));
         CT_CK(cudaStreamSynchronize(st));
     }
     ct_stats s;
@@ -771,6 +781,7 @@ ct_status ct_set_x_zero(ct_solver* s) {
     CT_SOLVER_OK(s);
     s->impl.x_zero = true;
     CT_CUDA(cudaMemsetAsync(s->impl.x, 0, (size_t)s->impl.n * 8, s->impl.st));
+    if (s->impl.xwc) CT_CUDA(cudaMemsetAsync(s->impl.xwc, 0, (size_t)s->impl.n * 8, s->impl.st));
     return CT_OK;
 }
 
@@ -780,10 +791,8 @@ ct_status ct_set_x(ct_solver* s, const double* T) {
     s->impl.x_zero = false;
     ct::Solver& v = s->impl;
     CT_CUDA(cudaMemcpyAsync(v.nat, T, v.ncells * 8, cudaMemcpyHostToDevice, v.st));
-    if (v.dw)
-        ct::launch_natural_to_dw(v.st, v.g0, v.nat, v.xw());
-    else
-        ct::launch_to_split_d(v.st, v.g0, v.nat, v.x);
+    ct::launch_to_split_d(v.st, v.g0, v.nat, v.x);
+    if (v.xwc) CT_CUDA(cudaMemsetAsync(v.xwc, 0, (size_t)v.n * 8, v.st));
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaStreamSynchronize(v.st));
     return CT_OK;
@@ -799,7 +808,7 @@ ct_status ct_set_rhs_steady(ct_solver* s) {
 ct_status ct_set_rhs_transient(ct_solver* s) {
     CT_SOLVER_OK(s);
     ct::Solver& v = s->impl;
-    const double* xd = v.x_as_double(v.xold);  // in place when the x_old copy is the conversion
+    const double* xd = v.x_as_double(nullptr);
     ct::launch_rhs_transient(v.st, v.n, v.cap, v.inv_dt, v.P, xd, v.b, v.xold);
     CT_CUDA(cudaGetLastError());
     return CT_OK;
@@ -834,10 +843,7 @@ ct_status ct_get_x(ct_solver* s, double* T) {
     CT_SOLVER_OK(s);
     if (!T) return fail(CT_BAD_ARG, "ct_get_x: null");
     ct::Solver& v = s->impl;
-    if (v.dw)
-        ct::launch_dw_to_natural(v.st, v.g0, v.xw(), v.nat);
-    else
-        ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
+    ct::launch_to_natural_d(v.st, v.g0, v.x_as_double(nullptr), v.nat);
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaMemcpyAsync(T, v.nat, v.ncells * 8, cudaMemcpyDeviceToHost, v.st));
     CT_CUDA(cudaStreamSynchronize(v.st));
@@ -848,10 +854,7 @@ ct_status ct_device_x(ct_solver* s, const double** T_dev) {
     CT_SOLVER_OK(s);
     if (!T_dev) return fail(CT_BAD_ARG, "ct_device_x: null");
     ct::Solver& v = s->impl;
-    if (v.dw)
-        ct::launch_dw_to_natural(v.st, v.g0, v.xw(), v.nat);
-    else
-        ct::launch_to_natural_d(v.st, v.g0, v.x, v.nat);
+    ct::launch_to_natural_d(v.st, v.g0, v.x_as_double(nullptr), v.nat);
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaStreamSynchronize(v.st));
     *T_dev = v.nat;
@@ -876,7 +879,7 @@ ct_status ct_true_relres(ct_solver* s, double* out) {
     CT_SOLVER_OK(s);
     if (!out) return fail(CT_BAD_ARG, "ct_true_relres: null");
     ct::Solver& v = s->impl;
-    ct::launch_true_residual(v.st, v.op(), v.P, v.x_as_double(v.Ap), v.ctl, v.red_cols(ct::SL_AUX));
+    ct::launch_true_residual(v.st, v.op(), v.P, v.x_as_double(nullptr), v.ctl, v.red_cols(ct::SL_AUX));
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaMemcpyAsync(v.h_ctl, v.ctl, sizeof(ct::Ctl), cudaMemcpyDeviceToHost, v.st));
     CT_CUDA(cudaStreamSynchronize(v.st));
@@ -888,7 +891,7 @@ ct_status ct_solver_step_record(ct_solver* s, double dt, ct_step_record* out) {
     CT_SOLVER_OK(s);
     if (!out || !(dt > 0)) return fail(CT_BAD_ARG, "ct_solver_step_record: null output or dt <= 0");
     ct::Solver& v = s->impl;
-    ct::launch_step_record(v.st, v.op(), v.x_as_double(v.Ap), v.xold, v.ctl, v.red_cols(ct::SL_AUX));
+    ct::launch_step_record(v.st, v.op(), v.x_as_double(nullptr), v.xold, v.ctl, v.red_cols(ct::SL_AUX));
     CT_CUDA(cudaGetLastError());
     CT_CUDA(cudaMemcpyAsync(v.h_ctl, v.ctl, sizeof(ct::Ctl), cudaMemcpyDeviceToHost, v.st));
     CT_CUDA(cudaStreamSynchronize(v.st));
