@@ -1,0 +1,736 @@
+// batch.cu - the batched solver behind ct_batch_*: many independent stacks of
+// uneven lateral size and layer count (floorplan or power-map sweeps), each a
+// full MG-PCG solve of its own, run together so that every stage of the
+// iteration is ONE launch for all of them.
+//
+// Set-up reuses the single solver: each instance is a Solver (its arena, its
+// multigrid levels, factors and boundary conversions), created on the batch's
+// stream without graphs of its own. The batch adds device tables over those
+// arrays (BInst per instance, LevelView per instance and depth, the small-level
+// descriptors) and block tables (batch.h) per stage.
+//
+// Size buckets. Instances are grouped by the number of levels their V-cycle
+// runs as separate sweeps (the rest run in the one-block shared-memory kernel),
+// which follows their lateral size. Each bucket has its own stream and ONE
+// captured CUDA graph per solve:
+//     fold x;  r = b - A x (FP64);  WHILE (any instance active) {
+//         guard;  V-cycle stages per depth;  small levels;  dot;  p;  Ap;
+//         x, r update and test;  residual replacement of instances whose
+//         first phase ended }
+// so instances converge one by one (their blocks return at entry) and the
+// loop ends when the bucket's last one does. Buckets run concurrently.
+//
+// Column tiles. The sweep and restriction stages' items per block are picked
+// per bucket and depth by timing candidate tiles at creation (the autotuner);
+// CT_BATCH_TILE=<items> fixes them instead.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "batch.h"
+#include "cthermal.h"
+#include "solver.h"
+#include "status.h"
+
+namespace ct {
+
+namespace {
+
+#define CT_BK(call)                                                                              \
+    do {                                                                                         \
+        const cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                                   \
+            return ct::fail(e_ == cudaErrorMemoryAllocation ? CT_OUT_OF_MEMORY : CT_CUDA_ERROR,  \
+                            "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+// Items per block of the stages whose tile is not tuned.
+constexpr unsigned kVecChunk = 4096;   // value pairs (fold, update, dot, p, rhs)
+constexpr unsigned kColChunk = 512;    // fine columns (FP64 residual)
+constexpr unsigned kCellChunk = 2048;  // fine cells (operator apply)
+// Candidate tiles of the autotuner (columns per block for the sweeps, coarse
+// cells per block for the restriction).
+constexpr unsigned kSweepTiles[] = {256, 512, 1024, 2048};
+constexpr unsigned kRestrictTiles[] = {256, 512, 1024, 2048, 4096};
+
+// Host form of a block table; first/count are indexed by instance.
+struct HPlan {
+    std::vector<Task> tasks;
+    std::vector<int> first, count;
+};
+
+HPlan make_plan(int ni, const std::vector<int>& insts, const std::vector<unsigned>& items,
+                unsigned chunk) {
+    HPlan h;
+    h.first.assign((size_t)ni, 0);
+    h.count.assign((size_t)ni, 0);
+    for (size_t a = 0; a < insts.size(); ++a) {
+        const int i = insts[a];
+        h.first[(size_t)i] = (int)h.tasks.size();
+        for (unsigned b = 0; b < items[a]; b += chunk)
+            h.tasks.push_back(Task{i, b, std::min(items[a], b + chunk)});
+        h.count[(size_t)i] = (int)h.tasks.size() - h.first[(size_t)i];
+    }
+    return h;
+}
+
+}  // namespace
+
+class Batch {
+  public:
+    int ni = 0;
+    std::vector<std::unique_ptr<ct_solver>> sv;  // the instances (ct_solver wraps a Solver)
+    cudaStream_t st = nullptr;  // set-up, copies, per-instance calls
+    int sms = 0;
+    double rr_thr = 1e-5;
+    bool use_cond = true;
+    bool prof = false;
+    cudaError_t launch_error = cudaSuccess;  // first failed launch of the small-level kernel
+
+    struct Bucket {
+        std::vector<int> inst;
+        int depth = 0;    // V-cycle levels run as batched sweeps
+        int mz = 1;       // largest nz
+        size_t smem = 0;  // shared memory of the small-level kernel
+        cudaStream_t st = nullptr, st_body = nullptr;
+        cudaGraphExec_t gx = nullptr;
+        BCtl* bc = nullptr;
+        Plan vec{}, cols{}, cells{};
+        BRed r_res{}, r_apply{}, r_update{}, r_dot{};
+        std::vector<Plan> sweep, restr;
+        std::vector<unsigned> sweep_tile, restr_tile;
+        int* small_insts = nullptr;
+    };
+    std::vector<Bucket> bk;
+
+    // device tables
+    BInst* bi = nullptr;
+    Ctl* ctl = nullptr;
+    Ctl* h_ctl = nullptr;  // pinned mirror
+    std::vector<LevelView<float>*> views;  // per depth: LevelView per instance
+    TailLevels<float>* small = nullptr;
+    std::vector<void*> bufs;               // every device allocation of the batch
+    cudaEvent_t ev_start = nullptr;
+    std::vector<cudaEvent_t> ev_done;
+
+    ~Batch() {
+        if (st) cudaStreamSynchronize(st);
+        for (Bucket& b : bk) {
+            if (b.st) cudaStreamSynchronize(b.st);
+            if (b.gx) cudaGraphExecDestroy(b.gx);
+            if (b.st_body) cudaStreamDestroy(b.st_body);
+            if (b.st) cudaStreamDestroy(b.st);
+        }
+        for (cudaEvent_t e : ev_done) cudaEventDestroy(e);
+        if (ev_start) cudaEventDestroy(ev_start);
+        sv.clear();  // the instances synchronise on st before it goes
+        for (void* p : bufs) cudaFree(p);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    template <class T>
+    ct_status dalloc(T** out, size_t bytes) {
+        void* p = nullptr;
+        const cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CT_OUT_OF_MEMORY, "batch: cudaMalloc of %.1f MB failed: %s", bytes / 1e6,
+                        cudaGetErrorString(e));
+        }
+        bufs.push_back(p);
+        *out = static_cast<T*>(p);
+        return CT_OK;
+    }
+
+    template <class T>
+    ct_status upload(T** out, const std::vector<T>& v) {
+        ct_status s = dalloc(out, v.size() * sizeof(T));
+        if (s != CT_OK) return s;
+        if (!v.empty()) CT_BK(cudaMemcpyAsync(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+        return CT_OK;
+    }
+
+    ct_status upload_plan(const HPlan& h, Plan* p) {
+        Task* t = nullptr;
+        int *f = nullptr, *c = nullptr;
+        ct_status s;
+        if ((s = upload(&t, h.tasks)) != CT_OK) return s;
+        if ((s = upload(&f, h.first)) != CT_OK) return s;
+        if ((s = upload(&c, h.count)) != CT_OK) return s;
+        *p = Plan{t, (int)h.tasks.size(), f, c};
+        return CT_OK;
+    }
+
+    ct_status make_red(const Plan& p, BRed* r) {
+        ct_status s;
+        if ((s = dalloc(&r->part, (size_t)2 * std::max(1, p.ntasks) * sizeof(double))) != CT_OK) return s;
+        if ((s = dalloc(&r->tickets, (size_t)ni * sizeof(unsigned))) != CT_OK) return s;
+        CT_BK(cudaMemsetAsync(r->tickets, 0, (size_t)ni * sizeof(unsigned), st));
+        return CT_OK;
+    }
+
+    Solver& inst(int i) const { return sv[(size_t)i]->impl; }
+    int small_k0(int i) const { return (int)inst(i).small_k0; }
+
+    ct_status create(int n, const ct_model* const* models);
+    ct_status build_bucket(Bucket& b);
+    ct_status tune_bucket(Bucket& b);
+    ct_status record(Bucket& b);
+    ct_status set_dt(const double* dt);
+    ct_status solve(double tol, int maxit, ct_stats* out);
+
+    // One bucket's launches.
+    void enqueue_init(Bucket& b, cudaStream_t s, Cond cond);
+    void enqueue_body(Bucket& b, cudaStream_t s, Cond cond);
+    void vcycle(Bucket& b, cudaStream_t s);
+};
+
+ct_status Batch::create(int n, const ct_model* const* models) {
+    if (n < 1) return fail(CT_BAD_ARG, "ct_batch_create: n must be >= 1");
+    if (!models) return fail(CT_BAD_ARG, "ct_batch_create: null model list");
+    for (int i = 0; i < n; ++i)
+        if (!models[i]) return fail(CT_BAD_ARG, "ct_batch_create: null model %d", i);
+    ni = n;
+    if (const char* e = std::getenv("CT_RR_THRESHOLD")) rr_thr = std::atof(e);
+    if (const char* e = std::getenv("CT_COND_GRAPHS")) use_cond = e[0] != '0';
+    int dev = 0;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CT_NO_DEVICE, "no CUDA device");
+    }
+    CT_BK(cudaGetDevice(&dev));
+    CT_BK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CT_BK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CT_BK(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
+
+    // Instances: the single solver's set-up on the batch stream.
+    sv.reserve((size_t)n);
+    int maxdepth = 0;
+    for (int i = 0; i < n; ++i) {
+        std::unique_ptr<ct_solver> h(new (std::nothrow) ct_solver());
+        if (!h) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
+        Solver* s = &h->impl;
+        s->st = st;
+        s->skip_graphs = true;
+        s->rr_thr = rr_thr;
+        const ct_status cs = s->create(models[i], CT_MULTIGRID, CT_MG_FP32_FLEX_DW);
+        if (cs != CT_OK) {
+            const std::string why = ct_last_error();
+            return fail(cs, "ct_batch_create: instance %d: %s", i, why.c_str());
+        }
+        if (s->small_k0 >= s->lv.size())
+            return fail(CT_BAD_ARG, "ct_batch_create: instance %d: coarsest level too large for one block", i);
+        maxdepth = std::max(maxdepth, (int)s->small_k0);
+        sv.push_back(std::move(h));
+    }
+
+    // Tables over the instances' arrays.
+    std::vector<BInst> hb((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const Solver& s = inst(i);
+        BInst& I = hb[(size_t)i];
+        I.o = s.op();
+        I.P = s.P;
+        I.x = s.x;
+        I.b = s.b;
+        I.diag = s.diag;
+        I.xw = s.xwc;
+        I.r = s.rw();
+        I.p = s.pw();
+        I.Ap = s.Apw();
+        I.dgw = s.dgw;
+        I.b0 = s.at<float>(s.lv[0].o_b);
+        I.z = s.at<float>(s.lv[0].o_x);
+        I.xold = s.xold;
+        I.n = s.n;
+    }
+    ct_status s;
+    if ((s = upload(&bi, hb)) != CT_OK) return s;
+    views.assign((size_t)maxdepth + 1, nullptr);
+    for (int d = 0; d <= maxdepth; ++d) {
+        std::vector<LevelView<float>> hv((size_t)n);
+        for (int i = 0; i < n; ++i)
+            if ((size_t)d < inst(i).lv.size()) hv[(size_t)i] = inst(i).view<float>((size_t)d);
+            else std::memset(&hv[(size_t)i], 0, sizeof(LevelView<float>));
+        if ((s = upload(&views[(size_t)d], hv)) != CT_OK) return s;
+    }
+    std::vector<TailLevels<float>> ht((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const Solver& v = inst(i);
+        TailLevels<float>& tl = ht[(size_t)i];
+        std::memset(&tl, 0, sizeof tl);
+        tl.n = (int)(v.lv.size() - v.small_k0);
+        for (int q = 0; q < tl.n; ++q) tl.L[q] = v.view<float>(v.small_k0 + (size_t)q);
+    }
+    if ((s = upload(&small, ht)) != CT_OK) return s;
+    if ((s = dalloc(&ctl, (size_t)n * sizeof(Ctl))) != CT_OK) return s;
+    CT_BK(cudaMemsetAsync(ctl, 0, (size_t)n * sizeof(Ctl), st));
+    CT_BK(cudaMallocHost(&h_ctl, (size_t)n * sizeof(Ctl)));
+    std::memset(h_ctl, 0, (size_t)n * sizeof(Ctl));
+
+    // Buckets by V-cycle depth.
+    for (int d = 0; d <= maxdepth; ++d) {
+        Bucket b;
+        for (int i = 0; i < n; ++i)
+            if (small_k0(i) == d) b.inst.push_back(i);
+        if (b.inst.empty()) continue;
+        b.depth = d;
+        bk.push_back(std::move(b));
+    }
+    for (Bucket& b : bk) {
+        if ((s = build_bucket(b)) != CT_OK) return s;
+    }
+    CT_BK(cudaStreamSynchronize(st));
+    for (Bucket& b : bk) {
+        if ((s = tune_bucket(b)) != CT_OK) return s;
+    }
+    for (Bucket& b : bk) {
+        if ((s = record(b)) != CT_OK) return s;
+        cudaEvent_t e = nullptr;
+        CT_BK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ev_done.push_back(e);
+    }
+    CT_BK(cudaStreamSynchronize(st));
+    return CT_OK;
+}
+
+ct_status Batch::build_bucket(Bucket& b) {
+    CT_BK(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking));
+    CT_BK(cudaStreamCreateWithFlags(&b.st_body, cudaStreamNonBlocking));
+    ct_status s;
+    if ((s = dalloc(&b.bc, sizeof(BCtl))) != CT_OK) return s;
+    CT_BK(cudaMemsetAsync(b.bc, 0, sizeof(BCtl), st));
+    std::vector<unsigned> pairs, cols, cells;
+    for (int i : b.inst) {
+        const Solver& v = inst(i);
+        pairs.push_back(v.n / 2);
+        cols.push_back(v.g0.plane);
+        cells.push_back(v.n);
+        b.mz = std::max(b.mz, v.g0.nz);
+        TailLevels<float> tl;
+        tl.n = (int)(v.lv.size() - v.small_k0);
+        for (int q = 0; q < tl.n; ++q) tl.L[q] = v.view<float>(v.small_k0 + (size_t)q);
+        b.smem = std::max(b.smem, small_smem_bytes(tl));
+    }
+    if ((s = upload_plan(make_plan(ni, b.inst, pairs, kVecChunk), &b.vec)) != CT_OK) return s;
+    if ((s = upload_plan(make_plan(ni, b.inst, cols, kColChunk), &b.cols)) != CT_OK) return s;
+    if ((s = upload_plan(make_plan(ni, b.inst, cells, kCellChunk), &b.cells)) != CT_OK) return s;
+    if ((s = make_red(b.cols, &b.r_res)) != CT_OK) return s;
+    if ((s = make_red(b.cells, &b.r_apply)) != CT_OK) return s;
+    if ((s = make_red(b.vec, &b.r_update)) != CT_OK) return s;
+    if ((s = make_red(b.vec, &b.r_dot)) != CT_OK) return s;
+    if ((s = upload(&b.small_insts, b.inst)) != CT_OK) return s;
+    b.sweep.assign((size_t)b.depth, Plan{});
+    b.restr.assign((size_t)b.depth, Plan{});
+    b.sweep_tile.assign((size_t)b.depth, 512);
+    b.restr_tile.assign((size_t)b.depth, 1024);
+    return CT_OK;
+}
+
+// Picks the sweep and restriction tiles of each depth by timing the
+// candidates on the bucket's own levels (the level arrays are scratch between
+// solves, so the timing runs leave nothing behind that a solve reads).
+ct_status Batch::tune_bucket(Bucket& b) {
+    unsigned fixed = 0;
+    if (const char* e = std::getenv("CT_BATCH_TILE")) fixed = (unsigned)std::atol(e);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CT_BK(cudaEventCreate(&e0));
+    CT_BK(cudaEventCreate(&e1));
+    ct_status s = CT_OK;
+    for (int d = 0; d < b.depth && s == CT_OK; ++d) {
+        std::vector<unsigned> sweep_items, restr_items;
+        for (int i : b.inst) {
+            const Geo& g = inst(i).lv[(size_t)d].g;
+            const Geo& c = inst(i).lv[(size_t)d + 1].g;
+            sweep_items.push_back((unsigned)g.ny * (unsigned)g.hx);
+            restr_items.push_back((unsigned)c.nx * (unsigned)c.ny * (unsigned)c.nz);
+        }
+        auto time_of = [&](auto&& launch) -> float {
+            launch();  // warm
+            float best = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+                cudaEventRecord(e0, b.st);
+                launch();
+                cudaEventRecord(e1, b.st);
+                cudaEventSynchronize(e1);
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                best = std::min(best, ms);
+            }
+            return best;
+        };
+        // sweeps
+        {
+            std::vector<unsigned> cands;
+            if (fixed) cands.push_back(fixed);
+            else cands.assign(std::begin(kSweepTiles), std::end(kSweepTiles));
+            float best = 1e30f;
+            for (unsigned tile : cands) {
+                Plan p;
+                if ((s = upload_plan(make_plan(ni, b.inst, sweep_items, tile), &p)) != CT_OK) break;
+                CT_BK(cudaStreamSynchronize(st));
+                const float t = cands.size() == 1 ? 0.0f : time_of([&] {
+                    launch_b_sweep(b.st, p, views[(size_t)d], views[(size_t)d], 1, false, false, b.mz, ctl);
+                });
+                if (t < best) {
+                    best = t;
+                    b.sweep[(size_t)d] = p;
+                    b.sweep_tile[(size_t)d] = tile;
+                }
+            }
+        }
+        // restriction
+        {
+            std::vector<unsigned> cands;
+            if (fixed) cands.push_back(fixed);
+            else cands.assign(std::begin(kRestrictTiles), std::end(kRestrictTiles));
+            float best = 1e30f;
+            for (unsigned tile : cands) {
+                Plan p;
+                if ((s = upload_plan(make_plan(ni, b.inst, restr_items, tile), &p)) != CT_OK) break;
+                CT_BK(cudaStreamSynchronize(st));
+                const float t = cands.size() == 1 ? 0.0f : time_of([&] {
+                    launch_b_restrict(b.st, p, views[(size_t)d], views[(size_t)d + 1], ctl);
+                });
+                if (t < best) {
+                    best = t;
+                    b.restr[(size_t)d] = p;
+                    b.restr_tile[(size_t)d] = tile;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != CT_OK) return s;
+    CT_BK(cudaGetLastError());
+    CT_BK(cudaStreamSynchronize(b.st));
+    return CT_OK;
+}
+
+void Batch::vcycle(Bucket& b, cudaStream_t s) {
+    for (int d = 0; d < b.depth; ++d) {
+        const LevelView<float>* L = views[(size_t)d];
+        const LevelView<float>* C = views[(size_t)d + 1];
+        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, true, false, b.mz, ctl);
+        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, false, b.mz, ctl);
+        launch_b_restrict(s, b.restr[(size_t)d], L, C, ctl);
+    }
+    const cudaError_t e = launch_b_small(s, b.small_insts, (int)b.inst.size(), small, b.smem, b.mz, ctl);
+    if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
+    for (int d = b.depth; d-- > 0;) {
+        const LevelView<float>* L = views[(size_t)d];
+        const LevelView<float>* C = views[(size_t)d + 1];
+        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, true, b.mz, ctl);
+        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, false, false, b.mz, ctl);
+    }
+}
+
+void Batch::enqueue_init(Bucket& b, cudaStream_t s, Cond cond) {
+    launch_b_fold(s, b.vec, bi, ctl, 0);
+    launch_b_residual(s, b.cols, bi, ctl, b.r_res, 1, b.bc, cond);
+}
+
+void Batch::enqueue_body(Bucket& b, cudaStream_t s, Cond cond) {
+    launch_b_guard(s, b.bc, cond);
+    vcycle(b, s);
+    launch_b_dot(s, b.vec, bi, ctl, b.r_dot, b.bc, cond);
+    launch_b_update_p(s, b.vec, bi, ctl);
+    launch_b_apply(s, b.cells, bi, ctl, b.r_apply, b.bc, cond);
+    launch_b_update(s, b.vec, bi, ctl, b.r_update, b.bc, cond);
+    // residual replacement of the instances whose first phase just ended
+    launch_b_fold(s, b.vec, bi, ctl, 1);
+    launch_b_residual(s, b.cols, bi, ctl, b.r_res, 0, b.bc, cond);
+}
+
+ct_status Batch::record(Bucket& b) {
+    if (!use_cond) return CT_OK;
+    cudaGraph_t graph = nullptr;
+    CT_BK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h{};
+    bool ok = cudaGraphConditionalHandleCreate(&h, graph, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok)
+        ok = cudaStreamBeginCaptureToGraph(b.st, graph, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        enqueue_init(b, b.st, Cond{h, 1});
+        cudaStreamCaptureStatus cst;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaGraph_t cg = nullptr;
+        ok = cudaStreamGetCaptureInfo(b.st, &cst, nullptr, &cg, &deps, nullptr, &ndeps) == cudaSuccess;
+        cudaGraphNode_t cnode = nullptr;
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        if (ok) {
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            ok = cudaGraphAddNode(&cnode, cg, deps, nullptr, ndeps, &cp) == cudaSuccess;
+        }
+        if (ok)
+            ok = cudaStreamBeginCaptureToGraph(b.st_body, cp.conditional.phGraph_out[0], nullptr,
+                                               nullptr, 0, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            enqueue_body(b, b.st_body, Cond{h, 1});
+            cudaGraph_t bg = nullptr;
+            ok = cudaStreamEndCapture(b.st_body, &bg) == cudaSuccess;
+        }
+        if (ok)
+            ok = cudaStreamUpdateCaptureDependencies(b.st, &cnode, nullptr, 1,
+                                                     cudaStreamSetCaptureDependencies) == cudaSuccess;
+        cudaGraph_t outg = nullptr;
+        const bool ended = cudaStreamEndCapture(b.st, &outg) == cudaSuccess;
+        ok = ok && ended;
+        if (ok) ok = cudaGraphInstantiate(&b.gx, graph, 0) == cudaSuccess;
+    }
+    cudaGraphDestroy(graph);
+    if (launch_error != cudaSuccess)
+        return fail(CT_CUDA_ERROR, "batch: small-level kernel launch failed: %s", cudaGetErrorString(launch_error));
+    if (!ok) {
+        cudaGetLastError();
+        if (b.gx) cudaGraphExecDestroy(b.gx);
+        b.gx = nullptr;
+        use_cond = false;  // every bucket falls back to host-driven launches
+    }
+    return CT_OK;
+}
+
+ct_status Batch::set_dt(const double* dt) {
+    for (int i = 0; i < ni; ++i) {
+        const double v = dt ? dt[i] : 0.0;
+        const ct_status s = inst(i).set_dt(v);
+        if (s != CT_OK) {
+            const std::string why = ct_last_error();
+            return fail(s, "ct_batch_set_dt: instance %d: %s", i, why.c_str());
+        }
+        h_ctl[i].inv_dt = inst(i).inv_dt;
+    }
+    CT_BK(cudaMemcpyAsync(ctl, h_ctl, (size_t)ni * sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    CT_BK(cudaStreamSynchronize(st));
+    return CT_OK;
+}
+
+ct_status Batch::solve(double tol, int maxit, ct_stats* out) {
+    if (!(tol >= 0)) return fail(CT_BAD_ARG, "ct_batch_solve: tol must be >= 0");
+    if (maxit > 100000000) return fail(CT_BAD_ARG, "ct_batch_solve: maxit above 1e8");
+    for (int i = 0; i < ni; ++i) {
+        Solver& v = inst(i);
+        Ctl& c = h_ctl[i];
+        std::memset(&c, 0, sizeof c);
+        c.tol = tol;
+        c.maxit = maxit;
+        c.inv_dt = v.inv_dt;
+        c.stop = std::max(tol, rr_thr);
+        c.x_zero = v.x_zero ? 1 : 0;
+        v.x_zero = false;
+    }
+    CT_BK(cudaMemcpyAsync(ctl, h_ctl, (size_t)ni * sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    for (Bucket& b : bk) {
+        const BCtl c{(int)b.inst.size(), 0, maxit + 2, 0};
+        CT_BK(cudaMemcpyAsync(b.bc, &c, sizeof c, cudaMemcpyHostToDevice, st));
+    }
+    CT_BK(cudaStreamSynchronize(st));  // the pageable BCtl copies are done
+    CT_BK(cudaEventRecord(ev_start, st));
+    const Cond none{0, 0};
+    for (size_t q = 0; q < bk.size(); ++q) {
+        Bucket& b = bk[q];
+        CT_BK(cudaStreamWaitEvent(b.st, ev_start, 0));
+        if (use_cond && b.gx && !prof) {
+            CT_BK(cudaGraphLaunch(b.gx, b.st));
+        } else {
+            // Host-driven: direct launches with a check of the bucket's
+            // active count after every body.
+            enqueue_init(b, b.st, none);
+            BCtl hc{};
+            for (int it = 0; it <= maxit + 2; ++it) {
+                CT_BK(cudaMemcpyAsync(&hc, b.bc, sizeof hc, cudaMemcpyDeviceToHost, b.st));
+                CT_BK(cudaStreamSynchronize(b.st));
+                if (hc.active <= 0) break;
+                enqueue_body(b, b.st, none);
+            }
+        }
+        CT_BK(cudaGetLastError());
+        if (launch_error != cudaSuccess)
+            return fail(CT_CUDA_ERROR, "batch: small-level kernel launch failed: %s",
+                        cudaGetErrorString(launch_error));
+        CT_BK(cudaEventRecord(ev_done[q], b.st));
+        CT_BK(cudaStreamWaitEvent(st, ev_done[q], 0));
+    }
+    CT_BK(cudaMemcpyAsync(h_ctl, ctl, (size_t)ni * sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CT_BK(cudaStreamSynchronize(st));
+    int nbreak = 0, nconv = 0;
+    for (int i = 0; i < ni; ++i) {
+        const Ctl& c = h_ctl[i];
+        Solver& v = inst(i);
+        if (c.bb_zero) {  // no heat in: x = 0 (src/pcg3d_cpu.cpp:146)
+            CT_BK(cudaMemsetAsync(v.x, 0, (size_t)v.n * 8, st));
+            CT_BK(cudaMemsetAsync(v.xwc, 0, (size_t)v.n * 8, st));
+        }
+        if (out) {
+            out[i].iters = c.iter;
+            out[i].relres = c.relres;
+            out[i].converged = c.converged;
+            out[i].breakdown = c.breakdown;
+        }
+        nbreak += c.breakdown ? 1 : 0;
+        nconv += c.converged ? 1 : 0;
+    }
+    CT_BK(cudaStreamSynchronize(st));
+    if (nbreak) return fail(CT_BREAKDOWN, "PCG breakdown in %d of %d instances", nbreak, ni);
+    if (nconv < ni) return fail(CT_NOT_CONVERGED, "%d of %d instances not converged", ni - nconv, ni);
+    return CT_OK;
+}
+
+}  // namespace ct
+
+// ---- C ABI ----------------------------------------------------------------
+
+struct ct_batch {
+    ct::Batch impl;
+};
+
+using ct::fail;
+
+#define CT_BATCH_OK(b) \
+    if (!(b)) return fail(CT_BAD_ARG, "%s: null batch", __func__)
+#define CT_BATCH_INST(b, i)                                                     \
+    do {                                                                        \
+        CT_BATCH_OK(b);                                                         \
+        if ((i) < 0 || (i) >= (b)->impl.ni)                                     \
+            return fail(CT_BAD_ARG, "%s: instance %d out of range", __func__, i); \
+    } while (0)
+
+extern "C" {
+
+ct_status ct_batch_create(int n, const ct_model* const* models, ct_batch** out) {
+    if (!out) return fail(CT_BAD_ARG, "ct_batch_create: null output");
+    *out = nullptr;
+    ct_batch* b = new (std::nothrow) ct_batch();
+    if (!b) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
+    const ct_status s = b->impl.create(n, models);
+    if (s != CT_OK) {
+        delete b;
+        return s;
+    }
+    *out = b;
+    return CT_OK;
+}
+
+ct_status ct_batch_destroy(ct_batch* b) {
+    delete b;
+    return CT_OK;
+}
+
+ct_status ct_batch_size(const ct_batch* b, int* n) {
+    CT_BATCH_OK(b);
+    if (!n) return fail(CT_BAD_ARG, "ct_batch_size: null");
+    *n = b->impl.ni;
+    return CT_OK;
+}
+
+ct_status ct_batch_set_dt(ct_batch* b, const double* dt) {
+    CT_BATCH_OK(b);
+    return b->impl.set_dt(dt);
+}
+
+ct_status ct_batch_set_x_zero(ct_batch* b) {
+    CT_BATCH_OK(b);
+    for (int i = 0; i < b->impl.ni; ++i) {
+        const ct_status s = ct_set_x_zero(b->impl.sv[(size_t)i].get());
+        if (s != CT_OK) return s;
+    }
+    return CT_OK;
+}
+
+ct_status ct_batch_set_rhs_steady(ct_batch* b) {
+    CT_BATCH_OK(b);
+    for (int i = 0; i < b->impl.ni; ++i) {
+        const ct_status s = ct_set_rhs_steady(b->impl.sv[(size_t)i].get());
+        if (s != CT_OK) return s;
+    }
+    return CT_OK;
+}
+
+ct_status ct_batch_set_rhs_transient(ct_batch* b) {
+    CT_BATCH_OK(b);
+    ct::Batch& B = b->impl;
+    for (ct::Batch::Bucket& k : B.bk) {
+        ct::launch_b_fold(B.st, k.vec, B.bi, B.ctl, 0);
+        ct::launch_b_rhs_transient(B.st, k.vec, B.bi, B.ctl);
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CT_CUDA_ERROR, "ct_batch_set_rhs_transient: %s", cudaGetErrorString(e));
+    return CT_OK;
+}
+
+ct_status ct_batch_set_power(ct_batch* b, int i, const double* P) {
+    CT_BATCH_INST(b, i);
+    return ct_set_power(b->impl.sv[(size_t)i].get(), P);
+}
+
+ct_status ct_batch_set_x(ct_batch* b, int i, const double* T) {
+    CT_BATCH_INST(b, i);
+    return ct_set_x(b->impl.sv[(size_t)i].get(), T);
+}
+
+ct_status ct_batch_solve(ct_batch* b, double tol, int maxit, ct_stats* stats) {
+    CT_BATCH_OK(b);
+    return b->impl.solve(tol, maxit, stats);
+}
+
+ct_status ct_batch_step_transient(ct_batch* b, const double* dt, double tol, int maxit,
+                                  ct_stats* stats) {
+    CT_BATCH_OK(b);
+    if (!dt) return fail(CT_BAD_ARG, "ct_batch_step_transient: null dt");
+    ct_status s = b->impl.set_dt(dt);
+    if (s != CT_OK) return s;
+    s = ct_batch_set_rhs_transient(b);
+    if (s != CT_OK) return s;
+    return b->impl.solve(tol, maxit, stats);
+}
+
+ct_status ct_batch_get_x(ct_batch* b, int i, double* T) {
+    CT_BATCH_INST(b, i);
+    return ct_get_x(b->impl.sv[(size_t)i].get(), T);
+}
+
+ct_status ct_batch_true_relres(ct_batch* b, int i, double* out) {
+    CT_BATCH_INST(b, i);
+    return ct_true_relres(b->impl.sv[(size_t)i].get(), out);
+}
+
+ct_status ct_batch_step_record(ct_batch* b, int i, double dt, ct_step_record* out) {
+    CT_BATCH_INST(b, i);
+    return ct_solver_step_record(b->impl.sv[(size_t)i].get(), dt, out);
+}
+
+ct_status ct_batch_num_buckets(const ct_batch* b, int* nbuckets) {
+    CT_BATCH_OK(b);
+    if (!nbuckets) return fail(CT_BAD_ARG, "ct_batch_num_buckets: null");
+    *nbuckets = (int)b->impl.bk.size();
+    return CT_OK;
+}
+
+ct_status ct_batch_bucket_info(const ct_batch* b, int k, int* ninst, int* depth, unsigned* sweep_tiles,
+                               unsigned* restrict_tiles) {
+    CT_BATCH_OK(b);
+    if (k < 0 || k >= (int)b->impl.bk.size()) return fail(CT_BAD_ARG, "ct_batch_bucket_info: bad bucket");
+    const ct::Batch::Bucket& B = b->impl.bk[(size_t)k];
+    if (ninst) *ninst = (int)B.inst.size();
+    if (depth) *depth = B.depth;
+    for (int d = 0; d < B.depth; ++d) {
+        if (sweep_tiles) sweep_tiles[d] = B.sweep_tile[(size_t)d];
+        if (restrict_tiles) restrict_tiles[d] = B.restr_tile[(size_t)d];
+    }
+    return CT_OK;
+}
+
+}  // extern "C"

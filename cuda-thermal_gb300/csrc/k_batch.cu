@@ -1,0 +1,489 @@
+// k_batch.cu - batched solver kernels: the double-word outer PCG and the
+// FP32 V-cycle stages for many instances per launch (see batch.h for the
+// block table and the per-instance reductions).
+//
+// Each kernel is the batched form of a single-solver kernel and uses the same
+// per-column / per-cell device code (dw_dev.cuh, mg_dev.cuh), so one instance
+// of a batch computes what a single solver computes for it.
+#include <algorithm>
+#include <cmath>
+
+#include "batch.h"
+#include "dw_dev.cuh"
+#include "mg_dev.cuh"
+#include "reduce.cuh"
+
+namespace ct {
+
+using namespace dwdev;
+using namespace mgdev;
+
+namespace {
+
+__device__ __forceinline__ bool inst_done(const Ctl* c) { return *(volatile const int*)&c->done != 0; }
+
+// Marks the instance done; the batch's last active instance ends the loop.
+__device__ __forceinline__ void inst_stop(Ctl* c, BCtl* bc, const Cond& cond) {
+    if (c->done) return;
+    c->done = 1;
+    if (atomicSub(&bc->active, 1) == 1 && cond.use) cudaGraphSetConditional(cond.h, 0u);
+}
+
+// The block's (a, b) go to its slot of the stage; true in the instance's
+// last block.
+__device__ __forceinline__ bool publish_inst(double a, double b, const BRed& red, int ntasks,
+                                             int inst, int count) {
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        red.part[blockIdx.x] = a;
+        red.part[ntasks + blockIdx.x] = b;
+        __threadfence();
+        const unsigned t = atomicAdd(&red.tickets[inst], 1u);
+        last = (t == (unsigned)count - 1u) ? 1 : 0;
+    }
+    __syncthreads();
+    return last != 0;
+}
+
+// In the instance's last block: its totals in block-table order (thread 0).
+__device__ __forceinline__ void gather_inst(const BRed& red, int ntasks, int inst, int first,
+                                            int count, double& A, double& B) {
+    __threadfence();
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < count; k += NT) {
+        a += __ldcg(red.part + first + k);
+        b += __ldcg(red.part + ntasks + first + k);
+    }
+    block_sum2(a, b);
+    if (threadIdx.x == 0) {
+        A = a;
+        B = b;
+        red.tickets[inst] = 0u;
+    }
+}
+
+// Start of every loop body: ends the loop once no instance is active, and
+// bounds the number of bodies.
+__global__ void kb_guard(BCtl* bc, Cond cond) {
+    if (threadIdx.x != 0) return;
+    bc->body += 1;
+    if (bc->active <= 0 || bc->body > bc->maxbody) {
+        if (cond.use) cudaGraphSetConditional(cond.h, 0u);
+    }
+}
+
+__global__ void __launch_bounds__(NT)
+    kb_fold(Plan p, const BInst* __restrict__ bi, const Ctl* ctl, int only_phase_end) {
+    const Task t = p.tasks[blockIdx.x];
+    const Ctl* c = &ctl[t.inst];
+    if (only_phase_end && (inst_done(c) || !c->phase_end)) return;
+    double2* xb = reinterpret_cast<double2*>(bi[t.inst].x);
+    float4* xw = reinterpret_cast<float4*>(bi[t.inst].xw);
+    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
+        const float4 w = xw[k];
+        if (w.x != 0.0f || w.z != 0.0f) {
+            double2 v = xb[k];
+            v.x += dw_d(make_float2(w.x, w.y));
+            v.y += dw_d(make_float2(w.z, w.w));
+            xb[k] = v;
+            xw[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
+// r = b - A x in FP64 from the FP64 base x: the start of a solve, or (start
+// = 0) the residual replacement of instances whose first phase ended.
+__global__ void __launch_bounds__(NT)
+    kb_residual(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, int start, BCtl* bc,
+                Cond cond) {
+    const Task t = p.tasks[blockIdx.x];
+    Ctl* c = &ctl[t.inst];
+    if (inst_done(c) || (!start && !c->phase_end)) return;
+    const BInst I = bi[t.inst];
+    const Geo& g = I.o.g;
+    const bool zero = start && c->x_zero;
+    double rr = 0.0, bb = 0.0;
+    for (unsigned s = t.begin + threadIdx.x; s < t.end; s += NT) {
+        const Col cl = col_of_slot(g, s);
+        if (!cl.valid) {
+            for (int l = 0; l < g.nz; ++l) {
+                I.r[(unsigned)l * g.plane + s] = make_float2(0.0f, 0.0f);
+                I.b0[(unsigned)l * g.plane + s] = 0.0f;
+            }
+            continue;
+        }
+        if (zero) {
+            for (int l = 0; l < g.nz; ++l) {
+                const unsigned id = (unsigned)l * g.plane + cl.s;
+                const double bv = I.b[id];
+                const float2 rw = dw_of(bv);
+                I.r[id] = rw;
+                I.b0[id] = rw.x;
+                bb += bv * bv;
+                rr += bv * bv;
+            }
+            continue;
+        }
+        double x_c = I.x[cl.s], x_b = 0.0;
+        float gu_b = 0.0f;
+        for (int l = 0; l < g.nz; ++l) {
+            const unsigned base = (unsigned)l * g.plane, id = base + cl.s;
+            const bool up = l < g.nz - 1;
+            const double x_a = up ? I.x[id + g.plane] : 0.0;
+            const float gu = I.o.gU[id];
+            double off = 0.0;
+            if (cl.i > 0) off += (double)I.o.gE[base + cl.sw] * I.x[base + cl.sw];
+            if (cl.i < g.nx - 1) off += (double)I.o.gE[id] * I.x[base + cl.se];
+            if (cl.j > 0) off += (double)I.o.gN[base + cl.ss] * I.x[base + cl.ss];
+            if (cl.j < g.ny - 1) off += (double)I.o.gN[id] * I.x[base + cl.sn];
+            if (l > 0) off += (double)gu_b * x_b;
+            if (up) off += (double)gu * x_a;
+            const double bv = I.b[id];
+            const double rv = bv - (I.diag[id] * x_c - off);
+            const float2 rw = dw_of(rv);
+            I.r[id] = rw;
+            I.b0[id] = rw.x;
+            rr += rv * rv;
+            bb += bv * bv;
+            x_b = x_c;
+            x_c = x_a;
+            gu_b = gu;
+        }
+    }
+    block_sum2(rr, bb);
+    if (publish_inst(rr, bb, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
+        double RR, BB;
+        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], RR, BB);
+        if (threadIdx.x == 0) {
+            c->rr = RR;
+            if (start) {
+                c->bb = BB;
+                if (BB == 0.0) {
+                    c->bb_zero = 1;
+                    c->converged = 1;
+                    c->relres = 0.0;
+                    inst_stop(c, bc, cond);
+                    return;
+                }
+            }
+            const double rel = sqrt(RR / c->bb);
+            c->relres = rel;
+            c->phase_end = 0;
+            if (!start) c->stop = c->tol;
+            if (rel < c->tol) {
+                c->converged = 1;
+                inst_stop(c, bc, cond);
+            } else if (!isfinite(rel)) {
+                c->breakdown = 1;
+                inst_stop(c, bc, cond);
+            } else if (c->iter >= c->maxit) {
+                inst_stop(c, bc, cond);
+            }
+        }
+    }
+}
+
+// Ap = d p - sum G p_nbr over cells [begin, end), p.Ap, alpha.
+__global__ void __launch_bounds__(NT)
+    kb_apply(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    const Task t = p.tasks[blockIdx.x];
+    Ctl* c = &ctl[t.inst];
+    if (inst_done(c)) return;
+    const OpView o = bi[t.inst].o;
+    const float2* __restrict__ pv = bi[t.inst].p;
+    const float2* __restrict__ dgw = bi[t.inst].dgw;
+    float2* __restrict__ Ap = bi[t.inst].Ap;
+    const Geo& g = o.g;
+    float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll 2
+    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
+        const unsigned l = k / g.plane;
+        const unsigned s = k - l * g.plane;
+        const Col cl = col_of_slot(g, s);
+        if (!cl.valid) {
+            Ap[k] = make_float2(0.0f, 0.0f);
+            continue;
+        }
+        const unsigned base = l * g.plane;
+        float2 off = make_float2(0.0f, 0.0f);
+        if (cl.i > 0) off = dw_add(off, dw_mul_f(pv[base + cl.sw], o.gE[base + cl.sw]));
+        if (cl.i < g.nx - 1) off = dw_add(off, dw_mul_f(pv[base + cl.se], o.gE[k]));
+        if (cl.j > 0) off = dw_add(off, dw_mul_f(pv[base + cl.ss], o.gN[base + cl.ss]));
+        if (cl.j < g.ny - 1) off = dw_add(off, dw_mul_f(pv[base + cl.sn], o.gN[k]));
+        if (l > 0) off = dw_add(off, dw_mul_f(pv[k - g.plane], o.gU[k - g.plane]));
+        if ((int)l < g.nz - 1) off = dw_add(off, dw_mul_f(pv[k + g.plane], o.gU[k]));
+        const float2 pc = pv[k];
+        const float2 a = dw_add(dw_mul(dgw[k], pc), dw_neg(off));
+        Ap[k] = a;
+        acc = dw_add(acc, dw_mul(pc, a));
+    }
+    double pap = dw_d(acc), unused = 0.0;
+    block_sum2(pap, unused);
+    if (publish_inst(pap, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
+        double PAP, U;
+        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], PAP, U);
+        if (threadIdx.x == 0) {
+            c->pAp = PAP;
+            if (!(PAP > 0.0) || !isfinite(PAP)) {
+                c->breakdown = 1;
+                c->alpha = 0.0;
+                inst_stop(c, bc, cond);
+            } else {
+                c->alpha = c->rz / PAP;
+                c->alpha_w = dw_of(c->alpha);
+            }
+        }
+    }
+}
+
+// x += alpha p, r -= alpha Ap, b0 = r, ||r||^2, the instance's convergence
+// test. Items are value pairs.
+__global__ void __launch_bounds__(NT)
+    kb_update(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    const Task t = p.tasks[blockIdx.x];
+    Ctl* c = &ctl[t.inst];
+    if (inst_done(c)) return;
+    const float2 a = c->alpha_w;
+    const float4* __restrict__ pp = reinterpret_cast<const float4*>(bi[t.inst].p);
+    const float4* __restrict__ ap = reinterpret_cast<const float4*>(bi[t.inst].Ap);
+    float4* __restrict__ x = reinterpret_cast<float4*>(bi[t.inst].xw);
+    float4* __restrict__ r = reinterpret_cast<float4*>(bi[t.inst].r);
+    float2* __restrict__ b0 = reinterpret_cast<float2*>(bi[t.inst].b0);
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
+        const float4 pv = pp[k], av = ap[k];
+        const float4 xv = x[k], rv = r[k];
+        const float2 x0 = dw_add(make_float2(xv.x, xv.y), dw_mul(a, make_float2(pv.x, pv.y)));
+        const float2 x1 = dw_add(make_float2(xv.z, xv.w), dw_mul(a, make_float2(pv.z, pv.w)));
+        const float2 r0 = dw_add(make_float2(rv.x, rv.y), dw_neg(dw_mul(a, make_float2(av.x, av.y))));
+        const float2 r1 = dw_add(make_float2(rv.z, rv.w), dw_neg(dw_mul(a, make_float2(av.z, av.w))));
+        x[k] = make_float4(x0.x, x0.y, x1.x, x1.y);
+        r[k] = make_float4(r0.x, r0.y, r1.x, r1.y);
+        b0[k] = make_float2(r0.x, r1.x);
+        acc = dw_add(acc, dw_mul(r0, r0));
+        acc = dw_add(acc, dw_mul(r1, r1));
+    }
+    double rr = dw_d(acc), unused = 0.0;
+    block_sum2(rr, unused);
+    if (publish_inst(rr, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
+        double RR, U;
+        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], RR, U);
+        if (threadIdx.x == 0) {
+            c->rr = RR;
+            c->iter += 1;
+            const double rel = sqrt(RR / c->bb);
+            c->relres = rel;
+            if (rel < c->tol) {
+                c->converged = 1;
+                inst_stop(c, bc, cond);
+            } else if (!isfinite(rel)) {
+                c->breakdown = 1;
+                inst_stop(c, bc, cond);
+            } else if (c->iter >= c->maxit) {
+                inst_stop(c, bc, cond);
+            } else if (rel < c->stop) {
+                c->phase_end = 1;  // the replacement at the end of this body
+            }
+        }
+    }
+}
+
+// rz = r.z, z.Ap, flexible beta.
+__global__ void __launch_bounds__(NT)
+    kb_dot(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    const Task t = p.tasks[blockIdx.x];
+    Ctl* c = &ctl[t.inst];
+    if (inst_done(c)) return;
+    const float4* __restrict__ r = reinterpret_cast<const float4*>(bi[t.inst].r);
+    const float4* __restrict__ ap = reinterpret_cast<const float4*>(bi[t.inst].Ap);
+    const float2* __restrict__ z = reinterpret_cast<const float2*>(bi[t.inst].z);
+    float2 rz = make_float2(0.0f, 0.0f), zap = make_float2(0.0f, 0.0f);
+    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
+        const float4 rv = r[k], av = ap[k];
+        const float2 zv = z[k];
+        rz = dw_add(rz, dw_mul_f(make_float2(rv.x, rv.y), zv.x));
+        rz = dw_add(rz, dw_mul_f(make_float2(rv.z, rv.w), zv.y));
+        zap = dw_add(zap, dw_mul_f(make_float2(av.x, av.y), zv.x));
+        zap = dw_add(zap, dw_mul_f(make_float2(av.z, av.w), zv.y));
+    }
+    double RZ0 = dw_d(rz), ZAP0 = dw_d(zap);
+    block_sum2(RZ0, ZAP0);
+    if (publish_inst(RZ0, ZAP0, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
+        double RZ, ZAP;
+        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], RZ, ZAP);
+        if (threadIdx.x == 0) {
+            c->beta = c->iter > 0 ? -ZAP / c->pAp : 0.0;
+            c->beta_w = dw_of(c->beta);
+            c->rz = RZ;
+            c->zAp = ZAP;
+            if (!isfinite(RZ) || !isfinite(c->beta)) {
+                c->breakdown = 1;
+                inst_stop(c, bc, cond);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NT)
+    kb_update_p(Plan p, const BInst* __restrict__ bi, const Ctl* ctl) {
+    const Task t = p.tasks[blockIdx.x];
+    const Ctl* c = &ctl[t.inst];
+    if (inst_done(c)) return;
+    const float2 beta = c->beta_w;
+    const bool first = c->iter == 0;
+    const float2* __restrict__ z = reinterpret_cast<const float2*>(bi[t.inst].z);
+    float4* __restrict__ pp = reinterpret_cast<float4*>(bi[t.inst].p);
+    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
+        const float2 zv = z[k];
+        if (first) {
+            pp[k] = make_float4(zv.x, 0.0f, zv.y, 0.0f);
+        } else {
+            const float4 pv = pp[k];
+            const float2 p0 = dw_add(dw_mul(beta, make_float2(pv.x, pv.y)), make_float2(zv.x, 0.0f));
+            const float2 p1 = dw_add(dw_mul(beta, make_float2(pv.z, pv.w)), make_float2(zv.y, 0.0f));
+            pp[k] = make_float4(p0.x, p0.y, p1.x, p1.y);
+        }
+    }
+}
+
+// Pairs of values: b = P + C/dt x (x = FP64 base, folded), x_old = x.
+__global__ void __launch_bounds__(NT)
+    kb_rhs_transient(Plan p, const BInst* __restrict__ bi, const Ctl* ctl) {
+    const Task t = p.tasks[blockIdx.x];
+    const double inv_dt = ctl[t.inst].inv_dt;
+    const BInst I = bi[t.inst];
+    const double2* __restrict__ P = reinterpret_cast<const double2*>(I.P);
+    const double2* __restrict__ x = reinterpret_cast<const double2*>(I.x);
+    const float2* __restrict__ cap = reinterpret_cast<const float2*>(I.o.cap);
+    double2* __restrict__ b = reinterpret_cast<double2*>(I.b);
+    double2* __restrict__ xold = reinterpret_cast<double2*>(I.xold);
+    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
+        const double2 xv = x[k], pv = P[k];
+        const float2 cv = cap[k];
+        b[k] = make_double2(__dadd_rn(pv.x, __dmul_rn(__dmul_rn((double)cv.x, inv_dt), xv.x)),
+                            __dadd_rn(pv.y, __dmul_rn(__dmul_rn((double)cv.y, inv_dt), xv.y)));
+        xold[k] = xv;
+    }
+}
+
+template <int MZ, bool ZERO, bool PRO>
+__global__ void __launch_bounds__(NT)
+    kb_sweep(Plan p, const LevelView<float>* __restrict__ views,
+             const LevelView<float>* __restrict__ cviews, int color, const Ctl* ctl) {
+    const Task t = p.tasks[blockIdx.x];
+    if (inst_done(&ctl[t.inst])) return;
+    const LevelView<float> L = views[t.inst];
+    const LevelView<float> C = PRO ? cviews[t.inst] : L;
+    for (unsigned q = t.begin + threadIdx.x; q < t.end; q += NT)
+        sweep_column<float, MZ, ZERO, PRO, false>(L, C, color, q);
+}
+
+__global__ void __launch_bounds__(NT)
+    kb_restrict(Plan p, const LevelView<float>* __restrict__ views,
+                const LevelView<float>* __restrict__ cviews, const Ctl* ctl) {
+    const Task t = p.tasks[blockIdx.x];
+    const Ctl* c = &ctl[t.inst];
+    if (inst_done(c)) return;
+    const LevelView<float> L = views[t.inst];
+    const LevelView<float> C = cviews[t.inst];
+    const float inv_dt = (float)c->inv_dt;
+    const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
+    for (unsigned w = t.begin + threadIdx.x; w < t.end; w += NT) {
+        const int l = (int)(w / ccols);
+        restrict_cell<float, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
+    }
+}
+
+template <int MZ>
+__global__ void __launch_bounds__(kSmallThreads, 1)
+    kb_small(const int* __restrict__ insts, const TailLevels<float>* __restrict__ small,
+             const Ctl* ctl) {
+    const int i = insts[blockIdx.x];
+    if (inst_done(&ctl[i])) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    vsmall_body<float, MZ>(small[i], (float)ctl[i].inv_dt, smem);
+}
+
+}  // namespace
+
+void launch_b_guard(cudaStream_t st, BCtl* bc, Cond cond) { kb_guard<<<1, 32, 0, st>>>(bc, cond); }
+
+void launch_b_fold(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, int only_phase_end) {
+    kb_fold<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, only_phase_end);
+}
+
+void launch_b_residual(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
+                       int start, BCtl* bc, Cond cond) {
+    kb_residual<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, start, bc, cond);
+}
+
+void launch_b_apply(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
+                    BCtl* bc, Cond cond) {
+    kb_apply<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+}
+
+void launch_b_update(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
+                     BCtl* bc, Cond cond) {
+    kb_update<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+}
+
+void launch_b_dot(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
+                  Cond cond) {
+    kb_dot<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+}
+
+void launch_b_update_p(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl) {
+    kb_update_p<<<p.ntasks, NT, 0, st>>>(p, bi, ctl);
+}
+
+void launch_b_rhs_transient(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl) {
+    kb_rhs_transient<<<p.ntasks, NT, 0, st>>>(p, bi, ctl);
+}
+
+void launch_b_sweep(cudaStream_t st, const Plan& p, const LevelView<float>* views,
+                    const LevelView<float>* cviews, int color, bool zero_x, bool prolong, int mz,
+                    const Ctl* ctl) {
+#define CT_BSWEEP(MZ)                                                                          \
+    do {                                                                                       \
+        if (zero_x)                                                                            \
+            kb_sweep<MZ, true, false><<<p.ntasks, NT, 0, st>>>(p, views, cviews, color, ctl);  \
+        else if (prolong)                                                                      \
+            kb_sweep<MZ, false, true><<<p.ntasks, NT, 0, st>>>(p, views, cviews, color, ctl);  \
+        else                                                                                   \
+            kb_sweep<MZ, false, false><<<p.ntasks, NT, 0, st>>>(p, views, cviews, color, ctl); \
+    } while (0)
+    if (mz <= 8)
+        CT_BSWEEP(8);
+    else if (mz <= 12)
+        CT_BSWEEP(12);
+    else if (mz <= 16)
+        CT_BSWEEP(16);
+    else if (mz <= 32)
+        CT_BSWEEP(32);
+    else
+        CT_BSWEEP(0);
+#undef CT_BSWEEP
+}
+
+void launch_b_restrict(cudaStream_t st, const Plan& p, const LevelView<float>* views,
+                       const LevelView<float>* cviews, const Ctl* ctl) {
+    kb_restrict<<<p.ntasks, NT, 0, st>>>(p, views, cviews, ctl);
+}
+
+cudaError_t launch_b_small(cudaStream_t st, const int* insts, int n,
+                           const TailLevels<float>* small, size_t smem, int mz, const Ctl* ctl) {
+    auto go = [&](auto kern) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSmallSmemMax);
+        if (e != cudaSuccess) return e;
+        kern<<<n, kSmallThreads, smem, st>>>(insts, small, ctl);
+        return cudaGetLastError();
+    };
+    if (mz <= 8) return go(kb_small<8>);
+    if (mz <= 12) return go(kb_small<12>);
+    if (mz <= 16) return go(kb_small<16>);
+    if (mz <= 32) return go(kb_small<32>);
+    return go(kb_small<0>);
+}
+
+}  // namespace ct

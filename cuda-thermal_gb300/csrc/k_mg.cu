@@ -17,11 +17,14 @@
 #include <cooperative_groups.h>
 
 #include "kernels.h"
+#include "mg_dev.cuh"
 #include "reduce.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace ct {
+
+using namespace mgdev;
 
 namespace {
 
@@ -130,201 +133,6 @@ __global__ void k_coarsen(Geo fg, const float* __restrict__ fgE, const float* __
     }
 }
 
-// Neighbour slots of an active column, and (for fused prolongation) the
-// coarse slots of those neighbours' parents.
-struct Nbr {
-    unsigned s, sw, se, ss, sn;
-    unsigned pw, pe, ps, pn;
-    bool w, e, so, no;
-};
-
-template <bool PRO>
-__device__ __forceinline__ Nbr neighbours(const Geo& g, const Geo& cg, int i, int j, int t,
-                                          int color) {
-    Nbr n;
-    const int oc = color ^ 1;
-    const unsigned row_o = (unsigned)(2 * j + oc) * (unsigned)g.hx;
-    n.s = (unsigned)(2 * j + color) * (unsigned)g.hx + (unsigned)t;
-    n.w = i > 0;
-    n.e = i < g.nx - 1;
-    n.so = j > 0;
-    n.no = j < g.ny - 1;
-    n.sw = row_o + (unsigned)((i - 1) >> 1);
-    n.se = row_o + (unsigned)((i + 1) >> 1);
-    n.ss = (unsigned)(2 * j - 2 + oc) * (unsigned)g.hx + (unsigned)t;
-    n.sn = (unsigned)(2 * j + 2 + oc) * (unsigned)g.hx + (unsigned)t;
-    if (PRO) {
-        n.pw = n.w ? scol(cg, (i - 1) >> 1, j >> 1) : 0u;
-        n.pe = n.e ? scol(cg, (i + 1) >> 1, j >> 1) : 0u;
-        n.ps = n.so ? scol(cg, i >> 1, (j - 1) >> 1) : 0u;
-        n.pn = n.no ? scol(cg, i >> 1, (j + 1) >> 1) : 0u;
-    }
-    return n;
-}
-
-// Loads of values that other blocks of the same kernel may have written
-// (x and b inside the cluster tail kernel) go to L2 (CG = true); everything
-// else may use the L1 path.
-template <bool CG, class T>
-__device__ __forceinline__ T ldm(const T* p) {
-    if (CG) return __ldcg(p);
-    return *p;
-}
-
-// Lateral neighbour sum of op_lat_sum (src/operator3d.h:62-78) at plane l:
-// west, east, south, north; with PRO each neighbour value carries its
-// parent's coarse correction.
-template <class T, bool PRO, bool CG>
-__device__ __forceinline__ T lat_sum(const LevelView<T>& L, const LevelView<T>& C, const Nbr& n,
-                                     int l) {
-    const unsigned base = (unsigned)l * L.g.plane;
-    const unsigned cbase = PRO ? (unsigned)l * C.g.plane : 0u;
-    T s = 0;
-    if (n.w) {
-        T xv = ldm<CG>(L.x + base + n.sw);
-        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.pw);
-        s += (T)L.gE[base + n.sw] * xv;
-    }
-    if (n.e) {
-        T xv = ldm<CG>(L.x + base + n.se);
-        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.pe);
-        s += (T)L.gE[base + n.s] * xv;
-    }
-    if (n.so) {
-        T xv = ldm<CG>(L.x + base + n.ss);
-        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.ps);
-        s += (T)L.gN[base + n.ss] * xv;
-    }
-    if (n.no) {
-        T xv = ldm<CG>(L.x + base + n.sn);
-        if (PRO) xv = xv + ldm<CG>(C.x + cbase + n.pn);
-        s += (T)L.gN[base + n.s] * xv;
-    }
-    return s;
-}
-
-// Line solve of the q-th column of colour `color` (mg_line_solve,
-// src/mg3d.h:179-196). With MZ > 0 (nz <= MZ) the column stays in registers:
-// every plane's right-hand side (b plus the lateral sum) is gathered first,
-// all loads independent of one another, then the Thomas recurrence runs on
-// registers and x is written once. MZ = 0 is the general path for deep
-// columns, with forward values going through x as in the reference.
-template <class T, int MZ, bool ZERO, bool PRO, bool CG>
-__device__ __forceinline__ void sweep_column(const LevelView<T>& L, const LevelView<T>& C,
-                                             int color, unsigned q) {
-    const Geo& g = L.g;
-    const int j = (int)(q / (unsigned)g.hx), t = (int)(q - (unsigned)j * g.hx);
-    const int i = 2 * t + ((j + color) & 1);
-    if (i >= g.nx) return;
-    const Nbr n = neighbours<PRO>(g, C.g, i, j, t, color);
-    if constexpr (MZ > 0) {
-        // Gather: every operand of every plane, all loads independent, so the
-        // whole column costs about one memory latency.
-        T v[MZ], fi[MZ], fc[MZ];
-        float gu[MZ];
-#pragma unroll
-        for (int l = 0; l < MZ; ++l) {
-            if (l < g.nz) {
-                const unsigned id = (unsigned)l * g.plane + n.s;
-                T rhs = ldm<CG>(L.b + id);
-                if (!ZERO) rhs = rhs + lat_sum<T, PRO, CG>(L, C, n, l);
-                v[l] = rhs;
-                fi[l] = L.finv[id];
-                fc[l] = L.fcp[id];
-                gu[l] = L.gU[id];
-            }
-        }
-        // Thomas recurrence on registers.
-        T prev = 0;
-#pragma unroll
-        for (int l = 0; l < MZ; ++l) {
-            if (l < g.nz) {
-                const T lower = l > 0 ? -(T)gu[l - 1] : T(0);
-                prev = (v[l] - lower * prev) * fi[l];
-                v[l] = prev;
-            }
-        }
-#pragma unroll
-        for (int l = MZ - 2; l >= 0; --l)
-            if (l < g.nz - 1) v[l] -= fc[l] * v[l + 1];
-#pragma unroll
-        for (int l = 0; l < MZ; ++l)
-            if (l < g.nz) L.x[(unsigned)l * g.plane + n.s] = v[l];
-    } else {
-        T prev = 0;
-        float gu_b = 0.0f;
-        for (int l = 0; l < g.nz; ++l) {
-            const unsigned id = (unsigned)l * g.plane + n.s;
-            T rhs = ldm<CG>(L.b + id);
-            if (!ZERO) rhs = rhs + lat_sum<T, PRO, CG>(L, C, n, l);
-            const T lower = l > 0 ? -(T)gu_b : T(0);
-            prev = (rhs - lower * prev) * L.finv[id];
-            L.x[id] = prev;
-            gu_b = L.gU[id];
-        }
-        for (int l = g.nz - 2; l >= 0; --l) {
-            const unsigned id = (unsigned)l * g.plane + n.s;
-            prev = ldm<CG>(L.x + id) - L.fcp[id] * prev;
-            L.x[id] = prev;
-        }
-    }
-}
-
-// (b - (A + C/dt) x) at fine cell (i, j, l), in op_apply's order
-// (src/operator3d.h:108-112): diagonal (lateral faces, up, down or ambient,
-// C/dt) times x, minus the six neighbour terms.
-template <class T, bool CG>
-__device__ __forceinline__ T residual_at(const LevelView<T>& F, T inv_dt, int i, int j, int l) {
-    const Geo& fg = F.g;
-    const Nbr n = neighbours<false>(fg, fg, i, j, i >> 1, (i + j) & 1);
-    const unsigned base = (unsigned)l * fg.plane, id = base + n.s;
-    const bool up = l < fg.nz - 1;
-    const T xc = ldm<CG>(F.x + id);
-    T d = 0, off = 0;
-    if (n.w) {
-        const T ge = (T)F.gE[base + n.sw];
-        d += ge;
-        off += ge * ldm<CG>(F.x + base + n.sw);
-    }
-    if (n.e) {
-        const T ge = (T)F.gE[id];
-        d += ge;
-        off += ge * ldm<CG>(F.x + base + n.se);
-    }
-    if (n.so) {
-        const T gn = (T)F.gN[base + n.ss];
-        d += gn;
-        off += gn * ldm<CG>(F.x + base + n.ss);
-    }
-    if (n.no) {
-        const T gn = (T)F.gN[id];
-        d += gn;
-        off += gn * ldm<CG>(F.x + base + n.sn);
-    }
-    const float gu = F.gU[id];
-    d += (T)gu;
-    d += l > 0 ? (T)F.gU[id - fg.plane] : (T)F.gB[n.s];
-    d += (T)F.cap[id] * inv_dt;
-    if (l > 0) off += (T)F.gU[id - fg.plane] * ldm<CG>(F.x + id - fg.plane);
-    if (up) off += (T)gu * ldm<CG>(F.x + id + fg.plane);
-    return ldm<CG>(F.b + id) - (d * xc - off);
-}
-
-// Restriction (src/pcg3d_cpu.cpp:87-100) of coarse cell (I, J, l), q = J cnx + I:
-// the sum over the (up to 4) children, j then i, of the fine residual.
-template <class T, bool CG>
-__device__ __forceinline__ void restrict_cell(const LevelView<T>& F, const LevelView<T>& C,
-                                              T inv_dt, unsigned q, int l) {
-    const Geo& fg = F.g;
-    const Geo& cg = C.g;
-    const int J = (int)(q / (unsigned)cg.nx), I = (int)(q - (unsigned)J * cg.nx);
-    const int i1 = min(2 * I + 2, fg.nx), j1 = min(2 * J + 2, fg.ny);
-    T sum = 0;
-    for (int j = 2 * J; j < j1; ++j)
-        for (int i = 2 * I; i < i1; ++i) sum += residual_at<T, CG>(F, inv_dt, i, j, l);
-    C.b[(unsigned)l * cg.plane + scol(cg, I, J)] = sum;
-}
-
 template <class T, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(NT)
     k_sweep(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
@@ -392,105 +200,13 @@ __global__ void __launch_bounds__(kTailThreads, 1)
     }
 }
 
-// The bottom of the V-cycle (levels k0 .. single column) in ONE block, with
-// every one of those levels held in shared memory: operator, factors, x and b
-// are copied in (the levels are a few tens of KB), the phases run with block
-// barriers, and level k0's x goes back out for the prolongation above it.
-// Same line-solve and restriction code as the grid-wide kernels, pointed at
-// shared memory.
+// The bottom of the V-cycle in one block from shared memory (mgdev::vsmall_body).
 template <class T, int MZ>
 __global__ void __launch_bounds__(kSmallThreads, 1)
     k_vsmall(TailLevels<T> tl, const Ctl* ctl, Cond cond) {
     if (loop_done(ctl, cond)) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ TailLevels<T> sl;  // views of the same levels, in shared memory
-    if (threadIdx.x == 0) sl.n = tl.n;
-    {
-        unsigned char* q = smem;
-        auto take = [&](size_t bytes) {
-            unsigned char* r = q;
-            q += (bytes + 15) & ~size_t(15);
-            return r;
-        };
-        for (int k = 0; k < tl.n; ++k) {
-            const LevelView<T>& G = tl.L[k];
-            LevelView<T> S;
-            const unsigned ln = G.g.plane * (unsigned)G.g.nz;
-            S.g = G.g;
-            float* gE = (float*)take(ln * 4);
-            float* gN = (float*)take(ln * 4);
-            float* gU = (float*)take(ln * 4);
-            float* cap = (float*)take(ln * 4);
-            float* gB = (float*)take(G.g.plane * 4);
-            T* fcp = (T*)take(ln * sizeof(T));
-            T* finv = (T*)take(ln * sizeof(T));
-            T* x = (T*)take(ln * sizeof(T));
-            T* b = (T*)take(ln * sizeof(T));
-            for (unsigned i = threadIdx.x; i < ln; i += kSmallThreads) {
-                gE[i] = G.gE[i];
-                gN[i] = G.gN[i];
-                gU[i] = G.gU[i];
-                cap[i] = G.cap[i];
-                fcp[i] = G.fcp[i];
-                finv[i] = G.finv[i];
-                if (k == 0) b[i] = G.b[i];
-            }
-            for (unsigned i = threadIdx.x; i < G.g.plane; i += kSmallThreads) gB[i] = G.gB[i];
-            S.gE = gE;
-            S.gN = gN;
-            S.gU = gU;
-            S.cap = cap;
-            S.gB = gB;
-            S.fcp = fcp;
-            S.finv = finv;
-            S.x = x;
-            S.b = b;
-            if (threadIdx.x == 0) sl.L[k] = S;
-        }
-    }
-    __syncthreads();
-    const unsigned tid = threadIdx.x, nth = kSmallThreads;
-    const T inv_dt = (T)ctl->inv_dt;
-    const int last = sl.n - 1;
-    // Each phase works on register copies of the level views: the views live
-    // in shared memory, where the sweeps also store x through generic
-    // pointers, so reading them in place would reload every field after
-    // every store.
-    for (int k = 0; k < last; ++k) {
-        const LevelView<T> L = sl.L[k];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
-        __syncthreads();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 1, q);
-        __syncthreads();
-        const LevelView<T> C = sl.L[k + 1];
-        const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
-        const unsigned work = ccols * (unsigned)C.g.nz;
-        for (unsigned w = tid; w < work; w += nth) {
-            const int l = (int)(w / ccols);
-            restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
-        }
-        __syncthreads();
-    }
-    {
-        const LevelView<T> L = sl.L[last];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
-        __syncthreads();
-    }
-    for (int k = last - 1; k >= 0; --k) {
-        const LevelView<T> L = sl.L[k];
-        const LevelView<T> C = sl.L[k + 1];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false>(L, C, 1, q);
-        __syncthreads();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 0, q);
-        __syncthreads();
-    }
-    const LevelView<T> S0 = sl.L[0];
-    const unsigned ln0 = S0.g.plane * (unsigned)S0.g.nz;
-    T* out = tl.L[0].x;
-    for (unsigned i = tid; i < ln0; i += nth) out[i] = S0.x[i];
+    mgdev::vsmall_body<T, MZ>(tl, (T)ctl->inv_dt, smem);
 }
 
 unsigned blocks_for(unsigned n) { return n == 0 ? 1u : (n + NT - 1) / NT; }

@@ -29,6 +29,7 @@
 
 #include "cthermal.h"
 #include "kernels.h"
+#include "solver.h"
 #include "status.h"
 
 namespace ct {
@@ -52,162 +53,7 @@ double ms_since(clk::time_point t) {
                             "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
-// Bump allocator over one device allocation, 256-byte aligned.
-struct Arena {
-    size_t used = 0;
-    size_t take(size_t bytes) {
-        const size_t off = used;
-        used += (bytes + 255) & ~size_t(255);
-        return off;
-    }
-};
-
-// Host-side record of one multigrid level.
-struct Level {
-    Geo g;
-    size_t o_gE, o_gN, o_gU, o_gB, o_cap, o_fcp, o_finv, o_x, o_b, o_dx, o_dy;
-    std::vector<double> dx, dy;  // cell widths (m), for the coarsening
-};
-
-// mg_coarse_widths (src/mg3d.h:250-256).
-std::vector<double> coarse_widths(const std::vector<double>& f) {
-    std::vector<double> c;
-    const int n = (int)f.size();
-    for (int I = 0; I < (n + 1) / 2; ++I) c.push_back(f[2 * I] + (2 * I + 1 < n ? f[2 * I + 1] : 0.0));
-    return c;
-}
-
-struct ProfEntry {
-    std::string name;
-    double bytes;
-    cudaEvent_t a, b;
-};
-
 }  // namespace
-
-class Solver {
-  public:
-    ct_precond pc = CT_MULTIGRID;
-    ct_precision prec = CT_MG_FP32_FLEX;
-    MgType mt = MG_F32;
-    bool flex = true;
-    bool dw = false;       // double-word outer iteration (CT_MG_FP32_FLEX_DW)
-    bool x_zero = true;    // x is known to be 0 (set_x_zero since the last solve)
-    cudaError_t launch_error = cudaSuccess;  // first failed launch of a shaped (cluster/smem) kernel
-    double rr_thr = 1e-5;  // relres of the FP64 residual replacement (dw)
-    size_t tsize = 4;  // bytes per V-cycle value
-    Geo g0{};
-    unsigned n = 0;      // slots of all planes (split layout, with padding)
-    size_t ncells = 0;   // nx * ny * nz
-    double dx = 0, dy = 0;
-    int sms = 0;
-    cudaStream_t st = nullptr;
-    cudaStream_t st_body = nullptr;  // captures the graph loops' bodies
-    cudaStream_t cs = nullptr;       // stream the enqueue_* functions launch on
-    char* base = nullptr;
-    size_t bytes = 0;
-    // fine operator and PCG vectors (split layout)
-    float *gE = nullptr, *gN = nullptr, *gU = nullptr, *gB = nullptr, *cap = nullptr;
-    double *P = nullptr, *x = nullptr, *b = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr;
-    double *diag = nullptr, *invd = nullptr, *xold = nullptr, *nat = nullptr, *part = nullptr;
-    float2* dgw = nullptr;  // double-word diagonal (dw)
-    float2* xwc = nullptr;  // double-word correction of x (dw); x is then its FP64 base
-    Ctl* ctl = nullptr;
-    Ctl* h_ctl = nullptr;  // pinned mirror
-    std::vector<Level> lv;
-    int maxb = 0;
-    double inv_dt = 0;
-    bool use_graphs = true;
-    bool have_cond = false;
-    size_t tail_k0 = 0;    // levels from tail_k0 down run in one cluster launch
-    size_t small_k0 = 0;   // levels from small_k0 down run in one block from shared memory
-    int tail_cluster = 1;  // CTAs in that cluster
-    cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
-    ct_setup_times times{};
-    // per-kernel timing (ct_profile_solve)
-    bool prof = false;
-    std::vector<ProfEntry> prof_log;
-
-    ~Solver() {
-        if (st) cudaStreamSynchronize(st);
-        for (cudaGraphExec_t g : {gx_solve, gx_init, gx_body, gx_replace})
-            if (g) cudaGraphExecDestroy(g);
-        if (base) cudaFree(base);
-        if (h_ctl) cudaFreeHost(h_ctl);
-        if (st_body) cudaStreamDestroy(st_body);
-        if (st) cudaStreamDestroy(st);
-    }
-
-    template <class T>
-    T* at(size_t off) const { return reinterpret_cast<T*>(base + off); }
-
-    OpView op() const { return OpView{g0, gE, gN, gU, gB, cap}; }
-
-    template <class T>
-    LevelView<T> view(size_t k) const {
-        const Level& L = lv[k];
-        LevelView<T> v;
-        v.g = L.g;
-        v.gE = at<float>(L.o_gE);
-        v.gN = at<float>(L.o_gN);
-        v.gU = at<float>(L.o_gU);
-        v.gB = at<float>(L.o_gB);
-        v.cap = at<float>(L.o_cap);
-        v.fcp = at<T>(L.o_fcp);
-        v.finv = at<T>(L.o_finv);
-        v.x = at<T>(L.o_x);
-        v.b = at<T>(L.o_b);
-        return v;
-    }
-
-    Red red(int blocks_wanted, Slot sl) const {
-        Red rd;
-        rd.part = part + (size_t)sl * 4 * maxb;
-        rd.maxb = maxb;
-        rd.blocks = std::max(1, std::min(blocks_wanted, maxb));
-        return rd;
-    }
-    Red red_cols(Slot sl) const { return red((int)((g0.plane + NT - 1) / NT), sl); }
-    Red red_vec(Slot sl) const { return red((int)((n / 2 + NT - 1) / NT), sl); }
-
-    ct_status create(const ct_model* m, ct_precond pc_, ct_precision prec_);
-    ct_status set_dt(double dt);
-    ct_status solve(double tol, int maxit, ct_stats* out);
-    ct_status record_graphs();
-
-    // Enqueues one kernel launch; in profiling mode brackets it with events.
-    template <class F>
-    void enq(const char* name, double nbytes, F&& launch) {
-        if (!prof) {
-            launch();
-            return;
-        }
-        ProfEntry e{name, nbytes, nullptr, nullptr};
-        cudaEventCreate(&e.a);
-        cudaEventCreate(&e.b);
-        cudaEventRecord(e.a, cs);
-        launch();
-        cudaEventRecord(e.b, cs);
-        prof_log.push_back(e);
-    }
-
-    void enqueue_init(Cond cond);
-    void enqueue_body(Cond cond);
-    void enqueue_replace(Cond cond);
-    // The double-word views of x, r, p, Ap (same storage as the FP64 vectors).
-    float2* xw() const { return xwc; }
-    float2* rw() const { return reinterpret_cast<float2*>(r); }
-    float2* pw() const { return reinterpret_cast<float2*>(p); }
-    float2* Apw() const { return reinterpret_cast<float2*>(Ap); }
-    // x as split-layout FP64: in the double-word mode the correction is first
-    // folded into the FP64 base (which leaves x unchanged).
-    const double* x_as_double(double*) const {
-        if (dw) launch_fold(st, n, x, xwc, ctl, false);
-        return x;
-    }
-    template <class T>
-    void vcycle(size_t k, Cond cond);
-};
 
 // ---- setup ---------------------------------------------------------------
 
@@ -251,8 +97,11 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     maxb = std::max(1, sms * (2048 / NT));
 
     auto t0 = clk::now();
-    CT_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    CT_CK(cudaStreamCreateWithFlags(&st_body, cudaStreamNonBlocking));
+    if (st)
+        own_stream = false;  // a batch's stream
+    else
+        CT_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    if (!skip_graphs) CT_CK(cudaStreamCreateWithFlags(&st_body, cudaStreamNonBlocking));
     cs = st;
     CT_CK(cudaMallocHost(&h_ctl, sizeof(Ctl)));
     std::memset(h_ctl, 0, sizeof(Ctl));
@@ -408,7 +257,7 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     times.factor_ms = ms_since(t0);
 
     t0 = clk::now();
-    if (use_graphs) {
+    if (use_graphs && !skip_graphs) {
         s = record_graphs();
         if (s != CT_OK) return s;
     }
@@ -710,10 +559,6 @@ ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
 }  // namespace ct
 
 // ---- C ABI ----------------------------------------------------------------
-
-struct ct_solver {
-    ct::Solver impl;
-};
 
 using ct::fail;
 

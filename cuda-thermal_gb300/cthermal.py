@@ -110,6 +110,22 @@ def _signatures():
         "ct_level_factors": (i, [vp, i, vp, vp]),
         "ct_profile_solve": (i, [vp, d, i, C.POINTER(CtStats), C.POINTER(CtKernelTime), i, ip]),
         "ct_true_relres_noalloc": (i, [C.POINTER(CtModel), vp, vp, vp]),
+        "ct_batch_create": (i, [i, vp, C.POINTER(vp)]),
+        "ct_batch_destroy": (i, [vp]),
+        "ct_batch_size": (i, [vp, ip]),
+        "ct_batch_set_dt": (i, [vp, vp]),
+        "ct_batch_set_x_zero": (i, [vp]),
+        "ct_batch_set_x": (i, [vp, i, vp]),
+        "ct_batch_set_rhs_steady": (i, [vp]),
+        "ct_batch_set_rhs_transient": (i, [vp]),
+        "ct_batch_set_power": (i, [vp, i, vp]),
+        "ct_batch_solve": (i, [vp, d, i, vp]),
+        "ct_batch_step_transient": (i, [vp, vp, d, i, vp]),
+        "ct_batch_get_x": (i, [vp, i, vp]),
+        "ct_batch_true_relres": (i, [vp, i, dp]),
+        "ct_batch_step_record": (i, [vp, i, d, C.POINTER(CtStepRecord)]),
+        "ct_batch_num_buckets": (i, [vp, ip]),
+        "ct_batch_bucket_info": (i, [vp, i, ip, ip, vp, vp]),
         "ct_model_planes": (i, [lp, i, ip, vp, vp]),
         "ct_model_finalize": (i, [gp, lp, vp, vp, d, d, d, d, vp, vp, vp, vp, vp, vp]),
         "ct_model_add_power_block": (i, [gp, lp, vp, i, d, d, d, d, d, vp]),
@@ -485,6 +501,113 @@ class GpuPcg:
         rows = [dict(name=out[k].name.decode(), launches=out[k].launches,
                      total_ms=out[k].total_ms, bytes=out[k].bytes) for k in range(n.value)]
         return PcgStats(st.iters, st.relres, bool(st.converged), bool(st.breakdown)), rows
+
+
+class GpuBatch:
+    """Many independent stacks solved together (ct_batch_*): one launch per
+    stage for all instances, per-instance scalars and convergence, one graph
+    per size bucket. Instance i is models[i]."""
+
+    def __init__(self, models):
+        self.models = list(models)
+        self._cms = [m.ct_model() for m in self.models]
+        arr = (C.POINTER(CtModel) * len(self._cms))(*[C.pointer(c) for c in self._cms])
+        h = C.c_void_p()
+        _check(lib().ct_batch_create(len(self._cms), C.cast(arr, C.c_void_p), C.byref(h)))
+        self._h = h
+
+    def __len__(self):
+        return len(self.models)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ct_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_dt(self, dt=None):
+        if dt is None:
+            _check(lib().ct_batch_set_dt(self._h, None))
+            return
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float64), (len(self),)))
+        _check(lib().ct_batch_set_dt(self._h, _ptr(d)))
+
+    def set_x_zero(self):
+        _check(lib().ct_batch_set_x_zero(self._h))
+
+    def set_x(self, i, T):
+        T = np.ascontiguousarray(T, np.float64)
+        assert T.size == self.models[i].ncells()
+        _check(lib().ct_batch_set_x(self._h, int(i), _ptr(T)))
+
+    def set_rhs_steady(self):
+        _check(lib().ct_batch_set_rhs_steady(self._h))
+
+    def set_rhs_transient(self):
+        _check(lib().ct_batch_set_rhs_transient(self._h))
+
+    def set_power(self, i, P):
+        P = np.ascontiguousarray(P, np.float64)
+        assert P.size == self.models[i].ncells()
+        _check(lib().ct_batch_set_power(self._h, int(i), _ptr(P)))
+
+    @staticmethod
+    def _stats(arr):
+        return [PcgStats(s.iters, s.relres, bool(s.converged), bool(s.breakdown)) for s in arr]
+
+    def solve(self, tol, maxit) -> List[PcgStats]:
+        st = (CtStats * len(self))()
+        _check(lib().ct_batch_solve(self._h, float(tol), int(maxit), C.cast(st, C.c_void_p)),
+               allow=(CT_OK, CT_NOT_CONVERGED, CT_BREAKDOWN))
+        return self._stats(st)
+
+    def step_transient(self, dt, tol, maxit) -> List[PcgStats]:
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float64), (len(self),)))
+        st = (CtStats * len(self))()
+        _check(lib().ct_batch_step_transient(self._h, _ptr(d), float(tol), int(maxit),
+                                             C.cast(st, C.c_void_p)),
+               allow=(CT_OK, CT_NOT_CONVERGED, CT_BREAKDOWN))
+        return self._stats(st)
+
+    def get_x(self, i, out: Optional[np.ndarray] = None) -> np.ndarray:
+        T = out if out is not None else np.empty(self.models[i].ncells())
+        _check(lib().ct_batch_get_x(self._h, int(i), _ptr(T)))
+        return T
+
+    def true_relres(self, i) -> float:
+        v = C.c_double()
+        _check(lib().ct_batch_true_relres(self._h, int(i), C.byref(v)))
+        return v.value
+
+    def step_record(self, i, dt) -> CtStepRecord:
+        r = CtStepRecord()
+        _check(lib().ct_batch_step_record(self._h, int(i), float(dt), C.byref(r)))
+        return r
+
+    def buckets(self) -> List[dict]:
+        nb = C.c_int()
+        _check(lib().ct_batch_num_buckets(self._h, C.byref(nb)))
+        out = []
+        for k in range(nb.value):
+            n, dep = C.c_int(), C.c_int()
+            _check(lib().ct_batch_bucket_info(self._h, k, C.byref(n), C.byref(dep), None, None))
+            sw = (C.c_uint * max(1, dep.value))()
+            rs = (C.c_uint * max(1, dep.value))()
+            _check(lib().ct_batch_bucket_info(self._h, k, None, None, sw, rs))
+            out.append(dict(instances=n.value, depth=dep.value,
+                            sweep_tiles=list(sw)[:dep.value], restrict_tiles=list(rs)[:dep.value]))
+        return out
 
 
 @dataclass

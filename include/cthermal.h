@@ -192,6 +192,44 @@ ct_status ct_level_factors(ct_solver* s, int k, double* fcp, double* finv);
 ct_status ct_true_relres_noalloc(const ct_model* m_dev, const double* T_dev, double* out_dev,
                                  void* stream);
 
+/* ---- batched solver -------------------------------------------------------- */
+/* No single counterpart in the reference, which solves one stack per GpuPcg
+ * (src/pcg3d.h:115-163); a batch is N independent GpuPcg-style solves of
+ * stacks of uneven size (nx, ny, nz per instance), advanced together: every
+ * stage of the iteration is one launch for all instances, each instance with
+ * its own scalars and convergence test, and the loop of each size bucket is
+ * one CUDA graph. Precision is fixed: FP32 V-cycle inside the flexible PCG
+ * with FP64 residuals (CT_MG_FP32_FLEX_DW). Instances are numbered 0..n-1 in
+ * the order of `models`, which are copied at creation. Per-instance calls
+ * mirror the single-solver calls (ct_set_power, ct_get_x, ...). */
+typedef struct ct_batch ct_batch;
+ct_status ct_batch_create(int n, const ct_model* const* models, ct_batch** out);
+ct_status ct_batch_destroy(ct_batch* b);
+ct_status ct_batch_size(const ct_batch* b, int* n);
+/* Per-instance time step (dt[i] = 0: steady); NULL: all steady. */
+ct_status ct_batch_set_dt(ct_batch* b, const double* dt);
+ct_status ct_batch_set_x_zero(ct_batch* b);
+ct_status ct_batch_set_x(ct_batch* b, int i, const double* T);
+ct_status ct_batch_set_rhs_steady(ct_batch* b);
+ct_status ct_batch_set_rhs_transient(ct_batch* b);
+ct_status ct_batch_set_power(ct_batch* b, int i, const double* P);
+/* Solves every instance to its own relres < tol (or maxit); stats[i] per
+ * instance (stats may be NULL). Returns CT_BREAKDOWN / CT_NOT_CONVERGED if
+ * any instance did. */
+ct_status ct_batch_solve(ct_batch* b, double tol, int maxit, ct_stats* stats);
+/* One backward-Euler step of every instance (step_once,
+ * src/transient3d.h:52-69): set_dt(dt), b = P + C/dt T, solve from T. */
+ct_status ct_batch_step_transient(ct_batch* b, const double* dt, double tol, int maxit,
+                                  ct_stats* stats);
+ct_status ct_batch_get_x(ct_batch* b, int i, double* T);
+ct_status ct_batch_true_relres(ct_batch* b, int i, double* out);
+ct_status ct_batch_step_record(ct_batch* b, int i, double dt, ct_step_record* out);
+/* Size buckets and the column tiles the autotuner picked for each of their
+ * depths (sweep_tiles / restrict_tiles: depth entries, may be NULL). */
+ct_status ct_batch_num_buckets(const ct_batch* b, int* nbuckets);
+ct_status ct_batch_bucket_info(const ct_batch* b, int k, int* ninst, int* depth,
+                               unsigned* sweep_tiles, unsigned* restrict_tiles);
+
 /* ---- per-kernel timing --------------------------------------------------- */
 typedef struct ct_kernel_time {
     char name[32];     /* kernel family, e.g. "mg_sweep_l0" */

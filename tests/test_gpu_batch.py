@@ -1,0 +1,206 @@
+"""Batched solver (ct_batch_*) against the oracle and the single solver,
+through the C ABI.
+
+Tolerances (written here, used below):
+  * every instance of a steady batch vs the FP64 oracle: max|dT| <= 1e-7 * Tmax
+    (far inside the stated 5e-4 K bound, also asserted) and FP64 true residual
+    <= 1.5e-10 for solves to 1e-10;
+  * vs the single solver in the same precision (CT_MG_FP32_FLEX_DW): iteration
+    counts within 1 (the per-instance reductions add the same values in a
+    different grouping);
+  * a batch run through graphs and the same batch run through direct launches
+    (fixed tiles): bit-identical;
+  * batched backward-Euler steps vs the single solver's steps: max|dT| <=
+    1e-7 * Tmax, the same step records within 1e-7, energy balance per step
+    within 1e-5 of the power (the step just after a power switch, solved to
+    1e-9 of ||P + C/dt T||, balances to about 1e-6).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import build_spec_model
+
+pytestmark = pytest.mark.gpu
+
+DT_BOUND_K = 5e-4
+
+
+def mixed_models(ct, golden):
+    """Uneven stacks: random floorplan stacks of the batched workload's kind,
+    plus golden cases of odd shapes (a single column, a single row, a tiny
+    grid)."""
+    import workloads
+    rng = np.random.default_rng(11)
+    ms = []
+    for _ in range(5):
+        m = workloads.batch_instance(rng)
+        ms.append(m)
+    for name in ("hotspot64", "blocks_tsv_17x13", "column1x1", "row1x9", "tiny3x5"):
+        ms.append(build_spec_model(ct, golden["cases"][name]["spec"]))
+    return ms
+
+
+def single_solve(ct, m, tol):
+    with ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX_DW) as s:
+        s.set_x_zero()
+        s.set_rhs_steady()
+        st = s.solve(tol, 50000)
+        return st, s.get_x()
+
+
+@pytest.fixture(scope="module")
+def mixed(ct, golden):
+    return mixed_models(ct, golden)
+
+
+def test_batch_steady_matches_oracle_and_single(ct, orc, mixed):
+    with ct.GpuBatch(mixed) as b:
+        b.set_x_zero()
+        b.set_rhs_steady()
+        stats = b.solve(1e-10, 50000)
+        for i, m in enumerate(mixed):
+            st = stats[i]
+            assert st.converged and not st.breakdown, (i, st)
+            T = b.get_x(i)
+            ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
+            tmax = np.abs(ref.T).max()
+            dT = np.abs(T - ref.T).max()
+            assert dT <= DT_BOUND_K
+            assert dT <= 1e-7 * tmax, (i, dT, tmax)
+            assert orc.true_relres(m, T) <= 1.5e-10
+            s1, T1 = single_solve(ct, m, 1e-10)
+            assert abs(st.iters - s1.iters) <= 1, (i, st.iters, s1.iters)
+            assert np.abs(T - T1).max() <= 1e-7 * tmax
+
+
+def test_batch_buckets_cover_instances(ct, mixed):
+    with ct.GpuBatch(mixed) as b:
+        info = b.buckets()
+        assert sum(k["instances"] for k in info) == len(mixed)
+        for k in info:
+            assert len(k["sweep_tiles"]) == k["depth"]
+            assert all(t in (256, 512, 1024, 2048) for t in k["sweep_tiles"])
+            assert all(t in (256, 512, 1024, 2048, 4096) for t in k["restrict_tiles"])
+
+
+def test_batch_resolve_and_power_change(ct, orc, mixed):
+    """Two solves in a row with a power map changed in between: the second
+    solve sees the new map, the other instances are unchanged."""
+    with ct.GpuBatch(mixed) as b:
+        b.set_x_zero()
+        b.set_rhs_steady()
+        b.solve(1e-10, 50000)
+        first = [b.get_x(i) for i in range(len(mixed))]
+        m0 = mixed[0]
+        P2 = m0.P * 2.0
+        b.set_power(0, P2)
+        b.set_x_zero()
+        b.set_rhs_steady()
+        stats = b.solve(1e-10, 50000)
+        assert all(s.converged for s in stats)
+        T0 = b.get_x(0)
+        # linear in P with T measured above ambient 0
+        assert np.abs(T0 - 2.0 * first[0]).max() <= 1e-7 * np.abs(T0).max()
+        for i in range(1, len(mixed)):
+            assert np.abs(b.get_x(i) - first[i]).max() <= 1e-9 * np.abs(first[i]).max()
+        b.set_power(0, m0.P)
+
+
+def test_batch_zero_power_instance(ct, golden):
+    """An instance with no heat converges at once with T = 0 (the reference's
+    bb = 0 exit, src/pcg3d_cpu.cpp:146) and leaves the others alone."""
+    m = build_spec_model(ct, golden["cases"]["hotspot64"]["spec"])
+    z = build_spec_model(ct, golden["cases"]["hotspot64"]["spec"])
+    z.P[:] = 0.0
+    with ct.GpuBatch([m, z, m]) as b:
+        b.set_x_zero()
+        b.set_rhs_steady()
+        stats = b.solve(1e-10, 50000)
+        assert stats[1].converged and stats[1].iters == 0
+        assert not b.get_x(1).any()
+        assert stats[0].iters == stats[2].iters > 0
+        assert np.array_equal(b.get_x(0), b.get_x(2))
+
+
+def test_batch_not_converged_reports(ct, mixed):
+    with ct.GpuBatch(mixed[:3]) as b:
+        b.set_x_zero()
+        b.set_rhs_steady()
+        stats = b.solve(1e-14, 2)
+        assert all(s.iters <= 2 for s in stats)
+        assert not all(s.converged for s in stats)
+
+
+def test_batch_graph_and_direct_bitwise(ct, mixed):
+    old = {k: os.environ.get(k) for k in ("CT_BATCH_TILE", "CT_COND_GRAPHS")}
+    try:
+        os.environ["CT_BATCH_TILE"] = "512"
+        out = []
+        for cond in ("1", "0"):
+            os.environ["CT_COND_GRAPHS"] = cond
+            with ct.GpuBatch(mixed) as b:
+                b.set_x_zero()
+                b.set_rhs_steady()
+                st = b.solve(1e-10, 50000)
+                out.append(([s.iters for s in st], [b.get_x(i) for i in range(len(mixed))]))
+        assert out[0][0] == out[1][0]
+        for a, c in zip(out[0][1], out[1][1]):
+            assert np.array_equal(a, c)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def test_batch_transient_matches_single(ct, golden):
+    """Backward-Euler steps with a different dt per instance, warm-started
+    from the steady field: the batch's steps equal the single solver's."""
+    import workloads
+    rng = np.random.default_rng(5)
+    ms = [workloads.batch_instance(rng) for _ in range(3)]
+    ms.append(build_spec_model(ct, golden["cases"]["blocks_tsv_17x13"]["spec"]))
+    n = len(ms)
+    dts = np.array([1e-5, 3e-5, 2e-4, 1e-3][:n])
+    singles = []
+    for m in ms:
+        s = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX_DW)
+        s.set_x_zero()
+        s.set_rhs_steady()
+        s.solve(1e-10, 50000)
+        singles.append(s)
+    powers = [ct.total_power(m) for m in ms]
+    with ct.GpuBatch(ms) as b:
+        b.set_x_zero()
+        b.set_rhs_steady()
+        b.solve(1e-10, 50000)
+        for step in range(4):
+            # change the power halfway (a switching schedule's event)
+            if step == 2:
+                for i, m in enumerate(ms):
+                    P = m.P * (0.5 + 0.25 * i)
+                    b.set_power(i, P)
+                    singles[i].set_power(P)
+                    powers[i] = float(np.sum(P))
+            dt = dts * (1.1 ** step)
+            stats = b.step_transient(dt, 1e-9, 50000)
+            for i, m in enumerate(ms):
+                s = singles[i]
+                s.set_dt(dt[i])
+                s.set_rhs_transient()
+                st1 = s.solve(1e-9, 50000)
+                assert stats[i].converged
+                assert abs(stats[i].iters - st1.iters) <= 1
+                T, T1 = b.get_x(i), s.get_x()
+                assert np.abs(T - T1).max() <= 1e-7 * np.abs(T1).max()
+                r, r1 = b.step_record(i, dt[i]), s.step_record(dt[i])
+                assert abs(r.q_out - r1.q_out) <= 1e-7 * abs(r1.q_out)
+                assert abs(r.q_stored - r1.q_stored) <= 1e-7 * max(abs(r1.q_stored), powers[i])
+                # energy balance: tol 1e-9 is relative to ||P + C/dt T||, so the
+                # balance holds to about 1e-6 of the power right after a switch
+                assert abs(r.q_out + r.q_stored - powers[i]) / powers[i] < 1e-5
+    for s in singles:
+        s.close()
