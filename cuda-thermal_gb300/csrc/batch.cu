@@ -27,6 +27,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -91,6 +92,7 @@ class Batch {
     double rr_thr = 1e-5;
     bool use_cond = true;
     bool prof = false;
+    std::vector<ProfEntry> prof_log;
     cudaError_t launch_error = cudaSuccess;  // first failed launch of the small-level kernel
 
     struct Bucket {
@@ -177,6 +179,32 @@ class Batch {
     }
 
     Solver& inst(int i) const { return sv[(size_t)i]->impl; }
+
+    // Enqueues one launch; in profiling mode brackets it with events.
+    template <class F>
+    void enq(cudaStream_t s, const std::string& name, double nbytes, F&& launch) {
+        if (!prof) {
+            launch();
+            return;
+        }
+        ProfEntry e{name, nbytes, nullptr, nullptr};
+        cudaEventCreate(&e.a);
+        cudaEventCreate(&e.b);
+        cudaEventRecord(e.a, s);
+        launch();
+        cudaEventRecord(e.b, s);
+        prof_log.push_back(e);
+    }
+    // Algorithmic bytes of a bucket's stage: per-cell bytes times the cells
+    // of level d of its instances (d < 0: fine cells).
+    double cells_of(const Bucket& b, int d) const {
+        double c = 0;
+        for (int i : b.inst) {
+            const Geo& g = inst(i).lv[(size_t)std::max(d, 0)].g;
+            c += (double)g.nx * g.ny * g.nz;
+        }
+        return c;
+    }
     int small_k0(int i) const { return (int)inst(i).small_k0; }
 
     ct_status create(int n, const ct_model* const* models);
@@ -417,38 +445,63 @@ ct_status Batch::tune_bucket(Bucket& b) {
 }
 
 void Batch::vcycle(Bucket& b, cudaStream_t s) {
+    // algorithmic bytes per level cell, as in the single solver
     for (int d = 0; d < b.depth; ++d) {
         const LevelView<float>* L = views[(size_t)d];
         const LevelView<float>* C = views[(size_t)d + 1];
-        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, true, false, b.mz, ctl);
-        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, false, b.mz, ctl);
-        launch_b_restrict(s, b.restr[(size_t)d], L, C, ctl);
+        const double N = cells_of(b, d);
+        const std::string lvl = "_d" + std::to_string(d);
+        enq(s, "b_sweep0" + lvl, N * 10,
+            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, true, false, b.mz, ctl); });
+        enq(s, "b_sweep" + lvl, N * 20,
+            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, false, b.mz, ctl); });
+        enq(s, "b_restrict" + lvl, N * 25, [&] { launch_b_restrict(s, b.restr[(size_t)d], L, C, ctl); });
     }
-    const cudaError_t e = launch_b_small(s, b.small_insts, (int)b.inst.size(), small, b.smem, b.mz, ctl);
-    if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
+    double smb = 0;
+    for (int i : b.inst) {
+        const Solver& v = inst(i);
+        for (size_t k = v.small_k0; k < v.lv.size(); ++k) {
+            const Geo& g = v.lv[k].g;
+            smb += (double)g.nx * g.ny * g.nz * (4 * 4 + 4 + 2 * 4 + 16);
+        }
+    }
+    enq(s, "b_small", smb, [&] {
+        const cudaError_t e = launch_b_small(s, b.small_insts, (int)b.inst.size(), small, b.smem, b.mz, ctl);
+        if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
+    });
     for (int d = b.depth; d-- > 0;) {
         const LevelView<float>* L = views[(size_t)d];
         const LevelView<float>* C = views[(size_t)d + 1];
-        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, true, b.mz, ctl);
-        launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, false, false, b.mz, ctl);
+        const double N = cells_of(b, d);
+        const std::string lvl = "_d" + std::to_string(d);
+        enq(s, "b_sweep" + lvl, N * 21,
+            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, true, b.mz, ctl); });
+        enq(s, "b_sweep" + lvl, N * 20,
+            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, false, false, b.mz, ctl); });
     }
 }
 
 void Batch::enqueue_init(Bucket& b, cudaStream_t s, Cond cond) {
-    launch_b_fold(s, b.vec, bi, ctl, 0);
-    launch_b_residual(s, b.cols, bi, ctl, b.r_res, 1, b.bc, cond);
+    const double N = cells_of(b, -1);
+    enq(s, "b_fold", N * 32, [&] { launch_b_fold(s, b.vec, bi, ctl, 0); });
+    enq(s, "b_residual", N * 56,
+        [&] { launch_b_residual(s, b.cols, bi, ctl, b.r_res, 1, b.bc, cond); });
 }
 
 void Batch::enqueue_body(Bucket& b, cudaStream_t s, Cond cond) {
+    const double N = cells_of(b, -1);
     launch_b_guard(s, b.bc, cond);
     vcycle(b, s);
-    launch_b_dot(s, b.vec, bi, ctl, b.r_dot, b.bc, cond);
-    launch_b_update_p(s, b.vec, bi, ctl);
-    launch_b_apply(s, b.cells, bi, ctl, b.r_apply, b.bc, cond);
-    launch_b_update(s, b.vec, bi, ctl, b.r_update, b.bc, cond);
+    enq(s, "b_dot", N * 20, [&] { launch_b_dot(s, b.vec, bi, ctl, b.r_dot, b.bc, cond); });
+    enq(s, "b_update_p", N * 20, [&] { launch_b_update_p(s, b.vec, bi, ctl); });
+    enq(s, "b_apply", N * 36, [&] { launch_b_apply(s, b.cells, bi, ctl, b.r_apply, b.bc, cond); });
+    enq(s, "b_update_xr", N * 52,
+        [&] { launch_b_update(s, b.vec, bi, ctl, b.r_update, b.bc, cond); });
     // residual replacement of the instances whose first phase just ended
-    launch_b_fold(s, b.vec, bi, ctl, 1);
-    launch_b_residual(s, b.cols, bi, ctl, b.r_res, 0, b.bc, cond);
+    // (blocks of the other instances return at entry)
+    enq(s, "b_fold_pe", 0, [&] { launch_b_fold(s, b.vec, bi, ctl, 1); });
+    enq(s, "b_residual_pe", 0,
+        [&] { launch_b_residual(s, b.cols, bi, ctl, b.r_res, 0, b.bc, cond); });
 }
 
 ct_status Batch::record(Bucket& b) {
@@ -710,6 +763,39 @@ ct_status ct_batch_true_relres(ct_batch* b, int i, double* out) {
 ct_status ct_batch_step_record(ct_batch* b, int i, double dt, ct_step_record* out) {
     CT_BATCH_INST(b, i);
     return ct_solver_step_record(b->impl.sv[(size_t)i].get(), dt, out);
+}
+
+ct_status ct_batch_profile_solve(ct_batch* b, double tol, int maxit, ct_stats* stats,
+                                 ct_kernel_time* out, int max, int* n) {
+    CT_BATCH_OK(b);
+    ct::Batch& B = b->impl;
+    B.prof = true;
+    B.prof_log.clear();
+    const ct_status s = B.solve(tol, maxit, stats);
+    B.prof = false;
+    cudaDeviceSynchronize();
+    std::vector<ct_kernel_time> agg;
+    for (const ct::ProfEntry& e : B.prof_log) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e.a, e.b);
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+        ct_kernel_time* k = nullptr;
+        for (ct_kernel_time& a : agg)
+            if (e.name == a.name) k = &a;
+        if (!k) {
+            agg.push_back(ct_kernel_time{});
+            k = &agg.back();
+            std::snprintf(k->name, sizeof k->name, "%s", e.name.c_str());
+        }
+        k->launches += 1;
+        k->total_ms += ms;
+        k->bytes += e.bytes;
+    }
+    B.prof_log.clear();
+    if (n) *n = (int)agg.size();
+    for (int k = 0; k < (int)agg.size() && k < max && out; ++k) out[k] = agg[(size_t)k];
+    return s;
 }
 
 ct_status ct_batch_num_buckets(const ct_batch* b, int* nbuckets) {

@@ -244,7 +244,12 @@ __device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
                 cap[i] = G.cap[i];
                 fcp[i] = G.fcp[i];
                 finv[i] = G.finv[i];
-                if (k == 0) b[i] = G.b[i];
+                // Padding slots are never written by the phases below but go
+                // back out with level k0's x: start every slot at zero, as the
+                // global arrays' padding is, so no stale shared-memory value
+                // (possibly a NaN) reaches the outer iteration.
+                x[i] = T(0);
+                b[i] = k == 0 ? G.b[i] : T(0);
             }
             for (unsigned i = threadIdx.x; i < G.g.plane; i += kSmallThreads) gB[i] = G.gB[i];
             S.gE = gE;

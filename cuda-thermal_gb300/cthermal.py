@@ -125,6 +125,7 @@ def _signatures():
         "ct_batch_true_relres": (i, [vp, i, dp]),
         "ct_batch_step_record": (i, [vp, i, d, C.POINTER(CtStepRecord)]),
         "ct_batch_num_buckets": (i, [vp, ip]),
+        "ct_batch_profile_solve": (i, [vp, d, i, vp, C.POINTER(CtKernelTime), i, ip]),
         "ct_batch_bucket_info": (i, [vp, i, ip, ip, vp, vp]),
         "ct_model_planes": (i, [lp, i, ip, vp, vp]),
         "ct_model_finalize": (i, [gp, lp, vp, vp, d, d, d, d, vp, vp, vp, vp, vp, vp]),
@@ -594,6 +595,17 @@ class GpuBatch:
         r = CtStepRecord()
         _check(lib().ct_batch_step_record(self._h, int(i), float(dt), C.byref(r)))
         return r
+
+    def profile_solve(self, tol, maxit):
+        st = (CtStats * len(self))()
+        out = (CtKernelTime * 256)()
+        n = C.c_int()
+        _check(lib().ct_batch_profile_solve(self._h, float(tol), int(maxit), C.cast(st, C.c_void_p),
+                                            out, 256, C.byref(n)),
+               allow=(CT_OK, CT_NOT_CONVERGED, CT_BREAKDOWN))
+        rows = [dict(name=out[k].name.decode(), launches=out[k].launches,
+                     total_ms=out[k].total_ms, bytes=out[k].bytes) for k in range(n.value)]
+        return self._stats(st), rows
 
     def buckets(self) -> List[dict]:
         nb = C.c_int()

@@ -242,6 +242,10 @@ typedef struct ct_kernel_time {
  * kernel family, and *n with the count. */
 ct_status ct_profile_solve(ct_solver* s, double tol, int maxit, ct_stats* st,
                            ct_kernel_time* out, int max, int* n);
+/* The same for a batch: every launch direct, the buckets one after another,
+ * per kernel family ("b_sweep_d0", "b_apply", ...) over all buckets. */
+ct_status ct_batch_profile_solve(ct_batch* b, double tol, int maxit, ct_stats* stats,
+                                 ct_kernel_time* out, int max, int* n);
 
 #ifdef __cplusplus
 }

@@ -176,7 +176,10 @@ def test_batch_transient_matches_single(ct, golden):
     with ct.GpuBatch(ms) as b:
         b.set_x_zero()
         b.set_rhs_steady()
-        b.solve(1e-10, 50000)
+        st0 = b.solve(1e-10, 50000)
+        for i in range(n):
+            assert st0[i].converged
+            assert b.true_relres(i) <= 1.5e-10, (i, st0[i], b.true_relres(i))
         for step in range(4):
             # change the power halfway (a switching schedule's event)
             if step == 2:
@@ -193,8 +196,8 @@ def test_batch_transient_matches_single(ct, golden):
                 s.set_rhs_transient()
                 st1 = s.solve(1e-9, 50000)
                 assert stats[i].converged
-                assert abs(stats[i].iters - st1.iters) <= 1
                 T, T1 = b.get_x(i), s.get_x()
+                assert abs(stats[i].iters - st1.iters) <= 1, (step, i, stats[i], st1, b.true_relres(i))
                 assert np.abs(T - T1).max() <= 1e-7 * np.abs(T1).max()
                 r, r1 = b.step_record(i, dt[i]), s.step_record(dt[i])
                 assert abs(r.q_out - r1.q_out) <= 1e-7 * abs(r1.q_out)
