@@ -4,15 +4,17 @@
 // Layout in HBM. Every vector and every operator array of every multigrid
 // level, the finest included, uses the colour-split layout: each row j of a
 // z-plane stores its red columns ((i + j) even) first and its black columns
-// after them, hx = ceil(nx / 2) slots each, so column (i, j) sits at
+// after them, hx slots each (ceil(nx / 2) rounded up to a multiple of 4, so
+// that every half-row starts on a 16-byte boundary, as bulk tensor copies
+// require), so column (i, j) sits at
 //     scol(i, j) = (2 j + ((i + j) & 1)) * hx + i / 2
 // and cell (i, j, l) at l * plane + scol(i, j), plane = ny * 2 * hx. A
 // red-black sweep then reads and writes one contiguous half-row per colour,
 // and its lateral neighbours are the other half of the same and adjacent rows.
 // The outer PCG vectors share this layout, so the fine level's operator is
 // stored once and the V-cycle reads the PCG residual with no permutation.
-// Padding slots (odd nx: one per row and colour parity) hold zero in every
-// vector and are never read as neighbours.
+// Padding slots (up to 4 per half-row) hold zero in every vector and are
+// never read as neighbours.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -32,7 +34,7 @@ __host__ __device__ inline Geo geo_of(int nx, int ny, int nz) {
     g.nx = nx;
     g.ny = ny;
     g.nz = nz;
-    g.hx = (nx + 1) / 2;
+    g.hx = (((nx + 1) / 2) + 3) & ~3;
     g.plane = (unsigned)ny * 2u * (unsigned)g.hx;
     return g;
 }
@@ -53,7 +55,7 @@ struct Ctl {
     // set by the host before a solve
     double tol;
     int maxit;
-    int pad0;
+    int err;  // set by a kernel whose bounded wait ran out (the solve then stops)
     // scalars of the iteration
     double inv_dt;
     double bb, rr, rz, pAp, zAp, alpha, beta, relres;

@@ -2,6 +2,7 @@
 // Every launcher enqueues on the given stream and returns without
 // synchronising, so the whole iteration can be captured into a CUDA graph.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "device.h"
@@ -118,6 +119,27 @@ void launch_factor(cudaStream_t st, const LevelView<T>& L, T inv_dt);
 template <class T>
 void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x,
                   const LevelView<T>* coarse_for_prolong, const Ctl* ctl, Cond cond);
+// The same sweep for the large FP32 levels, operands staged in shared memory
+// by bulk tensor copies (k_sweep_tma.cu). Tiles of kTileT x kTileJ columns,
+// one thread per column; the tensor maps cover one colour's rows of each
+// array (make_sweep_maps, built once per level and colour at set-up).
+constexpr int kTileT = 32;  // slots per tile row
+constexpr int kTileJ = 8;   // rows per tile
+constexpr int kTileThreads = kTileT * kTileJ;
+constexpr int kSweepStages = 4;  // planes in flight per block
+struct SweepMaps {
+    CUtensorMap b, fi, fc, gu, ge, gn;  // the sweep colour's rows, box kTileT x kTileJ
+    CUtensorMap ox;                     // other colour's x, box (kTileT + 8) x (kTileJ + 2)
+    CUtensorMap oge;                    // other colour's gE, box (kTileT + 8) x kTileJ
+    CUtensorMap ogn;                    // other colour's gN, box kTileT x (kTileJ + 1)
+};
+bool sweep_tma_fits(const Geo& g);  // nz <= 32 and at least one full tile row
+size_t sweep_tma_smem(bool zero_x);
+bool make_sweep_maps(const LevelView<float>& L, int color, SweepMaps* m, int tile_t = kTileT,
+                     int tile_j = kTileJ);
+void launch_sweep_tma(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L,
+                      const LevelView<float>* coarse_for_prolong, int color, bool zero_x, Ctl* ctl,
+                      Cond cond);
 // coarse b = sum over the children of (b - (A + C/dt) x).
 template <class T>
 void launch_restrict(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,

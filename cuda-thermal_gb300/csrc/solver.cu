@@ -25,6 +25,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "cthermal.h"
@@ -214,6 +215,20 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     CT_CK(cudaStreamSynchronize(st));
     times.alloc_ms = ms_since(t0);
 
+    // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
+    // (FP32 levels with at least one full tile row, above the shared-memory
+    // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernel.
+    {
+        const char* e = std::getenv("CT_SWEEP_TMA");
+        const bool want = mt == MG_F32 && !(e && e[0] == '0');
+        for (size_t k = 0; want && k < lv.size() && k < small_k0; ++k) {
+            Level& L = lv[k];
+            if (!sweep_tma_fits(L.g)) continue;
+            const LevelView<float> v = view<float>(k);
+            L.tma = make_sweep_maps(v, 0, &L.maps[0]) && make_sweep_maps(v, 1, &L.maps[1]);
+        }
+    }
+
     // Upload the fine operator and P through the natural staging buffer.
     t0 = clk::now();
     float* natf = reinterpret_cast<float*>(nat);
@@ -286,6 +301,18 @@ ct_status Solver::set_dt(double dt) {
 // ---- one PCG iteration ----------------------------------------------------
 
 template <class T>
+void Solver::sweep(size_t k, const LevelView<T>& L, int color, bool zero_x, const LevelView<T>* coarse,
+                   Cond cond) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (lv[k].tma) {
+            launch_sweep_tma(cs, lv[k].maps[color], L, coarse, color, zero_x, ctl, cond);
+            return;
+        }
+    }
+    launch_sweep<T>(cs, L, color, zero_x, coarse, ctl, cond);
+}
+
+template <class T>
 void Solver::vcycle(size_t k, Cond cond) {
     if (k == small_k0) {
         TailLevels<T> tl;
@@ -323,19 +350,18 @@ void Solver::vcycle(size_t k, Cond cond) {
     const double b_zero = cells / 2 * (4 * t + 4);
     const double b_sweep = cells / 2 * (4 * t + 12) + cells / 2 * (t + 8);
     if (k + 1 == lv.size()) {
-        enq(("mg_sweep0" + lvl).c_str(), b_zero,
-            [&] { launch_sweep<T>(cs, L, 0, true, nullptr, ctl, cond); });
+        enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
         return;
     }
     const LevelView<T> C = view<T>(k + 1);
-    enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { launch_sweep<T>(cs, L, 0, true, nullptr, ctl, cond); });
-    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(cs, L, 1, false, nullptr, ctl, cond); });
+    enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
+    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { sweep<T>(k, L, 1, false, nullptr, cond); });
     enq(("mg_restrict" + lvl).c_str(), cells * (2 * t + 16) + cells / 4 * t,
         [&] { launch_restrict<T>(cs, L, C, ctl, cond); });
     vcycle<T>(k + 1, cond);
     enq(("mg_sweep" + lvl).c_str(), b_sweep + cells / 4 * t,
-        [&] { launch_sweep<T>(cs, L, 1, false, &C, ctl, cond); });
-    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { launch_sweep<T>(cs, L, 0, false, nullptr, ctl, cond); });
+        [&] { sweep<T>(k, L, 1, false, &C, cond); });
+    enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { sweep<T>(k, L, 0, false, nullptr, cond); });
 }
 
 void Solver::enqueue_init(Cond cond) {
@@ -545,6 +571,9 @@ ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
         if (xwc) CT_CK(cudaMemsetAsync(xwc, 0, (size_t)n * 8, st));
         CT_CK(cudaStreamSynchronize(st));
     }
+    if (h_ctl->err)
+        return fail(CT_TIMEOUT, "a bounded wait for staged level data ran out (solve stopped after %d iterations)",
+                    h_ctl->iter);
     ct_stats s;
     s.iters = h_ctl->iter;
     s.relres = h_ctl->relres;

@@ -27,6 +27,8 @@ struct Level {
     Geo g;
     size_t o_gE, o_gN, o_gU, o_gB, o_cap, o_fcp, o_finv, o_x, o_b, o_dx, o_dy;
     std::vector<double> dx, dy;  // cell widths (m), for the coarsening
+    bool tma = false;            // sweeps staged by bulk tensor copies (maps per colour)
+    SweepMaps maps[2];
 };
 
 // mg_coarse_widths (src/mg3d.h:250-256).
@@ -168,6 +170,10 @@ class Solver {
     }
     template <class T>
     void vcycle(size_t k, Cond cond);
+    // One sweep of level k (the staged kernel where the level has its maps).
+    template <class T>
+    void sweep(size_t k, const LevelView<T>& L, int color, bool zero_x, const LevelView<T>* coarse,
+               Cond cond);
 };
 
 

@@ -1,0 +1,85 @@
+// tma.cuh - bulk tensor copies (TMA) into shared memory and the mbarriers
+// that track them, as inline PTX for sm_103a.
+//
+// Every wait on an mbarrier is bounded: after kWaitLimit polls it gives up and
+// returns false, and the caller records the failure and leaves (after waiting,
+// again bounded, for its own copies still in flight).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace ct {
+namespace tma {
+
+constexpr unsigned kWaitLimit = 1u << 22;  // polls of one mbarrier wait (about a second)
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+// Makes initialised mbarriers visible to the async proxy (TMA).
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// One arrival that also announces `bytes` of incoming transactions.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (unsigned k = 0; k < kWaitLimit; ++k)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// 3-D tiled bulk tensor load of one box into shared memory, completing on
+// `bar`. Coordinates are element indices (x innermost); x * 4 bytes must be a
+// multiple of 16 (the caller keeps x a multiple of 4 for 4-byte elements).
+// Out-of-range elements of the box are filled with zeros.
+__device__ __forceinline__ void load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                        uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+}  // namespace tma
+
+// Host: encodes a 3-D float tensor map over a split-layout array (rows of one
+// colour: x = slot within the half-row, y = row j, z = plane) with box
+// (bx, by, 1). base = the array plus the colour's half-row offset.
+// Returns false if the driver rejects it.
+bool encode_rows_map(CUtensorMap* out, const float* base, int hx, int ny, int nz,
+                     unsigned plane, unsigned bx, unsigned by);
+
+}  // namespace ct
