@@ -9,7 +9,10 @@ double-word arithmetic on the FP32 pipes with one FP64 residual replacement
 larger than L2 (the fine level alone moves > 1 GB per iteration), so no L2
 flush is needed between steps.
 
-Reported beside it, on the same GPU: the FP32 V-cycle in FP64 flexible PCG
+Reported beside it, on the same GPU: the batched form on a 256-instance
+floorplan sweep (uneven stacks solved together, instance solves/s against
+the plain FP64 MG-PCG solving the same instances one by one), the FP32
+V-cycle in FP64 flexible PCG
 (CT_MG_FP32_FLEX), the plain FP64 MG-PCG (FP64 V-cycle), max|dT| and the
 FP64 true residual of each, the end-to-end rate through the C ABI with the
 power map copied in and the temperatures copied out every step, the
@@ -41,6 +44,8 @@ N_GRID = 800
 TOL = 1e-10
 MAXIT = 1000
 SEED = 2
+BATCH_N = 256   # instances of the batched floorplan sweep
+BATCH_SEED = 4
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -75,10 +80,20 @@ class ClockSampler:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.file, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the timed region starts once the sampler is producing samples
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0:
+            try:
+                if os.path.getsize(self.file.name) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.02)
 
     def stop(self):
         if not self.proc:
@@ -263,6 +278,90 @@ def traffic_from_profiles(kernel_name):
     return None
 
 
+def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
+    """The batched form on the 256-instance floorplan sweep: uneven stacks
+    (nx, ny in 64..512, 6-16 planes), all solved to 1e-10 together, against
+    the plain FP64 MG-PCG solving the same instances one after another."""
+    import workloads
+    t0 = time.perf_counter()
+    models = workloads.batch_instances(BATCH_N, seed=BATCH_SEED)
+    cells = sum(m.ncells() for m in models)
+    b = ct.GpuBatch(models)
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        b.set_x_zero()
+        b.set_rhs_steady()
+        b.solve(TOL, MAXIT)
+    stream = torch.cuda.ExternalStream(b.stream())
+    kb = max(3, args.steps // 3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(kb):
+        b.set_x_zero()
+        b.set_rhs_steady()
+        st = b.solve(TOL, MAXIT)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / kb
+    iters = [s.iters for s in st]
+    conv = sum(1 for s in st if s.converged)
+    Tb = [b.get_x(i) for i in range(len(models))]
+    true_max = max(b.true_relres(i) for i in range(len(models)))
+    # per-kernel profile of one batched solve (direct launches, buckets in turn)
+    b.set_x_zero()
+    b.set_rhs_steady()
+    _, rows = b.profile_solve(TOL, MAXIT)
+    rows.sort(key=lambda r: -r["total_ms"])
+    top = rows[0]
+    achieved = top["bytes"] / (top["total_ms"] / 1e3) / 1e9
+    buckets = b.buckets()
+    b.close()
+    # the same instances, one FP64 MG-PCG solve each, back to back
+    ms64 = 0.0
+    it64 = []
+    max_dT = 0.0
+    for i, m in enumerate(models):
+        with ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP64) as s:
+            s.set_x_zero()
+            s.set_rhs_steady()
+            s.solve(TOL, MAXIT)
+            ev = torch.cuda.ExternalStream(s.stream())
+            torch.cuda.synchronize()
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(ev)
+            s.set_x_zero()
+            s.set_rhs_steady()
+            r = s.solve(TOL, MAXIT)
+            a1.record(ev)
+            torch.cuda.synchronize()
+            ms64 += a0.elapsed_time(a1)
+            it64.append(r.iters)
+            max_dT = max(max_dT, float(np.abs(s.get_x() - Tb[i]).max()))
+    value = len(models) / (ms / 1e3)
+    value64 = len(models) / (ms64 / 1e3)
+    return {
+        "value": value, "unit": "instance solves/s",
+        "workload": f"{len(models)} seeded stacks, nx, ny in 64..512 step 32, 6-16 planes, "
+                    f"12 log-normal floorplan blocks per tier, tol {TOL:g} per instance",
+        "instances": len(models), "cells": cells, "ms_per_batch_solve": ms, "batch_solves": kb,
+        "iters_min": min(iters), "iters_max": max(iters), "converged": conv,
+        "true_relres_max": true_max, "max_dT_K_vs_fp64": max_dT,
+        "fp64_mg_pcg_sequential": {"value": value64, "unit": "instance solves/s",
+                                   "ms_total": ms64, "iters_max": max(it64)},
+        "speedup_vs_fp64": value / value64,
+        "setup_s": setup_s,
+        "buckets": [{"instances": k["instances"], "depth": k["depth"], "staged": k["staged"],
+                     "sweep_tiles": k["sweep_tiles"]} for k in buckets],
+        "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_kind": peak_kind, "share": top["total_ms"] / sum(r["total_ms"] for r in rows)},
+        "kernels": [{"name": r["name"], "launches": r["launches"], "ms": round(r["total_ms"], 3),
+                     "GBs": round(r["bytes"] / (r["total_ms"] / 1e3) / 1e9, 1)} for r in rows[:8]],
+        "gpu_launches_per_batch_solve": sum(r["launches"] for r in rows),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -270,6 +369,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched 256-instance run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -300,7 +400,6 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     ms32, st32 = timed_solves(ct, s32, args.steps, world)
-    clk = clocks.stop()
     T32 = s32.get_x()
     true32 = s32.true_relres()
     ms32 = max_over_ranks(ms32, world)
@@ -362,6 +461,14 @@ def main():
     nlev = s32.num_levels()
     launches_per_solve = sum(r["launches"] for r in rows)
 
+    batched = None
+    if not args.no_batch:
+        batched = bench_batched(ct, np, torch, args, hbm_peak, peak_kind)
+        if world > 1:
+            batched["value"] = sum_over_ranks(batched["value"], world)
+    # clocks sampled over every timed region above (headline, FP64, e2e, batched)
+    clk = clocks.stop()
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = host_threads()
@@ -408,6 +515,8 @@ def main():
             "gpu_launches": launches_per_solve * args.steps,
             "clocks": clk,
         }
+        if batched:
+            out["batched"] = batched
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)

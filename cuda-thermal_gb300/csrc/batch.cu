@@ -58,6 +58,8 @@ constexpr unsigned kCellChunk = 2048;  // fine cells (operator apply)
 // Candidate tiles of the autotuner (columns per block for the sweeps, coarse
 // cells per block for the restriction).
 constexpr unsigned kSweepTiles[] = {256, 512, 1024, 2048};
+// ... and tiles per block of the staged sweeps (k_sweep_tma.cu).
+constexpr unsigned kTmaTiles[] = {1, 2, 4, 8};
 constexpr unsigned kRestrictTiles[] = {256, 512, 1024, 2048, 4096};
 
 // Host form of a block table; first/count are indexed by instance.
@@ -107,6 +109,7 @@ class Batch {
         BRed r_res{}, r_apply{}, r_update{}, r_dot{};
         std::vector<Plan> sweep, restr;
         std::vector<unsigned> sweep_tile, restr_tile;
+        std::vector<char> tma;  // per depth: sweeps staged by bulk tensor copies
         int* small_insts = nullptr;
     };
     std::vector<Bucket> bk;
@@ -116,6 +119,8 @@ class Batch {
     Ctl* ctl = nullptr;
     Ctl* h_ctl = nullptr;  // pinned mirror
     std::vector<LevelView<float>*> views;  // per depth: LevelView per instance
+    std::vector<SweepMaps*> bmaps;         // per depth and colour (2 d + c): maps per instance
+    std::vector<std::vector<char>> fits;   // [d][i]: instance i's level d has maps
     TailLevels<float>* small = nullptr;
     std::vector<void*> bufs;               // every device allocation of the batch
     cudaEvent_t ev_start = nullptr;
@@ -217,7 +222,8 @@ class Batch {
     // One bucket's launches.
     void enqueue_init(Bucket& b, cudaStream_t s, Cond cond);
     void enqueue_body(Bucket& b, cudaStream_t s, Cond cond);
-    void vcycle(Bucket& b, cudaStream_t s);
+    void vcycle(Bucket& b, cudaStream_t s, Cond cond);
+    void sweep(Bucket& b, cudaStream_t s, int d, int color, bool zero_x, bool prolong, Cond cond);
 };
 
 ct_status Batch::create(int n, const ct_model* const* models) {
@@ -290,6 +296,26 @@ ct_status Batch::create(int n, const ct_model* const* models) {
             else std::memset(&hv[(size_t)i], 0, sizeof(LevelView<float>));
         if ((s = upload(&views[(size_t)d], hv)) != CT_OK) return s;
     }
+    // Tensor maps of the levels whose sweeps are staged (CT_SWEEP_TMA=0: none).
+    {
+        const char* e = std::getenv("CT_SWEEP_TMA");
+        const bool want = !(e && e[0] == '0');
+        bmaps.assign((size_t)2 * (maxdepth + 1), nullptr);
+        fits.assign((size_t)maxdepth + 1, std::vector<char>((size_t)n, 0));
+        for (int d = 0; d <= maxdepth; ++d) {
+            std::vector<SweepMaps> hm[2] = {std::vector<SweepMaps>((size_t)n),
+                                            std::vector<SweepMaps>((size_t)n)};
+            for (int c = 0; c < 2; ++c) std::memset(hm[c].data(), 0, sizeof(SweepMaps) * (size_t)n);
+            for (int i = 0; i < n; ++i) {
+                if (!want || d >= small_k0(i) || !sweep_tma_fits(inst(i).lv[(size_t)d].g)) continue;
+                const LevelView<float> v = inst(i).view<float>((size_t)d);
+                fits[(size_t)d][(size_t)i] = make_sweep_maps(v, 0, &hm[0][(size_t)i]) &&
+                                             make_sweep_maps(v, 1, &hm[1][(size_t)i]);
+            }
+            for (int c = 0; c < 2; ++c)
+                if ((s = upload(&bmaps[(size_t)(2 * d + c)], hm[c])) != CT_OK) return s;
+        }
+    }
     std::vector<TailLevels<float>> ht((size_t)n);
     for (int i = 0; i < n; ++i) {
         const Solver& v = inst(i);
@@ -359,6 +385,12 @@ ct_status Batch::build_bucket(Bucket& b) {
     b.sweep.assign((size_t)b.depth, Plan{});
     b.restr.assign((size_t)b.depth, Plan{});
     b.sweep_tile.assign((size_t)b.depth, 512);
+    b.tma.assign((size_t)b.depth, 0);
+    for (int d = 0; d < b.depth; ++d) {
+        bool all = true;
+        for (int i : b.inst) all = all && fits[(size_t)d][(size_t)i];
+        b.tma[(size_t)d] = all ? 1 : 0;
+    }
     b.restr_tile.assign((size_t)b.depth, 1024);
     return CT_OK;
 }
@@ -367,8 +399,9 @@ ct_status Batch::build_bucket(Bucket& b) {
 // candidates on the bucket's own levels (the level arrays are scratch between
 // solves, so the timing runs leave nothing behind that a solve reads).
 ct_status Batch::tune_bucket(Bucket& b) {
-    unsigned fixed = 0;
+    unsigned fixed = 0, fixed_tma = 0;
     if (const char* e = std::getenv("CT_BATCH_TILE")) fixed = (unsigned)std::atol(e);
+    if (const char* e = std::getenv("CT_BATCH_TMA_TILES")) fixed_tma = (unsigned)std::atol(e);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CT_BK(cudaEventCreate(&e0));
     CT_BK(cudaEventCreate(&e1));
@@ -378,7 +411,8 @@ ct_status Batch::tune_bucket(Bucket& b) {
         for (int i : b.inst) {
             const Geo& g = inst(i).lv[(size_t)d].g;
             const Geo& c = inst(i).lv[(size_t)d + 1].g;
-            sweep_items.push_back((unsigned)g.ny * (unsigned)g.hx);
+            sweep_items.push_back(b.tma[(size_t)d] ? (unsigned)sweep_tma_tiles(g)
+                                                   : (unsigned)g.ny * (unsigned)g.hx);
             restr_items.push_back((unsigned)c.nx * (unsigned)c.ny * (unsigned)c.nz);
         }
         auto time_of = [&](auto&& launch) -> float {
@@ -397,8 +431,11 @@ ct_status Batch::tune_bucket(Bucket& b) {
         };
         // sweeps
         {
+            const bool tma = b.tma[(size_t)d] != 0;
             std::vector<unsigned> cands;
-            if (fixed) cands.push_back(fixed);
+            if (tma && fixed_tma) cands.push_back(fixed_tma);
+            else if (tma) cands.assign(std::begin(kTmaTiles), std::end(kTmaTiles));
+            else if (fixed) cands.push_back(fixed);
             else cands.assign(std::begin(kSweepTiles), std::end(kSweepTiles));
             float best = 1e30f;
             for (unsigned tile : cands) {
@@ -406,7 +443,11 @@ ct_status Batch::tune_bucket(Bucket& b) {
                 if ((s = upload_plan(make_plan(ni, b.inst, sweep_items, tile), &p)) != CT_OK) break;
                 CT_BK(cudaStreamSynchronize(st));
                 const float t = cands.size() == 1 ? 0.0f : time_of([&] {
-                    launch_b_sweep(b.st, p, views[(size_t)d], views[(size_t)d], 1, false, false, b.mz, ctl);
+                    if (tma)
+                        launch_b_sweep_tma(b.st, p, bmaps[(size_t)(2 * d + 1)], views[(size_t)d],
+                                           views[(size_t)d], 1, false, false, b.mz, ctl, b.bc, Cond{0, 0});
+                    else
+                        launch_b_sweep(b.st, p, views[(size_t)d], views[(size_t)d], 1, false, false, b.mz, ctl);
                 });
                 if (t < best) {
                     best = t;
@@ -444,7 +485,17 @@ ct_status Batch::tune_bucket(Bucket& b) {
     return CT_OK;
 }
 
-void Batch::vcycle(Bucket& b, cudaStream_t s) {
+void Batch::sweep(Bucket& b, cudaStream_t s, int d, int color, bool zero_x, bool prolong, Cond cond) {
+    const LevelView<float>* L = views[(size_t)d];
+    const LevelView<float>* C = views[(size_t)d + 1];
+    if (b.tma[(size_t)d])
+        launch_b_sweep_tma(s, b.sweep[(size_t)d], bmaps[(size_t)(2 * d + color)], L, C, color, zero_x,
+                           prolong, b.mz, ctl, b.bc, cond);
+    else
+        launch_b_sweep(s, b.sweep[(size_t)d], L, C, color, zero_x, prolong, b.mz, ctl);
+}
+
+void Batch::vcycle(Bucket& b, cudaStream_t s, Cond cond) {
     // algorithmic bytes per level cell, as in the single solver
     for (int d = 0; d < b.depth; ++d) {
         const LevelView<float>* L = views[(size_t)d];
@@ -452,9 +503,9 @@ void Batch::vcycle(Bucket& b, cudaStream_t s) {
         const double N = cells_of(b, d);
         const std::string lvl = "_d" + std::to_string(d);
         enq(s, "b_sweep0" + lvl, N * 10,
-            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, true, false, b.mz, ctl); });
+            [&] { sweep(b, s, d, 0, true, false, cond); });
         enq(s, "b_sweep" + lvl, N * 20,
-            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, false, b.mz, ctl); });
+            [&] { sweep(b, s, d, 1, false, false, cond); });
         enq(s, "b_restrict" + lvl, N * 25, [&] { launch_b_restrict(s, b.restr[(size_t)d], L, C, ctl); });
     }
     double smb = 0;
@@ -470,14 +521,12 @@ void Batch::vcycle(Bucket& b, cudaStream_t s) {
         if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
     });
     for (int d = b.depth; d-- > 0;) {
-        const LevelView<float>* L = views[(size_t)d];
-        const LevelView<float>* C = views[(size_t)d + 1];
         const double N = cells_of(b, d);
         const std::string lvl = "_d" + std::to_string(d);
         enq(s, "b_sweep" + lvl, N * 21,
-            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 1, false, true, b.mz, ctl); });
+            [&] { sweep(b, s, d, 1, false, true, cond); });
         enq(s, "b_sweep" + lvl, N * 20,
-            [&] { launch_b_sweep(s, b.sweep[(size_t)d], L, C, 0, false, false, b.mz, ctl); });
+            [&] { sweep(b, s, d, 0, false, false, cond); });
     }
 }
 
@@ -491,7 +540,7 @@ void Batch::enqueue_init(Bucket& b, cudaStream_t s, Cond cond) {
 void Batch::enqueue_body(Bucket& b, cudaStream_t s, Cond cond) {
     const double N = cells_of(b, -1);
     launch_b_guard(s, b.bc, cond);
-    vcycle(b, s);
+    vcycle(b, s, cond);
     enq(s, "b_dot", N * 20, [&] { launch_b_dot(s, b.vec, bi, ctl, b.r_dot, b.bc, cond); });
     enq(s, "b_update_p", N * 20, [&] { launch_b_update_p(s, b.vec, bi, ctl); });
     enq(s, "b_apply", N * 36, [&] { launch_b_apply(s, b.cells, bi, ctl, b.r_apply, b.bc, cond); });
@@ -619,7 +668,7 @@ ct_status Batch::solve(double tol, int maxit, ct_stats* out) {
     }
     CT_BK(cudaMemcpyAsync(h_ctl, ctl, (size_t)ni * sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     CT_BK(cudaStreamSynchronize(st));
-    int nbreak = 0, nconv = 0;
+    int nbreak = 0, nconv = 0, nerr = 0;
     for (int i = 0; i < ni; ++i) {
         const Ctl& c = h_ctl[i];
         Solver& v = inst(i);
@@ -634,9 +683,12 @@ ct_status Batch::solve(double tol, int maxit, ct_stats* out) {
             out[i].breakdown = c.breakdown;
         }
         nbreak += c.breakdown ? 1 : 0;
+        nerr += c.err ? 1 : 0;
         nconv += c.converged ? 1 : 0;
     }
     CT_BK(cudaStreamSynchronize(st));
+    if (nerr)
+        return fail(CT_TIMEOUT, "a bounded wait for staged level data ran out in %d of %d instances", nerr, ni);
     if (nbreak) return fail(CT_BREAKDOWN, "PCG breakdown in %d of %d instances", nbreak, ni);
     if (nconv < ni) return fail(CT_NOT_CONVERGED, "%d of %d instances not converged", ni - nconv, ni);
     return CT_OK;
@@ -798,6 +850,13 @@ ct_status ct_batch_profile_solve(ct_batch* b, double tol, int maxit, ct_stats* s
     return s;
 }
 
+ct_status ct_batch_stream(const ct_batch* b, void** stream) {
+    CT_BATCH_OK(b);
+    if (!stream) return fail(CT_BAD_ARG, "ct_batch_stream: null");
+    *stream = (void*)b->impl.st;
+    return CT_OK;
+}
+
 ct_status ct_batch_num_buckets(const ct_batch* b, int* nbuckets) {
     CT_BATCH_OK(b);
     if (!nbuckets) return fail(CT_BAD_ARG, "ct_batch_num_buckets: null");
@@ -806,7 +865,7 @@ ct_status ct_batch_num_buckets(const ct_batch* b, int* nbuckets) {
 }
 
 ct_status ct_batch_bucket_info(const ct_batch* b, int k, int* ninst, int* depth, unsigned* sweep_tiles,
-                               unsigned* restrict_tiles) {
+                               unsigned* restrict_tiles, int* staged) {
     CT_BATCH_OK(b);
     if (k < 0 || k >= (int)b->impl.bk.size()) return fail(CT_BAD_ARG, "ct_batch_bucket_info: bad bucket");
     const ct::Batch::Bucket& B = b->impl.bk[(size_t)k];
@@ -815,6 +874,7 @@ ct_status ct_batch_bucket_info(const ct_batch* b, int k, int* ninst, int* depth,
     for (int d = 0; d < B.depth; ++d) {
         if (sweep_tiles) sweep_tiles[d] = B.sweep_tile[(size_t)d];
         if (restrict_tiles) restrict_tiles[d] = B.restr_tile[(size_t)d];
+        if (staged) staged[d] = B.tma[(size_t)d];
     }
     return CT_OK;
 }

@@ -83,6 +83,14 @@ void launch_b_sweep(cudaStream_t st, const Plan& p, const LevelView<float>* view
                     const Ctl* ctl);
 void launch_b_restrict(cudaStream_t st, const Plan& p, const LevelView<float>* views,
                        const LevelView<float>* cviews, const Ctl* ctl);
+// The same sweep staged by bulk tensor copies (k_sweep_tma.cu): the plan's
+// items are the tiles of each instance's level (sweep_tma_tiles), maps[i]
+// instance i's tensor maps for this level and colour. A wait that runs out
+// sets that instance's ctl->err and stops it.
+void launch_b_sweep_tma(cudaStream_t st, const Plan& p, const SweepMaps* maps,
+                        const LevelView<float>* views, const LevelView<float>* cviews, int color,
+                        bool zero_x, bool prolong, int mz, Ctl* ctl, BCtl* bc, Cond cond);
+int sweep_tma_tiles(const Geo& g);
 // The bottom of every instance's V-cycle: one block per instance in `insts`.
 cudaError_t launch_b_small(cudaStream_t st, const int* insts, int n,
                            const TailLevels<float>* small, size_t smem, int mz, const Ctl* ctl);

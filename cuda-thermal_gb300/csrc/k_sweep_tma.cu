@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cudaTypedefs.h>
 
+#include "batch.h"
 #include "kernels.h"
 #include "reduce.cuh"
 #include "tma.cuh"
@@ -56,63 +57,67 @@ __device__ void fail_wait(Ctl* ctl, Cond cond) {
     if (cond.use) cudaGraphSetConditional(cond.h, 0u);
 }
 
+// The tiles a block works on: first, first + step, ... (my_tiles of them).
+struct TileList {
+    int first, step, count;
+    __device__ int tile(int mt) const { return first + mt * step; }
+};
+
 // Item w of a block = plane w % nz of its (w / nz)-th tile, into stage
 // w % NS: one arrival with the stage's byte count, then the boxes.
 template <int TT, int TJ, int NS, bool ZERO>
-__device__ __forceinline__ void issue_plane(const SweepMaps& m, float* sm, uint64_t* full, int w,
-                                            int nz, int tilesx) {
+__device__ __forceinline__ void issue_plane(const SweepMaps* m, float* sm, uint64_t* full, int w,
+                                            int nz, int tilesx, const TileList& tl) {
     using S = Stage<TT, TJ>;
     constexpr int stage_f = ZERO ? S::zero : S::full;
     const int s = w % NS;
     const int mt = w / nz, l = w - mt * nz;
-    const int tile = (int)blockIdx.x + mt * (int)gridDim.x;
+    const int tile = tl.tile(mt);
     const int tyi = tile / tilesx;
     const int t0 = (tile - tyi * tilesx) * TT, j0 = tyi * TJ;
     float* st = sm + s * stage_f;
     uint64_t* bar = &full[s];
     mbar_arrive_expect_tx(bar, ZERO ? S::tx_zero : S::tx_full);
-    load_3d(st, &m.b, t0, j0, l, bar);
-    load_3d(st + S::own, &m.fi, t0, j0, l, bar);
-    load_3d(st + 2 * S::own, &m.fc, t0, j0, l, bar);
-    load_3d(st + 3 * S::own, &m.gu, t0, j0, l, bar);
+    load_3d(st, &m->b, t0, j0, l, bar);
+    load_3d(st + S::own, &m->fi, t0, j0, l, bar);
+    load_3d(st + 2 * S::own, &m->fc, t0, j0, l, bar);
+    load_3d(st + 3 * S::own, &m->gu, t0, j0, l, bar);
     if (!ZERO) {
-        load_3d(st + 4 * S::own, &m.ge, t0, j0, l, bar);
-        load_3d(st + 5 * S::own, &m.gn, t0, j0, l, bar);
-        load_3d(st + 6 * S::own, &m.ox, t0 - 4, j0 - 1, l, bar);
-        load_3d(st + 6 * S::own + S::ox, &m.oge, t0 - 4, j0, l, bar);
-        load_3d(st + 6 * S::own + S::ox + S::oge, &m.ogn, t0, j0 - 1, l, bar);
+        load_3d(st + 4 * S::own, &m->ge, t0, j0, l, bar);
+        load_3d(st + 5 * S::own, &m->gn, t0, j0, l, bar);
+        load_3d(st + 6 * S::own, &m->ox, t0 - 4, j0 - 1, l, bar);
+        load_3d(st + 6 * S::own + S::ox, &m->oge, t0 - 4, j0, l, bar);
+        load_3d(st + 6 * S::own + S::ox + S::oge, &m->ogn, t0, j0 - 1, l, bar);
     }
 }
 
+// The line solves of a block's tiles (all threads of the block call it).
+// Returns false if a wait ran out; the block's copies still in flight have
+// then landed (bounded) and the caller records the failure.
 template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
-__global__ void __launch_bounds__(TT * TJ)
-    k_sweep_tma(const __grid_constant__ SweepMaps m, LevelView<float> L, LevelView<float> C,
-                int color, Ctl* ctl, Cond cond) {
+__device__ __forceinline__ bool sweep_tiles(const SweepMaps* m, const LevelView<float>& L,
+                                            const LevelView<float>& C, int color,
+                                            const TileList& tl, float* sm, uint64_t* full) {
     using S = Stage<TT, TJ>;
-    if (loop_done(ctl, cond)) return;
-    extern __shared__ __align__(128) float sm[];
-    __shared__ uint64_t full[NS];
     constexpr int stage_f = ZERO ? S::zero : S::full;
     const Geo& g = L.g;
     const int nz = g.nz;
     const int tilesx = (g.hx + TT - 1) / TT;
-    const int ntiles = tilesx * ((g.ny + TJ - 1) / TJ);
-    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const int nitems = my_tiles * nz;
+    const int nitems = tl.count * nz;
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
         fence_barrier_init();
     }
     __syncthreads();
     if (threadIdx.x == 0)
-        for (int w = 0; w < NS && w < nitems; ++w) issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w, nz, tilesx);
+        for (int w = 0; w < NS && w < nitems; ++w) issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w, nz, tilesx, tl);
 
     const int tx = (int)threadIdx.x % TT, ty = (int)threadIdx.x / TT;
     const int o = ty * TT + tx;
     int w = 0;
     bool ok = true;
-    for (int mt = 0; mt < my_tiles && ok; ++mt) {
-        const int tile = (int)blockIdx.x + mt * (int)gridDim.x;
+    for (int mt = 0; mt < tl.count && ok; ++mt) {
+        const int tile = tl.tile(mt);
         const int tyi = tile / tilesx;
         const int t = (tile - tyi * tilesx) * TT + tx, j = tyi * TJ + ty;
         const int e = (j + color) & 1;
@@ -185,7 +190,7 @@ __global__ void __launch_bounds__(TT * TJ)
                 ok = __syncthreads_and(got) != 0;
                 if (!ok) break;
                 if (threadIdx.x == 0 && w + NS < nitems)
-                    issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w + NS, nz, tilesx);
+                    issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w + NS, nz, tilesx, tl);
                 ++w;
             }
         }
@@ -201,9 +206,49 @@ __global__ void __launch_bounds__(TT * TJ)
         }
     }
     if (!ok && threadIdx.x == 0) {
-        fail_wait(ctl, cond);
         // let this block's copies still in flight land before it leaves
         for (int q = w; q < w + NS && q < nitems; ++q) mbar_wait(&full[q % NS], (unsigned)(q / NS) & 1u);
+    }
+    return ok;
+}
+
+// Single solver: the level's tiles spread over a persistent grid.
+template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
+__global__ void __launch_bounds__(TT * TJ, 2)
+    k_sweep_tma(const __grid_constant__ SweepMaps m, LevelView<float> L, LevelView<float> C,
+                int color, Ctl* ctl, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    extern __shared__ __align__(128) float sm[];
+    __shared__ uint64_t full[NS];
+    const Geo& g = L.g;
+    const int ntiles = ((g.hx + TT - 1) / TT) * ((g.ny + TJ - 1) / TJ);
+    const int count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const TileList tl{(int)blockIdx.x, (int)gridDim.x, count};
+    if (!sweep_tiles<TT, TJ, NS, MZ, ZERO, PRO>(&m, L, C, color, tl, sm, full) && threadIdx.x == 0)
+        fail_wait(ctl, cond);
+}
+
+// Batch: block b runs task b of the plan (consecutive tiles of one
+// instance's level); maps[i] are instance i's maps for this level and colour.
+template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
+__global__ void __launch_bounds__(TT * TJ, 2)
+    kb_sweep_tma(Plan p, const SweepMaps* __restrict__ maps, const LevelView<float>* __restrict__ views,
+                 const LevelView<float>* __restrict__ cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
+    const Task t = p.tasks[blockIdx.x];
+    Ctl* c = &ctl[t.inst];
+    if (*(volatile const int*)&c->done) return;
+    extern __shared__ __align__(128) float sm[];
+    __shared__ uint64_t full[NS];
+    const LevelView<float> L = views[t.inst];
+    const LevelView<float> C = PRO ? cviews[t.inst] : L;
+    const TileList tl{(int)t.begin, 1, (int)(t.end - t.begin)};
+    if (!sweep_tiles<TT, TJ, NS, MZ, ZERO, PRO>(&maps[t.inst], L, C, color, tl, sm, full) &&
+        threadIdx.x == 0) {
+        // stop this instance (once, whichever of its blocks gets here first)
+        atomicExch(&c->err, 1);
+        *(volatile int*)&c->breakdown = 1;
+        if (atomicExch(&c->done, 1) == 0 && atomicSub(&bc->active, 1) == 1 && cond.use)
+            cudaGraphSetConditional(cond.h, 0u);
     }
 }
 
@@ -267,6 +312,43 @@ void launch_sweep_tma(cudaStream_t st, const SweepMaps& m, const LevelView<float
     else
         go_sweep<32>(st, m, L, coarse_for_prolong, color, zero_x, ctl, cond);
 }
+
+namespace {
+template <int MZ, bool ZERO, bool PRO>
+void go_b(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView<float>* views,
+          const LevelView<float>* cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
+    constexpr int TT = kTileT, TJ = kTileJ, NS = kSweepStages;
+    kb_sweep_tma<TT, TJ, NS, MZ, ZERO, PRO><<<p.ntasks, TT * TJ, stage_bytes<TT, TJ, NS>(ZERO), st>>>(
+        p, maps, views, cviews, color, ctl, bc, cond);
+}
+template <int MZ>
+void go_b_sweep(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView<float>* views,
+                const LevelView<float>* cviews, int color, bool zero_x, bool prolong, Ctl* ctl,
+                BCtl* bc, Cond cond) {
+    if (zero_x)
+        go_b<MZ, true, false>(st, p, maps, views, cviews, color, ctl, bc, cond);
+    else if (prolong)
+        go_b<MZ, false, true>(st, p, maps, views, cviews, color, ctl, bc, cond);
+    else
+        go_b<MZ, false, false>(st, p, maps, views, cviews, color, ctl, bc, cond);
+}
+}  // namespace
+
+void launch_b_sweep_tma(cudaStream_t st, const Plan& p, const SweepMaps* maps,
+                        const LevelView<float>* views, const LevelView<float>* cviews, int color,
+                        bool zero_x, bool prolong, int mz, Ctl* ctl, BCtl* bc, Cond cond) {
+    if (p.ntasks <= 0) return;
+    if (mz <= 8)
+        go_b_sweep<8>(st, p, maps, views, cviews, color, zero_x, prolong, ctl, bc, cond);
+    else if (mz <= 12)
+        go_b_sweep<12>(st, p, maps, views, cviews, color, zero_x, prolong, ctl, bc, cond);
+    else if (mz <= 16)
+        go_b_sweep<16>(st, p, maps, views, cviews, color, zero_x, prolong, ctl, bc, cond);
+    else
+        go_b_sweep<32>(st, p, maps, views, cviews, color, zero_x, prolong, ctl, bc, cond);
+}
+
+int sweep_tma_tiles(const Geo& g) { return ((g.hx + kTileT - 1) / kTileT) * ((g.ny + kTileJ - 1) / kTileJ); }
 
 // ---- tensor maps -------------------------------------------------------------
 

@@ -125,8 +125,9 @@ def _signatures():
         "ct_batch_true_relres": (i, [vp, i, dp]),
         "ct_batch_step_record": (i, [vp, i, d, C.POINTER(CtStepRecord)]),
         "ct_batch_num_buckets": (i, [vp, ip]),
+        "ct_batch_stream": (i, [vp, C.POINTER(vp)]),
         "ct_batch_profile_solve": (i, [vp, d, i, vp, C.POINTER(CtKernelTime), i, ip]),
-        "ct_batch_bucket_info": (i, [vp, i, ip, ip, vp, vp]),
+        "ct_batch_bucket_info": (i, [vp, i, ip, ip, vp, vp, vp]),
         "ct_model_planes": (i, [lp, i, ip, vp, vp]),
         "ct_model_finalize": (i, [gp, lp, vp, vp, d, d, d, d, vp, vp, vp, vp, vp, vp]),
         "ct_model_add_power_block": (i, [gp, lp, vp, i, d, d, d, d, d, vp]),
@@ -607,18 +608,26 @@ class GpuBatch:
                      total_ms=out[k].total_ms, bytes=out[k].bytes) for k in range(n.value)]
         return self._stats(st), rows
 
+    def stream(self) -> int:
+        p = C.c_void_p()
+        _check(lib().ct_batch_stream(self._h, C.byref(p)))
+        return p.value or 0
+
     def buckets(self) -> List[dict]:
         nb = C.c_int()
         _check(lib().ct_batch_num_buckets(self._h, C.byref(nb)))
         out = []
         for k in range(nb.value):
             n, dep = C.c_int(), C.c_int()
-            _check(lib().ct_batch_bucket_info(self._h, k, C.byref(n), C.byref(dep), None, None))
+            _check(lib().ct_batch_bucket_info(self._h, k, C.byref(n), C.byref(dep), None, None,
+                                              None))
             sw = (C.c_uint * max(1, dep.value))()
             rs = (C.c_uint * max(1, dep.value))()
-            _check(lib().ct_batch_bucket_info(self._h, k, None, None, sw, rs))
+            sg = (C.c_int * max(1, dep.value))()
+            _check(lib().ct_batch_bucket_info(self._h, k, None, None, sw, rs, sg))
             out.append(dict(instances=n.value, depth=dep.value,
-                            sweep_tiles=list(sw)[:dep.value], restrict_tiles=list(rs)[:dep.value]))
+                            sweep_tiles=list(sw)[:dep.value], restrict_tiles=list(rs)[:dep.value],
+                            staged=[bool(v) for v in list(sg)[:dep.value]]))
         return out
 
 

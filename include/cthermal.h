@@ -224,11 +224,17 @@ ct_status ct_batch_step_transient(ct_batch* b, const double* dt, double tol, int
 ct_status ct_batch_get_x(ct_batch* b, int i, double* T);
 ct_status ct_batch_true_relres(ct_batch* b, int i, double* out);
 ct_status ct_batch_step_record(ct_batch* b, int i, double dt, ct_step_record* out);
-/* Size buckets and the column tiles the autotuner picked for each of their
- * depths (sweep_tiles / restrict_tiles: depth entries, may be NULL). */
+/* Size buckets and the tiles the autotuner picked for each of their depths
+ * (arrays of depth entries, each may be NULL): staged[d] = 1 where the
+ * sweeps of depth d are staged by bulk tensor copies, sweep_tiles[d] the
+ * 32 x 8-column tiles per block there, else the columns per block of the grid
+ * sweep; restrict_tiles[d] the coarse cells per block of the restriction. */
 ct_status ct_batch_num_buckets(const ct_batch* b, int* nbuckets);
+/* The batch's stream (a cudaStream_t): every ct_batch_* call is ordered on it,
+ * and a solve's work on the buckets' own streams is joined back into it. */
+ct_status ct_batch_stream(const ct_batch* b, void** stream);
 ct_status ct_batch_bucket_info(const ct_batch* b, int k, int* ninst, int* depth,
-                               unsigned* sweep_tiles, unsigned* restrict_tiles);
+                               unsigned* sweep_tiles, unsigned* restrict_tiles, int* staged);
 
 /* ---- per-kernel timing --------------------------------------------------- */
 typedef struct ct_kernel_time {

@@ -80,9 +80,12 @@ def test_batch_buckets_cover_instances(ct, mixed):
         info = b.buckets()
         assert sum(k["instances"] for k in info) == len(mixed)
         for k in info:
-            assert len(k["sweep_tiles"]) == k["depth"]
-            assert all(t in (256, 512, 1024, 2048) for t in k["sweep_tiles"])
+            assert len(k["sweep_tiles"]) == k["depth"] == len(k["staged"])
+            for t, staged in zip(k["sweep_tiles"], k["staged"]):
+                assert t in ((1, 2, 4, 8) if staged else (256, 512, 1024, 2048))
             assert all(t in (256, 512, 1024, 2048, 4096) for t in k["restrict_tiles"])
+        # the large levels of the workload's stacks are staged
+        assert any(any(k["staged"]) for k in info)
 
 
 def test_batch_resolve_and_power_change(ct, orc, mixed):
@@ -207,3 +210,37 @@ def test_batch_transient_matches_single(ct, golden):
                 assert abs(r.q_out + r.q_stored - powers[i]) / powers[i] < 1e-5
     for s in singles:
         s.close()
+
+
+def _env(**kv):
+    old = {k: os.environ.get(k) for k in kv}
+    for k, v in kv.items():
+        os.environ[k] = v
+    return old
+
+
+def _restore(old):
+    for k, v in old.items():
+        if v is None:
+            os.environ.pop(k, None)
+        else:
+            os.environ[k] = v
+
+
+def test_batch_staged_sweeps_bitwise(ct, mixed):
+    """The sweeps staged by bulk tensor copies compute exactly what the grid
+    sweeps compute: same iterations, same bits."""
+    out = []
+    for flag in ("0", "1"):
+        old = _env(CT_SWEEP_TMA=flag)
+        try:
+            with ct.GpuBatch(mixed) as b:
+                b.set_x_zero()
+                b.set_rhs_steady()
+                st = b.solve(1e-10, 50000)
+                out.append(([s.iters for s in st], [b.get_x(i) for i in range(len(mixed))]))
+        finally:
+            _restore(old)
+    assert out[0][0] == out[1][0]
+    for a, c in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, c)

@@ -246,3 +246,25 @@ def test_dw_true_residual_meets_tol_on_larger_grid(ct, orc):
         st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, prec)
         assert st.converged
         assert orc.true_relres(m, T) <= 1.5e-10
+
+
+@pytest.mark.parametrize("prec", ["MG_FP32", "MG_FP32_FLEX", "MG_FP32_FLEX_DW"])
+def test_staged_sweeps_bitwise(ct, prec):
+    """Sweeps staged in shared memory by bulk tensor copies give the grid
+    sweeps' results bit for bit (odd sizes: partial tiles, padded half-rows)."""
+    import os
+    import workloads
+    m = workloads.steady_hotspot(203, seed=7)
+    out = []
+    for flag in ("0", "1"):
+        old = os.environ.get("CT_SWEEP_TMA")
+        os.environ["CT_SWEEP_TMA"] = flag
+        try:
+            out.append(gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, getattr(ct.Precision, prec)))
+        finally:
+            if old is None:
+                os.environ.pop("CT_SWEEP_TMA", None)
+            else:
+                os.environ["CT_SWEEP_TMA"] = old
+    assert out[0][0].iters == out[1][0].iters
+    assert np.array_equal(out[0][1], out[1][1])
