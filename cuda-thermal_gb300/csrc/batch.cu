@@ -54,7 +54,7 @@ namespace {
 // Items per block of the stages whose tile is not tuned.
 constexpr unsigned kVecChunk = 4096;   // value pairs (fold, update, dot, p, rhs)
 constexpr unsigned kColChunk = 512;    // fine columns (FP64 residual)
-constexpr unsigned kCellChunk = 2048;  // fine cells (operator apply)
+constexpr unsigned kRowChunk = 16;     // fine rows of one colour and plane (operator apply)
 // Candidate tiles of the autotuner (columns per block for the sweeps, coarse
 // cells per block for the restriction).
 constexpr unsigned kSweepTiles[] = {256, 512, 1024, 2048};
@@ -105,7 +105,7 @@ class Batch {
         cudaStream_t st = nullptr, st_body = nullptr;
         cudaGraphExec_t gx = nullptr;
         BCtl* bc = nullptr;
-        Plan vec{}, cols{}, cells{};
+        Plan vec{}, cols{}, rows{};  // value pairs, fine columns, fine rows
         BRed r_res{}, r_apply{}, r_update{}, r_dot{};
         std::vector<Plan> sweep, restr;
         std::vector<unsigned> sweep_tile, restr_tile;
@@ -362,12 +362,12 @@ ct_status Batch::build_bucket(Bucket& b) {
     ct_status s;
     if ((s = dalloc(&b.bc, sizeof(BCtl))) != CT_OK) return s;
     CT_BK(cudaMemsetAsync(b.bc, 0, sizeof(BCtl), st));
-    std::vector<unsigned> pairs, cols, cells;
+    std::vector<unsigned> pairs, cols, rows;
     for (int i : b.inst) {
         const Solver& v = inst(i);
         pairs.push_back(v.n / 2);
         cols.push_back(v.g0.plane);
-        cells.push_back(v.n);
+        rows.push_back(2u * (unsigned)v.g0.ny * (unsigned)v.g0.nz);
         b.mz = std::max(b.mz, v.g0.nz);
         TailLevels<float> tl;
         tl.n = (int)(v.lv.size() - v.small_k0);
@@ -376,9 +376,9 @@ ct_status Batch::build_bucket(Bucket& b) {
     }
     if ((s = upload_plan(make_plan(ni, b.inst, pairs, kVecChunk), &b.vec)) != CT_OK) return s;
     if ((s = upload_plan(make_plan(ni, b.inst, cols, kColChunk), &b.cols)) != CT_OK) return s;
-    if ((s = upload_plan(make_plan(ni, b.inst, cells, kCellChunk), &b.cells)) != CT_OK) return s;
+    if ((s = upload_plan(make_plan(ni, b.inst, rows, kRowChunk), &b.rows)) != CT_OK) return s;
     if ((s = make_red(b.cols, &b.r_res)) != CT_OK) return s;
-    if ((s = make_red(b.cells, &b.r_apply)) != CT_OK) return s;
+    if ((s = make_red(b.rows, &b.r_apply)) != CT_OK) return s;
     if ((s = make_red(b.vec, &b.r_update)) != CT_OK) return s;
     if ((s = make_red(b.vec, &b.r_dot)) != CT_OK) return s;
     if ((s = upload(&b.small_insts, b.inst)) != CT_OK) return s;
@@ -543,7 +543,7 @@ void Batch::enqueue_body(Bucket& b, cudaStream_t s, Cond cond) {
     vcycle(b, s, cond);
     enq(s, "b_dot", N * 20, [&] { launch_b_dot(s, b.vec, bi, ctl, b.r_dot, b.bc, cond); });
     enq(s, "b_update_p", N * 20, [&] { launch_b_update_p(s, b.vec, bi, ctl); });
-    enq(s, "b_apply", N * 36, [&] { launch_b_apply(s, b.cells, bi, ctl, b.r_apply, b.bc, cond); });
+    enq(s, "b_apply", N * 36, [&] { launch_b_apply(s, b.rows, bi, ctl, b.r_apply, b.bc, cond); });
     enq(s, "b_update_xr", N * 52,
         [&] { launch_b_update(s, b.vec, bi, ctl, b.r_update, b.bc, cond); });
     // residual replacement of the instances whose first phase just ended

@@ -4,7 +4,7 @@
 // "Tight and rigorous error bounds for basic building blocks of double-word
 // arithmetic" (2017).
 #pragma once
-#include "device.h"
+#include "kernels.h"
 
 namespace ct {
 namespace dwdev {
@@ -53,6 +53,85 @@ __device__ __forceinline__ float2 dw_of(double d) {
 }
 
 __device__ __forceinline__ double dw_d(float2 a) { return (double)a.x + (double)a.y; }
+
+// ---- sums of float x double-word products ------------------------------------
+// (s, c): s collects the products' high parts through TwoSum, c the exact
+// rounding errors of the products and the sums plus the products of the low
+// parts; renormalised once at the end (fast_two_sum(s, c)). Each term costs
+// eleven FP32 operations instead of the seventeen of dw_mul_f + dw_add, with
+// an error of the same order (a few units of 2^-48 of the largest term).
+struct DwAcc {
+    float s, c;
+};
+
+// a += h + lo with |lo| << |h|.
+__device__ __forceinline__ void acc_add(DwAcc& a, float h, float lo) {
+    const float s = a.s + h;
+    const float bp = s - a.s;
+    const float err = (a.s - (s - bp)) + (h - bp);
+    a.s = s;
+    a.c += err + lo;
+}
+
+// a += g * p.
+__device__ __forceinline__ void acc_mul_f(DwAcc& a, float2 p, float g) {
+    const float h = g * p.x;
+    acc_add(a, h, fmaf(g, p.y, fmaf(g, p.x, -h)));
+}
+
+// a += u * v (both double words; the lo * lo term is below the error).
+__device__ __forceinline__ void acc_mul(DwAcc& a, float2 u, float2 v) {
+    const float h = u.x * v.x;
+    acc_add(a, h, fmaf(u.x, v.y, fmaf(u.y, v.x, fmaf(u.x, v.x, -h))));
+}
+
+// Ap = (A + C/dt) p on one row of one plane (hx slots of one colour of row j),
+// op_apply's order of terms (src/operator3d.h:108-112): the stored diagonal
+// times p minus the west, east, south, north, down and up neighbour terms.
+// The calling warp strides over the row; p.Ap of its cells is added to pap.
+// R = l * 2 ny + 2 j + colour.
+__device__ __forceinline__ void apply_row(const OpView& o, const float2* __restrict__ dgw,
+                                          const float2* __restrict__ p, float2* __restrict__ Ap,
+                                          unsigned R, int lane, DwAcc& pap) {
+    const Geo& g = o.g;
+    const unsigned rows = 2u * (unsigned)g.ny;
+    const unsigned l = R / rows;
+    const unsigned r = R - l * rows;
+    const int j = (int)(r >> 1), c = (int)(r & 1u), e = (j + c) & 1;
+    const unsigned hx = (unsigned)g.hx;
+    const unsigned base = l * g.plane;
+    const unsigned row = base + r * hx;
+    const unsigned orow = base + (unsigned)(2 * j + (c ^ 1)) * hx;  // other colour, same j
+    const bool hs = j > 0, hn = j < g.ny - 1, hd = l > 0, hu = (int)l < g.nz - 1;
+    for (unsigned t = (unsigned)lane; t < hx; t += 32u) {
+        const unsigned k = row + t;
+        const int i = 2 * (int)t + e;
+        if (i >= g.nx) {
+            Ap[k] = make_float2(0.0f, 0.0f);
+            continue;
+        }
+        DwAcc off = {0.0f, 0.0f};
+        if (i > 0) {
+            const unsigned w = orow + t - 1u + (unsigned)e;
+            acc_mul_f(off, p[w], o.gE[w]);
+        }
+        if (i < g.nx - 1) acc_mul_f(off, p[orow + t + (unsigned)e], o.gE[k]);
+        if (hs) {
+            const unsigned sl = orow - 2u * hx + t;
+            acc_mul_f(off, p[sl], o.gN[sl]);
+        }
+        if (hn) acc_mul_f(off, p[orow + 2u * hx + t], o.gN[k]);
+        if (hd) acc_mul_f(off, p[k - g.plane], o.gU[k - g.plane]);
+        if (hu) acc_mul_f(off, p[k + g.plane], o.gU[k]);
+        const float2 pc = p[k], dg = dgw[k];
+        const float h = dg.x * pc.x;
+        DwAcc a = {h, fmaf(dg.x, pc.y, fmaf(dg.y, pc.x, fmaf(dg.x, pc.x, -h)))};
+        acc_add(a, -off.s, -off.c);
+        const float2 av = fast_two_sum(a.s, a.c);
+        Ap[k] = av;
+        acc_mul(pap, pc, av);
+    }
+}
 
 // ---- column walk (split layout), as in k_outer.cu ----------------------------
 struct Col {

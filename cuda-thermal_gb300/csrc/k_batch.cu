@@ -183,7 +183,8 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
-// Ap = d p - sum G p_nbr over cells [begin, end), p.Ap, alpha.
+// Ap = d p - sum G p_nbr over rows [begin, end) of the instance (one warp
+// per row of one colour of one plane, apply_row), p.Ap, alpha.
 __global__ void __launch_bounds__(NT)
     kb_apply(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
     const Task t = p.tasks[blockIdx.x];
@@ -193,30 +194,11 @@ __global__ void __launch_bounds__(NT)
     const float2* __restrict__ pv = bi[t.inst].p;
     const float2* __restrict__ dgw = bi[t.inst].dgw;
     float2* __restrict__ Ap = bi[t.inst].Ap;
-    const Geo& g = o.g;
-    float2 acc = make_float2(0.0f, 0.0f);
-#pragma unroll 2
-    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
-        const unsigned l = k / g.plane;
-        const unsigned s = k - l * g.plane;
-        const Col cl = col_of_slot(g, s);
-        if (!cl.valid) {
-            Ap[k] = make_float2(0.0f, 0.0f);
-            continue;
-        }
-        const unsigned base = l * g.plane;
-        float2 off = make_float2(0.0f, 0.0f);
-        if (cl.i > 0) off = dw_add(off, dw_mul_f(pv[base + cl.sw], o.gE[base + cl.sw]));
-        if (cl.i < g.nx - 1) off = dw_add(off, dw_mul_f(pv[base + cl.se], o.gE[k]));
-        if (cl.j > 0) off = dw_add(off, dw_mul_f(pv[base + cl.ss], o.gN[base + cl.ss]));
-        if (cl.j < g.ny - 1) off = dw_add(off, dw_mul_f(pv[base + cl.sn], o.gN[k]));
-        if (l > 0) off = dw_add(off, dw_mul_f(pv[k - g.plane], o.gU[k - g.plane]));
-        if ((int)l < g.nz - 1) off = dw_add(off, dw_mul_f(pv[k + g.plane], o.gU[k]));
-        const float2 pc = pv[k];
-        const float2 a = dw_add(dw_mul(dgw[k], pc), dw_neg(off));
-        Ap[k] = a;
-        acc = dw_add(acc, dw_mul(pc, a));
-    }
+    const int lane = (int)(threadIdx.x & 31u);
+    DwAcc pacc = {0.0f, 0.0f};
+    for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32)
+        apply_row(o, dgw, pv, Ap, R, lane, pacc);
+    const float2 acc = make_float2(pacc.s, pacc.c);
     double pap = dw_d(acc), unused = 0.0;
     block_sum2(pap, unused);
     if (publish_inst(pap, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {

@@ -192,6 +192,37 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
+// Same as k_apply_dw, one warp per row of one colour of one plane (no
+// integer division per cell), products summed with DwAcc.
+__global__ void __launch_bounds__(NT)
+    k_apply_dw_rows(OpView o, const float2* __restrict__ dgw, const float2* __restrict__ p,
+                    float2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    if (loop_done(ctl, cond)) return;
+    const Geo& g = o.g;
+    const unsigned rows = 2u * (unsigned)g.ny * (unsigned)g.nz;
+    const int lane = (int)(threadIdx.x & 31u);
+    DwAcc acc = {0.0f, 0.0f};
+    for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows; R += gridDim.x * (NT / 32))
+        apply_row(o, dgw, p, Ap, R, lane, acc);
+    double pap = (double)acc.s + (double)acc.c, unused = 0.0;
+    block_sum2(pap, unused);
+    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
+        double PAP, U;
+        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
+        if (threadIdx.x == 0) {
+            ctl->pAp = PAP;
+            if (!(PAP > 0.0) || !isfinite(PAP)) {
+                ctl->breakdown = 1;
+                ctl->alpha = 0.0;
+                stop_loop(ctl, cond);
+            } else {
+                ctl->alpha = ctl->rz / PAP;
+                ctl->alpha_w = dw_of(ctl->alpha);
+            }
+        }
+    }
+}
+
 // Same as k_apply_dw, one cell per loop step instead of one column: the steps
 // are independent (no value carried from plane to plane), so consecutive
 // cells' loads overlap; vertical neighbours come from L1/L2.
@@ -428,11 +459,21 @@ void launch_residual_x(cudaStream_t st, const OpView& o, const double* diag, con
 
 void launch_apply_dw(cudaStream_t st, const OpView& o, const float2* dgw, const float2* p,
                      float2* Ap, Ctl* ctl, const Red& red, Cond cond) {
-    static const bool cells = [] {
-        const char* e = std::getenv("CT_APPLY_COLUMNS");
-        return !(e && e[0] == '1');
+    // CT_APPLY=cells / columns selects the earlier forms (one cell or one
+    // column per thread); the default is one warp per row.
+    static const int form = [] {
+        const char* e = std::getenv("CT_APPLY");
+        if (e && e[0] == 'c' && e[1] == 'e') return 1;
+        if (e && e[0] == 'c' && e[1] == 'o') return 2;
+        return 0;
     }();
-    if (cells) {
+    if (form == 0) {
+        static const int wb = wave_blocks(k_apply_dw_rows, 1 << 30);
+        k_apply_dw_rows<<<std::min(red.maxb, wb), NT, 0, st>>>(o, dgw, p, Ap, ctl, red.part, red.maxb,
+                                                              cond);
+        return;
+    }
+    if (form == 1) {
         static const int wb = wave_blocks(k_apply_dw_cells, 1 << 30);
         k_apply_dw_cells<<<std::min(red.maxb, wb), NT, 0, st>>>(o, dgw, p, Ap, ctl, red.part,
                                                                red.maxb, cond);
