@@ -85,6 +85,111 @@ __device__ __forceinline__ void acc_mul(DwAcc& a, float2 u, float2 v) {
     acc_add(a, h, fmaf(u.x, v.y, fmaf(u.y, v.x, fmaf(u.x, v.x, -h))));
 }
 
+// ---- streaming ranges of value pairs ------------------------------------------
+// Items k = k0, k0 + stride, ... < end; each item is a pair of values (float4
+// = two double words). kU items are loaded before any is used, so a thread
+// keeps kU times the bytes of one item in flight. The single solver's kernels
+// (grid-stride) and the batched kernels (one block per task) share these.
+constexpr int kU = 4;
+
+// rz += r.z, zap += Ap.z.
+__device__ __forceinline__ void dot_range(unsigned k, unsigned end, unsigned stride,
+                                          const float4* __restrict__ r, const float2* __restrict__ z,
+                                          const float4* __restrict__ Ap, DwAcc& rz, DwAcc& zap) {
+    for (; k + (kU - 1) * stride < end; k += kU * stride) {
+        float4 rv[kU], av[kU];
+        float2 zv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            rv[u] = r[k + u * stride];
+            av[u] = Ap[k + u * stride];
+            zv[u] = z[k + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            acc_mul_f(rz, make_float2(rv[u].x, rv[u].y), zv[u].x);
+            acc_mul_f(rz, make_float2(rv[u].z, rv[u].w), zv[u].y);
+            acc_mul_f(zap, make_float2(av[u].x, av[u].y), zv[u].x);
+            acc_mul_f(zap, make_float2(av[u].z, av[u].w), zv[u].y);
+        }
+    }
+    for (; k < end; k += stride) {
+        const float4 rv = r[k], av = Ap[k];
+        const float2 zv = z[k];
+        acc_mul_f(rz, make_float2(rv.x, rv.y), zv.x);
+        acc_mul_f(rz, make_float2(rv.z, rv.w), zv.y);
+        acc_mul_f(zap, make_float2(av.x, av.y), zv.x);
+        acc_mul_f(zap, make_float2(av.z, av.w), zv.y);
+    }
+}
+
+// x += a p, r -= a Ap, b0 = r (hi words), rr += r.r.
+__device__ __forceinline__ void update_one(float2 a, const float4& pv, const float4& av, float4* x,
+                                           float4* r, float2* b0, unsigned k, const float4& xv,
+                                           const float4& rv, DwAcc& rr) {
+    const float2 x0 = dw_add(make_float2(xv.x, xv.y), dw_mul(a, make_float2(pv.x, pv.y)));
+    const float2 x1 = dw_add(make_float2(xv.z, xv.w), dw_mul(a, make_float2(pv.z, pv.w)));
+    const float2 r0 = dw_add(make_float2(rv.x, rv.y), dw_neg(dw_mul(a, make_float2(av.x, av.y))));
+    const float2 r1 = dw_add(make_float2(rv.z, rv.w), dw_neg(dw_mul(a, make_float2(av.z, av.w))));
+    x[k] = make_float4(x0.x, x0.y, x1.x, x1.y);
+    r[k] = make_float4(r0.x, r0.y, r1.x, r1.y);
+    b0[k] = make_float2(r0.x, r1.x);
+    acc_mul(rr, r0, r0);
+    acc_mul(rr, r1, r1);
+}
+
+__device__ __forceinline__ void update_range(unsigned k, unsigned end, unsigned stride, float2 a,
+                                             const float4* __restrict__ p,
+                                             const float4* __restrict__ Ap, float4* __restrict__ x,
+                                             float4* __restrict__ r, float2* __restrict__ b0,
+                                             DwAcc& rr) {
+    constexpr int U = kU / 2;  // four arrays per item: half the items of dot_range
+    for (; k + (U - 1) * stride < end; k += U * stride) {
+        float4 pv[U], av[U], xv[U], rv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            pv[u] = p[k + u * stride];
+            av[u] = Ap[k + u * stride];
+            xv[u] = x[k + u * stride];
+            rv[u] = r[k + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) update_one(a, pv[u], av[u], x, r, b0, k + u * stride, xv[u], rv[u], rr);
+    }
+    for (; k < end; k += stride) update_one(a, p[k], Ap[k], x, r, b0, k, x[k], r[k], rr);
+}
+
+// p = z + beta p (p = z when first).
+__device__ __forceinline__ void update_p_range(unsigned k, unsigned end, unsigned stride,
+                                               float2 beta, bool first,
+                                               const float2* __restrict__ z,
+                                               float4* __restrict__ p) {
+    if (first) {
+        for (; k < end; k += stride) {
+            const float2 zv = z[k];
+            p[k] = make_float4(zv.x, 0.0f, zv.y, 0.0f);
+        }
+        return;
+    }
+    auto one = [&](unsigned q, const float2& zv, const float4& pv) {
+        const float2 p0 = dw_add(dw_mul(beta, make_float2(pv.x, pv.y)), make_float2(zv.x, 0.0f));
+        const float2 p1 = dw_add(dw_mul(beta, make_float2(pv.z, pv.w)), make_float2(zv.y, 0.0f));
+        p[q] = make_float4(p0.x, p0.y, p1.x, p1.y);
+    };
+    for (; k + (kU - 1) * stride < end; k += kU * stride) {
+        float2 zv[kU];
+        float4 pv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            zv[u] = z[k + u * stride];
+            pv[u] = p[k + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) one(k + u * stride, zv[u], pv[u]);
+    }
+    for (; k < end; k += stride) one(k, z[k], p[k]);
+}
+
 // Ap = (A + C/dt) p on one row of one plane (hx slots of one colour of row j),
 // op_apply's order of terms (src/operator3d.h:108-112): the stored diagonal
 // times p minus the west, east, south, north, down and up neighbour terms.

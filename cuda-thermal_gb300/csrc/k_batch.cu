@@ -198,8 +198,7 @@ __global__ void __launch_bounds__(NT)
     DwAcc pacc = {0.0f, 0.0f};
     for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32)
         apply_row(o, dgw, pv, Ap, R, lane, pacc);
-    const float2 acc = make_float2(pacc.s, pacc.c);
-    double pap = dw_d(acc), unused = 0.0;
+    double pap = (double)pacc.s + (double)pacc.c, unused = 0.0;
     block_sum2(pap, unused);
     if (publish_inst(pap, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double PAP, U;
@@ -225,27 +224,13 @@ __global__ void __launch_bounds__(NT)
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
-    const float2 a = c->alpha_w;
-    const float4* __restrict__ pp = reinterpret_cast<const float4*>(bi[t.inst].p);
-    const float4* __restrict__ ap = reinterpret_cast<const float4*>(bi[t.inst].Ap);
-    float4* __restrict__ x = reinterpret_cast<float4*>(bi[t.inst].xw);
-    float4* __restrict__ r = reinterpret_cast<float4*>(bi[t.inst].r);
-    float2* __restrict__ b0 = reinterpret_cast<float2*>(bi[t.inst].b0);
-    float2 acc = make_float2(0.0f, 0.0f);
-    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
-        const float4 pv = pp[k], av = ap[k];
-        const float4 xv = x[k], rv = r[k];
-        const float2 x0 = dw_add(make_float2(xv.x, xv.y), dw_mul(a, make_float2(pv.x, pv.y)));
-        const float2 x1 = dw_add(make_float2(xv.z, xv.w), dw_mul(a, make_float2(pv.z, pv.w)));
-        const float2 r0 = dw_add(make_float2(rv.x, rv.y), dw_neg(dw_mul(a, make_float2(av.x, av.y))));
-        const float2 r1 = dw_add(make_float2(rv.z, rv.w), dw_neg(dw_mul(a, make_float2(av.z, av.w))));
-        x[k] = make_float4(x0.x, x0.y, x1.x, x1.y);
-        r[k] = make_float4(r0.x, r0.y, r1.x, r1.y);
-        b0[k] = make_float2(r0.x, r1.x);
-        acc = dw_add(acc, dw_mul(r0, r0));
-        acc = dw_add(acc, dw_mul(r1, r1));
-    }
-    double rr = dw_d(acc), unused = 0.0;
+    DwAcc acc = {0.0f, 0.0f};
+    update_range(t.begin + threadIdx.x, t.end, NT, c->alpha_w,
+                 reinterpret_cast<const float4*>(bi[t.inst].p),
+                 reinterpret_cast<const float4*>(bi[t.inst].Ap),
+                 reinterpret_cast<float4*>(bi[t.inst].xw), reinterpret_cast<float4*>(bi[t.inst].r),
+                 reinterpret_cast<float2*>(bi[t.inst].b0), acc);
+    double rr = (double)acc.s + (double)acc.c, unused = 0.0;
     block_sum2(rr, unused);
     if (publish_inst(rr, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RR, U;
@@ -276,19 +261,11 @@ __global__ void __launch_bounds__(NT)
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
-    const float4* __restrict__ r = reinterpret_cast<const float4*>(bi[t.inst].r);
-    const float4* __restrict__ ap = reinterpret_cast<const float4*>(bi[t.inst].Ap);
-    const float2* __restrict__ z = reinterpret_cast<const float2*>(bi[t.inst].z);
-    float2 rz = make_float2(0.0f, 0.0f), zap = make_float2(0.0f, 0.0f);
-    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
-        const float4 rv = r[k], av = ap[k];
-        const float2 zv = z[k];
-        rz = dw_add(rz, dw_mul_f(make_float2(rv.x, rv.y), zv.x));
-        rz = dw_add(rz, dw_mul_f(make_float2(rv.z, rv.w), zv.y));
-        zap = dw_add(zap, dw_mul_f(make_float2(av.x, av.y), zv.x));
-        zap = dw_add(zap, dw_mul_f(make_float2(av.z, av.w), zv.y));
-    }
-    double RZ0 = dw_d(rz), ZAP0 = dw_d(zap);
+    DwAcc rz = {0.0f, 0.0f}, zap = {0.0f, 0.0f};
+    dot_range(t.begin + threadIdx.x, t.end, NT, reinterpret_cast<const float4*>(bi[t.inst].r),
+              reinterpret_cast<const float2*>(bi[t.inst].z),
+              reinterpret_cast<const float4*>(bi[t.inst].Ap), rz, zap);
+    double RZ0 = (double)rz.s + (double)rz.c, ZAP0 = (double)zap.s + (double)zap.c;
     block_sum2(RZ0, ZAP0);
     if (publish_inst(RZ0, ZAP0, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RZ, ZAP;
@@ -311,21 +288,8 @@ __global__ void __launch_bounds__(NT)
     const Task t = p.tasks[blockIdx.x];
     const Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
-    const float2 beta = c->beta_w;
-    const bool first = c->iter == 0;
-    const float2* __restrict__ z = reinterpret_cast<const float2*>(bi[t.inst].z);
-    float4* __restrict__ pp = reinterpret_cast<float4*>(bi[t.inst].p);
-    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
-        const float2 zv = z[k];
-        if (first) {
-            pp[k] = make_float4(zv.x, 0.0f, zv.y, 0.0f);
-        } else {
-            const float4 pv = pp[k];
-            const float2 p0 = dw_add(dw_mul(beta, make_float2(pv.x, pv.y)), make_float2(zv.x, 0.0f));
-            const float2 p1 = dw_add(dw_mul(beta, make_float2(pv.z, pv.w)), make_float2(zv.y, 0.0f));
-            pp[k] = make_float4(p0.x, p0.y, p1.x, p1.y);
-        }
-    }
+    update_p_range(t.begin + threadIdx.x, t.end, NT, c->beta_w, c->iter == 0,
+                   reinterpret_cast<const float2*>(bi[t.inst].z), reinterpret_cast<float4*>(bi[t.inst].p));
 }
 
 // Pairs of values: b = P + C/dt x (x = FP64 base, folded), x_old = x.

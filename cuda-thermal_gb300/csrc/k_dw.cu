@@ -37,6 +37,17 @@ using namespace dwdev;
 
 namespace {
 
+// Block b of the grid streams the contiguous items [begin, end) with stride
+// NT (as a batched task does) rather than striding over the whole vector.
+struct BlockRange {
+    unsigned begin, end;
+};
+__device__ __forceinline__ BlockRange block_range(unsigned n) {
+    const unsigned per = ((n + gridDim.x - 1) / gridDim.x + NT * kU - 1) / (NT * kU) * (NT * kU);
+    const unsigned b = blockIdx.x * per;
+    return BlockRange{b + threadIdx.x, b + per < n ? b + per : n};
+}
+
 // ---- FP64 residual from a double-word x: start and replacement -------------
 
 // r = b - (A + C/dt) x in FP64 with x = hi + lo, the stored FP64 diagonal;
@@ -281,22 +292,10 @@ __global__ void __launch_bounds__(NT)
                 float4* __restrict__ x, float4* __restrict__ r, float2* __restrict__ b0, Ctl* ctl,
                 double* part, int maxb, Cond cond) {
     if (loop_done(ctl, cond)) return;
-    const float2 a = ctl->alpha_w;
-    float2 acc = make_float2(0.0f, 0.0f);
-    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
-        const float4 pv = p[k], av = Ap[k];
-        float4 xv = x[k], rv = r[k];
-        const float2 x0 = dw_add(make_float2(xv.x, xv.y), dw_mul(a, make_float2(pv.x, pv.y)));
-        const float2 x1 = dw_add(make_float2(xv.z, xv.w), dw_mul(a, make_float2(pv.z, pv.w)));
-        const float2 r0 = dw_add(make_float2(rv.x, rv.y), dw_neg(dw_mul(a, make_float2(av.x, av.y))));
-        const float2 r1 = dw_add(make_float2(rv.z, rv.w), dw_neg(dw_mul(a, make_float2(av.z, av.w))));
-        x[k] = make_float4(x0.x, x0.y, x1.x, x1.y);
-        r[k] = make_float4(r0.x, r0.y, r1.x, r1.y);
-        b0[k] = make_float2(r0.x, r1.x);
-        acc = dw_add(acc, dw_mul(r0, r0));
-        acc = dw_add(acc, dw_mul(r1, r1));
-    }
-    double rr = dw_d(acc), unused = 0.0;
+    DwAcc acc = {0.0f, 0.0f};
+    const BlockRange br = block_range(n2);
+    update_range(br.begin, br.end, NT, ctl->alpha_w, p, Ap, x, r, b0, acc);
+    double rr = (double)acc.s + (double)acc.c, unused = 0.0;
     block_sum2(rr, unused);
     if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
         double RR, U;
@@ -328,16 +327,10 @@ __global__ void __launch_bounds__(NT)
     k_dot_dw(unsigned n2, const float4* __restrict__ r, const float2* __restrict__ z,
              const float4* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
     if (loop_done(ctl, cond)) return;
-    float2 rz = make_float2(0.0f, 0.0f), zap = make_float2(0.0f, 0.0f);
-    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
-        const float4 rv = r[k], av = Ap[k];
-        const float2 zv = z[k];
-        rz = dw_add(rz, dw_mul_f(make_float2(rv.x, rv.y), zv.x));
-        rz = dw_add(rz, dw_mul_f(make_float2(rv.z, rv.w), zv.y));
-        zap = dw_add(zap, dw_mul_f(make_float2(av.x, av.y), zv.x));
-        zap = dw_add(zap, dw_mul_f(make_float2(av.z, av.w), zv.y));
-    }
-    double RZ0 = dw_d(rz), ZAP0 = dw_d(zap);
+    DwAcc rz = {0.0f, 0.0f}, zap = {0.0f, 0.0f};
+    const BlockRange br = block_range(n2);
+    dot_range(br.begin, br.end, NT, r, z, Ap, rz, zap);
+    double RZ0 = (double)rz.s + (double)rz.c, ZAP0 = (double)zap.s + (double)zap.c;
     block_sum2(RZ0, ZAP0);
     if (publish2(RZ0, ZAP0, part, maxb, &ctl->ticket[SL_DOT])) {
         double RZ, ZAP;
@@ -360,19 +353,8 @@ __global__ void __launch_bounds__(NT)
     k_update_p_dw(unsigned n2, const float2* __restrict__ z, float4* __restrict__ p, const Ctl* ctl,
                   Cond cond) {
     if (loop_done(ctl, cond)) return;
-    const float2 beta = ctl->beta_w;
-    const bool first = ctl->iter == 0;
-    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
-        const float2 zv = z[k];
-        if (first) {
-            p[k] = make_float4(zv.x, 0.0f, zv.y, 0.0f);
-        } else {
-            const float4 pv = p[k];
-            const float2 p0 = dw_add(dw_mul(beta, make_float2(pv.x, pv.y)), make_float2(zv.x, 0.0f));
-            const float2 p1 = dw_add(dw_mul(beta, make_float2(pv.z, pv.w)), make_float2(zv.y, 0.0f));
-            p[k] = make_float4(p0.x, p0.y, p1.x, p1.y);
-        }
-    }
+    const BlockRange br = block_range(n2);
+    update_p_range(br.begin, br.end, NT, ctl->beta_w, ctl->iter == 0, z, p);
 }
 
 // xb += xw (in FP64), xw = 0: the double-word correction goes into the base.
