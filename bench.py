@@ -9,7 +9,9 @@ double-word arithmetic on the FP32 pipes with one FP64 residual replacement
 larger than L2 (the fine level alone moves > 1 GB per iteration), so no L2
 flush is needed between steps.
 
-Reported beside it, on the same GPU: the batched form on a 256-instance
+Reported beside it, on the same GPU: the batched backward-Euler run (64
+switching 256 x 256 x 10 stacks, 500 steps, per-instance dt), the batched form
+on a 256-instance
 floorplan sweep (uneven stacks solved together, instance solves/s against
 the plain FP64 MG-PCG solving the same instances one by one), the FP32
 V-cycle in FP64 flexible PCG
@@ -46,6 +48,9 @@ MAXIT = 1000
 SEED = 2
 BATCH_N = 256   # instances of the batched floorplan sweep
 BATCH_SEED = 4
+TR_N, TR_GRID, TR_SEED = 64, 256, 5   # batched transient: instances, lateral size, seed
+TR_DT0, TR_GROWTH, TR_DT_MAX, TR_TOL = 1e-5, 1.1, 0.05, 1e-9
+TR_CHECK = 4   # instances re-run with the plain FP64 solver for max|dT| and its rate
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -362,6 +367,88 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
     }
 
 
+def bench_transient_batched(ct, np, args, steps):
+    """The batched transient: 64 instances of the 256 x 256 x 10 stack, each
+    with 9 blocks switching at Poisson times (mean 5 ms), backward-Euler steps
+    with per-instance dt (10 us growing 10 % per step, capped at 50 ms, reset
+    to 10 us on a switch), warm-started from the steady field of the initial
+    power, tol 1e-9 per step. Timed end to end on the host clock: switching
+    (power maps uploaded), set_dt, b = P + C/dt T, the batched solve and the
+    batched step records of every step."""
+    import workloads
+    ws = workloads.switching_instances(TR_N, TR_GRID, seed=TR_SEED)
+    n = len(ws)
+    b = ct.GpuBatch([w.model for w in ws])
+    for i, w in enumerate(ws):
+        b.set_power(i, w.power())
+    b.set_x_zero()
+    b.set_rhs_steady()
+    b.solve(TOL, MAXIT)
+    dt = np.full(n, TR_DT0)
+    t = np.zeros(n)
+    ptot = np.array([w.power().sum() for w in ws])
+    eb, its, switches = [], [], 0
+    dts = []
+    t0 = time.perf_counter()
+    for k in range(steps):
+        for i, w in enumerate(ws):
+            if w.advance(t[i]):
+                b.set_power(i, w.power())
+                ptot[i] = ws[i].power().sum()
+                dt[i] = TR_DT0
+                switches += 1
+        st = b.step_transient(dt, TR_TOL, MAXIT)
+        rec = b.step_records(dt)
+        on = ptot > 0
+        if on.any():
+            eb.append(float(np.max(np.abs(rec[on, 1] + rec[on, 2] - ptot[on]) / ptot[on])))
+        its.append(max(s.iters for s in st))
+        dts.append(dt.copy())
+        t += dt
+        dt = np.minimum(dt * TR_GROWTH, TR_DT_MAX)
+    sec = time.perf_counter() - t0
+    Tb = [b.get_x(i) for i in range(TR_CHECK)]
+    b.close()
+    # the same steps for the first instances with the plain FP64 MG-PCG, one by one
+    ref = workloads.switching_instances(TR_CHECK, TR_GRID, seed=TR_SEED)
+    sec64, max_dT = 0.0, 0.0
+    for i, w in enumerate(ref):
+        s = ct.GpuPcg(w.model, ct.Precond.Multigrid, ct.Precision.MG_FP64)
+        s.set_power(w.power())
+        s.set_x_zero()
+        s.set_rhs_steady()
+        s.solve(TOL, MAXIT)
+        tt = 0.0
+        a0 = time.perf_counter()
+        for k in range(steps):
+            if w.advance(tt):
+                s.set_power(w.power())
+            s.set_dt(float(dts[k][i]))
+            s.set_rhs_transient()
+            s.solve(TR_TOL, MAXIT)
+            tt += float(dts[k][i])
+        sec64 += time.perf_counter() - a0
+        max_dT = max(max_dT, float(np.abs(s.get_x() - Tb[i]).max()))
+        s.close()
+    value = n * steps / sec
+    value64 = TR_CHECK * steps / sec64
+    return {
+        "value": value, "unit": "instance steps/s",
+        "workload": f"{n} x {TR_GRID}x{TR_GRID}x10 default stack, 9 blocks per instance toggled at "
+                    f"Poisson times (mean 5 ms), {steps} backward-Euler steps, per-instance dt "
+                    f"{TR_DT0:g} s x {TR_GROWTH} per step (max {TR_DT_MAX:g}), reset on a switch, "
+                    f"tol {TR_TOL:g}",
+        "steps": steps, "batch_steps_per_s": steps / sec, "switches": switches,
+        "iters_max_per_step_median": float(np.median(its)), "iters_max_per_step_max": int(max(its)),
+        "energy_balance_err_max": max(eb) if eb else None,
+        "energy_balance_err_median": float(np.median(eb)) if eb else None,
+        "fp64_mg_pcg_sequential": {"value": value64, "unit": "instance steps/s",
+                                   "instances": TR_CHECK},
+        "speedup_vs_fp64": value / value64,
+        "max_dT_K_vs_fp64": max_dT,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -370,6 +457,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 256-instance run")
+    ap.add_argument("--transient-steps", type=int, default=500,
+                    help="backward-Euler steps of the batched transient (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -466,6 +555,9 @@ def main():
         batched = bench_batched(ct, np, torch, args, hbm_peak, peak_kind)
         if world > 1:
             batched["value"] = sum_over_ranks(batched["value"], world)
+    transient = None
+    if args.transient_steps > 0:
+        transient = bench_transient_batched(ct, np, args, args.transient_steps)
     # clocks sampled over every timed region above (headline, FP64, e2e, batched)
     clk = clocks.stop()
 
@@ -517,6 +609,8 @@ def main():
         }
         if batched:
             out["batched"] = batched
+        if transient:
+            out["batched_transient"] = transient
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)

@@ -118,7 +118,14 @@ class Batch {
     BInst* bi = nullptr;
     Ctl* ctl = nullptr;
     Ctl* h_ctl = nullptr;  // pinned mirror
-    std::vector<LevelView<float>*> views;  // per depth: LevelView per instance
+    std::vector<LevelView<float>*> views;  // per level index: LevelView per instance
+    Plan diag_plan{};                      // set_dt: natural fine columns of every instance
+    Plan rec_plan{};                       // step records: fine column slots of every instance
+    BRed rec_red{};
+    double* rec_mx = nullptr;              // per task of rec_plan
+    double* rec_dev = nullptr;             // 3 per instance
+    std::vector<double> rec_host;
+    std::vector<Plan> factor_plans;        // set_dt: natural columns of level k of every instance
     std::vector<SweepMaps*> bmaps;         // per depth and colour (2 d + c): maps per instance
     std::vector<std::vector<char>> fits;   // [d][i]: instance i's level d has maps
     TailLevels<float>* small = nullptr;
@@ -288,13 +295,44 @@ ct_status Batch::create(int n, const ct_model* const* models) {
     }
     ct_status s;
     if ((s = upload(&bi, hb)) != CT_OK) return s;
-    views.assign((size_t)maxdepth + 1, nullptr);
-    for (int d = 0; d <= maxdepth; ++d) {
+    int maxlev = 0;
+    for (int i = 0; i < n; ++i) maxlev = std::max(maxlev, (int)inst(i).lv.size());
+    views.assign((size_t)maxlev, nullptr);
+    for (int d = 0; d < maxlev; ++d) {
         std::vector<LevelView<float>> hv((size_t)n);
         for (int i = 0; i < n; ++i)
             if ((size_t)d < inst(i).lv.size()) hv[(size_t)i] = inst(i).view<float>((size_t)d);
             else std::memset(&hv[(size_t)i], 0, sizeof(LevelView<float>));
         if ((s = upload(&views[(size_t)d], hv)) != CT_OK) return s;
+    }
+    // set_dt plans: every instance's fine columns; per level index the
+    // instances that have that level.
+    {
+        std::vector<int> all;
+        std::vector<unsigned> cols;
+        for (int i = 0; i < n; ++i) {
+            all.push_back(i);
+            cols.push_back((unsigned)inst(i).g0.nx * (unsigned)inst(i).g0.ny);
+        }
+        if ((s = upload_plan(make_plan(ni, all, cols, 4 * NT), &diag_plan)) != CT_OK) return s;
+        std::vector<unsigned> slots;
+        for (int i = 0; i < n; ++i) slots.push_back(inst(i).g0.plane);
+        if ((s = upload_plan(make_plan(ni, all, slots, 4 * NT), &rec_plan)) != CT_OK) return s;
+        if ((s = make_red(rec_plan, &rec_red)) != CT_OK) return s;
+        if ((s = dalloc(&rec_mx, (size_t)std::max(1, rec_plan.ntasks) * sizeof(double))) != CT_OK) return s;
+        if ((s = dalloc(&rec_dev, (size_t)3 * n * sizeof(double))) != CT_OK) return s;
+        rec_host.assign((size_t)3 * n, 0.0);
+        factor_plans.assign((size_t)maxlev, Plan{});
+        for (int k = 0; k < maxlev; ++k) {
+            std::vector<int> has;
+            std::vector<unsigned> kc;
+            for (int i = 0; i < n; ++i)
+                if ((size_t)k < inst(i).lv.size()) {
+                    has.push_back(i);
+                    kc.push_back((unsigned)inst(i).lv[(size_t)k].g.nx * (unsigned)inst(i).lv[(size_t)k].g.ny);
+                }
+            if ((s = upload_plan(make_plan(ni, has, kc, NT), &factor_plans[(size_t)k])) != CT_OK) return s;
+        }
     }
     // Tensor maps of the levels whose sweeps are staged (CT_SWEEP_TMA=0: none).
     {
@@ -605,18 +643,22 @@ ct_status Batch::record(Bucket& b) {
     return CT_OK;
 }
 
+// set_dt for every instance in 1 + (levels) launches: 1/dt per instance goes
+// into its control block, then the batched diagonal and factor kernels run
+// the single solver's per-column arithmetic (same bits as Solver::set_dt).
 ct_status Batch::set_dt(const double* dt) {
     for (int i = 0; i < ni; ++i) {
         const double v = dt ? dt[i] : 0.0;
-        const ct_status s = inst(i).set_dt(v);
-        if (s != CT_OK) {
-            const std::string why = ct_last_error();
-            return fail(s, "ct_batch_set_dt: instance %d: %s", i, why.c_str());
-        }
-        h_ctl[i].inv_dt = inst(i).inv_dt;
+        if (!(v >= 0) || !std::isfinite(v)) return fail(CT_BAD_ARG, "ct_batch_set_dt: dt[%d] must be >= 0", i);
+        const double inv = v > 0 ? 1.0 / v : 0.0;
+        inst(i).inv_dt = inv;
+        h_ctl[i].inv_dt = inv;
     }
     CT_BK(cudaMemcpyAsync(ctl, h_ctl, (size_t)ni * sizeof(Ctl), cudaMemcpyHostToDevice, st));
-    CT_BK(cudaStreamSynchronize(st));
+    launch_b_diag(st, diag_plan, bi, ctl);
+    for (size_t k = 0; k < factor_plans.size(); ++k) launch_b_factor(st, factor_plans[k], views[k], ctl);
+    CT_BK(cudaGetLastError());
+    CT_BK(cudaStreamSynchronize(st));  // h_ctl is written again by the next call
     return CT_OK;
 }
 
@@ -854,6 +896,26 @@ ct_status ct_batch_stream(const ct_batch* b, void** stream) {
     CT_BATCH_OK(b);
     if (!stream) return fail(CT_BAD_ARG, "ct_batch_stream: null");
     *stream = (void*)b->impl.st;
+    return CT_OK;
+}
+
+ct_status ct_batch_step_records(ct_batch* b, const double* dt, ct_step_record* out) {
+    CT_BATCH_OK(b);
+    if (!dt || !out) return fail(CT_BAD_ARG, "ct_batch_step_records: null");
+    ct::Batch& B = b->impl;
+    for (ct::Batch::Bucket& k : B.bk) ct::launch_b_fold(B.st, k.vec, B.bi, B.ctl, 0);
+    ct::launch_b_step_record(B.st, B.rec_plan, B.bi, B.rec_red, B.rec_mx, B.rec_dev);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(B.rec_host.data(), B.rec_dev, B.rec_host.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost, B.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(B.st);
+    if (e != cudaSuccess) return fail(CT_CUDA_ERROR, "ct_batch_step_records: %s", cudaGetErrorString(e));
+    for (int i = 0; i < B.ni; ++i) {
+        out[i].T_max = B.rec_host[(size_t)3 * i];
+        out[i].q_out = B.rec_host[(size_t)3 * i + 1];
+        out[i].q_stored = B.rec_host[(size_t)3 * i + 2] / dt[i];
+    }
     return CT_OK;
 }
 

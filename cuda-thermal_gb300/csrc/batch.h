@@ -94,6 +94,16 @@ int sweep_tma_tiles(const Geo& g);
 // The bottom of every instance's V-cycle: one block per instance in `insts`.
 cudaError_t launch_b_small(cudaStream_t st, const int* insts, int n,
                            const TailLevels<float>* small, size_t smem, int mz, const Ctl* ctl);
+// set_dt for all instances (1/dt from ctl[i].inv_dt): the fine FP64 and
+// double-word diagonal (items: natural fine columns), and the column factors
+// of one level index (items: natural columns of that level; views[i] =
+// instance i's level).
+void launch_b_diag(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl);
+void launch_b_factor(cudaStream_t st, const Plan& p, const LevelView<float>* views, const Ctl* ctl);
+// Per-instance T_max, heat out and sum C (x - x_old) into rec[3 i + 0..2]
+// (items: fine column slots; x folded; mx: one double per task).
+void launch_b_step_record(cudaStream_t st, const Plan& p, const BInst* bi, BRed red, double* mx,
+                          double* rec);
 // b = P + cap / dt x (per-instance 1/dt from ctl), x_old = x, for all
 // instances (x folded first).
 void launch_b_rhs_transient(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl);

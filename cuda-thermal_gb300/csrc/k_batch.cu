@@ -12,6 +12,7 @@
 #include "dw_dev.cuh"
 #include "mg_dev.cuh"
 #include "reduce.cuh"
+#include "setup_dev.cuh"
 
 namespace ct {
 
@@ -312,6 +313,84 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
+// Step records of every instance (items: fine column slots): T_max,
+// heat_out = sum over the top and bottom faces of g x, and sum C (x - x_old)
+// (src/stack3d.h:252-273), x the folded FP64 base; rec[3 i + 0..2].
+__global__ void __launch_bounds__(NT)
+    kb_step_record(Plan p, const BInst* __restrict__ bi, BRed red, double* __restrict__ mx,
+                   double* __restrict__ rec) {
+    const Task t = p.tasks[blockIdx.x];
+    const BInst I = bi[t.inst];
+    const Geo& g = I.o.g;
+    double tmax = -INFINITY, qout = 0.0, qst = 0.0;
+    for (unsigned s = t.begin + threadIdx.x; s < t.end; s += NT) {
+        const Col c = col_of_slot(g, s);
+        if (!c.valid) continue;
+        for (int l = 0; l < g.nz; ++l) {
+            const unsigned id = (unsigned)l * g.plane + s;
+            const double xv = I.x[id];
+            tmax = fmax(tmax, xv);
+            qst += (double)I.o.cap[id] * (xv - I.xold[id]);
+        }
+        const unsigned top = (unsigned)(g.nz - 1) * g.plane + s;
+        qout += (double)I.o.gU[top] * I.x[top];
+        qout += (double)I.o.gB[s] * I.x[s];
+    }
+    __shared__ double sm[NT / 32];
+    double m = tmax;
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < NT / 32 ? sm[threadIdx.x] : -INFINITY;
+        for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+    }
+    block_sum2(qout, qst);
+    if (threadIdx.x == 0) mx[blockIdx.x] = m;
+    const int first = p.inst_first[t.inst], count = p.inst_count[t.inst];
+    if (publish_inst(qout, qst, red, p.ntasks, t.inst, count)) {
+        __threadfence();
+        double mm = -INFINITY;
+        for (int k = threadIdx.x; k < count; k += NT) mm = fmax(mm, __ldcg(mx + first + k));
+        for (int off = 16; off > 0; off >>= 1) mm = fmax(mm, __shfl_down_sync(0xffffffffu, mm, off));
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mm;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            mm = threadIdx.x < NT / 32 ? sm[threadIdx.x] : -INFINITY;
+            for (int off = 16; off > 0; off >>= 1) mm = fmax(mm, __shfl_down_sync(0xffffffffu, mm, off));
+        }
+        double QO, QS;
+        gather_inst(red, p.ntasks, t.inst, first, count, QO, QS);
+        if (threadIdx.x == 0) {
+            rec[3 * t.inst] = mm;
+            rec[3 * t.inst + 1] = QO;
+            rec[3 * t.inst + 2] = QS;
+        }
+    }
+}
+
+// set_dt of every instance: its FP64 (and double-word) diagonal, items =
+// natural fine columns; 1/dt per instance from its control block.
+__global__ void __launch_bounds__(NT) kb_diag(Plan p, const BInst* __restrict__ bi, const Ctl* ctl) {
+    const Task t = p.tasks[blockIdx.x];
+    const BInst& I = bi[t.inst];
+    const double inv_dt = ctl[t.inst].inv_dt;
+    for (unsigned q = t.begin + threadIdx.x; q < t.end; q += NT)
+        setupdev::diag_column(I.o, inv_dt, q, const_cast<double*>(I.diag), nullptr,
+                              const_cast<float2*>(I.dgw));
+}
+
+// ... and the column factors of one level index of every instance that has it
+// (items = natural columns of that level).
+__global__ void __launch_bounds__(NT)
+    kb_factor(Plan p, const LevelView<float>* __restrict__ views, const Ctl* ctl) {
+    const Task t = p.tasks[blockIdx.x];
+    const LevelView<float> L = views[t.inst];
+    const float inv_dt = (float)ctl[t.inst].inv_dt;
+    for (unsigned q = t.begin + threadIdx.x; q < t.end; q += NT) setupdev::factor_column<float>(L, inv_dt, q);
+}
+
 template <int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(NT)
     kb_sweep(Plan p, const LevelView<float>* __restrict__ views,
@@ -380,6 +459,19 @@ void launch_b_dot(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRe
 
 void launch_b_update_p(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl) {
     kb_update_p<<<p.ntasks, NT, 0, st>>>(p, bi, ctl);
+}
+
+void launch_b_step_record(cudaStream_t st, const Plan& p, const BInst* bi, BRed red, double* mx,
+                          double* rec) {
+    if (p.ntasks > 0) kb_step_record<<<p.ntasks, NT, 0, st>>>(p, bi, red, mx, rec);
+}
+
+void launch_b_diag(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl) {
+    if (p.ntasks > 0) kb_diag<<<p.ntasks, NT, 0, st>>>(p, bi, ctl);
+}
+
+void launch_b_factor(cudaStream_t st, const Plan& p, const LevelView<float>* views, const Ctl* ctl) {
+    if (p.ntasks > 0) kb_factor<<<p.ntasks, NT, 0, st>>>(p, views, ctl);
 }
 
 void launch_b_rhs_transient(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl) {

@@ -19,70 +19,23 @@
 #include "kernels.h"
 #include "mg_dev.cuh"
 #include "reduce.cuh"
+#include "setup_dev.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace ct {
 
 using namespace mgdev;
+using namespace setupdev;
 
 namespace {
-
-// Rounding-explicit arithmetic for the setup kernels: no contraction into
-// FMAs, so factors and coarse operators equal the CPU's bit for bit.
-template <class T>
-struct RN;
-template <>
-struct RN<float> {
-    static __device__ float add(float a, float b) { return __fadd_rn(a, b); }
-    static __device__ float sub(float a, float b) { return __fsub_rn(a, b); }
-    static __device__ float mul(float a, float b) { return __fmul_rn(a, b); }
-    static __device__ float div(float a, float b) { return __fdiv_rn(a, b); }
-};
-template <>
-struct RN<double> {
-    static __device__ double add(double a, double b) { return __dadd_rn(a, b); }
-    static __device__ double sub(double a, double b) { return __dsub_rn(a, b); }
-    static __device__ double mul(double a, double b) { return __dmul_rn(a, b); }
-    static __device__ double div(double a, double b) { return __ddiv_rn(a, b); }
-};
-
-// op_diag (src/operator3d.h:80-88) of cell (i, j, l), in T, rounding-explicit.
-template <class T>
-__device__ T diag_rn(const LevelView<T>& L, int i, int j, int l, T inv_dt) {
-    const Geo& g = L.g;
-    const unsigned base = (unsigned)l * g.plane;
-    const unsigned s = scol(g, i, j), id = base + s;
-    T d = 0;
-    if (i > 0) d = RN<T>::add(d, (T)L.gE[base + scol(g, i - 1, j)]);
-    if (i < g.nx - 1) d = RN<T>::add(d, (T)L.gE[id]);
-    if (j > 0) d = RN<T>::add(d, (T)L.gN[base + scol(g, i, j - 1)]);
-    if (j < g.ny - 1) d = RN<T>::add(d, (T)L.gN[id]);
-    d = RN<T>::add(d, (T)L.gU[id]);
-    d = RN<T>::add(d, l > 0 ? (T)L.gU[id - g.plane] : (T)L.gB[s]);
-    return RN<T>::add(d, RN<T>::mul((T)L.cap[id], inv_dt));
-}
 
 // mg_factor_column (src/mg3d.h:157-173): Thomas factors of every column.
 template <class T>
 __global__ void k_factor(LevelView<T> L, T inv_dt) {
-    const Geo& g = L.g;
-    const unsigned ncol = (unsigned)g.nx * g.ny;
-    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < ncol; q += gridDim.x * blockDim.x) {
-        const int j = (int)(q / g.nx), i = (int)(q - (unsigned)j * g.nx);
-        const unsigned s = scol(g, i, j);
-        T cp_prev = 0;
-        for (int l = 0; l < g.nz; ++l) {
-            const unsigned id = (unsigned)l * g.plane + s;
-            const T d = diag_rn(L, i, j, l, inv_dt);
-            const T lower = l > 0 ? -(T)L.gU[id - g.plane] : T(0);
-            const T upper = l < g.nz - 1 ? -(T)L.gU[id] : T(0);
-            const T inv = RN<T>::div(T(1), RN<T>::sub(d, RN<T>::mul(lower, cp_prev)));
-            L.finv[id] = inv;
-            cp_prev = RN<T>::mul(upper, inv);
-            L.fcp[id] = cp_prev;
-        }
-    }
+    const unsigned ncol = (unsigned)L.g.nx * L.g.ny;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < ncol; q += gridDim.x * blockDim.x)
+        factor_column<T>(L, inv_dt, q);
 }
 
 // mg_coarse_cell (src/mg3d.h:206-248) on split layouts: one thread per coarse

@@ -10,6 +10,7 @@
 
 #include "kernels.h"
 #include "reduce.cuh"
+#include "setup_dev.cuh"
 
 namespace ct {
 
@@ -357,26 +358,10 @@ __global__ void k_to_natural_d(Geo g, const double* __restrict__ in, double* __r
 // (no contraction), so the diagonal equals the CPU's bit for bit.
 __global__ void k_diag(OpView o, double inv_dt, double* __restrict__ diag,
                        double* __restrict__ invd) {
-    const Geo& g = o.g;
-    const size_t ncol = (size_t)g.nx * g.ny;
+    const size_t ncol = (size_t)o.g.nx * o.g.ny;
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < ncol;
-         q += (size_t)gridDim.x * blockDim.x) {
-        const int j = (int)(q / g.nx), i = (int)(q - (size_t)j * g.nx);
-        const unsigned s = scol(g, i, j);
-        for (int l = 0; l < g.nz; ++l) {
-            const unsigned base = (unsigned)l * g.plane, id = base + s;
-            double d = 0.0;
-            if (i > 0) d = __dadd_rn(d, (double)o.gE[base + scol(g, i - 1, j)]);
-            if (i < g.nx - 1) d = __dadd_rn(d, (double)o.gE[id]);
-            if (j > 0) d = __dadd_rn(d, (double)o.gN[base + scol(g, i, j - 1)]);
-            if (j < g.ny - 1) d = __dadd_rn(d, (double)o.gN[id]);
-            d = __dadd_rn(d, (double)o.gU[id]);
-            d = __dadd_rn(d, l > 0 ? (double)o.gU[id - g.plane] : (double)o.gB[s]);
-            d = __dadd_rn(d, __dmul_rn((double)o.cap[id], inv_dt));
-            diag[id] = d;
-            if (invd) invd[id] = __drcp_rn(d);
-        }
-    }
+         q += (size_t)gridDim.x * blockDim.x)
+        setupdev::diag_column(o, inv_dt, (unsigned)q, diag, invd, nullptr);
 }
 
 __global__ void k_rhs_transient(unsigned n, const float* __restrict__ cap, double inv_dt,

@@ -124,6 +124,7 @@ def _signatures():
         "ct_batch_get_x": (i, [vp, i, vp]),
         "ct_batch_true_relres": (i, [vp, i, dp]),
         "ct_batch_step_record": (i, [vp, i, d, C.POINTER(CtStepRecord)]),
+        "ct_batch_step_records": (i, [vp, vp, vp]),
         "ct_batch_num_buckets": (i, [vp, ip]),
         "ct_batch_stream": (i, [vp, C.POINTER(vp)]),
         "ct_batch_profile_solve": (i, [vp, d, i, vp, C.POINTER(CtKernelTime), i, ip]),
@@ -612,6 +613,13 @@ class GpuBatch:
         p = C.c_void_p()
         _check(lib().ct_batch_stream(self._h, C.byref(p)))
         return p.value or 0
+
+    def step_records(self, dt) -> np.ndarray:
+        """(n, 3) array: T_max, q_out, q_stored of every instance's last step."""
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float64), (len(self),)))
+        out = (CtStepRecord * len(self))()
+        _check(lib().ct_batch_step_records(self._h, _ptr(d), C.cast(out, C.c_void_p)))
+        return np.array([(r.T_max, r.q_out, r.q_stored) for r in out])
 
     def buckets(self) -> List[dict]:
         nb = C.c_int()

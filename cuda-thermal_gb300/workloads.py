@@ -14,6 +14,10 @@ those of the workloads the solver is measured on:
                    tier (median 30 W/cm^2, sigma 0.6), 20 W per tier.
   batch_instances  stacks of uneven size for batched solves: nx, ny in
                    {64, 96, ..., 512}, 6-16 cell layers from a layer table.
+  switching_instances  the default 256 x 256 x 10 stack, each instance with 9
+                   blocks on the Si tiers switched on and off at Poisson
+                   times (mean 5 ms between toggles of a block), for batched
+                   backward-Euler runs with per-instance dt.
 """
 from __future__ import annotations
 
@@ -138,3 +142,63 @@ def batch_instance(rng) -> ct.Model3D:
 def batch_instances(count: int = 256, seed: int = 4):
     rng = np.random.default_rng(seed)
     return [batch_instance(rng) for _ in range(count)]
+
+
+class Switching:
+    """One instance of the batched transient: its model (power all off), the
+    power map of each block, each block's toggle times and initial state."""
+
+    def __init__(self, model, maps, toggles, on):
+        self.model = model
+        self.maps = maps          # list of (ncells,) power maps, one per block
+        self.toggles = toggles    # list of sorted toggle times (s), one per block
+        self.on = list(on)        # block states at t = 0
+        self._next = [0] * len(maps)
+
+    def power(self) -> np.ndarray:
+        P = np.zeros(self.model.ncells())
+        for b, m in enumerate(self.maps):
+            if self.on[b]:
+                P += m
+        return P
+
+    def advance(self, t: float) -> bool:
+        """Applies every toggle at or before t; True if any block switched."""
+        changed = False
+        for b, times in enumerate(self.toggles):
+            while self._next[b] < len(times) and times[self._next[b]] <= t:
+                self.on[b] = not self.on[b]
+                self._next[b] += 1
+                changed = True
+        return changed
+
+
+def switching_instances(count: int = 64, n: int = 256, seed: int = 5, blocks: int = 9,
+                        mean_s: float = 5e-3, horizon_s: float = 1.0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        m = ct.default_model(n, n)
+        ct.finalize(m)
+        maps = []
+        for b in range(blocks):
+            layer = 0 if b % 2 == 0 else 2
+            w, h = rng.uniform(0.1, 0.3, size=2) * m.Lx
+            x0, y0 = rng.uniform(0, 1, size=2) * (m.Lx - w)
+            watts = float(rng.uniform(2.0, 6.0))
+            m.P[:] = 0.0
+            ct.add_power_block(m, layer, float(x0), float(y0), float(w), float(h), watts)
+            maps.append(np.array(m.P, dtype=np.float64))
+        toggles = []
+        for b in range(blocks):
+            ts, t = [], 0.0
+            while True:
+                t += float(rng.exponential(mean_s))
+                if t > horizon_s:
+                    break
+                ts.append(t)
+            toggles.append(ts)
+        on = rng.integers(0, 2, size=blocks).astype(bool)
+        m.P[:] = 0.0
+        out.append(Switching(m, maps, toggles, on))
+    return out

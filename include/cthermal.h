@@ -224,6 +224,9 @@ ct_status ct_batch_step_transient(ct_batch* b, const double* dt, double tol, int
 ct_status ct_batch_get_x(ct_batch* b, int i, double* T);
 ct_status ct_batch_true_relres(ct_batch* b, int i, double* out);
 ct_status ct_batch_step_record(ct_batch* b, int i, double dt, ct_step_record* out);
+/* The step records of every instance in one launch (out[i] for the step of
+ * length dt[i] that the last ct_batch_set_rhs_transient started). */
+ct_status ct_batch_step_records(ct_batch* b, const double* dt, ct_step_record* out);
 /* Size buckets and the tiles the autotuner picked for each of their depths
  * (arrays of depth entries, each may be NULL): staged[d] = 1 where the
  * sweeps of depth d are staged by bulk tensor copies, sweep_tiles[d] the

@@ -193,6 +193,7 @@ def test_batch_transient_matches_single(ct, golden):
                     powers[i] = float(np.sum(P))
             dt = dts * (1.1 ** step)
             stats = b.step_transient(dt, 1e-9, 50000)
+            all_rec = b.step_records(dt)  # one launch for every instance
             for i, m in enumerate(ms):
                 s = singles[i]
                 s.set_dt(dt[i])
@@ -203,6 +204,10 @@ def test_batch_transient_matches_single(ct, golden):
                 assert abs(stats[i].iters - st1.iters) <= 1, (step, i, stats[i], st1, b.true_relres(i))
                 assert np.abs(T - T1).max() <= 1e-7 * np.abs(T1).max()
                 r, r1 = b.step_record(i, dt[i]), s.step_record(dt[i])
+                # same sums, grouped per block differently: equal to ~1e-12
+                assert all_rec[i][0] == r.T_max
+                assert abs(all_rec[i][1] - r.q_out) <= 1e-12 * abs(r.q_out)
+                assert abs(all_rec[i][2] - r.q_stored) <= 1e-12 * max(abs(r.q_stored), powers[i])
                 assert abs(r.q_out - r1.q_out) <= 1e-7 * abs(r1.q_out)
                 assert abs(r.q_stored - r1.q_stored) <= 1e-7 * max(abs(r1.q_stored), powers[i])
                 # energy balance: tol 1e-9 is relative to ||P + C/dt T||, so the
