@@ -190,14 +190,77 @@ __device__ __forceinline__ void update_p_range(unsigned k, unsigned end, unsigne
     for (; k < end; k += stride) one(k, z[k], p[k]);
 }
 
-// Ap = (A + C/dt) p on one row of one plane (hx slots of one colour of row j),
-// op_apply's order of terms (src/operator3d.h:108-112): the stored diagonal
-// times p minus the west, east, south, north, down and up neighbour terms.
-// The calling warp strides over the row; p.Ap of its cells is added to pap.
-// R = l * 2 ny + 2 j + colour.
-__device__ __forceinline__ void apply_row(const OpView& o, const float2* __restrict__ dgw,
-                                          const float2* __restrict__ p, float2* __restrict__ Ap,
-                                          unsigned R, int lane, DwAcc& pap) {
+// Operands of one cell of the operator apply, loaded before any is used
+// (absent neighbours stay zero and are skipped by the same guards).
+struct ApplyCell {
+    float2 pc, dg, pw, pe, ps, pn, pd, pu;
+    float gw, ge, gs, gn, gd, gu;
+};
+
+__device__ __forceinline__ void apply_load(const OpView& o, const float2* __restrict__ dgw,
+                                           const float2* __restrict__ p, unsigned k, unsigned t,
+                                           unsigned orow, int i, int e, bool hs, bool hn, bool hd,
+                                           bool hu, ApplyCell& a) {
+    const Geo& g = o.g;
+    const unsigned hx = (unsigned)g.hx;
+    const float2 z = make_float2(0.0f, 0.0f);
+    a.pc = p[k];
+    a.dg = dgw[k];
+    a.pw = z, a.pe = z, a.ps = z, a.pn = z, a.pd = z, a.pu = z;
+    a.gw = 0.0f, a.ge = 0.0f, a.gs = 0.0f, a.gn = 0.0f, a.gd = 0.0f, a.gu = 0.0f;
+    if (i > 0) {
+        const unsigned w = orow + t - 1u + (unsigned)e;
+        a.pw = p[w];
+        a.gw = o.gE[w];
+    }
+    if (i < g.nx - 1) {
+        a.pe = p[orow + t + (unsigned)e];
+        a.ge = o.gE[k];
+    }
+    if (hs) {
+        const unsigned sl = orow - 2u * hx + t;
+        a.ps = p[sl];
+        a.gs = o.gN[sl];
+    }
+    if (hn) {
+        a.pn = p[orow + 2u * hx + t];
+        a.gn = o.gN[k];
+    }
+    if (hd) {
+        a.pd = p[k - g.plane];
+        a.gd = o.gU[k - g.plane];
+    }
+    if (hu) {
+        a.pu = p[k + g.plane];
+        a.gu = o.gU[k];
+    }
+}
+
+// Ap of the cell from its operands: the stored diagonal times p minus the
+// west, east, south, north, down and up neighbour terms (op_apply's order,
+// src/operator3d.h:108-112); p.Ap added to pap.
+__device__ __forceinline__ float2 apply_compute(const ApplyCell& a, bool w, bool e, bool s, bool n,
+                                                bool d, bool u, DwAcc& pap) {
+    DwAcc off = {0.0f, 0.0f};
+    if (w) acc_mul_f(off, a.pw, a.gw);
+    if (e) acc_mul_f(off, a.pe, a.ge);
+    if (s) acc_mul_f(off, a.ps, a.gs);
+    if (n) acc_mul_f(off, a.pn, a.gn);
+    if (d) acc_mul_f(off, a.pd, a.gd);
+    if (u) acc_mul_f(off, a.pu, a.gu);
+    const float h = a.dg.x * a.pc.x;
+    DwAcc r = {h, fmaf(a.dg.x, a.pc.y, fmaf(a.dg.y, a.pc.x, fmaf(a.dg.x, a.pc.x, -h)))};
+    acc_add(r, -off.s, -off.c);
+    const float2 av = fast_two_sum(r.s, r.c);
+    acc_mul(pap, a.pc, av);
+    return av;
+}
+
+// The same row with each neighbour term loaded and accumulated in turn: fewer
+// registers (more resident warps), one load latency per term.
+__device__ __forceinline__ void apply_row_seq(const OpView& o, const float2* __restrict__ dgw,
+                                              const float2* __restrict__ p, float2* __restrict__ Ap,
+                                              unsigned R, int lane, DwAcc& pap) {
     const Geo& g = o.g;
     const unsigned rows = 2u * (unsigned)g.ny;
     const unsigned l = R / rows;
@@ -206,7 +269,7 @@ __device__ __forceinline__ void apply_row(const OpView& o, const float2* __restr
     const unsigned hx = (unsigned)g.hx;
     const unsigned base = l * g.plane;
     const unsigned row = base + r * hx;
-    const unsigned orow = base + (unsigned)(2 * j + (c ^ 1)) * hx;  // other colour, same j
+    const unsigned orow = base + (unsigned)(2 * j + (c ^ 1)) * hx;
     const bool hs = j > 0, hn = j < g.ny - 1, hd = l > 0, hu = (int)l < g.nz - 1;
     for (unsigned t = (unsigned)lane; t < hx; t += 32u) {
         const unsigned k = row + t;
@@ -235,6 +298,43 @@ __device__ __forceinline__ void apply_row(const OpView& o, const float2* __restr
         const float2 av = fast_two_sum(a.s, a.c);
         Ap[k] = av;
         acc_mul(pap, pc, av);
+    }
+}
+
+// Ap = (A + C/dt) p on one row of one plane (hx slots of one colour of row j).
+// The calling warp strides over the row, U cells per lane and step (32 slots
+// apart) with every operand of all U loaded first; p.Ap of its cells is added
+// to pap in slot order. R = l * 2 ny + 2 j + colour.
+template <int U>
+__device__ __forceinline__ void apply_row(const OpView& o, const float2* __restrict__ dgw,
+                                          const float2* __restrict__ p, float2* __restrict__ Ap,
+                                          unsigned R, int lane, DwAcc& pap) {
+    const Geo& g = o.g;
+    const unsigned rows = 2u * (unsigned)g.ny;
+    const unsigned l = R / rows;
+    const unsigned r = R - l * rows;
+    const int j = (int)(r >> 1), c = (int)(r & 1u), e = (j + c) & 1;
+    const unsigned hx = (unsigned)g.hx;
+    const unsigned base = l * g.plane;
+    const unsigned row = base + r * hx;
+    const unsigned orow = base + (unsigned)(2 * j + (c ^ 1)) * hx;  // other colour, same j
+    const bool hs = j > 0, hn = j < g.ny - 1, hd = l > 0, hu = (int)l < g.nz - 1;
+    for (unsigned t0 = (unsigned)lane; t0 < hx; t0 += 32u * U) {
+        ApplyCell a[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const unsigned t = t0 + 32u * u;
+            const int i = 2 * (int)t + e;
+            if (t < hx && i < g.nx) apply_load(o, dgw, p, row + t, t, orow, i, e, hs, hn, hd, hu, a[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const unsigned t = t0 + 32u * u;
+            const int i = 2 * (int)t + e;
+            if (t < hx)
+                Ap[row + t] = i < g.nx ? apply_compute(a[u], i > 0, i < g.nx - 1, hs, hn, hd, hu, pap)
+                                       : make_float2(0.0f, 0.0f);
+        }
     }
 }
 

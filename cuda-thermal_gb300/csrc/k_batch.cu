@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(NT)
     const int lane = (int)(threadIdx.x & 31u);
     DwAcc pacc = {0.0f, 0.0f};
     for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32)
-        apply_row(o, dgw, pv, Ap, R, lane, pacc);
+        apply_row_seq(o, dgw, pv, Ap, R, lane, pacc);
     double pap = (double)pacc.s + (double)pacc.c, unused = 0.0;
     block_sum2(pap, unused);
     if (publish_inst(pap, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {

@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(NT)
     const int lane = (int)(threadIdx.x & 31u);
     DwAcc acc = {0.0f, 0.0f};
     for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows; R += gridDim.x * (NT / 32))
-        apply_row(o, dgw, p, Ap, R, lane, acc);
+        apply_row<2>(o, dgw, p, Ap, R, lane, acc);
     double pap = (double)acc.s + (double)acc.c, unused = 0.0;
     block_sum2(pap, unused);
     if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
