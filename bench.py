@@ -9,7 +9,8 @@ double-word arithmetic on the FP32 pipes with one FP64 residual replacement
 larger than L2 (the fine level alone moves > 1 GB per iteration), so no L2
 flush is needed between steps.
 
-Reported beside it, on the same GPU: the batched backward-Euler run (64
+Reported beside it, on the same GPU: the 1024 x 1024 x 16 four-tier stack
+(DW, FLEX and FP64 solves/s), the batched backward-Euler run (64
 switching 256 x 256 x 10 stacks, 500 steps, per-instance dt), the batched form
 on a 256-instance
 floorplan sweep (uneven stacks solved together, instance solves/s against
@@ -367,6 +368,38 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
     }
 
 
+def bench_four_tier(ct, np, torch, args):
+    """The 1024 x 1024 x 16 four-tier stack (TSV blocks, log-normal
+    floorplans, 80 W): DW, FLEX and plain FP64 steady solves/s on the same
+    GPU, max|dT|, FP64 true residuals."""
+    import workloads
+    m = workloads.four_tier(1024, seed=3)
+    out = {"workload": "steady solve 1024x1024x16 four-tier stack (Si/bond x4, TIM, Cu), 2 % Cu "
+                       "TSV 8x8 blocks in bond layers, 12 log-normal blocks per tier, 20 W per tier, "
+                       f"tol {TOL:g}", "cells": m.ncells()}
+    T = {}
+    for key, prec in (("dw", ct.Precision.MG_FP32_FLEX_DW), ("flex", ct.Precision.MG_FP32_FLEX),
+                      ("fp64", ct.Precision.MG_FP64)):
+        s = ct.GpuPcg(m, ct.Precond.Multigrid, prec)
+        for _ in range(2):
+            s.set_x_zero()
+            s.set_rhs_steady()
+            s.solve(TOL, MAXIT)
+        k = 3
+        ms, st = timed_solves(ct, s, k, 1)
+        T[key] = s.get_x()
+        out[key] = {"value": k / (ms / 1e3), "unit": "solves/s", "iters": st[-1].iters,
+                    "ms_per_solve": ms / k, "true_relres": s.true_relres()}
+        s.close()
+    out["value"] = out["dw"]["value"]
+    out["unit"] = "solves/s"
+    out["speedup_vs_fp64"] = out["dw"]["value"] / out["fp64"]["value"]
+    out["flex_speedup_vs_fp64"] = out["flex"]["value"] / out["fp64"]["value"]
+    out["max_dT_K"] = float(np.abs(T["dw"] - T["fp64"]).max())
+    out["max_dT_K_flex"] = float(np.abs(T["flex"] - T["fp64"]).max())
+    return out
+
+
 def bench_transient_batched(ct, np, args, steps):
     """The batched transient: 64 instances of the 256 x 256 x 10 stack, each
     with 9 blocks switching at Poisson times (mean 5 ms), backward-Euler steps
@@ -457,6 +490,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 256-instance run")
+    ap.add_argument("--no-four-tier", action="store_true", help="skip the 1024x1024x16 stack")
     ap.add_argument("--transient-steps", type=int, default=500,
                     help="backward-Euler steps of the batched transient (0: skip)")
     args = ap.parse_args()
@@ -555,6 +589,9 @@ def main():
         batched = bench_batched(ct, np, torch, args, hbm_peak, peak_kind)
         if world > 1:
             batched["value"] = sum_over_ranks(batched["value"], world)
+    four = None
+    if not args.no_four_tier:
+        four = bench_four_tier(ct, np, torch, args)
     transient = None
     if args.transient_steps > 0:
         transient = bench_transient_batched(ct, np, args, args.transient_steps)
@@ -611,6 +648,8 @@ def main():
             out["batched"] = batched
         if transient:
             out["batched_transient"] = transient
+        if four:
+            out["four_tier"] = four
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)
