@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(NT)
     k_residual_x(OpView o, const double* __restrict__ diag, const double* __restrict__ b,
                  const double* __restrict__ x, float2* __restrict__ r, float* __restrict__ b0,
                  int start, Ctl* ctl, double* part, int maxb, Cond cond) {
+    pdl_enter();
     if (!start && *(volatile const int*)&ctl->done) {  // converged or stopped in phase 1
         if (cond.use && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond.h, 0u);
         return;
@@ -208,6 +209,7 @@ __global__ void __launch_bounds__(NT)
 __global__ void __launch_bounds__(NT)
     k_apply_dw_rows(OpView o, const float2* __restrict__ dgw, const float2* __restrict__ p,
                     float2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     const Geo& g = o.g;
     const unsigned rows = 2u * (unsigned)g.ny * (unsigned)g.nz;
@@ -291,6 +293,7 @@ __global__ void __launch_bounds__(NT)
     k_update_dw(unsigned n2, const float4* __restrict__ p, const float4* __restrict__ Ap,
                 float4* __restrict__ x, float4* __restrict__ r, float2* __restrict__ b0, Ctl* ctl,
                 double* part, int maxb, Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     DwAcc acc = {0.0f, 0.0f};
     const BlockRange br = block_range(n2);
@@ -326,6 +329,7 @@ __global__ void __launch_bounds__(NT)
 __global__ void __launch_bounds__(NT)
     k_dot_dw(unsigned n2, const float4* __restrict__ r, const float2* __restrict__ z,
              const float4* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     DwAcc rz = {0.0f, 0.0f}, zap = {0.0f, 0.0f};
     const BlockRange br = block_range(n2);
@@ -352,6 +356,7 @@ __global__ void __launch_bounds__(NT)
 __global__ void __launch_bounds__(NT)
     k_update_p_dw(unsigned n2, const float2* __restrict__ z, float4* __restrict__ p, const Ctl* ctl,
                   Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     const BlockRange br = block_range(n2);
     update_p_range(br.begin, br.end, NT, ctl->beta_w, ctl->iter == 0, z, p);
@@ -362,6 +367,7 @@ __global__ void __launch_bounds__(NT)
 // replacement, which is what it serves.
 __global__ void k_fold(unsigned n2, double2* __restrict__ xb, float4* __restrict__ xw,
                        const Ctl* ctl, int check_done) {
+    pdl_enter();
     if (check_done && *(volatile const int*)&ctl->done) return;
     for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
         const float4 w = xw[k];
@@ -427,7 +433,7 @@ unsigned blocks_of(size_t n) {
 void launch_fold(cudaStream_t st, unsigned n, double* xb, float2* xw, const Ctl* ctl,
                  bool check_done) {
     static const int wb = wave_blocks(k_fold, 1 << 30);
-    k_fold<<<std::min((int)blocks_of(n / 2), wb), NT, 0, st>>>(n / 2, (double2*)xb, (float4*)xw, ctl,
+    launch_pdl(k_fold, std::min((int)blocks_of(n / 2), wb), NT, 0, st, n / 2, (double2*)xb, (float4*)xw, ctl,
                                                                check_done ? 1 : 0);
 }
 
@@ -435,7 +441,7 @@ void launch_residual_x(cudaStream_t st, const OpView& o, const double* diag, con
                        const double* x, float2* r, float* b0, bool start, Ctl* ctl,
                        const Red& red, Cond cond) {
     static const int wb = wave_blocks(k_residual_x, 1 << 30);
-    k_residual_x<<<std::min(red.blocks, wb), NT, 0, st>>>(o, diag, b, x, r, b0, start ? 1 : 0, ctl, red.part,
+    launch_pdl(k_residual_x, std::min(red.blocks, wb), NT, 0, st, o, diag, b, x, r, b0, start ? 1 : 0, ctl, red.part,
                                             red.maxb, cond);
 }
 
@@ -451,7 +457,7 @@ void launch_apply_dw(cudaStream_t st, const OpView& o, const float2* dgw, const 
     }();
     if (form == 0) {
         static const int wb = wave_blocks(k_apply_dw_rows, 1 << 30);
-        k_apply_dw_rows<<<std::min(red.maxb, wb), NT, 0, st>>>(o, dgw, p, Ap, ctl, red.part, red.maxb,
+        launch_pdl(k_apply_dw_rows, std::min(red.maxb, wb), NT, 0, st, o, dgw, p, Ap, ctl, red.part, red.maxb,
                                                               cond);
         return;
     }
@@ -468,21 +474,22 @@ void launch_apply_dw(cudaStream_t st, const OpView& o, const float2* dgw, const 
 void launch_update_dw(cudaStream_t st, unsigned n, const float2* p, const float2* Ap, float2* x,
                       float2* r, float* b0, Ctl* ctl, const Red& red, Cond cond) {
     static const int wb = wave_blocks(k_update_dw, 1 << 30);
-    k_update_dw<<<std::min(red.blocks, wb), NT, 0, st>>>(n / 2, (const float4*)p, (const float4*)Ap, (float4*)x,
+    launch_pdl(k_update_dw, std::min(red.blocks, wb), NT, 0, st, n / 2, (const float4*)p, (const float4*)Ap, (float4*)x,
                                            (float4*)r, (float2*)b0, ctl, red.part, red.maxb, cond);
 }
 
 void launch_dot_dw(cudaStream_t st, unsigned n, const float2* r, const float* z, const float2* Ap,
                    Ctl* ctl, const Red& red, Cond cond) {
     static const int wb = wave_blocks(k_dot_dw, 1 << 30);
-    k_dot_dw<<<std::min(red.blocks, wb), NT, 0, st>>>(n / 2, (const float4*)r, (const float2*)z,
+    launch_pdl(k_dot_dw, std::min(red.blocks, wb), NT, 0, st, n / 2, (const float4*)r, (const float2*)z,
                                         (const float4*)Ap, ctl, red.part, red.maxb, cond);
 }
 
 void launch_update_p_dw(cudaStream_t st, unsigned n, const float* z, float2* p, Ctl* ctl,
                         Cond cond) {
     static const int wb = wave_blocks(k_update_p_dw, 1 << 30);
-    k_update_p_dw<<<std::min((int)blocks_of(n / 2), wb), NT, 0, st>>>(n / 2, (const float2*)z, (float4*)p, ctl, cond);
+    launch_pdl(k_update_p_dw, std::min((int)blocks_of(n / 2), wb), NT, 0, st, n / 2, (const float2*)z, (float4*)p, ctl,
+               cond);
 }
 
 void launch_to_dw(cudaStream_t st, unsigned n, const double* in, float2* out) {

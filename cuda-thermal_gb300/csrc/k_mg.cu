@@ -89,6 +89,7 @@ __global__ void k_coarsen(Geo fg, const float* __restrict__ fgE, const float* __
 template <class T, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(NT)
     k_sweep(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     const unsigned q = blockIdx.x * NT + threadIdx.x;
     if (q >= (unsigned)L.g.ny * (unsigned)L.g.hx) return;
@@ -99,6 +100,7 @@ __global__ void __launch_bounds__(NT)
 template <class T>
 __global__ void __launch_bounds__(NT)
     k_restrict(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     const unsigned q = blockIdx.x * NT + threadIdx.x;
     if (q >= (unsigned)C.g.nx * (unsigned)C.g.ny) return;
@@ -157,6 +159,7 @@ __global__ void __launch_bounds__(kTailThreads, 1)
 template <class T, int MZ>
 __global__ void __launch_bounds__(kSmallThreads, 1)
     k_vsmall(TailLevels<T> tl, const Ctl* ctl, Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     extern __shared__ __align__(16) unsigned char smem[];
     mgdev::vsmall_body<T, MZ>(tl, (T)ctl->inv_dt, smem);
@@ -189,11 +192,11 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
 #define CT_SWEEP(MZ)                                                                    \
     do {                                                                                \
         if (zero_x)                                                                     \
-            k_sweep<T, MZ, true, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);   \
+            launch_pdl(k_sweep<T, MZ, true, false>, grid, NT, 0, st, L, color, C, ctl, cond);  \
         else if (coarse)                                                                \
-            k_sweep<T, MZ, false, true><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);   \
+            launch_pdl(k_sweep<T, MZ, false, true>, grid, NT, 0, st, L, color, C, ctl, cond);  \
         else                                                                            \
-            k_sweep<T, MZ, false, false><<<grid, NT, 0, st>>>(L, color, C, ctl, cond);  \
+            launch_pdl(k_sweep<T, MZ, false, false>, grid, NT, 0, st, L, color, C, ctl, cond); \
     } while (0)
     if (nz <= 8)
         CT_SWEEP(8);
@@ -212,7 +215,7 @@ template <class T>
 void launch_restrict(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,
                      Cond cond) {
     const dim3 grid(blocks_for((unsigned)C.g.nx * C.g.ny), (unsigned)C.g.nz);
-    k_restrict<T><<<grid, NT, 0, st>>>(F, C, ctl, cond);
+    launch_pdl(k_restrict<T>, grid, NT, 0, st, F, C, ctl, cond);
 }
 
 template <class T>
@@ -318,7 +321,7 @@ cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, const Ctl* c
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              kSmallSmemMax);
         if (e != cudaSuccess) return e;
-        kern<<<1, kSmallThreads, smem, st>>>(tl, ctl, cond);
+        launch_pdl(kern, 1, kSmallThreads, smem, st, tl, ctl, cond);
         return cudaGetLastError();
     };
     if (mz <= 8) return go(k_vsmall<T, 8>);

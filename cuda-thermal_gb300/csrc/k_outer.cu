@@ -7,6 +7,7 @@
 // of a warp is one contiguous run of the split layout.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "kernels.h"
 #include "reduce.cuh"
@@ -493,6 +494,14 @@ unsigned grid_for(size_t n, int threads = NT) {
 }
 
 }  // namespace
+
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("CT_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
 
 void launch_residual(cudaStream_t st, MgType mt, const OpView& o, const double* diag,
                      const double* b, const double* x, double* r, void* b0, Ctl* ctl,

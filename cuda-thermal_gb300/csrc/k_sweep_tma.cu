@@ -217,6 +217,7 @@ template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(TT * TJ, 2)
     k_sweep_tma(const __grid_constant__ SweepMaps m, LevelView<float> L, LevelView<float> C,
                 int color, Ctl* ctl, Cond cond) {
+    pdl_enter();
     if (loop_done(ctl, cond)) return;
     extern __shared__ __align__(128) float sm[];
     __shared__ uint64_t full[NS];
@@ -279,7 +280,7 @@ void go(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L, const Le
     const Geo& g = L.g;
     const int ntiles = ((g.hx + TT - 1) / TT) * ((g.ny + TJ - 1) / TJ);
     const int grid = std::max(1, std::min(ntiles, full_wave));
-    kern<<<grid, TT * TJ, stage_bytes<TT, TJ, NS>(ZERO), st>>>(m, L, C, color, ctl, cond);
+    launch_pdl(kern, grid, TT * TJ, stage_bytes<TT, TJ, NS>(ZERO), st, m, L, C, color, ctl, cond);
 }
 
 template <int MZ>

@@ -45,6 +45,33 @@ inline int wave_blocks(K kernel, int cap) {
     return b < cap ? b : cap;
 }
 
+// Programmatic dependent launch: the solve-loop kernels are launched with
+// programmatic stream serialization, so a kernel's launch overlaps the end of
+// its predecessor (each block of the predecessor releases it as it exits);
+// every such kernel starts with pdl_enter() (wait until the predecessor grid
+// has completed and its memory is visible) before it touches memory. Without
+// the launch attribute both instructions are no-ops. CT_PDL=0 turns the
+// attribute off.
+bool pdl_enabled();
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+template <class... KArgs, class... Args>
+inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // ---- outer PCG (FP64), k_outer.cu ----------------------------------------
 // r = b - (A + C/dt) x, b0 = r in the V-cycle precision; rr, bb; start test.
 void launch_residual(cudaStream_t st, MgType mt, const OpView& o, const double* diag,
