@@ -86,14 +86,14 @@ __global__ void k_coarsen(Geo fg, const float* __restrict__ fgE, const float* __
     }
 }
 
-template <class T, int MZ, bool ZERO, bool PRO>
+template <class T, int MZ, bool ZERO, bool PRO, bool BF>
 __global__ void __launch_bounds__(NT)
     k_sweep(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
     const unsigned q = blockIdx.x * NT + threadIdx.x;
     if (q >= (unsigned)L.g.ny * (unsigned)L.g.hx) return;
-    sweep_column<T, MZ, ZERO, PRO, false>(L, C, color, q);
+    sweep_column<T, MZ, ZERO, PRO, false, BF>(L, C, color, q);
 }
 
 // One thread per coarse cell: blockIdx.y is the plane.
@@ -189,14 +189,23 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
     const unsigned grid = blocks_for((unsigned)L.g.ny * (unsigned)L.g.hx);
     const LevelView<T> C = coarse ? *coarse : L;
     const int nz = L.g.nz;
-#define CT_SWEEP(MZ)                                                                    \
-    do {                                                                                \
-        if (zero_x)                                                                     \
-            launch_pdl(k_sweep<T, MZ, true, false>, grid, NT, 0, st, L, color, C, ctl, cond);  \
-        else if (coarse)                                                                \
-            launch_pdl(k_sweep<T, MZ, false, true>, grid, NT, 0, st, L, color, C, ctl, cond);  \
-        else                                                                            \
-            launch_pdl(k_sweep<T, MZ, false, false>, grid, NT, 0, st, L, color, C, ctl, cond); \
+    // small levels (L2-resident, latency-bound): the branch-free gather
+    const bool bf = (unsigned)L.g.nx * (unsigned)L.g.ny <= kSweepBfColumns;
+#define CT_SWEEP2(MZ, BF)                                                                          \
+    do {                                                                                           \
+        if (zero_x)                                                                                \
+            launch_pdl(k_sweep<T, MZ, true, false, BF>, grid, NT, 0, st, L, color, C, ctl, cond);  \
+        else if (coarse)                                                                           \
+            launch_pdl(k_sweep<T, MZ, false, true, BF>, grid, NT, 0, st, L, color, C, ctl, cond);  \
+        else                                                                                       \
+            launch_pdl(k_sweep<T, MZ, false, false, BF>, grid, NT, 0, st, L, color, C, ctl, cond); \
+    } while (0)
+#define CT_SWEEP(MZ)              \
+    do {                          \
+        if (bf)                   \
+            CT_SWEEP2(MZ, true);  \
+        else                      \
+            CT_SWEEP2(MZ, false); \
     } while (0)
     if (nz <= 8)
         CT_SWEEP(8);
@@ -209,6 +218,7 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
     else
         CT_SWEEP(0);
 #undef CT_SWEEP
+#undef CT_SWEEP2
 }
 
 template <class T>

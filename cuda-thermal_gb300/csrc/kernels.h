@@ -143,6 +143,9 @@ void launch_factor(cudaStream_t st, const LevelView<T>& L, T inv_dt);
 // V-cycle), so lateral neighbours are not read. xc: when not null, the
 // coarser level's x is added to every neighbour value read (prolongation
 // fused into the sweep).
+// Levels of at most this many columns use the branch-free gather
+// (mgdev::sweep_column, BF).
+constexpr unsigned kSweepBfColumns = 128u * 128u;
 template <class T>
 void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x,
                   const LevelView<T>* coarse_for_prolong, const Ctl* ctl, Cond cond);

@@ -88,7 +88,13 @@ __device__ __forceinline__ T lat_sum(const LevelView<T>& L, const LevelView<T>& 
 // all loads independent of one another, then the Thomas recurrence runs on
 // registers and x is written once. MZ = 0 is the general path for deep
 // columns, with forward values going through x as in the reference.
-template <class T, int MZ, bool ZERO, bool PRO, bool CG>
+//
+// BF (branch-free gather, for levels held in shared memory or L2, where load
+// latency rather than bandwidth bounds a sweep): planes past nz read the last
+// plane (values unused) and an absent neighbour reads the column itself with
+// weight 0 — an exact zero added where lat_sum skips the term — so every
+// load of every plane can be in flight at once.
+template <class T, int MZ, bool ZERO, bool PRO, bool CG, bool BF = false>
 __device__ __forceinline__ void sweep_column(const LevelView<T>& L, const LevelView<T>& C,
                                              int color, unsigned q) {
     const Geo& g = L.g;
@@ -96,7 +102,55 @@ __device__ __forceinline__ void sweep_column(const LevelView<T>& L, const LevelV
     const int i = 2 * t + ((j + color) & 1);
     if (i >= g.nx) return;
     const Nbr n = neighbours<PRO>(g, C.g, i, j, t, color);
-    if constexpr (MZ > 0) {
+    if constexpr (MZ > 0 && BF) {
+        const unsigned sw = n.w ? n.sw : n.s, se = n.e ? n.se : n.s;
+        const unsigned ss = n.so ? n.ss : n.s, sn = n.no ? n.sn : n.s;
+        T v[MZ], fi[MZ], fc[MZ];
+        float gu[MZ];
+#pragma unroll
+        for (int l = 0; l < MZ; ++l) {
+            const unsigned lc = (unsigned)(l < g.nz ? l : g.nz - 1);
+            const unsigned base = lc * g.plane, id = base + n.s;
+            T rhs = ldm<CG>(L.b + id);
+            if (!ZERO) {
+                T xw = ldm<CG>(L.x + base + sw), xe = ldm<CG>(L.x + base + se);
+                T xs = ldm<CG>(L.x + base + ss), xn = ldm<CG>(L.x + base + sn);
+                if (PRO) {
+                    const T* cx = C.x + lc * C.g.plane;
+                    xw = xw + ldm<CG>(cx + n.pw);
+                    xe = xe + ldm<CG>(cx + n.pe);
+                    xs = xs + ldm<CG>(cx + n.ps);
+                    xn = xn + ldm<CG>(cx + n.pn);
+                }
+                const float ew = L.gE[base + sw], ee = L.gE[id], ns = L.gN[base + ss], nn = L.gN[id];
+                T sum = 0;  // op_lat_sum order: west, east, south, north
+                sum += (n.w ? (T)ew : T(0)) * xw;
+                sum += (n.e ? (T)ee : T(0)) * xe;
+                sum += (n.so ? (T)ns : T(0)) * xs;
+                sum += (n.no ? (T)nn : T(0)) * xn;
+                rhs = rhs + sum;
+            }
+            v[l] = rhs;
+            fi[l] = L.finv[id];
+            fc[l] = L.fcp[id];
+            gu[l] = L.gU[id];
+        }
+        T prev = 0;
+#pragma unroll
+        for (int l = 0; l < MZ; ++l) {
+            if (l < g.nz) {
+                const T lower = l > 0 ? -(T)gu[l - 1] : T(0);
+                prev = (v[l] - lower * prev) * fi[l];
+                v[l] = prev;
+            }
+        }
+#pragma unroll
+        for (int l = MZ - 2; l >= 0; --l)
+            if (l < g.nz - 1) v[l] -= fc[l] * v[l + 1];
+#pragma unroll
+        for (int l = 0; l < MZ; ++l)
+            if (l < g.nz) L.x[(unsigned)l * g.plane + n.s] = v[l];
+    } else if constexpr (MZ > 0) {
         // Gather: every operand of every plane, all loads independent, so the
         // whole column costs about one memory latency.
         T v[MZ], fi[MZ], fc[MZ];
@@ -274,9 +328,9 @@ __device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
     for (int k = 0; k < last; ++k) {
         const LevelView<T> L = sl.L[k];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false, true>(L, L, 0, q);
         __syncthreads();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 1, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false, true>(L, L, 1, q);
         __syncthreads();
         const LevelView<T> C = sl.L[k + 1];
         const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
@@ -290,16 +344,16 @@ __device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
     {
         const LevelView<T> L = sl.L[last];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false>(L, L, 0, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false, true>(L, L, 0, q);
         __syncthreads();
     }
     for (int k = last - 1; k >= 0; --k) {
         const LevelView<T> L = sl.L[k];
         const LevelView<T> C = sl.L[k + 1];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false>(L, C, 1, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false, true>(L, C, 1, q);
         __syncthreads();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false>(L, L, 0, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false, true>(L, L, 0, q);
         __syncthreads();
     }
     const LevelView<T> S0 = sl.L[0];
