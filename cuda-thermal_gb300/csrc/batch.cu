@@ -555,7 +555,8 @@ void Batch::vcycle(Bucket& b, cudaStream_t s, Cond cond) {
         }
     }
     enq(s, "b_small", smb, [&] {
-        const cudaError_t e = launch_b_small(s, b.small_insts, (int)b.inst.size(), small, b.smem, b.mz, ctl);
+        const cudaError_t e =
+            launch_b_small(s, b.small_insts, (int)b.inst.size(), small, b.smem, b.mz, ctl, b.bc, cond);
         if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
     });
     for (int d = b.depth; d-- > 0;) {

@@ -93,7 +93,8 @@ void launch_b_sweep_tma(cudaStream_t st, const Plan& p, const SweepMaps* maps,
 int sweep_tma_tiles(const Geo& g);
 // The bottom of every instance's V-cycle: one block per instance in `insts`.
 cudaError_t launch_b_small(cudaStream_t st, const int* insts, int n,
-                           const TailLevels<float>* small, size_t smem, int mz, const Ctl* ctl);
+                           const TailLevels<float>* small, size_t smem, int mz, Ctl* ctl, BCtl* bc,
+                           Cond cond);
 // set_dt for all instances (1/dt from ctl[i].inv_dt): the fine FP64 and
 // double-word diagonal (items: natural fine columns), and the column factors
 // of one level index (items: natural columns of that level; views[i] =

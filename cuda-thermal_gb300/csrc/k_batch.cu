@@ -422,11 +422,17 @@ __global__ void __launch_bounds__(NT)
 template <int MZ>
 __global__ void __launch_bounds__(kSmallThreads, 1)
     kb_small(const int* __restrict__ insts, const TailLevels<float>* __restrict__ small,
-             const Ctl* ctl) {
+             Ctl* ctl, BCtl* bc, Cond cond) {
     const int i = insts[blockIdx.x];
-    if (inst_done(&ctl[i])) return;
+    Ctl* c = &ctl[i];
+    if (inst_done(c)) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    vsmall_body<float, MZ>(small[i], (float)ctl[i].inv_dt, smem);
+    if (!vsmall_body<float, MZ>(small[i], (float)c->inv_dt, smem) && threadIdx.x == 0) {
+        // a bounded wait ran out: record it and stop this instance
+        atomicExch(&c->err, 1);
+        c->breakdown = 1;
+        inst_stop(c, bc, cond);
+    }
 }
 
 }  // namespace
@@ -509,12 +515,13 @@ void launch_b_restrict(cudaStream_t st, const Plan& p, const LevelView<float>* v
 }
 
 cudaError_t launch_b_small(cudaStream_t st, const int* insts, int n,
-                           const TailLevels<float>* small, size_t smem, int mz, const Ctl* ctl) {
+                           const TailLevels<float>* small, size_t smem, int mz, Ctl* ctl, BCtl* bc,
+                           Cond cond) {
     auto go = [&](auto kern) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              kSmallSmemMax);
         if (e != cudaSuccess) return e;
-        kern<<<n, kSmallThreads, smem, st>>>(insts, small, ctl);
+        kern<<<n, kSmallThreads, smem, st>>>(insts, small, ctl, bc, cond);
         return cudaGetLastError();
     };
     if (mz <= 8) return go(kb_small<8>);

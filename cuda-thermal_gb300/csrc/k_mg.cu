@@ -158,11 +158,16 @@ __global__ void __launch_bounds__(kTailThreads, 1)
 // The bottom of the V-cycle in one block from shared memory (mgdev::vsmall_body).
 template <class T, int MZ>
 __global__ void __launch_bounds__(kSmallThreads, 1)
-    k_vsmall(TailLevels<T> tl, const Ctl* ctl, Cond cond) {
+    k_vsmall(TailLevels<T> tl, Ctl* ctl, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    mgdev::vsmall_body<T, MZ>(tl, (T)ctl->inv_dt, smem);
+    if (!mgdev::vsmall_body<T, MZ>(tl, (T)ctl->inv_dt, smem) && threadIdx.x == 0) {
+        // a bounded wait ran out: record it and stop the solve
+        atomicExch(&ctl->err, 1);
+        ctl->breakdown = 1;
+        stop_loop(ctl, cond);
+    }
 }
 
 unsigned blocks_for(unsigned n) { return n == 0 ? 1u : (n + NT - 1) / NT; }
@@ -321,7 +326,7 @@ size_t small_smem_bytes(const TailLevels<T>& tl) {
 }
 
 template <class T>
-cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, const Ctl* ctl, Cond cond) {
+cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, Ctl* ctl, Cond cond) {
     const size_t smem = small_smem_bytes(tl);
     int mz = 0;
     for (int k = 0; k < tl.n; ++k) mz = tl.L[k].g.nz;
@@ -343,8 +348,8 @@ cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, const Ctl* c
 
 template size_t small_smem_bytes<float>(const TailLevels<float>&);
 template size_t small_smem_bytes<double>(const TailLevels<double>&);
-template cudaError_t launch_vsmall<float>(cudaStream_t, const TailLevels<float>&, const Ctl*, Cond);
-template cudaError_t launch_vsmall<double>(cudaStream_t, const TailLevels<double>&, const Ctl*,
+template cudaError_t launch_vsmall<float>(cudaStream_t, const TailLevels<float>&, Ctl*, Cond);
+template cudaError_t launch_vsmall<double>(cudaStream_t, const TailLevels<double>&, Ctl*,
                                            Cond);
 
 }  // namespace ct

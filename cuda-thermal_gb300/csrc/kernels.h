@@ -192,7 +192,7 @@ constexpr int kSmallSmemMax = 200 * 1024;
 template <class T>
 size_t small_smem_bytes(const TailLevels<T>& tl);
 template <class T>
-cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, const Ctl* ctl, Cond cond);
+cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, Ctl* ctl, Cond cond);
 template <class T>
 cudaError_t launch_vtail(cudaStream_t st, const TailLevels<T>& tl, int cluster, const Ctl* ctl,
                          Cond cond);

@@ -5,6 +5,7 @@
 // (src/pcg3d_cpu.cpp:87-100), and the shared-memory bottom of the V-cycle.
 #pragma once
 #include "kernels.h"
+#include "tma.cuh"
 
 namespace ct {
 namespace mgdev {
@@ -260,16 +261,24 @@ __device__ __forceinline__ void restrict_cell(const LevelView<T>& F, const Level
 
 
 // The bottom of the V-cycle (levels k0 .. single column) in ONE block, with
-// every one of those levels held in shared memory: operator, factors, x and b
-// are copied in (the levels are a few tens of KB), the phases run with block
+// every one of those levels held in shared memory: operator and factors of
+// every level and level k0's b come in by bulk copies (all in flight at once,
+// one mbarrier), x and the coarser b start at zero, the phases run with block
 // barriers, and level k0's x goes back out for the prolongation above it.
 // Same line-solve and restriction code as the grid-wide kernels, pointed at
-// shared memory.
+// shared memory. Returns false (nothing written) if the bounded wait for the
+// copies ran out.
 template <class T, int MZ>
-__device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
+__device__ __forceinline__ bool vsmall_body(const TailLevels<T>& tl, T inv_dt,
                                             unsigned char* smem) {
     __shared__ TailLevels<T> sl;  // views of the same levels, in shared memory
-    if (threadIdx.x == 0) sl.n = tl.n;
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        sl.n = tl.n;
+        tma::mbar_init(&bar, 1);
+        tma::fence_barrier_init();
+    }
+    __syncthreads();
     {
         unsigned char* q = smem;
         auto take = [&](size_t bytes) {
@@ -277,6 +286,15 @@ __device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
             q += (bytes + 15) & ~size_t(15);
             return r;
         };
+        if (threadIdx.x == 0) {
+            unsigned total = 0;
+            for (int k = 0; k < tl.n; ++k) {
+                const unsigned ln = tl.L[k].g.plane * (unsigned)tl.L[k].g.nz;
+                total += 4u * ln * 4u + tl.L[k].g.plane * 4u + 2u * ln * (unsigned)sizeof(T);
+                if (k == 0) total += ln * (unsigned)sizeof(T);
+            }
+            tma::mbar_arrive_expect_tx(&bar, total);
+        }
         for (int k = 0; k < tl.n; ++k) {
             const LevelView<T>& G = tl.L[k];
             LevelView<T> S;
@@ -291,21 +309,24 @@ __device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
             T* finv = (T*)take(ln * sizeof(T));
             T* x = (T*)take(ln * sizeof(T));
             T* b = (T*)take(ln * sizeof(T));
-            for (unsigned i = threadIdx.x; i < ln; i += kSmallThreads) {
-                gE[i] = G.gE[i];
-                gN[i] = G.gN[i];
-                gU[i] = G.gU[i];
-                cap[i] = G.cap[i];
-                fcp[i] = G.fcp[i];
-                finv[i] = G.finv[i];
-                // Padding slots are never written by the phases below but go
-                // back out with level k0's x: start every slot at zero, as the
-                // global arrays' padding is, so no stale shared-memory value
-                // (possibly a NaN) reaches the outer iteration.
-                x[i] = T(0);
-                b[i] = k == 0 ? G.b[i] : T(0);
+            if (threadIdx.x == 0) {
+                tma::bulk_load(gE, G.gE, ln * 4u, &bar);
+                tma::bulk_load(gN, G.gN, ln * 4u, &bar);
+                tma::bulk_load(gU, G.gU, ln * 4u, &bar);
+                tma::bulk_load(cap, G.cap, ln * 4u, &bar);
+                tma::bulk_load(gB, G.gB, G.g.plane * 4u, &bar);
+                tma::bulk_load(fcp, G.fcp, ln * (unsigned)sizeof(T), &bar);
+                tma::bulk_load(finv, G.finv, ln * (unsigned)sizeof(T), &bar);
+                if (k == 0) tma::bulk_load(b, G.b, ln * (unsigned)sizeof(T), &bar);
             }
-            for (unsigned i = threadIdx.x; i < G.g.plane; i += kSmallThreads) gB[i] = G.gB[i];
+            // Padding slots are never written by the phases below but go back
+            // out with level k0's x: start every slot at zero, as the global
+            // arrays' padding is, so no stale shared-memory value (possibly a
+            // NaN) reaches the outer iteration.
+            for (unsigned i = threadIdx.x; i < ln; i += kSmallThreads) {
+                x[i] = T(0);
+                if (k > 0) b[i] = T(0);
+            }
             S.gE = gE;
             S.gN = gN;
             S.gU = gU;
@@ -318,7 +339,11 @@ __device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
             if (threadIdx.x == 0) sl.L[k] = S;
         }
     }
-    __syncthreads();
+    const bool got = tma::mbar_wait(&bar, 0u);
+    if (!__syncthreads_and(got)) {
+        if (threadIdx.x == 0) tma::mbar_wait(&bar, 0u);  // let the copies land before leaving
+        return false;
+    }
     const unsigned tid = threadIdx.x, nth = kSmallThreads;
     const int last = sl.n - 1;
     // Each phase works on register copies of the level views: the views live
@@ -360,6 +385,7 @@ __device__ __forceinline__ void vsmall_body(const TailLevels<T>& tl, T inv_dt,
     const unsigned ln0 = S0.g.plane * (unsigned)S0.g.nz;
     T* out = tl.L[0].x;
     for (unsigned i = tid; i < ln0; i += nth) out[i] = S0.x[i];
+    return true;
 }
 
 
