@@ -125,9 +125,9 @@ __global__ void __launch_bounds__(kTailThreads, 1)
     for (int k = 0; k < last; ++k) {
         const LevelView<T>& L = tl.L[k];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true>(L, L, 0, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true, true>(L, L, 0, q);
         cl.sync();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true>(L, L, 1, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true, true>(L, L, 1, q);
         cl.sync();
         const LevelView<T>& C = tl.L[k + 1];
         const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
@@ -141,16 +141,16 @@ __global__ void __launch_bounds__(kTailThreads, 1)
     {
         const LevelView<T>& L = tl.L[last];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true>(L, L, 0, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true, true>(L, L, 0, q);
         cl.sync();
     }
     for (int k = last - 1; k >= 0; --k) {
         const LevelView<T>& L = tl.L[k];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
         for (unsigned q = tid; q < ncol; q += nth)
-            sweep_column<T, MZ, false, true, true>(L, tl.L[k + 1], 1, q);
+            sweep_column<T, MZ, false, true, true, true>(L, tl.L[k + 1], 1, q);
         cl.sync();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true>(L, L, 0, q);
+        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true, true>(L, L, 0, q);
         cl.sync();
     }
 }
