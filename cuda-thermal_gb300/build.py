@@ -29,8 +29,8 @@ HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-Wall"]
 CU_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
             "-Xcompiler", "-fPIC,-ffp-contract=off"]
 
-CPP_SOURCES = ["status.cpp", "model.cpp"]
-CU_SOURCES = ["k_outer.cu", "k_mg.cu", "k_dw.cu", "k_batch.cu", "k_sweep_tma.cu", "solver.cu", "batch.cu", "noalloc.cu"]
+CPP_SOURCES = ["status.cpp", "model.cpp", "case.cpp"]
+CU_SOURCES = ["k_outer.cu", "k_mg.cu", "k_dw.cu", "k_batch.cu", "k_sweep_tma.cu", "k_apply_tma.cu", "solver.cu", "batch.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

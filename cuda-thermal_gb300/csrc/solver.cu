@@ -215,6 +215,12 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     CT_CK(cudaStreamSynchronize(st));
     times.alloc_ms = ms_since(t0);
 
+    // The staged DW operator apply (CT_APPLY=rows / cells / columns: the
+    // earlier forms).
+    if (dw && apply_tma_fits(g0)) {
+        const char* e = std::getenv("CT_APPLY");
+        if (!(e && e[0] != 't')) apply_tma = make_apply_maps(op(), pw(), dgw, &amaps);
+    }
     // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
     // (FP32 levels with at least one full tile row, above the shared-memory
     // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernel.
@@ -397,8 +403,14 @@ void Solver::enqueue_body(Cond cond) {
         enq("pcg_dot", N * (8 + 4 + 8),
             [&] { launch_dot_dw(cs, n, rw(), zf, Apw(), ctl, red_vec(SL_DOT), cond); });
         enq("pcg_update_p", N * (4 + 16), [&] { launch_update_p_dw(cs, n, zf, pw(), ctl, cond); });
-        enq("pcg_apply", N * 36,
-            [&] { launch_apply_dw(cs, op(), dgw, pw(), Apw(), ctl, red_cols(SL_APPLY), cond); });
+        enq("pcg_apply", N * 36, [&] {
+            if (apply_tma) {
+                const cudaError_t e = launch_apply_tma(cs, amaps, op(), Apw(), ctl, red_cols(SL_APPLY), cond);
+                if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
+            } else {
+                launch_apply_dw(cs, op(), dgw, pw(), Apw(), ctl, red_cols(SL_APPLY), cond);
+            }
+        });
         enq("pcg_update_xr", N * (48 + 4), [&] {
             launch_update_dw(cs, n, pw(), Apw(), xw(), rw(), b0, ctl, red_vec(SL_UPDATE), cond);
         });

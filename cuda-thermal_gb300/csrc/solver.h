@@ -88,6 +88,8 @@ class Solver {
     bool prof = false;
     std::vector<ProfEntry> prof_log;
 
+    bool apply_tma = false;   // the DW apply staged by bulk tensor copies (maps below)
+    ApplyMaps amaps{};
     bool own_stream = true;   // false: st belongs to a batch that owns this solver
     bool skip_graphs = false; // batch members record no graphs of their own
 

@@ -139,6 +139,12 @@ def _signatures():
         "ct_model_heat_out": (d, [gp, vp, vp, vp]),
         "ct_model_heat_stored": (d, [gp, vp, vp, vp, d]),
         "ct_model_analytic_1d": (i, [gp, lp, vp, vp, d, vp, vp]),
+        "ct_case_load": (i, [C.c_char_p, C.POINTER(vp)]),
+        "ct_case_destroy": (i, [vp]),
+        "ct_case_info": (i, [vp, ip, ip, ip, dp, dp, dp, dp, dp]),
+        "ct_case_layer": (i, [vp, i, C.POINTER(CtLayer), C.c_char_p, i]),
+        "ct_case_block": (i, [vp, i, ip, dp, dp, C.c_char_p, i]),
+        "ct_case_tsv": (i, [vp, i, ip, dp, dp]),
         "ct_eff_kz": (d, [d, d, d]),
         "ct_eff_kxy": (d, [d, d, d]),
     }
@@ -343,6 +349,86 @@ def eff_kz(k, kc, f) -> float:
 
 def eff_kxy(k, kc, f) -> float:
     return lib().ct_eff_kxy(k, kc, f)
+
+
+# ---- cases (src/case3d.h) -----------------------------------------------------
+
+@dataclass
+class PowerBlock:
+    name: str
+    layer: int
+    x0: float  # m
+    y0: float
+    w: float
+    h: float
+    watts: float
+
+
+@dataclass
+class TsvRegion:
+    layer: int
+    x0: float  # m
+    y0: float
+    w: float
+    h: float
+    fraction: float
+
+
+@dataclass
+class CaseSpec:
+    layers: List[Layer] = field(default_factory=list)
+    Lx: float = 10e-3
+    Ly: float = 10e-3
+    h_top: float = 2e4
+    h_bot: float = 0.0
+    T_amb: float = 25.0
+    blocks: List[PowerBlock] = field(default_factory=list)
+    tsvs: List[TsvRegion] = field(default_factory=list)
+
+
+def load_case(folder: str) -> CaseSpec:
+    """load_case (src/case3d.h:86-156) through the library's CSV reader;
+    raises CtError with the reference's message on a bad case."""
+    h = C.c_void_p()
+    _check(lib().ct_case_load(os.fsencode(folder), C.byref(h)))
+    try:
+        nl, nb, nt = C.c_int(), C.c_int(), C.c_int()
+        Lx, Ly, ht, hb, ta = (C.c_double() for _ in range(5))
+        _check(lib().ct_case_info(h, C.byref(nl), C.byref(nb), C.byref(nt), C.byref(Lx), C.byref(Ly),
+                                  C.byref(ht), C.byref(hb), C.byref(ta)))
+        cs = CaseSpec(Lx=Lx.value, Ly=Ly.value, h_top=ht.value, h_bot=hb.value, T_amb=ta.value)
+        name = C.create_string_buffer(256)
+        for k in range(nl.value):
+            v = CtLayer()
+            _check(lib().ct_case_layer(h, k, C.byref(v), name, 256))
+            cs.layers.append(Layer(name.value.decode(), v.thickness, v.k, v.rho_c, v.ncells,
+                                   bool(v.active)))
+        rect = (C.c_double * 4)()
+        for k in range(nb.value):
+            L, w = C.c_int(), C.c_double()
+            _check(lib().ct_case_block(h, k, C.byref(L), rect, C.byref(w), name, 256))
+            cs.blocks.append(PowerBlock(name.value.decode(), L.value, rect[0], rect[1], rect[2],
+                                        rect[3], w.value))
+        for k in range(nt.value):
+            L, f = C.c_int(), C.c_double()
+            _check(lib().ct_case_tsv(h, k, C.byref(L), rect, C.byref(f)))
+            cs.tsvs.append(TsvRegion(L.value, rect[0], rect[1], rect[2], rect[3], f.value))
+        return cs
+    finally:
+        lib().ct_case_destroy(h)
+
+
+def build_case_model(cs: CaseSpec, nx: int, ny: int, with_tsv: bool = True) -> Model3D:
+    """build_case_model (src/case3d.h:158-168)."""
+    m = build_model(cs.layers, nx, ny, cs.Lx, cs.Ly, cs.h_top, cs.h_bot)
+    m.T_amb = cs.T_amb
+    for b in cs.blocks:
+        add_power_block(m, b.layer, b.x0, b.y0, b.w, b.h, b.watts)
+    if with_tsv:
+        for t in cs.tsvs:
+            add_tsv_region(m, t.layer, t.x0, t.y0, t.w, t.h, t.fraction)
+    finalize(m)
+    return m
 
 
 def hotspot_model(n: int) -> Model3D:

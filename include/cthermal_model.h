@@ -76,6 +76,27 @@ double ct_model_heat_stored(const ct_grid* g, const float* cap, const double* T_
 ct_status ct_model_analytic_1d(const ct_grid* g, const ct_layer* layers, const int* plane_layer,
                                const double* dz, double h_top, const double* P, double* T);
 
+/* ---- cases: a stack, floorplan and TSV layout from CSV files ---------------
+ * load_case (src/case3d.h:86-156): dir/stack.csv, dir/floorplan.csv and, if
+ * present, dir/tsv.csv, with the reference's format and checks. CT_IO_ERROR
+ * when a required file cannot be opened, CT_BAD_ARG (with the reference's
+ * message) for a malformed one. The model is then built with ct_model_planes,
+ * ct_model_add_power_block for every block, ct_model_add_tsv_region for every
+ * TSV region (when wanted) and ct_model_finalize, in that order
+ * (build_case_model, src/case3d.h:158-168). */
+typedef struct ct_case ct_case;
+ct_status ct_case_load(const char* dir, ct_case** out);
+ct_status ct_case_destroy(ct_case* c);
+ct_status ct_case_info(const ct_case* c, int* nlayers, int* nblocks, int* ntsvs, double* Lx,
+                       double* Ly, double* h_top, double* h_bot, double* T_amb);
+/* Layer k (bottom to top) and its name (at most name_cap bytes with the NUL). */
+ct_status ct_case_layer(const ct_case* c, int k, ct_layer* out, char* name, int name_cap);
+/* Power block k: layer index, rect = {x0, y0, w, h} in m, watts, name. */
+ct_status ct_case_block(const ct_case* c, int k, int* layer, double* rect, double* watts, char* name,
+                        int name_cap);
+/* TSV region k: layer index, rect in m, copper fraction. */
+ct_status ct_case_tsv(const ct_case* c, int k, int* layer, double* rect, double* fraction);
+
 /* eff_kz, eff_kxy (src/stack3d.h:104-108). */
 double ct_eff_kz(double k, double kc, double f);
 double ct_eff_kxy(double k, double kc, double f);

@@ -71,6 +71,22 @@ def solve_record(m, tol, precond):
                 heat_out=ref.heat_out(m, T)), T
 
 
+CASES = ("example", "tsv_under_core0", "validate_3dice", "validate_tsv")
+
+
+def copy_cases():
+    """The reference's four example case folders (its CSV inputs, a few KB),
+    as fixtures for the case-loader tests: tests/golden/cases/<case>/*.csv."""
+    import shutil
+    src_root = os.path.join(ref.REF_SRC, "cases")
+    for case in CASES:
+        dst = os.path.join(HERE, "cases", case)
+        os.makedirs(dst, exist_ok=True)
+        for f in sorted(os.listdir(os.path.join(src_root, case))):
+            if f.endswith(".csv"):
+                shutil.copyfile(os.path.join(src_root, case, f), os.path.join(dst, f))
+
+
 def main():
     for mgd in (False, True):
         ref.lib(mgd)
@@ -119,7 +135,8 @@ def main():
     # The example case from its CSV files (load_case + build_case_model).
     out["case_files"] = {}
     case_root = os.path.join(ref.REF_SRC, "cases")
-    for case in ("example", "tsv_under_core0", "validate_3dice", "validate_tsv"):
+    copy_cases()
+    for case in CASES:
         for with_tsv in (True, False):
             m = ref.case_model(os.path.join(case_root, case), 40, 40, with_tsv, mg_double=True)
             r, _ = solve_record(m, 1e-10, "multigrid")

@@ -1,0 +1,93 @@
+"""Case loader (load_case / build_case_model, src/case3d.h:86-168) against
+the reference's own loader: the four example cases (tests/golden/cases, the
+reference's CSV inputs) built on a 40 x 40 grid with and without TSVs give
+the same model arrays bit for bit (SHA-256 from the reference, golden.json)
+and the same total power; malformed cases fail with the reference's checks.
+The GPU test solves each case and matches the reference's FP64 result."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_DIR
+
+CASES = ["example", "tsv_under_core0", "validate_3dice", "validate_tsv"]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def case_dir(name):
+    return os.path.join(GOLDEN_DIR, "cases", name)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("with_tsv", [True, False])
+def test_case_model_matches_reference(ct, golden, name, with_tsv):
+    ref = golden["case_files"][f"{name}_{int(with_tsv)}"]
+    cs = ct.load_case(case_dir(name))
+    m = ct.build_case_model(cs, 40, 40, with_tsv)
+    assert m.nz == ref["nz"]
+    for k, h in ref["model_sha"].items():
+        assert sha(getattr(m, k)) == h, k
+    assert ct.total_power(m) == ref["total_power"]
+
+
+def test_case_settings_and_names(ct):
+    cs = ct.load_case(case_dir("example"))
+    assert cs.Lx == pytest.approx(10e-3) and cs.Ly == pytest.approx(10e-3)
+    assert cs.h_top == 2e4 and cs.h_bot == 0.0 and cs.T_amb == 25.0
+    assert [L.name for L in cs.layers][0] == "Si tier 2 (bottom)"
+    assert all(cs.layers[b.layer].active for b in cs.blocks)
+    assert len(cs.tsvs) > 0
+
+
+def write_case(tmp_path, stack, floorplan, tsv=None):
+    d = tmp_path / "case"
+    d.mkdir(exist_ok=True)
+    (d / "stack.csv").write_text(stack)
+    (d / "floorplan.csv").write_text(floorplan)
+    if tsv is not None:
+        (d / "tsv.csv").write_text(tsv)
+    return str(d)
+
+
+STACK = ("# die_mm, 5, 4\n# h_top, 1e4\nname, t, k, rc, planes, active\n"
+         "Si, 50, 130, 1.66e6, 2, 1\nCu, 1000, 400, 3.45e6, 2, 0\n")
+
+
+def test_case_errors(ct, tmp_path):
+    ok = write_case(tmp_path, STACK, "h\ncore, Si, 0.5, 0.5, 1, 1, 2\n")
+    cs = ct.load_case(ok)
+    assert cs.Lx == pytest.approx(5e-3) and cs.Ly == pytest.approx(4e-3) and cs.h_top == 1e4
+    assert len(cs.blocks) == 1 and cs.blocks[0].watts == 2.0 and cs.tsvs == []
+    bad = [
+        (STACK, "h\ncore, Cu, 0.5, 0.5, 1, 1, 2\n", None, "not active"),
+        (STACK, "h\ncore, Xx, 0.5, 0.5, 1, 1, 2\n", None, "unknown layer"),
+        (STACK, "h\ncore, Si, 4.5, 0.5, 1, 1, 2\n", None, "outside the die"),
+        (STACK, "h\ncore, Si, 0.5, 0.5, 1\n", None, "expected 7 columns"),
+        (STACK, "h\ncore, Si, 0.5, 0.5, one, 1, 2\n", None, "could not parse a number"),
+        (STACK, "h\ncore, Si, 0.5, 0.5, 1, 1, 2\n", "h\nSi, 0, 0, 1, 1, 1.5\n", "between 0 and 1"),
+        ("name, t, k, rc, planes, active\n", "h\n", None, "no layers"),
+    ]
+    for stack, fp, tsv, msg in bad:
+        d = write_case(tmp_path, stack, fp, tsv)
+        with pytest.raises(ct.CtError) as e:
+            ct.load_case(d)
+        assert msg in str(e.value), (msg, str(e.value))
+    with pytest.raises(ct.CtError) as e:
+        ct.load_case(str(tmp_path / "missing"))
+    assert e.value.status == 9  # CT_IO_ERROR
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_case_solve_matches_reference(ct, golden, name):
+    ref = golden["case_files"][f"{name}_1"]["mg_f64"]
+    m = ct.build_case_model(ct.load_case(case_dir(name)), 40, 40, True)
+    r = ct.gpu_pcg(m, 1e-10, 50000, ct.Precond.Multigrid, ct.Precision.MG_FP64)
+    assert r.converged and abs(r.iters - ref["iters"]) <= 1
+    assert abs(r.T.max() - ref["T_max"]) <= 1e-7 * ref["T_max"]
+    assert abs(r.T.min() - ref["T_min"]) <= 1e-7 * ref["T_max"]

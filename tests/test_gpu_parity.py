@@ -268,3 +268,29 @@ def test_staged_sweeps_bitwise(ct, prec):
                 os.environ["CT_SWEEP_TMA"] = old
     assert out[0][0].iters == out[1][0].iters
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("n", [203, 96])
+def test_staged_apply_matches_row_apply(ct, n):
+    """The operator apply staged by bulk tensor copies computes the row
+    kernel's Ap bit for bit (p.Ap is summed in another order): the same
+    iteration count and temperatures to 1e-9 of Tmax."""
+    import os
+    import subprocess
+    import sys
+    code = ("import sys, numpy as np; sys.path[:0]=['.', 'cuda-thermal_gb300']; import cthermal as ct, "
+            "workloads; m=workloads.steady_hotspot(%d, seed=5); s=ct.GpuPcg(m, ct.Precond.Multigrid, "
+            "ct.Precision.MG_FP32_FLEX_DW); s.set_x_zero(); s.set_rhs_steady(); st=s.solve(1e-10, 1000); "
+            "np.save(sys.argv[1], np.concatenate([[st.iters], s.get_x()]))" % n)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = []
+    for form in ("rows", "tma"):
+        f = os.path.join(root, "gpurun_out", f"_apply_{form}_{n}.npy")
+        os.makedirs(os.path.dirname(f), exist_ok=True)
+        env = dict(os.environ, CT_APPLY=form)  # the apply form is fixed per process
+        subprocess.run([sys.executable, "-c", code, f], check=True, cwd=root, env=env, timeout=300)
+        out.append(np.load(f))
+        os.remove(f)
+    assert out[0][0] == out[1][0]
+    T0, T1 = out[0][1:], out[1][1:]
+    assert np.abs(T0 - T1).max() <= 1e-9 * np.abs(T0).max()
