@@ -219,7 +219,7 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
     // earlier forms).
     if (dw && apply_tma_fits(g0)) {
         const char* e = std::getenv("CT_APPLY");
-        if (!(e && e[0] != 't')) apply_tma = make_apply_maps(op(), pw(), dgw, &amaps);
+        if (e && e[0] == 't') apply_tma = make_apply_maps(op(), pw(), dgw, &amaps);
     }
     // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
     // (FP32 levels with at least one full tile row, above the shared-memory
