@@ -139,6 +139,8 @@ def _signatures():
         "ct_model_heat_out": (d, [gp, vp, vp, vp]),
         "ct_model_heat_stored": (d, [gp, vp, vp, vp, d]),
         "ct_model_analytic_1d": (i, [gp, lp, vp, vp, d, vp, vp]),
+        "ct_colorize": (i, [vp, i, i, C.c_float, vp, vp, dp, ip, ip]),
+        "ct_block_temps": (i, [vp, i, i, d, d, d, d, dp, dp]),
         "ct_case_load": (i, [C.c_char_p, C.POINTER(vp)]),
         "ct_case_destroy": (i, [vp]),
         "ct_case_info": (i, [vp, ip, ip, ip, dp, dp, dp, dp, dp]),
@@ -349,6 +351,28 @@ def eff_kz(k, kc, f) -> float:
 
 def eff_kxy(k, kc, f) -> float:
     return lib().ct_eff_kxy(k, kc, f)
+
+
+def layer_planes(m: Model3D, layer: int):
+    """First and last plane of a layer."""
+    ls = [l for l in range(m.nz) if m.plane_layer[l] == layer]
+    return ls[0], ls[-1]
+
+
+def write_ppm(path: str, rgba: np.ndarray) -> None:
+    """An RGBA die map as a binary PPM image, top row = largest y."""
+    ny, nx = rgba.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6 %d %d 255\n" % (nx, ny))
+        f.write(np.ascontiguousarray(rgba[::-1, :, :3]).tobytes())
+
+
+def write_tmap(path: str, m: Model3D, tmap: np.ndarray) -> None:
+    """A layer's hottest-plane map as CSV in deg C (row = y from the top,
+    column = x, 3 decimals), the tmap_layer*.csv format (src/main3d.cu:303-323)."""
+    with open(path, "w") as f:
+        for j in range(m.ny - 1, -1, -1):
+            f.write(",".join("%.3f" % (float(t) + m.T_amb) for t in tmap[j]) + "\n")
 
 
 # ---- cases (src/case3d.h) -----------------------------------------------------
@@ -580,6 +604,26 @@ class GpuPcg:
         fcp, finv = np.empty(nx * ny * nz), np.empty(nx * ny * nz)
         _check(lib().ct_level_factors(self._h, k, _ptr(fcp), _ptr(finv)))
         return fcp, finv
+
+    def colorize(self, l0, l1, rise_hi):
+        """Die map of planes l0..l1 (ct_colorize): (rgba (ny, nx, 4) uint8, the
+        per-column maximum (ny, nx) float32, hottest rise, i, j). The device
+        buffers are torch CUDA tensors."""
+        import torch
+        nx, ny = self.m.nx, self.m.ny
+        rgba = torch.empty((ny, nx, 4), dtype=torch.uint8, device="cuda")
+        mp = torch.empty((ny, nx), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        mx, i, j = C.c_double(), C.c_int(), C.c_int()
+        _check(lib().ct_colorize(self._h, int(l0), int(l1), float(rise_hi), C.c_void_p(rgba.data_ptr()),
+                                 C.c_void_p(mp.data_ptr()), C.byref(mx), C.byref(i), C.byref(j)))
+        return rgba.cpu().numpy(), mp.cpu().numpy(), mx.value, i.value, j.value
+
+    def block_temps(self, l0, l1, x0, y0, w, h):
+        tmax, tavg = C.c_double(), C.c_double()
+        _check(lib().ct_block_temps(self._h, int(l0), int(l1), float(x0), float(y0), float(w),
+                                    float(h), C.byref(tmax), C.byref(tavg)))
+        return tmax.value, tavg.value
 
     def profile_solve(self, tol, maxit):
         st = CtStats()

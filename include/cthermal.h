@@ -239,6 +239,23 @@ ct_status ct_batch_stream(const ct_batch* b, void** stream);
 ct_status ct_batch_bucket_info(const ct_batch* b, int k, int* ninst, int* depth,
                                unsigned* sweep_tiles, unsigned* restrict_tiles, int* staged);
 
+/* ---- field products on the device ------------------------------------------ */
+/* The live view's die map without a window (k_colorize, src/viewer.cu:52-87):
+ * for every column the hottest of planes l0..l1 of the current solution (K
+ * above ambient), as RGBA on the scale [0, rise_hi] (black - purple - red -
+ * orange - pale yellow) into rgba_dev (nx*ny uchar4, device, row j = y), and
+ * as float into map_dev (nx*ny, device; the tmap_layer*.csv values,
+ * src/main3d.cu:303-323, before adding the ambient); either may be NULL. The
+ * hottest column's value and position come back through the 64-bit packed
+ * key (float bits, then the cell index; the later index wins a tie). */
+ct_status ct_colorize(ct_solver* s, int l0, int l1, float rise_hi, void* rgba_dev, void* map_dev,
+                      double* max_rise, int* max_i, int* max_j);
+/* block_temps (src/main3d.cu:286-300): the maximum and the area-weighted
+ * mean of the current solution over the rectangle [x0, x0+w] x [y0, y0+h]
+ * (m) in planes l0..l1, cells covered as for_each_overlap counts them. */
+ct_status ct_block_temps(ct_solver* s, int l0, int l1, double x0, double y0, double w, double h,
+                         double* tmax, double* tavg);
+
 /* ---- per-kernel timing --------------------------------------------------- */
 typedef struct ct_kernel_time {
     char name[32];     /* kernel family, e.g. "mg_sweep_l0" */
