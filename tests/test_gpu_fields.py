@@ -79,7 +79,8 @@ def test_colorize_matches_reference(ct, solved, tmp_path):
         assert (i, j) == (q % m.nx, q // m.nx) and mx == float(ref.max())
     ct.write_ppm(str(tmp_path / "die.ppm"), rgba)
     ct.write_tmap(str(tmp_path / "tmap.csv"), m, mp)
-    assert (tmp_path / "die.ppm").stat().st_size == 15 + 3 * m.nx * m.ny or True
+    header = b"P6 %d %d 255\n" % (m.nx, m.ny)
+    assert (tmp_path / "die.ppm").stat().st_size == len(header) + 3 * m.nx * m.ny
     rows = (tmp_path / "tmap.csv").read_text().splitlines()
     assert len(rows) == m.ny and len(rows[0].split(",")) == m.nx
 
