@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "build.h"
 #include "cthermal.h"
 #include "cthermal_model.h"
 #include "status.h"
@@ -200,6 +201,46 @@ struct ct_case {
         return CT_OK;
     }
 };
+
+namespace ct {
+
+// The device build of build_case_model (src/case3d.h:158-168): planes as
+// ct_model_planes lays them out, every power block, every TSV region (when
+// wanted), copper TSV material.
+ct_status case_build(const ct_case* c, int nx, int ny, bool with_tsv, DeviceBuild* b) {
+    if (!c || !b) return fail(CT_BAD_ARG, "case build: null argument");
+    if (nx < 1 || ny < 1) return fail(CT_BAD_ARG, "case build: bad grid %d x %d", nx, ny);
+    std::vector<ct_layer> ls;
+    for (const CaseLayer& L : c->layers) ls.push_back(L.v);
+    double dz[CT_MAXZ];
+    int nz = 0;
+    const ct_status s = ct_model_planes(ls.data(), (int)ls.size(), &nz, b->plane_layer, dz);
+    if (s != CT_OK) return s;
+    b->nx = nx;
+    b->ny = ny;
+    b->nz = nz;
+    b->Lx = c->Lx;
+    b->Ly = c->Ly;
+    b->dx = c->Lx / nx;
+    b->dy = c->Ly / ny;
+    b->h_top = c->h_top;
+    b->h_bot = c->h_bot;
+    for (int l = 0; l < nz; ++l) {
+        b->planes.k[l] = ls[(size_t)b->plane_layer[l]].k;
+        b->planes.rho_c[l] = ls[(size_t)b->plane_layer[l]].rho_c;
+        b->planes.dz[l] = dz[l];
+    }
+    b->layer_planes.clear();
+    for (const ct_layer& L : ls) b->layer_planes.push_back(L.ncells);
+    b->blocks.clear();
+    b->tsvs.clear();
+    for (const CaseBlock& k : c->blocks) b->blocks.push_back(BuildRect{k.layer, k.x0, k.y0, k.w, k.h, k.watts});
+    if (with_tsv)
+        for (const CaseTsv& t : c->tsvs) b->tsvs.push_back(BuildRect{t.layer, t.x0, t.y0, t.w, t.h, t.f});
+    return CT_OK;
+}
+
+}  // namespace ct
 
 namespace {
 void copy_name(const std::string& s, char* out, int cap) {

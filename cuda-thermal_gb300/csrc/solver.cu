@@ -58,14 +58,23 @@ double ms_since(clk::time_point t) {
 
 // ---- setup ---------------------------------------------------------------
 
-ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) {
+ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec_, const DeviceBuild* build) {
+    ct_model geo{};  // the geometry when the model is built on the device
+    if (build) {
+        geo.nx = build->nx;
+        geo.ny = build->ny;
+        geo.nz = build->nz;
+        geo.dx = build->dx;
+        geo.dy = build->dy;
+    }
+    const ct_model* m = build ? &geo : m_in;
     if (!m) return fail(CT_BAD_ARG, "ct_solver_create: null model");
     if (m->nx < 1 || m->ny < 1 || m->nz < 1 || m->nz > CT_MAXZ)
         return fail(CT_BAD_ARG, "ct_solver_create: bad size %d x %d x %d (nz must be 1..%d)", m->nx,
                     m->ny, m->nz, CT_MAXZ);
-    if (!m->gE || !m->gN || !m->gU || !m->gB || !m->cap)
+    if (!build && (!m->gE || !m->gN || !m->gU || !m->gB || !m->cap))
         return fail(CT_NOT_FINALIZED, "Model3D used before finalize()");
-    if (!m->P) return fail(CT_BAD_ARG, "ct_solver_create: null power map");
+    if (!build && !m->P) return fail(CT_BAD_ARG, "ct_solver_create: null power map");
     if (!(m->dx > 0) || !(m->dy > 0)) return fail(CT_BAD_ARG, "ct_solver_create: dx, dy must be > 0");
     if (pc_ != CT_JACOBI && pc_ != CT_MULTIGRID) return fail(CT_BAD_ARG, "bad preconditioner");
     if (prec_ != CT_MG_FP64 && prec_ != CT_MG_FP32 && prec_ != CT_MG_FP32_FLEX &&
@@ -235,19 +244,26 @@ ct_status Solver::create(const ct_model* m, ct_precond pc_, ct_precision prec_) 
         }
     }
 
-    // Upload the fine operator and P through the natural staging buffer.
+    // Upload the fine operator and P through the natural staging buffer, or
+    // build them on the device (TSV fractions in r, power in the staging
+    // buffer, both natural-layout scratch at this point).
     t0 = clk::now();
-    float* natf = reinterpret_cast<float*>(nat);
-    const float* src[4] = {m->gE, m->gN, m->gU, m->cap};
-    float* dst[4] = {gE, gN, gU, cap};
-    for (int a = 0; a < 4; ++a) {
-        CT_CK(cudaMemcpyAsync(natf, src[a], ncells * 4, cudaMemcpyHostToDevice, st));
-        launch_to_split_f(st, g0, g0.nz, natf, dst[a]);
+    if (build) {
+        CT_CK(launch_build(st, *build, g0, r, nat, gE, gN, gU, gB, cap));
+        launch_to_split_d(st, g0, nat, P);
+    } else {
+        float* natf = reinterpret_cast<float*>(nat);
+        const float* src[4] = {m->gE, m->gN, m->gU, m->cap};
+        float* dst[4] = {gE, gN, gU, cap};
+        for (int a = 0; a < 4; ++a) {
+            CT_CK(cudaMemcpyAsync(natf, src[a], ncells * 4, cudaMemcpyHostToDevice, st));
+            launch_to_split_f(st, g0, g0.nz, natf, dst[a]);
+        }
+        CT_CK(cudaMemcpyAsync(natf, m->gB, (size_t)m->nx * m->ny * 4, cudaMemcpyHostToDevice, st));
+        launch_to_split_f(st, g0, 1, natf, gB);
+        CT_CK(cudaMemcpyAsync(nat, m->P, ncells * 8, cudaMemcpyHostToDevice, st));
+        launch_to_split_d(st, g0, nat, P);
     }
-    CT_CK(cudaMemcpyAsync(natf, m->gB, (size_t)m->nx * m->ny * 4, cudaMemcpyHostToDevice, st));
-    launch_to_split_f(st, g0, 1, natf, gB);
-    CT_CK(cudaMemcpyAsync(nat, m->P, ncells * 8, cudaMemcpyHostToDevice, st));
-    launch_to_split_d(st, g0, nat, P);
     for (Level& L : lv) {
         CT_CK(cudaMemcpyAsync(base + L.o_dx, L.dx.data(), L.dx.size() * 8, cudaMemcpyHostToDevice, st));
         CT_CK(cudaMemcpyAsync(base + L.o_dy, L.dy.data(), L.dy.size() * 8, cudaMemcpyHostToDevice, st));
@@ -645,6 +661,24 @@ ct_status ct_solver_create(const ct_model* m, ct_precond pc, ct_precision prec, 
     ct_solver* s = new (std::nothrow) ct_solver();
     if (!s) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
     const ct_status st = s->impl.create(m, pc, prec);
+    if (st != CT_OK) {
+        delete s;
+        return st;
+    }
+    *out = s;
+    return CT_OK;
+}
+
+ct_status ct_solver_create_case(const ct_case* c, int nx, int ny, int with_tsv, ct_precond pc,
+                                ct_precision prec, ct_solver** out) {
+    if (!out) return fail(CT_BAD_ARG, "ct_solver_create_case: null output");
+    *out = nullptr;
+    ct::DeviceBuild b;
+    ct_status st = ct::case_build(c, nx, ny, with_tsv != 0, &b);
+    if (st != CT_OK) return st;
+    ct_solver* s = new (std::nothrow) ct_solver();
+    if (!s) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
+    st = s->impl.create(nullptr, pc, prec, &b);
     if (st != CT_OK) {
         delete s;
         return st;

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "build.h"
 #include "cthermal.h"
 #include "kernels.h"
 
@@ -135,7 +136,10 @@ class Solver {
     Red red_cols(Slot sl) const { return red((int)((g0.plane + NT - 1) / NT), sl); }
     Red red_vec(Slot sl) const { return red((int)((n / 2 + NT - 1) / NT), sl); }
 
-    ct_status create(const ct_model* m, ct_precond pc_, ct_precision prec_);
+    // From host arrays (m), or built on the device from a description (b, m
+    // null): the same arrays either way.
+    ct_status create(const ct_model* m, ct_precond pc_, ct_precision prec_,
+                     const DeviceBuild* build = nullptr);
     ct_status set_dt(double dt);
     ct_status solve(double tol, int maxit, ct_stats* out);
     ct_status record_graphs();

@@ -90,6 +90,7 @@ def _signatures():
         "ct_last_setup": (i, [C.POINTER(CtSetupTimes)]),
         "ct_solver_create": (i, [C.POINTER(CtModel), i, i, C.POINTER(vp)]),
         "ct_solver_destroy": (i, [vp]),
+        "ct_solver_create_case": (i, [vp, i, i, i, i, i, C.POINTER(vp)]),
         "ct_set_dt": (i, [vp, d]),
         "ct_set_x_zero": (i, [vp]),
         "ct_set_x": (i, [vp, vp]),
@@ -502,6 +503,29 @@ class GpuPcg:
         h = C.c_void_p()
         _check(lib().ct_solver_create(C.byref(self._cm), int(pc), int(precision), C.byref(h)))
         self._h = h
+
+    @classmethod
+    def from_case(cls, folder: str, nx: int, ny: int, with_tsv: bool = True,
+                  pc=Precond.Multigrid, precision=Precision.MG_FP32_FLEX) -> "GpuPcg":
+        """A solver for a case folder with the model built on the device
+        (ct_solver_create_case): no host arrays, no upload. self.m carries the
+        geometry (planes, no arrays)."""
+        cs = load_case(folder)
+        c = C.c_void_p()
+        _check(lib().ct_case_load(os.fsencode(folder), C.byref(c)))
+        try:
+            h = C.c_void_p()
+            _check(lib().ct_solver_create_case(c, int(nx), int(ny), 1 if with_tsv else 0, int(pc),
+                                               int(precision), C.byref(h)))
+        finally:
+            lib().ct_case_destroy(c)
+        self = cls.__new__(cls)
+        self.m = build_model(cs.layers, nx, ny, cs.Lx, cs.Ly, cs.h_top, cs.h_bot)
+        self.m.T_amb = cs.T_amb
+        self._cm = None
+        self.n = self.m.ncells()
+        self._h = h
+        return self
 
     def close(self):
         if getattr(self, "_h", None):

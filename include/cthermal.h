@@ -122,6 +122,15 @@ ct_status ct_last_setup(ct_setup_times* out);
 ct_status ct_solver_create(const ct_model* m, ct_precond pc, ct_precision prec, ct_solver** out);
 /* GpuPcg::~GpuPcg (src/pcg3d_gpu.cu:495-509). */
 ct_status ct_solver_destroy(ct_solver* s);
+/* No single counterpart in the reference: build_case_model
+ * (src/case3d.h:158-168) followed by the solver's construction, with the
+ * model built on the device (power blocks, TSV regions and the face
+ * conductances computed by kernels straight into the solver's layout; the
+ * same arrays, bit for bit, as ct_model_* on the host), so a floorplan sweep
+ * pays neither the host build nor the upload. */
+typedef struct ct_case ct_case;
+ct_status ct_solver_create_case(const ct_case* c, int nx, int ny, int with_tsv, ct_precond pc,
+                                ct_precision prec, ct_solver** out);
 /* GpuPcg::set_dt (src/pcg3d_gpu.cu:511-524): 0 = steady state. */
 ct_status ct_set_dt(ct_solver* s, double dt);
 /* GpuPcg::set_x_zero (src/pcg3d_gpu.cu:526). */

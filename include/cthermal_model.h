@@ -84,7 +84,6 @@ ct_status ct_model_analytic_1d(const ct_grid* g, const ct_layer* layers, const i
  * ct_model_add_power_block for every block, ct_model_add_tsv_region for every
  * TSV region (when wanted) and ct_model_finalize, in that order
  * (build_case_model, src/case3d.h:158-168). */
-typedef struct ct_case ct_case;
 ct_status ct_case_load(const char* dir, ct_case** out);
 ct_status ct_case_destroy(ct_case* c);
 ct_status ct_case_info(const ct_case* c, int* nlayers, int* nblocks, int* ntsvs, double* Lx,

@@ -91,3 +91,26 @@ def test_case_solve_matches_reference(ct, golden, name):
     assert r.converged and abs(r.iters - ref["iters"]) <= 1
     assert abs(r.T.max() - ref["T_max"]) <= 1e-7 * ref["T_max"]
     assert abs(r.T.min() - ref["T_min"]) <= 1e-7 * ref["T_max"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("nx,ny", [(40, 40), (203, 157)])
+def test_device_built_model_matches_host_build(ct, name, nx, ny):
+    """ct_solver_create_case builds the model on the device: every fine-level
+    operator array equals the host build's bit for bit, and the two solvers
+    give the same temperatures bit for bit (so the power maps agree too)."""
+    folder = case_dir(name)
+    for with_tsv in (True, False):
+        m = ct.build_case_model(ct.load_case(folder), nx, ny, with_tsv)
+        prec = ct.Precision.MG_FP32_FLEX_DW
+        with ct.GpuPcg(m, ct.Precond.Multigrid, prec) as a, \
+                ct.GpuPcg.from_case(folder, nx, ny, with_tsv, ct.Precond.Multigrid, prec) as b:
+            oa, ob = a.level_operator(0), b.level_operator(0)
+            for k in oa:
+                assert np.array_equal(oa[k], ob[k]), (name, with_tsv, k)
+            for s in (a, b):
+                s.set_x_zero()
+                s.set_rhs_steady()
+                assert s.solve(1e-10, 1000).converged
+            assert np.array_equal(a.get_x(), b.get_x())
