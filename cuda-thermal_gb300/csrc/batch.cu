@@ -219,7 +219,7 @@ class Batch {
     }
     int small_k0(int i) const { return (int)inst(i).small_k0; }
 
-    ct_status create(int n, const ct_model* const* models);
+    ct_status create(int n, const ct_model* const* models, const DeviceBuild* builds = nullptr);
     ct_status build_bucket(Bucket& b);
     ct_status tune_bucket(Bucket& b);
     ct_status record(Bucket& b);
@@ -233,10 +233,10 @@ class Batch {
     void sweep(Bucket& b, cudaStream_t s, int d, int color, bool zero_x, bool prolong, Cond cond);
 };
 
-ct_status Batch::create(int n, const ct_model* const* models) {
+ct_status Batch::create(int n, const ct_model* const* models, const DeviceBuild* builds) {
     if (n < 1) return fail(CT_BAD_ARG, "ct_batch_create: n must be >= 1");
-    if (!models) return fail(CT_BAD_ARG, "ct_batch_create: null model list");
-    for (int i = 0; i < n; ++i)
+    if (!models && !builds) return fail(CT_BAD_ARG, "ct_batch_create: null model list");
+    for (int i = 0; models && i < n; ++i)
         if (!models[i]) return fail(CT_BAD_ARG, "ct_batch_create: null model %d", i);
     ni = n;
     if (const char* e = std::getenv("CT_RR_THRESHOLD")) rr_thr = std::atof(e);
@@ -262,7 +262,8 @@ ct_status Batch::create(int n, const ct_model* const* models) {
         s->st = st;
         s->skip_graphs = true;
         s->rr_thr = rr_thr;
-        const ct_status cs = s->create(models[i], CT_MULTIGRID, CT_MG_FP32_FLEX_DW);
+        const ct_status cs = builds ? s->create(nullptr, CT_MULTIGRID, CT_MG_FP32_FLEX_DW, &builds[i])
+                                    : s->create(models[i], CT_MULTIGRID, CT_MG_FP32_FLEX_DW);
         if (cs != CT_OK) {
             const std::string why = ct_last_error();
             return fail(cs, "ct_batch_create: instance %d: %s", i, why.c_str());
@@ -764,6 +765,28 @@ ct_status ct_batch_create(int n, const ct_model* const* models, ct_batch** out) 
     ct_batch* b = new (std::nothrow) ct_batch();
     if (!b) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
     const ct_status s = b->impl.create(n, models);
+    if (s != CT_OK) {
+        delete b;
+        return s;
+    }
+    *out = b;
+    return CT_OK;
+}
+
+ct_status ct_batch_create_cases(int n, const ct_case* const* cases, const int* nx, const int* ny,
+                                const int* with_tsv, ct_batch** out) {
+    if (!out) return fail(CT_BAD_ARG, "ct_batch_create_cases: null output");
+    *out = nullptr;
+    if (n < 1 || !cases || !nx || !ny) return fail(CT_BAD_ARG, "ct_batch_create_cases: bad arguments");
+    std::vector<ct::DeviceBuild> builds((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const ct_status s = ct::case_build(cases[i], nx[i], ny[i], with_tsv ? with_tsv[i] != 0 : true,
+                                           &builds[(size_t)i]);
+        if (s != CT_OK) return s;
+    }
+    ct_batch* b = new (std::nothrow) ct_batch();
+    if (!b) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
+    const ct_status s = b->impl.create(n, nullptr, builds.data());
     if (s != CT_OK) {
         delete b;
         return s;

@@ -267,6 +267,41 @@ ct_status ct_case_load(const char* dir, ct_case** out) {
     return CT_OK;
 }
 
+ct_status ct_case_new(const ct_layer* layers, int nlayers, double Lx, double Ly, double h_top,
+                      double h_bot, ct_case** out) {
+    if (!out || !layers || nlayers < 1) return fail(CT_BAD_ARG, "ct_case_new: bad arguments");
+    if (!(Lx > 0) || !(Ly > 0)) return fail(CT_BAD_ARG, "ct_case_new: die size must be > 0");
+    *out = nullptr;
+    ct_case* c = new (std::nothrow) ct_case();
+    if (!c) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
+    for (int k = 0; k < nlayers; ++k) c->layers.push_back(CaseLayer{"layer" + std::to_string(k), layers[k]});
+    c->Lx = Lx;
+    c->Ly = Ly;
+    c->h_top = h_top;
+    c->h_bot = h_bot;
+    *out = c;
+    return CT_OK;
+}
+
+ct_status ct_case_add_block(ct_case* c, int layer, double x0, double y0, double w, double h,
+                            double watts) {
+    if (!c || layer < 0 || layer >= (int)c->layers.size())
+        return fail(CT_BAD_ARG, "ct_case_add_block: bad case or layer");
+    if (!c->layers[(size_t)layer].v.active) return fail(CT_BAD_ARG, "ct_case_add_block: layer %d is not active", layer);
+    if (!(w > 0) || !(h > 0)) return fail(CT_BAD_ARG, "ct_case_add_block: empty block");
+    c->blocks.push_back(CaseBlock{"block" + std::to_string(c->blocks.size()), layer, x0, y0, w, h, watts});
+    return CT_OK;
+}
+
+ct_status ct_case_add_tsv(ct_case* c, int layer, double x0, double y0, double w, double h,
+                          double fraction) {
+    if (!c || layer < 0 || layer >= (int)c->layers.size())
+        return fail(CT_BAD_ARG, "ct_case_add_tsv: bad case or layer");
+    if (fraction < 0 || fraction > 1) return fail(CT_BAD_ARG, "tsv.csv: cu_fraction must be between 0 and 1");
+    c->tsvs.push_back(CaseTsv{layer, x0, y0, w, h, fraction});
+    return CT_OK;
+}
+
 ct_status ct_case_destroy(ct_case* c) {
     delete c;
     return CT_OK;

@@ -144,6 +144,10 @@ def _signatures():
         "ct_block_temps": (i, [vp, i, i, d, d, d, d, dp, dp]),
         "ct_case_load": (i, [C.c_char_p, C.POINTER(vp)]),
         "ct_case_destroy": (i, [vp]),
+        "ct_case_new": (i, [C.POINTER(CtLayer), i, d, d, d, d, C.POINTER(vp)]),
+        "ct_case_add_block": (i, [vp, i, d, d, d, d, d]),
+        "ct_case_add_tsv": (i, [vp, i, d, d, d, d, d]),
+        "ct_batch_create_cases": (i, [i, vp, vp, vp, vp, C.POINTER(vp)]),
         "ct_case_info": (i, [vp, ip, ip, ip, dp, dp, dp, dp, dp]),
         "ct_case_layer": (i, [vp, i, C.POINTER(CtLayer), C.c_char_p, i]),
         "ct_case_block": (i, [vp, i, ip, dp, dp, C.c_char_p, i]),
@@ -443,6 +447,50 @@ def load_case(folder: str) -> CaseSpec:
         lib().ct_case_destroy(h)
 
 
+class _CaseHandle:
+    """A C ct_case built from a CaseSpec (ct_case_new + blocks + TSVs)."""
+
+    def __init__(self, cs: CaseSpec):
+        arr = (CtLayer * len(cs.layers))()
+        for k, L in enumerate(cs.layers):
+            arr[k] = CtLayer(L.thickness, L.k, L.rho_c, L.ncells, 1 if L.active else 0)
+        h = C.c_void_p()
+        _check(lib().ct_case_new(arr, len(cs.layers), cs.Lx, cs.Ly, cs.h_top, cs.h_bot, C.byref(h)))
+        self.h = h
+        for b in cs.blocks:
+            _check(lib().ct_case_add_block(h, b.layer, b.x0, b.y0, b.w, b.h, b.watts))
+        for t in cs.tsvs:
+            _check(lib().ct_case_add_tsv(h, t.layer, t.x0, t.y0, t.w, t.h, t.fraction))
+
+    def close(self):
+        if self.h:
+            lib().ct_case_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def case_geometry(cs: CaseSpec, nx: int, ny: int) -> Model3D:
+    """The grid and planes of a case's model, without its arrays."""
+    m = Model3D(nx=nx, ny=ny, Lx=cs.Lx, Ly=cs.Ly, dx=cs.Lx / nx, dy=cs.Ly / ny, h_top=cs.h_top,
+                h_bot=cs.h_bot, T_amb=cs.T_amb, layers=list(cs.layers))
+    arr = (CtLayer * len(cs.layers))()
+    for k, L in enumerate(cs.layers):
+        arr[k] = CtLayer(L.thickness, L.k, L.rho_c, L.ncells, 1 if L.active else 0)
+    pl = np.zeros(MAXZ, np.int32)
+    dz = np.zeros(MAXZ)
+    nz = C.c_int(0)
+    _check(lib().ct_model_planes(arr, len(cs.layers), C.byref(nz), _ptr(pl), _ptr(dz)))
+    m.nz = nz.value
+    m.plane_layer = pl[:m.nz].copy()
+    m.dz = dz[:m.nz].copy()
+    return m
+
+
 def build_case_model(cs: CaseSpec, nx: int, ny: int, with_tsv: bool = True) -> Model3D:
     """build_case_model (src/case3d.h:158-168)."""
     m = build_model(cs.layers, nx, ny, cs.Lx, cs.Ly, cs.h_top, cs.h_bot)
@@ -522,6 +570,24 @@ class GpuPcg:
         self = cls.__new__(cls)
         self.m = build_model(cs.layers, nx, ny, cs.Lx, cs.Ly, cs.h_top, cs.h_bot)
         self.m.T_amb = cs.T_amb
+        self._cm = None
+        self.n = self.m.ncells()
+        self._h = h
+        return self
+
+    @classmethod
+    def from_spec(cls, cs: "CaseSpec", nx: int, ny: int, with_tsv: bool = True,
+                  pc=Precond.Multigrid, precision=Precision.MG_FP32_FLEX) -> "GpuPcg":
+        """A solver for a CaseSpec with the model built on the device."""
+        c = _CaseHandle(cs)
+        try:
+            h = C.c_void_p()
+            _check(lib().ct_solver_create_case(c.h, int(nx), int(ny), 1 if with_tsv else 0, int(pc),
+                                               int(precision), C.byref(h)))
+        finally:
+            c.close()
+        self = cls.__new__(cls)
+        self.m = case_geometry(cs, nx, ny)
         self._cm = None
         self.n = self.m.ncells()
         self._h = h
@@ -672,6 +738,29 @@ class GpuBatch:
         h = C.c_void_p()
         _check(lib().ct_batch_create(len(self._cms), C.cast(arr, C.c_void_p), C.byref(h)))
         self._h = h
+
+    @classmethod
+    def from_specs(cls, specs, nx, ny, with_tsv=True) -> "GpuBatch":
+        """A batch whose instance i is CaseSpec specs[i] on an nx[i] x ny[i]
+        grid, every model built on the device (ct_batch_create_cases)."""
+        n = len(specs)
+        nxs = np.ascontiguousarray(np.broadcast_to(np.asarray(nx, np.int32), (n,)))
+        nys = np.ascontiguousarray(np.broadcast_to(np.asarray(ny, np.int32), (n,)))
+        wt = np.ascontiguousarray(np.broadcast_to(np.asarray(with_tsv, np.int32), (n,)))
+        handles = [_CaseHandle(cs) for cs in specs]
+        try:
+            arr = (C.c_void_p * n)(*[hd.h.value for hd in handles])
+            h = C.c_void_p()
+            _check(lib().ct_batch_create_cases(n, C.cast(arr, C.c_void_p), _ptr(nxs), _ptr(nys), _ptr(wt),
+                                               C.byref(h)))
+        finally:
+            for hd in handles:
+                hd.close()
+        self = cls.__new__(cls)
+        self.models = [case_geometry(cs, int(nxs[i]), int(nys[i])) for i, cs in enumerate(specs)]
+        self._cms = []
+        self._h = h
+        return self
 
     def __len__(self):
         return len(self.models)

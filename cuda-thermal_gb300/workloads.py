@@ -58,10 +58,9 @@ def uniform_power(n: int) -> ct.Model3D:
     return m
 
 
-def _floorplan(m: ct.Model3D, rng, layer: int, nblocks: int, watts: float) -> None:
+def _floorplan_blocks(Lx, Ly, rng, layer: int, nblocks: int, watts: float):
     """nblocks rectangles, log-normal density (median 30 W/cm^2, sigma 0.6),
     scaled so the tier dissipates `watts`."""
-    Lx, Ly = m.Lx, m.Ly
     w = rng.uniform(0.05, 0.3, size=nblocks) * Lx
     h = rng.uniform(0.05, 0.3, size=nblocks) * Ly
     x0 = rng.uniform(0, 1, size=nblocks) * (Lx - w)
@@ -69,9 +68,13 @@ def _floorplan(m: ct.Model3D, rng, layer: int, nblocks: int, watts: float) -> No
     dens = 30e4 * np.exp(0.6 * rng.standard_normal(nblocks))  # W/m^2
     pw = dens * w * h
     pw *= watts / pw.sum()
-    for k in range(nblocks):
-        ct.add_power_block(m, layer, float(x0[k]), float(y0[k]), float(w[k]), float(h[k]),
-                           float(pw[k]))
+    return [ct.PowerBlock(f"b{k}", layer, float(x0[k]), float(y0[k]), float(w[k]), float(h[k]),
+                          float(pw[k])) for k in range(nblocks)]
+
+
+def _floorplan(m: ct.Model3D, rng, layer: int, nblocks: int, watts: float) -> None:
+    for b in _floorplan_blocks(m.Lx, m.Ly, rng, layer, nblocks, watts):
+        ct.add_power_block(m, b.layer, b.x0, b.y0, b.w, b.h, b.watts)
 
 
 def _tsv_blocks(m: ct.Model3D, rng, layer: int, coverage: float, block: int = 8) -> None:
@@ -102,6 +105,44 @@ def four_tier(n: int = 1024, seed: int = 3) -> ct.Model3D:
             _tsv_blocks(m, rng, L, 0.02)
     ct.finalize(m)
     return m
+
+
+def batch_instance_spec(rng):
+    """One stack of the batched workload as a case description and its grid
+    (the same draws as batch_instance): (CaseSpec, nx, ny)."""
+    sizes = np.arange(64, 513, 32)
+    nx, ny = int(rng.choice(sizes)), int(rng.choice(sizes))
+    target = int(rng.integers(6, 17))
+    layers = [_layer(TIM, 1, False), _layer(CU, 1, False)]
+    cells = 2
+    tiers = 0
+    while True:
+        si_cells = int(rng.integers(1, 3))
+        need = si_cells + (1 if tiers > 0 else 0)
+        if cells + need > target:
+            break
+        new = [_layer(SI, si_cells, True)]
+        if tiers > 0:
+            new.append(_layer(BOND, 1, False))
+        layers = new + layers
+        cells += need
+        tiers += 1
+    if tiers == 0:
+        layers = [_layer(SI, 1, True)] + layers
+        cells += 1
+    cu = layers[-1]
+    layers[-1] = ct.Layer(cu.name, cu.thickness, cu.k, cu.rho_c, cu.ncells + (target - cells), False)
+    Lx, Ly = 10e-3 * nx / 256, 10e-3 * ny / 256
+    cs = ct.CaseSpec(layers=layers, Lx=Lx, Ly=Ly, h_top=2e4, h_bot=0.0)
+    for L, lay in enumerate(layers):
+        if lay.active:
+            cs.blocks += _floorplan_blocks(Lx, Ly, rng, L, 12, 20.0 * (nx * ny) / 256**2)
+    return cs, nx, ny
+
+
+def batch_instance_specs(count: int = 256, seed: int = 4):
+    rng = np.random.default_rng(seed)
+    return [batch_instance_spec(rng) for _ in range(count)]
 
 
 def batch_instance(rng) -> ct.Model3D:

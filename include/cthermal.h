@@ -213,6 +213,11 @@ ct_status ct_true_relres_noalloc(const ct_model* m_dev, const double* T_dev, dou
  * mirror the single-solver calls (ct_set_power, ct_get_x, ...). */
 typedef struct ct_batch ct_batch;
 ct_status ct_batch_create(int n, const ct_model* const* models, ct_batch** out);
+/* The same with every instance's model built on the device from a case on
+ * an nx[i] x ny[i] grid (with_tsv may be NULL: all with TSVs), as
+ * ct_solver_create_case builds it. */
+ct_status ct_batch_create_cases(int n, const ct_case* const* cases, const int* nx, const int* ny,
+                                const int* with_tsv, ct_batch** out);
 ct_status ct_batch_destroy(ct_batch* b);
 ct_status ct_batch_size(const ct_batch* b, int* n);
 /* Per-instance time step (dt[i] = 0: steady); NULL: all steady. */

@@ -86,6 +86,16 @@ ct_status ct_model_analytic_1d(const ct_grid* g, const ct_layer* layers, const i
  * (build_case_model, src/case3d.h:158-168). */
 ct_status ct_case_load(const char* dir, ct_case** out);
 ct_status ct_case_destroy(ct_case* c);
+/* A case built in code (no files): layers bottom to top (named layer0,
+ * layer1, ...), die size and sink coefficients; then blocks (on active
+ * layers) and TSV regions, in m. Used for floorplan sweeps with
+ * ct_batch_create_cases. */
+ct_status ct_case_new(const ct_layer* layers, int nlayers, double Lx, double Ly, double h_top,
+                      double h_bot, ct_case** out);
+ct_status ct_case_add_block(ct_case* c, int layer, double x0, double y0, double w, double h,
+                            double watts);
+ct_status ct_case_add_tsv(ct_case* c, int layer, double x0, double y0, double w, double h,
+                          double fraction);
 ct_status ct_case_info(const ct_case* c, int* nlayers, int* nblocks, int* ntsvs, double* Lx,
                        double* Ly, double* h_top, double* h_bot, double* T_amb);
 /* Layer k (bottom to top) and its name (at most name_cap bytes with the NUL). */

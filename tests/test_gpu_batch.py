@@ -249,3 +249,23 @@ def test_batch_staged_sweeps_bitwise(ct, mixed):
     assert out[0][0] == out[1][0]
     for a, c in zip(out[0][1], out[1][1]):
         assert np.array_equal(a, c)
+
+
+def test_batch_from_device_built_specs_bitwise(ct):
+    """A batch whose models are built on the device from case descriptions
+    (ct_batch_create_cases) solves exactly as the batch of host-built models."""
+    import workloads
+    specs = workloads.batch_instance_specs(6, seed=21)
+    models = [ct.build_case_model(cs, nx, ny, False) for cs, nx, ny in specs]
+    out = []
+    for make in (lambda: ct.GpuBatch(models),
+                 lambda: ct.GpuBatch.from_specs([s[0] for s in specs], [s[1] for s in specs],
+                                                [s[2] for s in specs], False)):
+        with make() as b:
+            b.set_x_zero()
+            b.set_rhs_steady()
+            st = b.solve(1e-10, 1000)
+            out.append(([s.iters for s in st], [b.get_x(i) for i in range(len(specs))]))
+    assert out[0][0] == out[1][0]
+    for a, c in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, c)
