@@ -17,6 +17,7 @@
 // Every mbarrier wait is bounded; a wait that runs out sets ctl->err and ends
 // the solve, and the block leaves after waiting (bounded) for its own copies.
 #include <algorithm>
+#include <cstdlib>
 #include <cudaTypedefs.h>
 
 #include "batch.h"
@@ -212,6 +213,171 @@ __device__ __forceinline__ bool sweep_tiles(const SweepMaps* m, const LevelView<
     return ok;
 }
 
+// The same line solves with a producer warp: TJ consumer warps (one tile row
+// each) and one more warp whose lane 0 issues the boxes. Consumers wait on a
+// stage's `full` barrier and, when their warp is done with it, arrive on its
+// `empty` barrier; the producer refills a stage once all TJ consumer warps
+// have arrived. No block-wide barrier inside the loop, so warps drift apart
+// and cover one another's waits. A wait that runs out raises `abort`, which
+// ends every other wait.
+template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
+__device__ __forceinline__ bool sweep_tiles_ws(const SweepMaps* m, const LevelView<float>& L,
+                                               const LevelView<float>& C, int color,
+                                               const TileList& tl, float* sm, uint64_t* full,
+                                               uint64_t* empty, volatile int* abort, volatile int* issued) {
+    static_assert(TT == 32, "one consumer warp per tile row");
+    using S = Stage<TT, TJ>;
+    constexpr int stage_f = ZERO ? S::zero : S::full;
+    const Geo& g = L.g;
+    const int nz = g.nz;
+    const int tilesx = (g.hx + TT - 1) / TT;
+    const int nitems = tl.count * nz;
+    const int warp = (int)threadIdx.x / 32, lane = (int)threadIdx.x % 32;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], TJ);
+        }
+        *abort = 0;
+        *issued = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (warp == TJ) {  // producer
+        if (lane == 0) {
+            for (int w = 0; w < nitems; ++w) {
+                const int s = w % NS;
+                if (w >= NS && !mbar_wait_or_abort(&empty[s], (unsigned)(w / NS - 1) & 1u, abort)) break;
+                issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w, nz, tilesx, tl);
+                *issued = w + 1;
+            }
+        }
+    } else {  // consumers: warp = tile row
+        const int tx = lane, ty = warp;
+        const int o = ty * TT + tx;
+        int w = 0;
+        for (int mt = 0; mt < tl.count && !*abort; ++mt) {
+            const int tile = tl.tile(mt);
+            const int tyi = tile / tilesx;
+            const int t = (tile - tyi * tilesx) * TT + tx, j = tyi * TJ + ty;
+            const int e = (j + color) & 1;
+            const int i = 2 * t + e;
+            const bool act = j < g.ny && i < g.nx;
+            const bool hw = i > 0, he = i < g.nx - 1, hs = j > 0, hn = j < g.ny - 1;
+            unsigned pw = 0, pe = 0, ps = 0, pn = 0;
+            if (PRO && act) {
+                if (hw) pw = scol(C.g, (i - 1) >> 1, j >> 1);
+                if (he) pe = scol(C.g, (i + 1) >> 1, j >> 1);
+                if (hs) ps = scol(C.g, i >> 1, (j - 1) >> 1);
+                if (hn) pn = scol(C.g, i >> 1, (j + 1) >> 1);
+            }
+            float v[MZ], fcr[MZ];
+            float prev = 0.0f, gu_prev = 0.0f;
+            bool ok = true;
+#pragma unroll
+            for (int l = 0; l < MZ; ++l) {
+                if (l < nz && ok) {
+                    float cw = 0.0f, ce = 0.0f, cs = 0.0f, cn = 0.0f;
+                    if (PRO && act) {
+                        const float* cx = C.x + (unsigned)l * C.g.plane;
+                        if (hw) cw = cx[pw];
+                        if (he) ce = cx[pe];
+                        if (hs) cs = cx[ps];
+                        if (hn) cn = cx[pn];
+                    }
+                    const int s = w % NS;
+                    ok = mbar_wait_or_abort(&full[s], (unsigned)(w / NS) & 1u, abort);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (ok) {
+                        const float* st = sm + s * stage_f;
+                        if (act) {
+                            float rhs = st[o];
+                            const float fi = st[S::own + o], fc = st[2 * S::own + o], gu = st[3 * S::own + o];
+                            if (!ZERO) {
+                                const float* ox = st + 6 * S::own;
+                                const float* oge = ox + S::ox;
+                                const float* ogn = oge + S::oge;
+                                constexpr int W = S::oxw;
+                                float sl = 0.0f;  // op_lat_sum order: west, east, south, north
+                                if (hw) {
+                                    float xv = ox[(ty + 1) * W + tx + 3 + e];
+                                    if (PRO) xv = xv + cw;
+                                    sl += oge[ty * W + tx + 3 + e] * xv;
+                                }
+                                if (he) {
+                                    float xv = ox[(ty + 1) * W + tx + 4 + e];
+                                    if (PRO) xv = xv + ce;
+                                    sl += st[4 * S::own + o] * xv;
+                                }
+                                if (hs) {
+                                    float xv = ox[ty * W + tx + 4];
+                                    if (PRO) xv = xv + cs;
+                                    sl += ogn[ty * TT + tx] * xv;
+                                }
+                                if (hn) {
+                                    float xv = ox[(ty + 2) * W + tx + 4];
+                                    if (PRO) xv = xv + cn;
+                                    sl += st[5 * S::own + o] * xv;
+                                }
+                                rhs = rhs + sl;
+                            }
+                            const float lower = l > 0 ? -gu_prev : 0.0f;
+                            prev = (rhs - lower * prev) * fi;
+                            v[l] = prev;
+                            fcr[l] = fc;
+                            gu_prev = gu;
+                        }
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&empty[s]);
+                        ++w;
+                    }
+                }
+            }
+            if (!ok) break;
+            if (act) {
+#pragma unroll
+                for (int l = MZ - 2; l >= 0; --l)
+                    if (l < nz - 1) v[l] -= fcr[l] * v[l + 1];
+                const unsigned s0 = (unsigned)(2 * j + color) * (unsigned)g.hx + (unsigned)t;
+#pragma unroll
+                for (int l = 0; l < MZ; ++l)
+                    if (l < nz) L.x[(unsigned)l * g.plane + s0] = v[l];
+            }
+        }
+    }
+    __syncthreads();
+    const bool failed = *abort != 0;
+    if (failed && threadIdx.x == 0) {
+        // let this block's copies still in flight land before it leaves: the
+        // last NS items issued (bounded)
+        volatile int never = 0;
+        const int n = *issued;
+        for (int q = n - 1; q >= 0 && q >= n - NS; --q)
+            mbar_wait_or_abort(&full[q % NS], (unsigned)(q / NS) & 1u, &never);
+    }
+    return !failed;
+}
+
+// Single solver: the level's tiles spread over a persistent grid.
+template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
+__global__ void __launch_bounds__(TT * TJ + 32, 2)
+    k_sweep_tma_ws(const __grid_constant__ SweepMaps m, LevelView<float> L, LevelView<float> C,
+                   int color, Ctl* ctl, Cond cond) {
+    pdl_enter();
+    if (loop_done(ctl, cond)) return;
+    extern __shared__ __align__(128) float sm[];
+    __shared__ uint64_t full[NS], empty[NS];
+    __shared__ int flags[2];  // abort, items issued
+    const Geo& g = L.g;
+    const int ntiles = ((g.hx + TT - 1) / TT) * ((g.ny + TJ - 1) / TJ);
+    const int count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const TileList tl{(int)blockIdx.x, (int)gridDim.x, count};
+    if (!sweep_tiles_ws<TT, TJ, NS, MZ, ZERO, PRO>(&m, L, C, color, tl, sm, full, empty, &flags[0],
+                                                     &flags[1]) &&
+        threadIdx.x == 0)
+        fail_wait(ctl, cond);
+}
+
 // Single solver: the level's tiles spread over a persistent grid.
 template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(TT * TJ, 2)
@@ -253,14 +419,82 @@ __global__ void __launch_bounds__(TT * TJ, 2)
     }
 }
 
+// The batch kernel with a producer warp (sweep_tiles_ws).
+template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
+__global__ void __launch_bounds__(TT * TJ + 32, 2)
+    kb_sweep_tma_ws(Plan p, const SweepMaps* __restrict__ maps, const LevelView<float>* __restrict__ views,
+                    const LevelView<float>* __restrict__ cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
+    const Task t = p.tasks[blockIdx.x];
+    Ctl* c = &ctl[t.inst];
+    if (*(volatile const int*)&c->done) return;
+    extern __shared__ __align__(128) float sm[];
+    __shared__ uint64_t full[NS], empty[NS];
+    __shared__ int flags[2];  // abort, items issued
+    const LevelView<float> L = views[t.inst];
+    const LevelView<float> C = PRO ? cviews[t.inst] : L;
+    const TileList tl{(int)t.begin, 1, (int)(t.end - t.begin)};
+    if (!sweep_tiles_ws<TT, TJ, NS, MZ, ZERO, PRO>(&maps[t.inst], L, C, color, tl, sm, full, empty, &flags[0],
+                                                   &flags[1]) &&
+        threadIdx.x == 0) {
+        atomicExch(&c->err, 1);
+        *(volatile int*)&c->breakdown = 1;
+        if (atomicExch(&c->done, 1) == 0 && atomicSub(&bc->active, 1) == 1 && cond.use)
+            cudaGraphSetConditional(cond.h, 0u);
+    }
+}
+
 template <int TT, int TJ, int NS>
 constexpr size_t stage_bytes(bool zero_x) {
     return (size_t)NS * (zero_x ? Stage<TT, TJ>::zero : Stage<TT, TJ>::full) * sizeof(float);
 }
 
+bool sweep_ws() {
+    static const bool on = [] {
+        const char* e = std::getenv("CT_SWEEP_WS");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+template <int NS, int MZ, bool ZERO, bool PRO>
+void go_ws_ns(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L, const LevelView<float>& C,
+              int color, Ctl* ctl, Cond cond) {
+    constexpr int TT = kTileT, TJ = kTileJ;
+    auto kern = k_sweep_tma_ws<TT, TJ, NS, MZ, ZERO, PRO>;
+    static int full_wave = 0;
+    if (!full_wave) {
+        int dev = 0, sms = 0, per = 0;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)stage_bytes<TT, TJ, NS>(ZERO));
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TT * TJ + 32,
+                                                          stage_bytes<TT, TJ, NS>(ZERO)) != cudaSuccess ||
+            per < 1) {
+            cudaGetLastError();
+            per = 1;
+        }
+        full_wave = std::max(1, sms) * per;
+    }
+    const Geo& g = L.g;
+    const int ntiles = ((g.hx + TT - 1) / TT) * ((g.ny + TJ - 1) / TJ);
+    const int grid = std::max(1, std::min(ntiles, full_wave));
+    launch_pdl(kern, grid, TT * TJ + 32, stage_bytes<TT, TJ, NS>(ZERO), st, m, L, C, color, ctl, cond);
+}
+
+template <int MZ, bool ZERO, bool PRO>
+void go_ws(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L, const LevelView<float>& C,
+           int color, Ctl* ctl, Cond cond) {
+    go_ws_ns<kSweepStagesWs, MZ, ZERO, PRO>(st, m, L, C, color, ctl, cond);
+}
+
 template <int MZ, bool ZERO, bool PRO>
 void go(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L, const LevelView<float>& C,
         int color, Ctl* ctl, Cond cond) {
+    if (sweep_ws()) {
+        go_ws<MZ, ZERO, PRO>(st, m, L, C, color, ctl, cond);
+        return;
+    }
     constexpr int TT = kTileT, TJ = kTileJ, NS = kSweepStages;
     auto kern = k_sweep_tma<TT, TJ, NS, MZ, ZERO, PRO>;
     // persistent grid: SMs x resident blocks of this instantiation, at most one per tile
@@ -319,8 +553,17 @@ template <int MZ, bool ZERO, bool PRO>
 void go_b(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView<float>* views,
           const LevelView<float>* cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
     constexpr int TT = kTileT, TJ = kTileJ, NS = kSweepStages;
-    kb_sweep_tma<TT, TJ, NS, MZ, ZERO, PRO><<<p.ntasks, TT * TJ, stage_bytes<TT, TJ, NS>(ZERO), st>>>(
-        p, maps, views, cviews, color, ctl, bc, cond);
+    if (sweep_ws()) {
+        constexpr int NW = kSweepStagesWs;
+        auto kern = kb_sweep_tma_ws<TT, TJ, NW, MZ, ZERO, PRO>;
+        static const bool attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)stage_bytes<TT, TJ, NW>(ZERO)) == cudaSuccess;
+        (void)attr;
+        kern<<<p.ntasks, TT * TJ + 32, stage_bytes<TT, TJ, NW>(ZERO), st>>>(p, maps, views, cviews, color, ctl,
+                                                                            bc, cond);
+    } else
+        kb_sweep_tma<TT, TJ, NS, MZ, ZERO, PRO><<<p.ntasks, TT * TJ, stage_bytes<TT, TJ, NS>(ZERO), st>>>(
+            p, maps, views, cviews, color, ctl, bc, cond);
 }
 template <int MZ>
 void go_b_sweep(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView<float>* views,

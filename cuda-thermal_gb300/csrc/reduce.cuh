@@ -16,9 +16,13 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Block sum of (a, b); the result is valid in thread 0.
+// Block sum of (a, b) over NTH threads (at most 32 warps); the result is
+// valid in thread 0.
+template <int NTH = NT>
 __device__ __forceinline__ void block_sum2(double& a, double& b) {
-    __shared__ double sa[NT / 32], sb[NT / 32];
+    constexpr int NW = NTH / 32;
+    static_assert(NTH % 32 == 0 && NW <= 32, "whole warps, at most 32");
+    __shared__ double sa[NW], sb[NW];
     a = warp_sum(a);
     b = warp_sum(b);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -28,8 +32,8 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
     }
     __syncthreads();
     if (w == 0) {
-        a = lane < NT / 32 ? sa[lane] : 0.0;
-        b = lane < NT / 32 ? sb[lane] : 0.0;
+        a = lane < NW ? sa[lane] : 0.0;
+        b = lane < NW ? sb[lane] : 0.0;
         a = warp_sum(a);
         b = warp_sum(b);
     }
@@ -51,16 +55,18 @@ __device__ __forceinline__ bool publish2(double a, double b, double* part, int m
     return last != 0;
 }
 
-// In the last block: the grid totals, valid in thread 0. Resets the ticket.
+// In the last block (NTH threads): the grid totals, valid in thread 0.
+// Resets the ticket.
+template <int NTH = NT>
 __device__ __forceinline__ void gather2(const double* part, int maxb, unsigned* ticket, double& A,
                                         double& B) {
     __threadfence();
     double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < (int)gridDim.x; k += NT) {
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += NTH) {
         a += __ldcg(part + k);
         b += __ldcg(part + maxb + k);
     }
-    block_sum2(a, b);
+    block_sum2<NTH>(a, b);
     if (threadIdx.x == 0) {
         A = a;
         B = b;
