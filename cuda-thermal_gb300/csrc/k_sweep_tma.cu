@@ -360,7 +360,7 @@ __device__ __forceinline__ bool sweep_tiles_ws(const SweepMaps* m, const LevelVi
 
 // Single solver: the level's tiles spread over a persistent grid.
 template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
-__global__ void __launch_bounds__(TT * TJ + 32, 2)
+__global__ void __launch_bounds__(TT * TJ + 32, MZ <= 16 ? kSweepWsBlocks : 2)
     k_sweep_tma_ws(const __grid_constant__ SweepMaps m, LevelView<float> L, LevelView<float> C,
                    int color, Ctl* ctl, Cond cond) {
     pdl_enter();
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(TT * TJ, 2)
 
 // The batch kernel with a producer warp (sweep_tiles_ws).
 template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
-__global__ void __launch_bounds__(TT * TJ + 32, 2)
+__global__ void __launch_bounds__(TT * TJ + 32, MZ <= 16 ? kSweepWsBlocks : 2)
     kb_sweep_tma_ws(Plan p, const SweepMaps* __restrict__ maps, const LevelView<float>* __restrict__ views,
                     const LevelView<float>* __restrict__ cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
     const Task t = p.tasks[blockIdx.x];

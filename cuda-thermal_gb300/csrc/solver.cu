@@ -232,13 +232,18 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     }
     // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
     // (FP32 levels with at least one full tile row, above the shared-memory
-    // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernel.
+    // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernel. Levels of
+    // at most kSweepBfColumns columns stay on the grid kernel too: they sit in
+    // L2, and a tile pipeline of a few tiles per block costs more latency than
+    // it hides (CT_SWEEP_TMA_COLS sets the smallest staged level instead).
     {
         const char* e = std::getenv("CT_SWEEP_TMA");
         const bool want = mt == MG_F32 && !(e && e[0] == '0');
+        long min_cols = (long)kSweepBfColumns + 1;
+        if (const char* c = std::getenv("CT_SWEEP_TMA_COLS")) min_cols = std::atol(c);
         for (size_t k = 0; want && k < lv.size() && k < small_k0; ++k) {
             Level& L = lv[k];
-            if (!sweep_tma_fits(L.g)) continue;
+            if (!sweep_tma_fits(L.g) || (long)L.g.nx * L.g.ny < min_cols) continue;
             const LevelView<float> v = view<float>(k);
             L.tma = make_sweep_maps(v, 0, &L.maps[0]) && make_sweep_maps(v, 1, &L.maps[1]);
         }
