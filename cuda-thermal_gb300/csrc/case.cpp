@@ -11,12 +11,15 @@
 // of blanks and double quotes. Numbers are read as leading decimal prefixes
 // (as std::stod / std::stoi read them). The model is then built with the
 // library's stack builder (build_case_model, src/case3d.h:158-168).
+#include <algorithm>
+#include <cctype>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <new>
 #include <string>
 #include <vector>
@@ -251,7 +254,226 @@ void copy_name(const std::string& s, char* out, int cap) {
 
 using ct::fail;
 
+// ---- export to 3D-ICE -----------------------------------------------------------
+// export_3dice / export_3dice_layout (src/case3d.h:195-383): the case as 3D-ICE
+// 4.0 input on a uniform grid of cell_um: <outdir>/case.stk (materials, top
+// heat sink, dimensions, one layer type per plane of a passive layer, one die
+// per active layer with its single source layer, the stack listed top to
+// bottom, steady solver, Tmap/Tflp outputs per die), L<k>.flp (the blocks of
+// active layer k) and LT<k>_<p>.lay (the TSV cells of plane p of passive
+// layer k, one anisotropic material per distinct copper fraction, runs of
+// equal cells along each row as rectangles). Units: um, W/(um K),
+// J/(um^3 K), K. The number formats are the reference's, so a 3D-ICE run sees
+// the same numbers.
+namespace {
+
+double overlap_len(double a0, double a1, double b0, double b1) {
+    return std::max(0.0, std::min(a1, b1) - std::max(a0, b0));
+}
+
+// Names 3D-ICE accepts: letters and digits kept, anything else '_'.
+std::string ice_id(const std::string& s) {
+    std::string out;
+    for (char ch : s) out += std::isalnum((unsigned char)ch) ? ch : '_';
+    return out;
+}
+
+struct ExportGrid {
+    ct_grid g;
+    int plane_layer[CT_MAXZ];
+    double dz[CT_MAXZ];
+    std::vector<double> frac;  // copper fraction per cell (natural layout)
+    size_t nxy() const { return (size_t)g.nx * g.ny; }
+    double at(int l, int i, int j) const { return frac[(size_t)l * nxy() + (size_t)j * g.nx + i]; }
+    bool plane_has_tsv(int l) const {
+        for (size_t c = 0; c < nxy(); ++c)
+            if (frac[(size_t)l * nxy() + c] > 0) return true;
+        return false;
+    }
+};
+
+ct_status write_layout(const ExportGrid& m, int l, const CaseLayer& ly, double cell_um,
+                       const std::string& path) {
+    const auto key = [&](int i, int j) { return std::llround(m.at(l, i, j) * 1e9); };
+    std::map<long long, std::vector<std::string>> rects;  // fraction key -> rectangles, key order
+    char buf[192];
+    for (int j = 0; j < m.g.ny; ++j)
+        for (int i = 0; i < m.g.nx;) {
+            const long long k = key(i, j);
+            int i1 = i + 1;
+            while (i1 < m.g.nx && key(i1, j) == k) ++i1;
+            if (k != 0) {
+                std::snprintf(buf, sizeof buf, "   rectangle (%.6f, %.6f, %.6f, %.6f) ;\n", i * cell_um,
+                              j * cell_um, (i1 - i) * cell_um, cell_um);
+                rects[k].push_back(buf);
+            }
+            i = i1;
+        }
+    FILE* g = std::fopen(path.c_str(), "w");
+    if (!g) return fail(CT_IO_ERROR, "cannot write %s", path.c_str());
+    std::fprintf(g, "// %s: TSV cells, one material per copper fraction\n\n", ly.name.c_str());
+    const double tk = 400.0, trc = 3.45e6;  // copper (src/stack3d.h:60-62)
+    int n = 0;
+    for (const auto& kv : rects) {
+        const double fr = kv.first * 1e-9;
+        const double kxy = ct_eff_kxy(ly.v.k, tk, fr), kz = ct_eff_kz(ly.v.k, tk, fr);
+        std::fprintf(g,
+                     "material TSV%d :   // Cu fraction %.6f\n"
+                     "   thermal conductivity     %.10e, %.10e, %.10e ;\n"
+                     "   volumetric heat capacity %.10e ;\n\n",
+                     n++, fr, kxy * 1e-6, kxy * 1e-6, kz * 1e-6, (fr * trc + (1 - fr) * ly.v.rho_c) * 1e-18);
+    }
+    n = 0;
+    for (const auto& kv : rects) {
+        std::fprintf(g, "TSV%d :\n", n++);
+        for (const std::string& r : kv.second) std::fputs(r.c_str(), g);
+        std::fprintf(g, "\n");
+    }
+    std::fclose(g);
+    return CT_OK;
+}
+
+}  // namespace
+
 extern "C" {
+
+ct_status ct_case_export_3dice(const ct_case* c, double cell_um, const char* outdir) {
+    if (!c || !outdir) return fail(CT_BAD_ARG, "ct_case_export_3dice: null argument");
+    if (!(cell_um > 0)) return fail(CT_BAD_ARG, "ct_case_export_3dice: cell size must be > 0");
+    const std::string dir(outdir);
+    const double Lx_um = c->Lx * 1e6, Ly_um = c->Ly * 1e6;
+    if (std::fabs(Lx_um / cell_um - std::round(Lx_um / cell_um)) > 1e-9 ||
+        std::fabs(Ly_um / cell_um - std::round(Ly_um / cell_um)) > 1e-9)
+        return fail(CT_BAD_ARG, "cell size must divide the die size");
+    // the grid and its per-cell copper fractions (build_case_model with TSVs)
+    ExportGrid m;
+    std::vector<ct_layer> ls;
+    for (const CaseLayer& L : c->layers) ls.push_back(L.v);
+    int nz = 0;
+    ct_status st = ct_model_planes(ls.data(), (int)ls.size(), &nz, m.plane_layer, m.dz);
+    if (st != CT_OK) return st;
+    m.g.nx = (int)std::lround(Lx_um / cell_um);
+    m.g.ny = (int)std::lround(Ly_um / cell_um);
+    m.g.nz = nz;
+    m.g.Lx = c->Lx;
+    m.g.Ly = c->Ly;
+    m.g.dx = c->Lx / m.g.nx;
+    m.g.dy = c->Ly / m.g.ny;
+    if (m.g.nx < 1 || m.g.ny < 1) return fail(CT_BAD_ARG, "cell size must divide the die size");
+    m.frac.assign(m.nxy() * (size_t)nz, 0.0);
+    for (const CaseTsv& t : c->tsvs) {
+        st = ct_model_add_tsv_region(&m.g, m.plane_layer, t.layer, t.x0, t.y0, t.w, t.h, t.f, m.frac.data());
+        if (st != CT_OK) return st;
+    }
+    std::vector<int> first(c->layers.size(), 0);  // lowest plane of each layer
+    for (int l = nz - 1; l >= 0; --l) first[(size_t)m.plane_layer[l]] = l;
+
+    // what 3D-ICE cannot express, in the reference's order of checks
+    for (size_t L = 0; L < c->layers.size(); ++L)
+        if (c->layers[L].v.active && m.plane_has_tsv(first[L]))
+            return fail(CT_BAD_ARG,
+                        "TSVs in active layer '%s' can't be exported (3D-ICE has no material layouts in "
+                        "source layers)",
+                        c->layers[L].name.c_str());
+    if (c->h_bot > 0) return fail(CT_BAD_ARG, "a bottom heat sink is not exported");
+    for (const CaseLayer& L : c->layers)
+        if (L.v.active && L.v.ncells != 1)
+            return fail(CT_BAD_ARG, "active layer '%s' must have 1 plane for 3D-ICE", L.name.c_str());
+    for (size_t a = 0; a < c->blocks.size(); ++a)
+        for (size_t b = a + 1; b < c->blocks.size(); ++b) {
+            const CaseBlock &p = c->blocks[a], &q = c->blocks[b];
+            if (p.layer == q.layer && overlap_len(p.x0, p.x0 + p.w, q.x0, q.x0 + q.w) *
+                                              overlap_len(p.y0, p.y0 + p.h, q.y0, q.y0 + q.h) >
+                                          0)
+                return fail(CT_BAD_ARG, "power blocks '%s' and '%s' overlap (3D-ICE needs disjoint blocks)",
+                            p.name.c_str(), q.name.c_str());
+        }
+
+    FILE* f = std::fopen((dir + "/case.stk").c_str(), "w");
+    if (!f) return fail(CT_IO_ERROR, "cannot write %s/case.stk (does the folder exist?)", dir.c_str());
+    std::fprintf(f, "// 3D-ICE stack description written by ct_case_export_3dice; um, W/(um K), J/(um^3 K), K\n\n");
+    for (size_t L = 0; L < c->layers.size(); ++L)
+        std::fprintf(f,
+                     "material M%zu :   // %s\n   thermal conductivity     %.10e ;\n"
+                     "   volumetric heat capacity %.10e ;\n\n",
+                     L, c->layers[L].name.c_str(), c->layers[L].v.k * 1e-6, c->layers[L].v.rho_c * 1e-18);
+    std::fprintf(f, "top heat sink :\n   heat transfer coefficient %.10e ;\n   temperature %.4f ;\n\n",
+                 c->h_top * 1e-12, c->T_amb + 273.15);
+    std::fprintf(f,
+                 "dimensions :\n   chip length %.6f, width %.6f ;\n   cell length %.6f, width %.6f ;\n"
+                 "   non-uniform false ;\n\n",
+                 Lx_um, Ly_um, cell_um, cell_um);
+    // layer types (one per plane of each passive layer) before the dies
+    struct Item {
+        bool die;
+        size_t layer;
+        int plane;
+    };
+    std::vector<Item> stack;  // bottom to top
+    for (size_t L = 0; L < c->layers.size(); ++L) {
+        const CaseLayer& ly = c->layers[L];
+        if (ly.v.active) {
+            stack.push_back({true, L, 0});
+            continue;
+        }
+        for (int p = 0; p < ly.v.ncells; ++p) {
+            std::fprintf(f, "layer LT%zu_%d :   // %s, plane %d\n   height %.6f ;\n   material M%zu ;\n", L, p,
+                         ly.name.c_str(), p, ly.v.thickness * 1e6 / ly.v.ncells, L);
+            const int l = first[L] + p;
+            if (m.plane_has_tsv(l)) {
+                const std::string lay = "LT" + std::to_string(L) + "_" + std::to_string(p) + ".lay";
+                st = write_layout(m, l, ly, cell_um, dir + "/" + lay);
+                if (st != CT_OK) {
+                    std::fclose(f);
+                    return st;
+                }
+                std::fprintf(f, "   layout \"./%s\" ;\n", lay.c_str());
+            }
+            std::fprintf(f, "\n");
+            stack.push_back({false, L, p});
+        }
+    }
+    for (size_t L = 0; L < c->layers.size(); ++L)
+        if (c->layers[L].v.active)
+            std::fprintf(f, "die DIE%zu :   // %s\n   source %.6f M%zu ;\n\n", L, c->layers[L].name.c_str(),
+                         c->layers[L].v.thickness * 1e6, L);
+    std::fprintf(f, "stack:\n");
+    for (size_t e = stack.size(); e-- > 0;) {  // top to bottom
+        const Item& it = stack[e];
+        if (it.die)
+            std::fprintf(f, "   die   D%zu DIE%zu floorplan \"./L%zu.flp\" ;\n", it.layer, it.layer, it.layer);
+        else
+            std::fprintf(f, "   layer P%zu_%d LT%zu_%d ;\n", it.layer, it.plane, it.layer, it.plane);
+    }
+    std::fprintf(f, "\nsolver:\n   steady ;\n   initial temperature %.4f ;\n   numofcores 1 ;\n\noutput:\n",
+                 c->T_amb + 273.15);
+    for (size_t L = 0; L < c->layers.size(); ++L) {
+        if (!c->layers[L].v.active) continue;
+        std::fprintf(f, "   Tmap ( D%zu, \"tmap_L%zu.txt\", final ) ;\n", L, L);
+        std::fprintf(f, "   Tflp ( D%zu, \"tflp_max_L%zu.txt\", maximum, final ) ;\n", L, L);
+        std::fprintf(f, "   Tflp ( D%zu, \"tflp_avg_L%zu.txt\", average, final ) ;\n", L, L);
+    }
+    std::fclose(f);
+
+    for (size_t L = 0; L < c->layers.size(); ++L) {
+        if (!c->layers[L].v.active) continue;
+        const std::string path = dir + "/L" + std::to_string(L) + ".flp";
+        FILE* g = std::fopen(path.c_str(), "w");
+        if (!g) return fail(CT_IO_ERROR, "cannot write %s", path.c_str());
+        int count = 0;
+        for (const CaseBlock& b : c->blocks) {
+            if ((size_t)b.layer != L) continue;
+            std::fprintf(g, "%s :\n   position %.6f, %.6f ;\n   dimension %.6f, %.6f ;\n   power values %.10e ;\n\n",
+                         ice_id(b.name).c_str(), b.x0 * 1e6, b.y0 * 1e6, b.w * 1e6, b.h * 1e6, b.watts);
+            ++count;
+        }
+        if (count == 0)  // a die needs at least one floorplan element
+            std::fprintf(g, "none :\n   position 0, 0 ;\n   dimension %.6f, %.6f ;\n   power values 0 ;\n\n", Lx_um,
+                         Ly_um);
+        std::fclose(g);
+    }
+    return CT_OK;
+}
 
 ct_status ct_case_load(const char* dir, ct_case** out) {
     if (!dir || !out) return fail(CT_BAD_ARG, "ct_case_load: null argument");

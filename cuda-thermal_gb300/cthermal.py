@@ -152,6 +152,7 @@ def _signatures():
         "ct_case_layer": (i, [vp, i, C.POINTER(CtLayer), C.c_char_p, i]),
         "ct_case_block": (i, [vp, i, ip, dp, dp, C.c_char_p, i]),
         "ct_case_tsv": (i, [vp, i, ip, dp, dp]),
+        "ct_case_export_3dice": (i, [vp, C.c_double, C.c_char_p]),
         "ct_eff_kz": (d, [d, d, d]),
         "ct_eff_kxy": (d, [d, d, d]),
     }
@@ -445,6 +446,33 @@ def load_case(folder: str) -> CaseSpec:
         return cs
     finally:
         lib().ct_case_destroy(h)
+
+
+def export_3dice(folder: str, cell_um: float, outdir: str) -> None:
+    """export_3dice (src/case3d.h:266-383) of the case in `folder` on a grid of
+    cell_um micrometres: case.stk, L<k>.flp and LT<k>_<p>.lay in the existing
+    folder outdir (3D-ICE 4.0 input). Raises CtError with the reference's
+    message when 3D-ICE cannot express the case."""
+    h = C.c_void_p()
+    _check(lib().ct_case_load(os.fsencode(folder), C.byref(h)))
+    try:
+        _check(lib().ct_case_export_3dice(h, float(cell_um), os.fsencode(outdir)))
+    finally:
+        lib().ct_case_destroy(h)
+
+
+def read_3dice_tmap(path: str) -> np.ndarray:
+    """read_3dice_tmap (src/case3d.h:386-401): a 3D-ICE Tmap text file ('%'
+    lines are comments) as a 2-D array, one row per line."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if not line.strip() or line.startswith("%"):
+                continue
+            vals = [float(v) for v in line.split()]
+            if vals:
+                rows.append(vals)
+    return np.array(rows)
 
 
 class _CaseHandle:
@@ -952,6 +980,17 @@ class TransientResult:
     ms: float = 0.0
     solve_ms: float = 0.0
     converged: bool = True
+
+
+def write_transient_csv(path: str, steps: List["StepRecord"], T_amb: float) -> None:
+    """The transient log of the reference driver (src/main3d.cu:549-557): one
+    row per step, t and dt in s, PCG iterations, hottest cell in C, heat out
+    and heat stored in W."""
+    with open(path, "w") as f:
+        f.write("t_s,dt_s,pcg_iters,T_max_C,heat_out_W,heat_stored_W\n")
+        for r in steps:
+            f.write("%.6e,%.6e,%d,%.6f,%.6f,%.6f\n" % (r.t, r.dt, r.iters, r.T_max + T_amb, r.q_out,
+                                                      r.q_stored))
 
 
 def run_transient(m: Model3D, o: TransientOptions = TransientOptions(),

@@ -106,6 +106,16 @@ ct_status ct_case_block(const ct_case* c, int k, int* layer, double* rect, doubl
 /* TSV region k: layer index, rect in m, copper fraction. */
 ct_status ct_case_tsv(const ct_case* c, int k, int* layer, double* rect, double* fraction);
 
+/* export_3dice (src/case3d.h:266-383): the case as 3D-ICE 4.0 input on a
+ * uniform grid of cell_um micrometres, written into the existing folder
+ * outdir: case.stk, L<k>.flp for every active layer k, LT<k>_<p>.lay for every
+ * TSV-carrying plane p of a passive layer k. CT_BAD_ARG (with the reference's
+ * message) when the cell size does not divide the die, TSVs sit in an active
+ * layer, there is a bottom heat sink, an active layer has more than one plane
+ * or two blocks of one layer overlap; CT_IO_ERROR when a file cannot be
+ * written. Host only. */
+ct_status ct_case_export_3dice(const ct_case* c, double cell_um, const char* outdir);
+
 /* eff_kz, eff_kxy (src/stack3d.h:104-108). */
 double ct_eff_kz(double k, double kc, double f);
 double ct_eff_kxy(double k, double kc, double f);

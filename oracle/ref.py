@@ -63,6 +63,8 @@ def lib(mg_double: bool):
                                 C.c_int, C.POINTER(RefTsv), C.c_int]
     L.ref_case_model.restype = vp
     L.ref_case_model.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_int]
+    L.ref_export_3dice.restype = C.c_int
+    L.ref_export_3dice.argtypes = [C.c_char_p, C.c_double, C.c_char_p, C.c_char_p, C.c_int]
     L.ref_example_case_model.restype = vp
     L.ref_example_case_model.argtypes = [C.c_int, C.c_int, C.c_int]
     L.ref_model_free.argtypes = [vp]
@@ -154,6 +156,15 @@ def case_model(folder, nx, ny, with_tsv=True, mg_double=True) -> RefModel:
     if not h:
         raise RuntimeError(err.value.decode())
     return _wrap(L, h, mg_double)
+
+
+def export_3dice(folder, cell_um, outdir):
+    """The reference's export_3dice of a case folder into outdir; None on
+    success, else its error message."""
+    L = lib(False)
+    err = C.create_string_buffer(512)
+    ok = L.ref_export_3dice(folder.encode(), float(cell_um), outdir.encode(), err, 512)
+    return None if ok else err.value.decode()
 
 
 def example_case_model(nx, ny, with_tsv=True, mg_double=True) -> RefModel:

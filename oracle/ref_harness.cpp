@@ -8,6 +8,7 @@
 // the order the caller lists: power operations first, then TSV regions, then
 // finalize(), as build_case_model (src/case3d.h:158-166) does.
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -180,6 +181,18 @@ int ref_run_transient(void* h, int precond, double dt0, double growth, double dt
     *total_iters = r.total_iters;
     *all_converged = r.converged ? 1 : 0;
     return (int)r.steps.size();
+}
+
+// export_3dice (src/case3d.h:266-383) of the case folder on a grid of cell_um:
+// 1 on success, else 0 with the reference's message in err.
+int ref_export_3dice(const char* folder, double cell_um, const char* outdir, char* err, int errcap) {
+    CaseSpec cs;
+    std::string e;
+    if (!load_case(folder, cs, e) || !export_3dice(cs, cell_um, outdir, e)) {
+        std::snprintf(err, (size_t)errcap, "%s", e.c_str());
+        return 0;
+    }
+    return 1;
 }
 
 }  // extern "C"

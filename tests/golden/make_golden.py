@@ -3,7 +3,8 @@ reference CPU solver (oracle/_ref, compiled from the reference sources by
 `make -C oracle ref`).
 
 Run where the reference sources are present:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          (everything)
+    python tests/golden/make_golden.py export   (the 3D-ICE export fixtures only)
 The fixtures pin both the C oracle (bit-for-bit: the same T bytes, iteration
 counts and residuals) and the library's model builder (bit-for-bit arrays).
 Large arrays are stored as SHA-256 digests of their little-endian bytes;
@@ -87,7 +88,67 @@ def copy_cases():
                 shutil.copyfile(os.path.join(src_root, case, f), os.path.join(dst, f))
 
 
+EXPORT_CELLS = (100.0, 250.0, 333.0)  # um; 333 does not divide the 10 mm die
+
+
+def export_variants():
+    """Case folders the 3D-ICE export must refuse, each made from
+    validate_3dice by one edit: tests/golden/cases_export/<variant>/."""
+    src = os.path.join(HERE, "cases", "validate_3dice")
+    stack = open(os.path.join(src, "stack.csv")).read()
+    plan = open(os.path.join(src, "floorplan.csv")).read()
+    variants = {
+        "bottom_sink": (stack.replace("# h_bottom, 0", "# h_bottom, 500"), plan),
+        "two_plane_die": (stack.replace("Si tier 1 (top), 50, 130, 1.66e6, 1, 1",
+                                        "Si tier 1 (top), 50, 130, 1.66e6, 2, 1"), plan),
+        "overlapping_blocks": (stack, plan + "hot_overlap, Si tier 2 (bottom), 1.5, 1.5, 1.0, 1.0, 1\n"),
+        "empty_die": (stack, "\n".join(l for l in plan.splitlines() if "Si tier 1" not in l) + "\n"),
+    }
+    names = []
+    for name, (st, fp) in variants.items():
+        assert st != stack or fp != plan, name
+        d = os.path.join(HERE, "cases_export", name)
+        os.makedirs(d, exist_ok=True)
+        with open(os.path.join(d, "stack.csv"), "w") as f:
+            f.write(st)
+        with open(os.path.join(d, "floorplan.csv"), "w") as f:
+            f.write(fp)
+        names.append(name)
+    return names
+
+
+def export_golden():
+    """The reference's 3D-ICE export of every case folder (and of the
+    variants above) at a few cell sizes: tests/golden/export3dice/<case>_<cell>/
+    holds the files it wrote, and index.json lists them (or the error message
+    when it refused)."""
+    import shutil
+    root = os.path.join(HERE, "export3dice")
+    index = {}
+    folders = [(c, os.path.join("cases", c)) for c in CASES]
+    folders += [(v, os.path.join("cases_export", v)) for v in export_variants()]
+    for case, rel in folders:
+        for cell in EXPORT_CELLS:
+            key = f"{case}_{int(cell)}"
+            d = os.path.join(root, key)
+            shutil.rmtree(d, ignore_errors=True)
+            os.makedirs(d)
+            err = ref.export_3dice(os.path.join(HERE, rel), cell, d)
+            if err is not None:
+                shutil.rmtree(d)
+                index[key] = dict(folder=rel, cell_um=cell, error=err)
+            else:
+                index[key] = dict(folder=rel, cell_um=cell, files=sorted(os.listdir(d)))
+            print("export", key, index[key].get("error", index[key].get("files")))
+    with open(os.path.join(root, "index.json"), "w") as f:
+        json.dump(index, f, indent=1)
+
+
 def main():
+    if sys.argv[1:] == ["export"]:
+        ref.lib(False)
+        export_golden()
+        return
     for mgd in (False, True):
         ref.lib(mgd)
     out = {"generator": "tests/golden/make_golden.py", "reference": "cuda-thermal src/pcg3d_cpu.cpp",
@@ -147,6 +208,7 @@ def main():
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1)
     np.savez_compressed(os.path.join(HERE, "golden_arrays.npz"), **arrays)
+    export_golden()
 
 
 if __name__ == "__main__":

@@ -114,3 +114,63 @@ def test_device_built_model_matches_host_build(ct, name, nx, ny):
                 s.set_rhs_steady()
                 assert s.solve(1e-10, 1000).converged
             assert np.array_equal(a.get_x(), b.get_x())
+
+
+def _export_index():
+    import json
+    with open(os.path.join(GOLDEN_DIR, "export3dice", "index.json")) as f:
+        return json.load(f)
+
+
+def _content_lines(path):
+    """A 3D-ICE file's lines with the // comments and trailing blanks removed
+    (the comments are free text; everything else is what 3D-ICE reads)."""
+    out = []
+    with open(path) as f:
+        for line in f:
+            k = line.find("//")
+            if k >= 0:
+                line = line[:k]
+            out.append(line.rstrip())
+    return out
+
+
+@pytest.mark.parametrize("key", sorted(_export_index()))
+def test_export_3dice_matches_reference(ct, key, tmp_path):
+    """export_3dice (src/case3d.h:266-383) against the reference's own export
+    of the same case folder and cell size: the same files with the same
+    contents line for line (comments aside), or the same refusal message."""
+    rec = _export_index()[key]
+    folder = os.path.join(GOLDEN_DIR, rec["folder"])
+    if "error" in rec:
+        with pytest.raises(ct.CtError) as e:
+            ct.export_3dice(folder, rec["cell_um"], str(tmp_path))
+        assert e.value.status == 5  # CT_BAD_ARG
+        assert str(e.value).endswith(rec["error"])
+        return
+    ct.export_3dice(folder, rec["cell_um"], str(tmp_path))
+    assert sorted(os.listdir(tmp_path)) == rec["files"]
+    for name in rec["files"]:
+        want = _content_lines(os.path.join(GOLDEN_DIR, "export3dice", key, name))
+        got = _content_lines(os.path.join(str(tmp_path), name))
+        assert got == want, name
+
+
+def test_export_3dice_io_error(ct, tmp_path):
+    with pytest.raises(ct.CtError) as e:
+        ct.export_3dice(case_dir("validate_3dice"), 100.0, str(tmp_path / "missing"))
+    assert e.value.status == 9  # CT_IO_ERROR
+
+
+def test_read_3dice_tmap_and_transient_csv(ct, tmp_path):
+    p = tmp_path / "tmap.txt"
+    p.write_text("% 3D-ICE Tmap\n% rows\n300.5 301.25\n\n302 303.5\n")
+    T = ct.read_3dice_tmap(str(p))
+    assert T.shape == (2, 2) and T[1, 1] == 303.5
+    steps = [ct.StepRecord(1e-5, 1e-5, 7, 1.25, 10.0, 40.0), ct.StepRecord(2.1e-5, 1.1e-5, 6, 2.5, 11.0, 39.0)]
+    f = tmp_path / "transient.csv"
+    ct.write_transient_csv(str(f), steps, 25.0)
+    lines = f.read_text().splitlines()
+    assert lines[0] == "t_s,dt_s,pcg_iters,T_max_C,heat_out_W,heat_stored_W"
+    assert lines[1] == "1.000000e-05,1.000000e-05,7,26.250000,10.000000,40.000000"
+    assert lines[2] == "2.100000e-05,1.100000e-05,6,27.500000,11.000000,39.000000"
