@@ -107,6 +107,59 @@ __global__ void __launch_bounds__(NT)
     restrict_cell<T, false>(F, C, (T)ctl->inv_dt, q, (int)blockIdx.y);
 }
 
+// Restriction F -> C fused with C's first sweep (x = 0, red columns). A
+// block is 32 coarse columns x nz planes, one thread per coarse cell as in
+// k_restrict; each thread also stages its cell's b and, for a red column,
+// the cell's Thomas factors and up face in shared memory. After one block
+// barrier, one thread per red column runs sweep_column<ZERO>'s recurrence on
+// them (same operations, same order) and writes the column's x.
+template <class T, int MZ>
+__global__ void __launch_bounds__(32 * MZ)
+    k_restrict_sweep0(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
+    pdl_enter();
+    if (loop_done(ctl, cond)) return;
+    __shared__ T sb[MZ][32], sfi[MZ][32], sfc[MZ][32];
+    __shared__ float sgu[MZ][32];
+    const Geo& cg = C.g;
+    const unsigned q = blockIdx.x * 32u + threadIdx.x;
+    const int l = (int)threadIdx.y;
+    const bool on = q < (unsigned)cg.nx * (unsigned)cg.ny;
+    const int J = on ? (int)(q / (unsigned)cg.nx) : 0, I = on ? (int)(q - (unsigned)J * cg.nx) : 0;
+    const bool red = on && ((I + J) & 1) == 0;
+    const unsigned cs = scol(cg, I, J);
+    if (on) {
+        const unsigned id = (unsigned)l * cg.plane + cs;
+        const T sum = restrict_sum<T, false>(F, (T)ctl->inv_dt, I, J, l);
+        C.b[id] = sum;
+        if (red) {
+            sb[l][threadIdx.x] = sum;
+            sfi[l][threadIdx.x] = C.finv[id];
+            sfc[l][threadIdx.x] = C.fcp[id];
+            sgu[l][threadIdx.x] = C.gU[id];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.y != 0 || !red) return;
+    const int nz = cg.nz;
+    T v[MZ], fcr[MZ];
+    T prev = 0;
+#pragma unroll
+    for (int k = 0; k < MZ; ++k) {
+        if (k < nz) {
+            const T lower = k > 0 ? -(T)sgu[k - 1][threadIdx.x] : T(0);
+            prev = (sb[k][threadIdx.x] - lower * prev) * sfi[k][threadIdx.x];
+            v[k] = prev;
+            fcr[k] = sfc[k][threadIdx.x];
+        }
+    }
+#pragma unroll
+    for (int k = MZ - 2; k >= 0; --k)
+        if (k < nz - 1) v[k] -= fcr[k] * v[k + 1];
+#pragma unroll
+    for (int k = 0; k < MZ; ++k)
+        if (k < nz) C.x[(unsigned)k * cg.plane + cs] = v[k];
+}
+
 // The V-cycle below level k0 (all levels from k0 to the single column) in ONE
 // launch of one thread-block cluster: the phases (sweeps, restrictions, the
 // coarsest solve, prolongation-sweeps back up) are separated by cluster
@@ -234,6 +287,23 @@ void launch_restrict(cudaStream_t st, const LevelView<T>& F, const LevelView<T>&
 }
 
 template <class T>
+bool launch_restrict_sweep0(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,
+                            Cond cond) {
+    const int nz = F.g.nz;
+    const unsigned grid = ((unsigned)C.g.nx * C.g.ny + 31u) / 32u;
+    const dim3 block(32, (unsigned)nz);
+    if (nz <= 8)
+        launch_pdl(k_restrict_sweep0<T, 8>, grid, block, 0, st, F, C, ctl, cond);
+    else if (nz <= 16)
+        launch_pdl(k_restrict_sweep0<T, 16>, grid, block, 0, st, F, C, ctl, cond);
+    else if (nz <= 32)
+        launch_pdl(k_restrict_sweep0<T, 32>, grid, block, 0, st, F, C, ctl, cond);
+    else
+        return false;
+    return true;
+}
+
+template <class T>
 int tail_cluster_size() {
     // Largest cluster this GPU can co-schedule for the tail kernel (16 needs
     // the non-portable opt-in; 8 is portable).
@@ -305,6 +375,10 @@ template void launch_restrict<float>(cudaStream_t, const LevelView<float>&,
                                      const LevelView<float>&, const Ctl*, Cond);
 template void launch_restrict<double>(cudaStream_t, const LevelView<double>&,
                                       const LevelView<double>&, const Ctl*, Cond);
+template bool launch_restrict_sweep0<float>(cudaStream_t, const LevelView<float>&, const LevelView<float>&,
+                                            const Ctl*, Cond);
+template bool launch_restrict_sweep0<double>(cudaStream_t, const LevelView<double>&, const LevelView<double>&,
+                                             const Ctl*, Cond);
 template int tail_cluster_size<float>();
 template int tail_cluster_size<double>();
 template cudaError_t launch_vtail<float>(cudaStream_t, const TailLevels<float>&, int, const Ctl*,

@@ -186,6 +186,12 @@ template <class T>
 void launch_restrict(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,
                      Cond cond);
 
+// The restriction F -> C fused with C's first sweep (x = 0, red columns).
+// false (nothing launched) for columns deeper than 32 planes.
+template <class T>
+bool launch_restrict_sweep0(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,
+                            Cond cond);
+
 // The levels below a threshold, run by one thread-block cluster in one launch.
 constexpr int kMaxTail = 24;
 constexpr int kTailThreads = 512;

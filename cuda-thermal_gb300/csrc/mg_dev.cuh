@@ -244,19 +244,25 @@ __device__ __forceinline__ T residual_at(const LevelView<T>& F, T inv_dt, int i,
     return ldm<CG>(F.b + id) - (d * xc - off);
 }
 
-// Restriction (src/pcg3d_cpu.cpp:87-100) of coarse cell (I, J, l), q = J cnx + I:
-// the sum over the (up to 4) children, j then i, of the fine residual.
+// Restriction (src/pcg3d_cpu.cpp:87-100) of coarse cell (I, J, l): the sum
+// over the (up to 4) children, j then i, of the fine residual.
 template <class T, bool CG>
-__device__ __forceinline__ void restrict_cell(const LevelView<T>& F, const LevelView<T>& C,
-                                              T inv_dt, unsigned q, int l) {
+__device__ __forceinline__ T restrict_sum(const LevelView<T>& F, T inv_dt, int I, int J, int l) {
     const Geo& fg = F.g;
-    const Geo& cg = C.g;
-    const int J = (int)(q / (unsigned)cg.nx), I = (int)(q - (unsigned)J * cg.nx);
     const int i1 = min(2 * I + 2, fg.nx), j1 = min(2 * J + 2, fg.ny);
     T sum = 0;
     for (int j = 2 * J; j < j1; ++j)
         for (int i = 2 * I; i < i1; ++i) sum += residual_at<T, CG>(F, inv_dt, i, j, l);
-    C.b[(unsigned)l * cg.plane + scol(cg, I, J)] = sum;
+    return sum;
+}
+
+// The same stored as coarse b; q = J cnx + I.
+template <class T, bool CG>
+__device__ __forceinline__ void restrict_cell(const LevelView<T>& F, const LevelView<T>& C,
+                                              T inv_dt, unsigned q, int l) {
+    const Geo& cg = C.g;
+    const int J = (int)(q / (unsigned)cg.nx), I = (int)(q - (unsigned)J * cg.nx);
+    C.b[(unsigned)l * cg.plane + scol(cg, I, J)] = restrict_sum<T, CG>(F, inv_dt, I, J, l);
 }
 
 

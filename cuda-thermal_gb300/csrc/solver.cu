@@ -230,6 +230,9 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
         const char* e = std::getenv("CT_APPLY");
         if (e && e[0] == 't') apply_tma = make_apply_maps(op(), pw(), dgw, &amaps);
     }
+    // CT_FUSE_SWEEP0=0 keeps each level's first sweep a launch of its own
+    // instead of riding along with the restriction into that level.
+    if (const char* e = std::getenv("CT_FUSE_SWEEP0")) fuse_sweep0 = e[0] != '0';
     // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
     // (FP32 levels with at least one full tile row, above the shared-memory
     // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernel. Levels of
@@ -340,7 +343,7 @@ void Solver::sweep(size_t k, const LevelView<T>& L, int color, bool zero_x, cons
 }
 
 template <class T>
-void Solver::vcycle(size_t k, Cond cond) {
+void Solver::vcycle(size_t k, Cond cond, bool first_sweep_done) {
     if (k == small_k0) {
         TailLevels<T> tl;
         tl.n = (int)(lv.size() - k);
@@ -377,15 +380,28 @@ void Solver::vcycle(size_t k, Cond cond) {
     const double b_zero = cells / 2 * (4 * t + 4);
     const double b_sweep = cells / 2 * (4 * t + 12) + cells / 2 * (t + 8);
     if (k + 1 == lv.size()) {
-        enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
+        if (!first_sweep_done)
+            enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
         return;
     }
     const LevelView<T> C = view<T>(k + 1);
-    enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
+    if (!first_sweep_done)
+        enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
     enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { sweep<T>(k, L, 1, false, nullptr, cond); });
-    enq(("mg_restrict" + lvl).c_str(), cells * (2 * t + 16) + cells / 4 * t,
-        [&] { launch_restrict<T>(cs, L, C, ctl, cond); });
-    vcycle<T>(k + 1, cond);
+    // The coarse level's first sweep rides along with the restriction unless
+    // a whole-tail kernel (shared-memory bottom, cluster tail) starts there,
+    // or the restriction is from the finest level: there it is bandwidth
+    // bound, and the block's serial line-solve tail costs more (measured at
+    // 800 x 800: 78 us fused against 51 + 13 us) than the launch it saves.
+    const bool fuse = fuse_sweep0 && k > 0 && k + 1 != small_k0 && k + 1 != tail_k0 && L.g.nz <= 32;
+    const double b_restrict = cells * (2 * t + 16) + cells / 4 * t;
+    const double cc = (double)C.g.nx * C.g.ny * C.g.nz;
+    if (fuse)
+        enq(("mg_restrict_sweep0" + lvl).c_str(), b_restrict + cc / 2 * (3 * t + 4),
+            [&] { launch_restrict_sweep0<T>(cs, L, C, ctl, cond); });
+    else
+        enq(("mg_restrict" + lvl).c_str(), b_restrict, [&] { launch_restrict<T>(cs, L, C, ctl, cond); });
+    vcycle<T>(k + 1, cond, fuse);
     enq(("mg_sweep" + lvl).c_str(), b_sweep + cells / 4 * t,
         [&] { sweep<T>(k, L, 1, false, &C, cond); });
     enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { sweep<T>(k, L, 0, false, nullptr, cond); });

@@ -82,6 +82,7 @@ class Solver {
     bool have_cond = false;
     size_t tail_k0 = 0;    // levels from tail_k0 down run in one cluster launch
     size_t small_k0 = 0;   // levels from small_k0 down run in one block from shared memory
+    bool fuse_sweep0 = true;  // a level's first (x = 0) sweep rides with the restriction into it
     int tail_cluster = 1;  // CTAs in that cluster
     cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
     ct_setup_times times{};
@@ -175,7 +176,7 @@ class Solver {
         return x;
     }
     template <class T>
-    void vcycle(size_t k, Cond cond);
+    void vcycle(size_t k, Cond cond, bool first_sweep_done = false);
     // One sweep of level k (the staged kernel where the level has its maps).
     template <class T>
     void sweep(size_t k, const LevelView<T>& L, int color, bool zero_x, const LevelView<T>* coarse,

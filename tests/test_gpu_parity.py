@@ -317,3 +317,38 @@ def test_producer_warp_sweeps_bitwise(ct, n, prec, tmp_path):
         subprocess.run([sys.executable, "-c", code, f], check=True, cwd=root, env=env, timeout=300)
         out.append(np.load(f))
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
+@pytest.mark.parametrize("n", [203, 130, 37])
+def test_fused_first_sweep_bitwise(ct, n, prec):
+    """Each level's first (x = 0) sweep run inside the restriction into that
+    level (the default) gives the separate launches' results bit for bit:
+    steady solve, then two backward-Euler steps."""
+    import os
+    import workloads
+    m = workloads.steady_hotspot(n, seed=13)
+    out = []
+    for flag in ("0", "1"):
+        old = os.environ.get("CT_FUSE_SWEEP0")
+        os.environ["CT_FUSE_SWEEP0"] = flag  # read when the solver is created
+        try:
+            with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
+                s.set_x_zero()
+                s.set_rhs_steady()
+                res = [s.solve(1e-10, 1000).iters, s.get_x()]
+                s.set_dt(1e-3)
+                for _ in range(2):
+                    s.set_rhs_transient()
+                    res += [s.solve(1e-9, 1000).iters, s.get_x()]
+                out.append(res)
+        finally:
+            if old is None:
+                os.environ.pop("CT_FUSE_SWEEP0", None)
+            else:
+                os.environ["CT_FUSE_SWEEP0"] = old
+    for a, b in zip(out[0], out[1]):
+        if isinstance(a, np.ndarray):
+            assert np.array_equal(a, b)
+        else:
+            assert a == b
