@@ -5,6 +5,7 @@
 // Each kernel is the batched form of a single-solver kernel and uses the same
 // per-column / per-cell device code (dw_dev.cuh, mg_dev.cuh), so one instance
 // of a batch computes what a single solver computes for it.
+#include <cstdlib>
 #include <algorithm>
 #include <cmath>
 
@@ -186,6 +187,7 @@ __global__ void __launch_bounds__(NT)
 
 // Ap = d p - sum G p_nbr over rows [begin, end) of the instance (one warp
 // per row of one colour of one plane, apply_row), p.Ap, alpha.
+template <int U>
 __global__ void __launch_bounds__(NT)
     kb_apply(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
     const Task t = p.tasks[blockIdx.x];
@@ -197,13 +199,17 @@ __global__ void __launch_bounds__(NT)
     float2* __restrict__ Ap = bi[t.inst].Ap;
     const int lane = (int)(threadIdx.x & 31u);
     DwAcc pacc = {0.0f, 0.0f};
-    for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32)
-        apply_row_seq(o, dgw, pv, Ap, R, lane, pacc);
+    for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32) {
+        if constexpr (U == 0)
+            apply_row_seq(o, dgw, pv, Ap, R, lane, pacc);
+        else
+            apply_row<U>(o, dgw, pv, Ap, R, lane, pacc);
+    }
     double pap = (double)pacc.s + (double)pacc.c, unused = 0.0;
     block_sum2(pap, unused);
     if (publish_inst(pap, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
-        double PAP, U;
-        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], PAP, U);
+        double PAP, unused2;
+        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], PAP, unused2);
         if (threadIdx.x == 0) {
             c->pAp = PAP;
             if (!(PAP > 0.0) || !isfinite(PAP)) {
@@ -450,7 +456,20 @@ void launch_b_residual(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl
 
 void launch_b_apply(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
                     BCtl* bc, Cond cond) {
-    kb_apply<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    // one cell per lane, every operand of it gathered at once (measured on the
+    // 256-instance floorplan batch: 40.7 ms per solve against 50.0 ms with the
+    // operands loaded term by term, CT_BATCH_APPLY=0, and 59.0 ms with two
+    // cells per lane, CT_BATCH_APPLY=2)
+    static const int form = [] {
+        const char* e = std::getenv("CT_BATCH_APPLY");
+        return e ? std::atoi(e) : 1;
+    }();
+    if (form == 1)
+        kb_apply<1><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    else if (form == 2)
+        kb_apply<2><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    else
+        kb_apply<0><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_update(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
