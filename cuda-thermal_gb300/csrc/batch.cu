@@ -109,7 +109,12 @@ class Batch {
         BRed r_res{}, r_apply{}, r_update{}, r_dot{};
         std::vector<Plan> sweep, restr;
         std::vector<unsigned> sweep_tile, restr_tile;
-        std::vector<char> tma;  // per depth: sweeps staged by bulk tensor copies
+        // per depth: 0 grid sweeps, 1 sweeps staged by bulk tensor copies,
+        // 2 mixed: the instances whose level fits a tile row staged (sweep),
+        // the others on the grid kernel (sweep_grid)
+        std::vector<char> tma;
+        std::vector<Plan> sweep_grid;
+        std::vector<unsigned> sweep_grid_tile;
         int* small_insts = nullptr;
     };
     std::vector<Bucket> bk;
@@ -422,13 +427,15 @@ ct_status Batch::build_bucket(Bucket& b) {
     if ((s = make_red(b.vec, &b.r_dot)) != CT_OK) return s;
     if ((s = upload(&b.small_insts, b.inst)) != CT_OK) return s;
     b.sweep.assign((size_t)b.depth, Plan{});
+    b.sweep_grid.assign((size_t)b.depth, Plan{});
     b.restr.assign((size_t)b.depth, Plan{});
     b.sweep_tile.assign((size_t)b.depth, 512);
+    b.sweep_grid_tile.assign((size_t)b.depth, 0);
     b.tma.assign((size_t)b.depth, 0);
     for (int d = 0; d < b.depth; ++d) {
-        bool all = true;
-        for (int i : b.inst) all = all && fits[(size_t)d][(size_t)i];
-        b.tma[(size_t)d] = all ? 1 : 0;
+        size_t nf = 0;
+        for (int i : b.inst) nf += fits[(size_t)d][(size_t)i] ? 1 : 0;
+        b.tma[(size_t)d] = nf == b.inst.size() ? 1 : nf > 0 ? 2 : 0;
     }
     b.restr_tile.assign((size_t)b.depth, 1024);
     return CT_OK;
@@ -446,12 +453,20 @@ ct_status Batch::tune_bucket(Bucket& b) {
     CT_BK(cudaEventCreate(&e1));
     ct_status s = CT_OK;
     for (int d = 0; d < b.depth && s == CT_OK; ++d) {
-        std::vector<unsigned> sweep_items, restr_items;
+        // staged instances (all of them in mode 1, the fitting ones in mode 2)
+        // and grid-swept ones (all in mode 0, the rest in mode 2)
+        std::vector<int> ins_t, ins_g;
+        std::vector<unsigned> items_t, items_g, restr_items;
         for (int i : b.inst) {
             const Geo& g = inst(i).lv[(size_t)d].g;
             const Geo& c = inst(i).lv[(size_t)d + 1].g;
-            sweep_items.push_back(b.tma[(size_t)d] ? (unsigned)sweep_tma_tiles(g)
-                                                   : (unsigned)g.ny * (unsigned)g.hx);
+            if (b.tma[(size_t)d] != 0 && fits[(size_t)d][(size_t)i]) {
+                ins_t.push_back(i);
+                items_t.push_back((unsigned)sweep_tma_tiles(g));
+            } else {
+                ins_g.push_back(i);
+                items_g.push_back((unsigned)g.ny * (unsigned)g.hx);
+            }
             restr_items.push_back((unsigned)c.nx * (unsigned)c.ny * (unsigned)c.nz);
         }
         auto time_of = [&](auto&& launch) -> float {
@@ -468,9 +483,15 @@ ct_status Batch::tune_bucket(Bucket& b) {
             }
             return best;
         };
-        // sweeps
-        {
-            const bool tma = b.tma[(size_t)d] != 0;
+        // sweeps: the staged part's tiles per block, then the grid part's;
+        // then, where anything is staged, the grid kernel over every instance,
+        // which replaces the staged form if it is faster (small levels)
+        float part_best[2] = {0.0f, 0.0f};
+        for (int part = 0; part < 2 && s == CT_OK; ++part) {
+            const bool tma = part == 0;
+            const std::vector<int>& ins = tma ? ins_t : ins_g;
+            const std::vector<unsigned>& items = tma ? items_t : items_g;
+            if (ins.empty()) continue;
             std::vector<unsigned> cands;
             if (tma && fixed_tma) cands.push_back(fixed_tma);
             else if (tma) cands.assign(std::begin(kTmaTiles), std::end(kTmaTiles));
@@ -479,7 +500,7 @@ ct_status Batch::tune_bucket(Bucket& b) {
             float best = 1e30f;
             for (unsigned tile : cands) {
                 Plan p;
-                if ((s = upload_plan(make_plan(ni, b.inst, sweep_items, tile), &p)) != CT_OK) break;
+                if ((s = upload_plan(make_plan(ni, ins, items, tile), &p)) != CT_OK) break;
                 CT_BK(cudaStreamSynchronize(st));
                 const float t = cands.size() == 1 ? 0.0f : time_of([&] {
                     if (tma)
@@ -490,8 +511,41 @@ ct_status Batch::tune_bucket(Bucket& b) {
                 });
                 if (t < best) {
                     best = t;
+                    // staged part (or everything in mode 0) in sweep, the grid
+                    // part of a mixed depth in sweep_grid
+                    if (tma || b.tma[(size_t)d] == 0) {
+                        b.sweep[(size_t)d] = p;
+                        b.sweep_tile[(size_t)d] = tile;
+                    } else {
+                        b.sweep_grid[(size_t)d] = p;
+                        b.sweep_grid_tile[(size_t)d] = tile;
+                    }
+                }
+            }
+            part_best[part] = best;
+        }
+        if (s == CT_OK && b.tma[(size_t)d] != 0 && !fixed_tma) {
+            std::vector<unsigned> items;
+            for (int i : b.inst) {
+                const Geo& g = inst(i).lv[(size_t)d].g;
+                items.push_back((unsigned)g.ny * (unsigned)g.hx);
+            }
+            const float staged = part_best[0] + (ins_g.empty() ? 0.0f : part_best[1]);
+            std::vector<unsigned> cands;
+            if (fixed) cands.push_back(fixed);
+            else cands.assign(std::begin(kSweepTiles), std::end(kSweepTiles));
+            for (unsigned tile : cands) {
+                Plan p;
+                if ((s = upload_plan(make_plan(ni, b.inst, items, tile), &p)) != CT_OK) break;
+                CT_BK(cudaStreamSynchronize(st));
+                const float t = time_of([&] {
+                    launch_b_sweep(b.st, p, views[(size_t)d], views[(size_t)d], 1, false, false, b.mz, ctl);
+                });
+                if (t < staged && (b.tma[(size_t)d] != 0 || t < part_best[1])) {
+                    b.tma[(size_t)d] = 0;
                     b.sweep[(size_t)d] = p;
                     b.sweep_tile[(size_t)d] = tile;
+                    part_best[1] = t;
                 }
             }
         }
@@ -527,11 +581,14 @@ ct_status Batch::tune_bucket(Bucket& b) {
 void Batch::sweep(Bucket& b, cudaStream_t s, int d, int color, bool zero_x, bool prolong, Cond cond) {
     const LevelView<float>* L = views[(size_t)d];
     const LevelView<float>* C = views[(size_t)d + 1];
-    if (b.tma[(size_t)d])
+    if (b.tma[(size_t)d]) {
         launch_b_sweep_tma(s, b.sweep[(size_t)d], bmaps[(size_t)(2 * d + color)], L, C, color, zero_x,
                            prolong, b.mz, ctl, b.bc, cond);
-    else
+        if (b.tma[(size_t)d] == 2)  // the instances that do not fit a tile row
+            launch_b_sweep(s, b.sweep_grid[(size_t)d], L, C, color, zero_x, prolong, b.mz, ctl);
+    } else {
         launch_b_sweep(s, b.sweep[(size_t)d], L, C, color, zero_x, prolong, b.mz, ctl);
+    }
 }
 
 void Batch::vcycle(Bucket& b, cudaStream_t s, Cond cond) {

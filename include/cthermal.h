@@ -243,9 +243,11 @@ ct_status ct_batch_step_record(ct_batch* b, int i, double dt, ct_step_record* ou
 ct_status ct_batch_step_records(ct_batch* b, const double* dt, ct_step_record* out);
 /* Size buckets and the tiles the autotuner picked for each of their depths
  * (arrays of depth entries, each may be NULL): staged[d] = 1 where the
- * sweeps of depth d are staged by bulk tensor copies, sweep_tiles[d] the
- * 32 x 8-column tiles per block there, else the columns per block of the grid
- * sweep; restrict_tiles[d] the coarse cells per block of the restriction. */
+ * sweeps of depth d are staged by bulk tensor copies, 2 where only the
+ * instances whose level holds a full tile row are (the others run the grid
+ * sweep), 0 where none is; sweep_tiles[d] the 32 x 8-column tiles per block
+ * of the staged part, else the columns per block of the grid sweep;
+ * restrict_tiles[d] the coarse cells per block of the restriction. */
 ct_status ct_batch_num_buckets(const ct_batch* b, int* nbuckets);
 /* The batch's stream (a cudaStream_t): every ct_batch_* call is ordered on it,
  * and a solve's work on the buckets' own streams is joined back into it. */

@@ -76,16 +76,28 @@ def test_batch_steady_matches_oracle_and_single(ct, orc, mixed):
 
 
 def test_batch_buckets_cover_instances(ct, mixed):
-    with ct.GpuBatch(mixed) as b:
-        info = b.buckets()
-        assert sum(k["instances"] for k in info) == len(mixed)
-        for k in info:
-            assert len(k["sweep_tiles"]) == k["depth"] == len(k["staged"])
-            for t, staged in zip(k["sweep_tiles"], k["staged"]):
-                assert t in ((1, 2, 4, 8) if staged else (256, 512, 1024, 2048))
-            assert all(t in (256, 512, 1024, 2048, 4096) for t in k["restrict_tiles"])
-        # the large levels of the workload's stacks are staged
-        assert any(any(k["staged"]) for k in info)
+    """Buckets cover every instance once; the tiles are candidates of the
+    tuner. Where the staged form is not forced, the tuner keeps it only where
+    it timed faster than the grid sweep; with a fixed number of tiles per
+    block (CT_BATCH_TMA_TILES) every level that holds a full tile row is
+    staged."""
+    for forced in (None, "2"):
+        old = _env(CT_BATCH_TMA_TILES=forced) if forced else {}
+        try:
+            with ct.GpuBatch(mixed) as b:
+                info = b.buckets()
+                assert sum(k["instances"] for k in info) == len(mixed)
+                for k in info:
+                    assert len(k["sweep_tiles"]) == k["depth"] == len(k["staged"])
+                    for t, staged in zip(k["sweep_tiles"], k["staged"]):
+                        assert t in ((1, 2, 4, 8) if staged else (256, 512, 1024, 2048))
+                    assert all(t in (256, 512, 1024, 2048, 4096) for t in k["restrict_tiles"])
+                if forced:
+                    # the large levels of the workload's stacks are staged
+                    assert any(any(k["staged"]) for k in info)
+                    assert all(t == 2 for k in info for t, st in zip(k["sweep_tiles"], k["staged"]) if st)
+        finally:
+            _restore(old)
 
 
 def test_batch_resolve_and_power_change(ct, orc, mixed):
@@ -233,11 +245,13 @@ def _restore(old):
 
 
 def test_batch_staged_sweeps_bitwise(ct, mixed):
-    """The sweeps staged by bulk tensor copies compute exactly what the grid
-    sweeps compute: same iterations, same bits."""
+    """The sweeps staged by bulk tensor copies (forced on every level that
+    holds a full tile row; mixed depths run the rest on the grid kernel)
+    compute exactly what the grid sweeps compute: same iterations, same
+    bits."""
     out = []
     for flag in ("0", "1"):
-        old = _env(CT_SWEEP_TMA=flag)
+        old = _env(CT_SWEEP_TMA=flag, CT_BATCH_TMA_TILES="1")
         try:
             with ct.GpuBatch(mixed) as b:
                 b.set_x_zero()
