@@ -244,11 +244,95 @@ __device__ __forceinline__ T residual_at(const LevelView<T>& F, T inv_dt, int i,
     return ldm<CG>(F.b + id) - (d * xc - off);
 }
 
+// residual_at's arithmetic on operands already loaded, in its order: the
+// diagonal (west, east, south, north faces, up face, down face or gB, C/dt)
+// times x minus the neighbour terms (west, east, south, north, down, up).
+template <class T>
+__device__ __forceinline__ T residual_of(T b, T xc, T xw, T xe, T xs, T xn, T xd, T xu, float gew, float gee,
+                                         float gns, float gnn, float gu, float gd, float cap, T inv_dt, bool w,
+                                         bool e, bool so, bool no, bool down, bool up) {
+    T d = 0, off = 0;
+    if (w) {
+        const T ge = (T)gew;
+        d += ge;
+        off += ge * xw;
+    }
+    if (e) {
+        const T ge = (T)gee;
+        d += ge;
+        off += ge * xe;
+    }
+    if (so) {
+        const T gn = (T)gns;
+        d += gn;
+        off += gn * xs;
+    }
+    if (no) {
+        const T gn = (T)gnn;
+        d += gn;
+        off += gn * xn;
+    }
+    d += (T)gu;
+    d += (T)gd;
+    d += (T)cap * inv_dt;
+    if (down) off += (T)gd * xd;
+    if (up) off += (T)gu * xu;
+    return b - (d * xc - off);
+}
+
+// The four children of an interior coarse cell at once: their x, faces and
+// the eight outside neighbours are loaded once each (48 values instead of
+// four residual_at's 60, with the index arithmetic shared), and each child's
+// residual is residual_at's, operation for operation.
+template <class T, bool CG>
+__device__ __forceinline__ T restrict_sum4(const LevelView<T>& F, T inv_dt, int I, int J, int l) {
+    const Geo& g = F.g;
+    const int i0 = 2 * I, j0 = 2 * J;
+    const bool w = i0 > 0, e = i0 + 2 < g.nx, so = j0 > 0, no = j0 + 2 < g.ny;
+    const bool down = l > 0, up = l < g.nz - 1;
+    const unsigned base = (unsigned)l * g.plane;
+    const unsigned c00 = base + scol(g, i0, j0), c10 = base + scol(g, i0 + 1, j0);
+    const unsigned c01 = base + scol(g, i0, j0 + 1), c11 = base + scol(g, i0 + 1, j0 + 1);
+    // outside neighbours (an absent one reads the child beside it; unused)
+    const unsigned w0 = w ? base + scol(g, i0 - 1, j0) : c00, w1 = w ? base + scol(g, i0 - 1, j0 + 1) : c01;
+    const unsigned e0 = e ? base + scol(g, i0 + 2, j0) : c10, e1 = e ? base + scol(g, i0 + 2, j0 + 1) : c11;
+    const unsigned s0 = so ? base + scol(g, i0, j0 - 1) : c00, s1 = so ? base + scol(g, i0 + 1, j0 - 1) : c10;
+    const unsigned n0 = no ? base + scol(g, i0, j0 + 2) : c01, n1 = no ? base + scol(g, i0 + 1, j0 + 2) : c11;
+    const unsigned dn = down ? g.plane : 0u, upo = up ? g.plane : 0u;
+    const T x00 = ldm<CG>(F.x + c00), x10 = ldm<CG>(F.x + c10), x01 = ldm<CG>(F.x + c01), x11 = ldm<CG>(F.x + c11);
+    const T xw0 = ldm<CG>(F.x + w0), xw1 = ldm<CG>(F.x + w1), xe0 = ldm<CG>(F.x + e0), xe1 = ldm<CG>(F.x + e1);
+    const T xs0 = ldm<CG>(F.x + s0), xs1 = ldm<CG>(F.x + s1), xn0 = ldm<CG>(F.x + n0), xn1 = ldm<CG>(F.x + n1);
+    const T d00 = ldm<CG>(F.x + c00 - dn), d10 = ldm<CG>(F.x + c10 - dn);
+    const T d01 = ldm<CG>(F.x + c01 - dn), d11 = ldm<CG>(F.x + c11 - dn);
+    const T u00 = ldm<CG>(F.x + c00 + upo), u10 = ldm<CG>(F.x + c10 + upo);
+    const T u01 = ldm<CG>(F.x + c01 + upo), u11 = ldm<CG>(F.x + c11 + upo);
+    const float gEw0 = F.gE[w0], gE00 = F.gE[c00], gE10 = F.gE[c10];
+    const float gEw1 = F.gE[w1], gE01 = F.gE[c01], gE11 = F.gE[c11];
+    const float gNs0 = F.gN[s0], gN00 = F.gN[c00], gNs1 = F.gN[s1], gN10 = F.gN[c10];
+    const float gN01 = F.gN[c01], gN11 = F.gN[c11];
+    const float gu00 = F.gU[c00], gu10 = F.gU[c10], gu01 = F.gU[c01], gu11 = F.gU[c11];
+    // down face: gU of the plane below, or gB at the bottom plane
+    const unsigned cb = (unsigned)l * g.plane;
+    const float gd00 = down ? F.gU[c00 - dn] : F.gB[c00 - cb], gd10 = down ? F.gU[c10 - dn] : F.gB[c10 - cb];
+    const float gd01 = down ? F.gU[c01 - dn] : F.gB[c01 - cb], gd11 = down ? F.gU[c11 - dn] : F.gB[c11 - cb];
+    T sum = 0;
+    sum += residual_of<T>(ldm<CG>(F.b + c00), x00, xw0, x10, xs0, x01, d00, u00, gEw0, gE00, gNs0, gN00, gu00, gd00,
+                          F.cap[c00], inv_dt, w, true, so, true, down, up);
+    sum += residual_of<T>(ldm<CG>(F.b + c10), x10, x00, xe0, xs1, x11, d10, u10, gE00, gE10, gNs1, gN10, gu10, gd10,
+                          F.cap[c10], inv_dt, true, e, so, true, down, up);
+    sum += residual_of<T>(ldm<CG>(F.b + c01), x01, xw1, x11, x00, xn0, d01, u01, gEw1, gE01, gN00, gN01, gu01, gd01,
+                          F.cap[c01], inv_dt, w, true, true, no, down, up);
+    sum += residual_of<T>(ldm<CG>(F.b + c11), x11, x01, xe1, x10, xn1, d11, u11, gE01, gE11, gN10, gN11, gu11, gd11,
+                          F.cap[c11], inv_dt, true, e, true, no, down, up);
+    return sum;
+}
+
 // Restriction (src/pcg3d_cpu.cpp:87-100) of coarse cell (I, J, l): the sum
 // over the (up to 4) children, j then i, of the fine residual.
 template <class T, bool CG>
 __device__ __forceinline__ T restrict_sum(const LevelView<T>& F, T inv_dt, int I, int J, int l) {
     const Geo& fg = F.g;
+    if (2 * I + 1 < fg.nx && 2 * J + 1 < fg.ny) return restrict_sum4<T, CG>(F, inv_dt, I, J, l);
     const int i1 = min(2 * I + 2, fg.nx), j1 = min(2 * J + 2, fg.ny);
     T sum = 0;
     for (int j = 2 * J; j < j1; ++j)
