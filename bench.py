@@ -486,6 +486,47 @@ def bench_transient_batched(ct, np, args, steps):
     }
 
 
+def bench_transient_800(ct, np, solvers, m, steps):
+    """The 800 x 800 x 10 stack's transient: backward-Euler steps from T = 0
+    with the power on at t = 0 (run_transient, src/transient3d.h:48-90), dt
+    10 us growing 10 % per step up to 50 ms, tol 1e-9, each step warm-started
+    from the last; per step set_dt, b = P + C/dt T, the solve and the step
+    record (T_max, heat out, heat stored reduced on the device). The double-
+    word solver against the plain FP64 MG-PCG on the same steps; the
+    solvers already hold the operator and hierarchy."""
+    ptot = float(np.sum(m.P))
+    res = {}
+    for name, s in solvers.items():
+        s.set_x_zero()
+        dt, last, its, eb = TR_DT0, -1.0, 0, 0.0
+        t0 = time.perf_counter()
+        for k in range(steps):
+            if dt != last:
+                s.set_dt(dt)
+                last = dt
+            s.set_rhs_transient()
+            its += s.solve(TR_TOL, MAXIT).iters
+            rec = s.step_record(dt)
+            eb = max(eb, abs(rec.q_out + rec.q_stored - ptot) / ptot)
+            dt = min(dt * TR_GROWTH, TR_DT_MAX)
+        sec = time.perf_counter() - t0
+        res[name] = dict(sec=sec, iters=its, eb=eb, T=s.get_x(), T_max=rec.T_max)
+        s.set_dt(0.0)
+    dw, f64 = res["dw"], res["fp64"]
+    return {
+        "value": steps / dw["sec"], "unit": "steps/s",
+        "workload": f"{N_GRID}x{N_GRID}x10 stack, {steps} backward-Euler steps from T = 0, dt "
+                    f"{TR_DT0:g} s x {TR_GROWTH} per step (max {TR_DT_MAX:g}), tol {TR_TOL:g}, "
+                    f"device step records",
+        "steps": steps, "iters_total": dw["iters"], "energy_balance_err_max": dw["eb"],
+        "T_max_end_K": dw["T_max"],
+        "fp64_mg_pcg": {"value": steps / f64["sec"], "unit": "steps/s", "iters_total": f64["iters"],
+                        "energy_balance_err_max": f64["eb"]},
+        "speedup_vs_fp64": f64["sec"] / dw["sec"],
+        "max_dT_K_vs_fp64": float(np.abs(dw["T"] - f64["T"]).max()),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -497,6 +538,8 @@ def main():
     ap.add_argument("--no-four-tier", action="store_true", help="skip the 1024x1024x16 stack")
     ap.add_argument("--transient-steps", type=int, default=500,
                     help="backward-Euler steps of the batched transient (0: skip)")
+    ap.add_argument("--transient-800-steps", type=int, default=300,
+                    help="backward-Euler steps of the 800x800x10 transient (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -599,6 +642,9 @@ def main():
     transient = None
     if args.transient_steps > 0:
         transient = bench_transient_batched(ct, np, args, args.transient_steps)
+    transient800 = None
+    if args.transient_800_steps > 0:
+        transient800 = bench_transient_800(ct, np, {"dw": s32, "fp64": s64}, m, args.transient_800_steps)
     # clocks sampled over every timed region above (headline, FP64, e2e, batched)
     clk = clocks.stop()
 
@@ -652,6 +698,8 @@ def main():
             out["batched"] = batched
         if transient:
             out["batched_transient"] = transient
+        if transient800:
+            out["transient_800"] = transient800
         if four:
             out["four_tier"] = four
         if cpu:
