@@ -289,6 +289,7 @@ ct_status Batch::create(int n, const ct_model* const* models, const DeviceBuild*
         I.x = s.x;
         I.b = s.b;
         I.diag = s.diag;
+        I.dface = s.dface;
         I.xw = s.xwc;
         I.r = s.rw();
         I.p = s.pw();

@@ -37,6 +37,7 @@ struct BInst {
     double* x;      // FP64 base of x
     double* b;
     const double* diag;
+    const double* dface;  // the diagonal's face sum
     float2* xw;     // double-word correction of x
     float2* r;
     float2* p;

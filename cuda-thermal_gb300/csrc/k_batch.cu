@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(NT) kb_diag(Plan p, const BInst* __restrict__ 
     const BInst& I = bi[t.inst];
     const double inv_dt = ctl[t.inst].inv_dt;
     for (unsigned q = t.begin + threadIdx.x; q < t.end; q += NT)
-        setupdev::diag_column(I.o, inv_dt, q, const_cast<double*>(I.diag), nullptr,
+        setupdev::diag_column(I.o, I.dface, inv_dt, q, const_cast<double*>(I.diag), nullptr,
                               const_cast<float2*>(I.dgw));
 }
 

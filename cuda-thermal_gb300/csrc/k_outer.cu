@@ -357,12 +357,20 @@ __global__ void k_to_natural_d(Geo g, const double* __restrict__ in, double* __r
 
 // op_diag (src/operator3d.h:80-88) in double with every rounding explicit
 // (no contraction), so the diagonal equals the CPU's bit for bit.
-__global__ void k_diag(OpView o, double inv_dt, double* __restrict__ diag,
+__global__ void k_diag(OpView o, const double* __restrict__ dface, double inv_dt, double* __restrict__ diag,
                        double* __restrict__ invd) {
     const size_t ncol = (size_t)o.g.nx * o.g.ny;
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < ncol;
          q += (size_t)gridDim.x * blockDim.x)
-        setupdev::diag_column(o, inv_dt, (unsigned)q, diag, invd, nullptr);
+        setupdev::diag_column(o, dface, inv_dt, (unsigned)q, diag, invd, nullptr);
+}
+
+// Its face part, once per operator.
+__global__ void k_faces(OpView o, double* __restrict__ dface) {
+    const size_t ncol = (size_t)o.g.nx * o.g.ny;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < ncol;
+         q += (size_t)gridDim.x * blockDim.x)
+        setupdev::faces_column(o, (unsigned)q, dface);
 }
 
 __global__ void k_rhs_transient(unsigned n, const float* __restrict__ cap, double inv_dt,
@@ -589,8 +597,13 @@ void launch_to_natural_d(cudaStream_t st, const Geo& g, const double* split, dou
     k_to_natural_d<<<grid_for((size_t)g.nx * g.ny * g.nz), NT, 0, st>>>(g, split, nat);
 }
 
-void launch_diag(cudaStream_t st, const OpView& o, double inv_dt, double* diag, double* invd) {
-    k_diag<<<grid_for((size_t)o.g.nx * o.g.ny), NT, 0, st>>>(o, inv_dt, diag, invd);
+void launch_faces(cudaStream_t st, const OpView& o, double* dface) {
+    k_faces<<<grid_for((size_t)o.g.nx * o.g.ny), NT, 0, st>>>(o, dface);
+}
+
+void launch_diag(cudaStream_t st, const OpView& o, const double* dface, double inv_dt, double* diag,
+                 double* invd) {
+    k_diag<<<grid_for((size_t)o.g.nx * o.g.ny), NT, 0, st>>>(o, dface, inv_dt, diag, invd);
 }
 
 void launch_rhs_transient(cudaStream_t st, unsigned n, const float* cap, double inv_dt,

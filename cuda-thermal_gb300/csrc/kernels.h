@@ -97,7 +97,11 @@ void launch_to_split_f(cudaStream_t st, const Geo& g, int planes, const float* n
 void launch_to_split_d(cudaStream_t st, const Geo& g, const double* nat, double* split);
 void launch_to_natural_d(cudaStream_t st, const Geo& g, const double* split, double* nat);
 // diag = op_diag (FP64, no contraction); invd = 1 / diag when invd != null.
-void launch_diag(cudaStream_t st, const OpView& o, double inv_dt, double* diag, double* invd);
+// The FP64 face sum of the diagonal (once per operator), and the diagonal
+// face sum + C/dt (per dt).
+void launch_faces(cudaStream_t st, const OpView& o, double* dface);
+void launch_diag(cudaStream_t st, const OpView& o, const double* dface, double inv_dt, double* diag,
+                 double* invd);
 // b = P + cap * inv_dt * x; xold = x.
 void launch_rhs_transient(cudaStream_t st, unsigned n, const float* cap, double inv_dt,
                           const double* P, const double* x, double* b, double* xold);

@@ -62,11 +62,10 @@ __device__ __forceinline__ void factor_column(const LevelView<T>& L, T inv_dt, u
     }
 }
 
-// FP64 diagonal of natural column q of the fine operator (and 1/d for Jacobi,
-// the double-word copy for the double-word mode, where requested).
-__device__ __forceinline__ void diag_column(const OpView& o, double inv_dt, unsigned q,
-                                            double* __restrict__ diag, double* __restrict__ invd,
-                                            float2* __restrict__ dgw) {
+// The face part of op_diag (src/operator3d.h:80-88) of natural column q of
+// the fine operator in FP64 — west, east, south, north, up, down or bottom
+// sink, summed in that order — which does not change with dt.
+__device__ __forceinline__ void faces_column(const OpView& o, unsigned q, double* __restrict__ dface) {
     const Geo& g = o.g;
     const int j = (int)(q / (unsigned)g.nx), i = (int)(q - (unsigned)j * g.nx);
     const unsigned s = scol(g, i, j);
@@ -79,7 +78,23 @@ __device__ __forceinline__ void diag_column(const OpView& o, double inv_dt, unsi
         if (j < g.ny - 1) d = __dadd_rn(d, (double)o.gN[id]);
         d = __dadd_rn(d, (double)o.gU[id]);
         d = __dadd_rn(d, l > 0 ? (double)o.gU[id - g.plane] : (double)o.gB[s]);
-        d = __dadd_rn(d, __dmul_rn((double)o.cap[id], inv_dt));
+        dface[id] = d;
+    }
+}
+
+// FP64 diagonal of natural column q of the fine operator: the stored face
+// sum plus C/dt, the last term of op_diag's sum, so the same bits as summing
+// it all here (and 1/d for Jacobi, the double-word copy for the double-word
+// mode, where requested).
+__device__ __forceinline__ void diag_column(const OpView& o, const double* __restrict__ dface, double inv_dt,
+                                            unsigned q, double* __restrict__ diag, double* __restrict__ invd,
+                                            float2* __restrict__ dgw) {
+    const Geo& g = o.g;
+    const int j = (int)(q / (unsigned)g.nx), i = (int)(q - (unsigned)j * g.nx);
+    const unsigned s = scol(g, i, j);
+    for (int l = 0; l < g.nz; ++l) {
+        const unsigned id = (unsigned)l * g.plane + s;
+        const double d = __dadd_rn(dface[id], __dmul_rn((double)o.cap[id], inv_dt));
         diag[id] = d;
         if (invd) invd[id] = __drcp_rn(d);
         if (dgw) {

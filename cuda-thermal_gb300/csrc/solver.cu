@@ -120,7 +120,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     Arena ar;
     const size_t o_gE = ar.take(n * 4), o_gN = ar.take(n * 4), o_gU = ar.take(n * 4);
     const size_t o_cap = ar.take(n * 4), o_gB = ar.take((size_t)g0.plane * 4);
-    size_t o_vec[8];
+    size_t o_vec[9];
     for (size_t& o : o_vec) o = ar.take((size_t)n * 8);
     const size_t o_invd = pc == CT_JACOBI ? ar.take((size_t)n * 8) : 0;
     const size_t o_dgw = dw ? ar.take((size_t)n * 8) : 0;
@@ -215,6 +215,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     Ap = at<double>(o_vec[5]);
     diag = at<double>(o_vec[6]);
     xold = at<double>(o_vec[7]);
+    dface = at<double>(o_vec[8]);
     invd = pc == CT_JACOBI ? at<double>(o_invd) : nullptr;
     dgw = dw ? at<float2>(o_dgw) : nullptr;
     xwc = dw ? at<float2>(o_xwc) : nullptr;
@@ -296,6 +297,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     times.levels_ms = ms_since(t0);
 
     t0 = clk::now();
+    launch_faces(st, op(), dface);
     ct_status s = set_dt(0.0);
     if (s != CT_OK) return s;
     CT_CK(cudaStreamSynchronize(st));
@@ -318,7 +320,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
 ct_status Solver::set_dt(double dt) {
     if (!(dt >= 0) || !std::isfinite(dt)) return fail(CT_BAD_ARG, "ct_set_dt: dt must be >= 0");
     inv_dt = dt > 0 ? 1.0 / dt : 0.0;
-    launch_diag(st, op(), inv_dt, diag, invd);
+    launch_diag(st, op(), dface, inv_dt, diag, invd);
     if (dw) launch_to_dw(st, n, diag, dgw);
     if (mt == MG_F32)
         for (size_t k = 0; k < lv.size(); ++k) launch_factor<float>(st, view<float>(k), (float)inv_dt);

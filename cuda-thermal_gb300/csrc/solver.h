@@ -71,6 +71,7 @@ class Solver {
     float *gE = nullptr, *gN = nullptr, *gU = nullptr, *gB = nullptr, *cap = nullptr;
     double *P = nullptr, *x = nullptr, *b = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr;
     double *diag = nullptr, *invd = nullptr, *xold = nullptr, *nat = nullptr, *part = nullptr;
+    double* dface = nullptr;  // FP64 face sum of the diagonal (the part that does not change with dt)
     float2* dgw = nullptr;  // double-word diagonal (dw)
     float2* xwc = nullptr;  // double-word correction of x (dw); x is then its FP64 base
     Ctl* ctl = nullptr;
