@@ -10,6 +10,7 @@
 #include <cstdlib>
 
 #include "kernels.h"
+#include "tma.cuh"
 #include "reduce.cuh"
 #include "setup_dev.cuh"
 
@@ -595,6 +596,28 @@ void launch_to_split_d(cudaStream_t st, const Geo& g, const double* nat, double*
 
 void launch_to_natural_d(cudaStream_t st, const Geo& g, const double* split, double* nat) {
     k_to_natural_d<<<grid_for((size_t)g.nx * g.ny * g.nz), NT, 0, st>>>(g, split, nat);
+}
+
+// Self-test of the bounded waits: one warp waits on an mbarrier whose phase
+// nothing completes (no arrival, no copy), with `limit` polls, through the
+// same wait the staged kernels use, and records in *status 1 when the wait
+// ran out, 2 if it (wrongly) completed. The kernel then returns normally.
+__global__ void k_wait_selftest(unsigned limit, int* status) {
+    __shared__ uint64_t bar;
+    __shared__ int abort;
+    if (threadIdx.x == 0) {
+        tma::mbar_init(&bar, 1);
+        abort = 0;
+        tma::fence_barrier_init();
+    }
+    __syncwarp();
+    const bool got = tma::mbar_wait_or_abort(&bar, 0u, &abort, limit);
+    if (threadIdx.x == 0) *status = got ? 2 : (abort ? 1 : 3);
+}
+
+cudaError_t launch_wait_selftest(cudaStream_t st, unsigned limit, int* status) {
+    k_wait_selftest<<<1, 32, 0, st>>>(limit, status);
+    return cudaGetLastError();
 }
 
 void launch_faces(cudaStream_t st, const OpView& o, double* dface) {

@@ -97,6 +97,9 @@ void launch_to_split_f(cudaStream_t st, const Geo& g, int planes, const float* n
 void launch_to_split_d(cudaStream_t st, const Geo& g, const double* nat, double* split);
 void launch_to_natural_d(cudaStream_t st, const Geo& g, const double* split, double* nat);
 // diag = op_diag (FP64, no contraction); invd = 1 / diag when invd != null.
+// One warp waiting, `limit` polls, on an mbarrier that nothing completes
+// (*status: 1 the wait ran out as it must, 2 it completed, 3 no abort flag).
+cudaError_t launch_wait_selftest(cudaStream_t st, unsigned limit, int* status);
 // The FP64 face sum of the diagonal (once per operator), and the diagonal
 // face sum + C/dt (per dt).
 void launch_faces(cudaStream_t st, const OpView& o, double* dface);

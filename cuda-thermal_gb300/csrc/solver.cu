@@ -671,6 +671,27 @@ extern "C" {
 
 void ct_use_graphs(int on) { ct::g_use_graphs = on != 0; }
 
+ct_status ct_selftest_bounded_wait(unsigned polls, int* timed_out) {
+    if (!timed_out) return fail(CT_BAD_ARG, "ct_selftest_bounded_wait: null");
+    if (polls == 0 || polls > (1u << 22)) return fail(CT_BAD_ARG, "ct_selftest_bounded_wait: polls in 1..2^22");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CT_NO_DEVICE, "no CUDA device");
+    }
+    int* d = nullptr;
+    int h = 0;
+    cudaError_t e = cudaMalloc(&d, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) e = ct::launch_wait_selftest(nullptr, polls, d);
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return fail(CT_CUDA_ERROR, "ct_selftest_bounded_wait: %s", cudaGetErrorString(e));
+    if (h != 1 && h != 2) return fail(CT_CUDA_ERROR, "ct_selftest_bounded_wait: status %d", h);
+    *timed_out = h == 1 ? 1 : 0;
+    return CT_OK;
+}
+
 ct_status ct_last_setup(ct_setup_times* out) {
     if (!out) return fail(CT_BAD_ARG, "ct_last_setup: null");
     std::lock_guard<std::mutex> lk(ct::g_setup_mu);

@@ -55,9 +55,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 // Bounded wait that also gives up once *abort is set (by another thread
-// whose own wait ran out).
-__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, unsigned parity, volatile int* abort) {
-    for (unsigned k = 0; k < kWaitLimit; ++k) {
+// whose own wait ran out); limit: polls before giving up.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, unsigned parity, volatile int* abort,
+                                                   unsigned limit = kWaitLimit) {
+    for (unsigned k = 0; k < limit; ++k) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort) return false;
     }

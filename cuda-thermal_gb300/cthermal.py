@@ -153,6 +153,7 @@ def _signatures():
         "ct_case_block": (i, [vp, i, ip, dp, dp, C.c_char_p, i]),
         "ct_case_tsv": (i, [vp, i, ip, dp, dp]),
         "ct_case_export_3dice": (i, [vp, C.c_double, C.c_char_p]),
+        "ct_selftest_bounded_wait": (i, [C.c_uint, ip]),
         "ct_eff_kz": (d, [d, d, d]),
         "ct_eff_kxy": (d, [d, d, d]),
     }
@@ -446,6 +447,14 @@ def load_case(folder: str) -> CaseSpec:
         return cs
     finally:
         lib().ct_case_destroy(h)
+
+
+def selftest_bounded_wait(polls: int) -> bool:
+    """Runs a device wait that nothing completes, bounded at `polls` polls;
+    True when it ran out and its kernel returned (the context stays usable)."""
+    t = C.c_int(0)
+    _check(lib().ct_selftest_bounded_wait(int(polls), C.byref(t)))
+    return bool(t.value)
 
 
 def export_3dice(folder: str, cell_um: float, outdir: str) -> None:

@@ -112,6 +112,13 @@ const char* ct_last_error(void);
  * each solve as one CUDA graph (on, the default) or launch every kernel
  * directly with a host check per iteration (off). */
 void ct_use_graphs(int on);
+
+/* Self-test of the device-side failure detection: one warp waits `polls`
+ * polls (1..2^22) on an mbarrier that nothing completes, through the bounded
+ * wait every staged kernel uses, and *timed_out = 1 when the wait ran out and
+ * the kernel returned (as it must; the solvers then report CT_TIMEOUT). The
+ * context stays usable. */
+ct_status ct_selftest_bounded_wait(unsigned polls, int* timed_out);
 /* gpu_last_setup (src/pcg3d_gpu.cu:87-88): setup times of the last solver
  * created on any thread. */
 ct_status ct_last_setup(ct_setup_times* out);

@@ -352,3 +352,14 @@ def test_fused_first_sweep_bitwise(ct, n, prec):
             assert np.array_equal(a, b)
         else:
             assert a == b
+
+
+def test_bounded_wait_runs_out_and_context_survives(ct):
+    """Failure detection without a fault: a device wait that nothing
+    completes runs out after its poll limit, its kernel returns and reports
+    it, and the context goes on to solve normally."""
+    import workloads
+    assert ct.selftest_bounded_wait(20000) is True
+    m = workloads.steady_hotspot(64, seed=1)
+    st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX_DW)
+    assert st.converged and np.isfinite(T).all()
