@@ -34,6 +34,7 @@
 #include <string>
 #include <vector>
 
+#include "trace.h"
 #include "batch.h"
 #include "cthermal.h"
 #include "solver.h"
@@ -239,6 +240,7 @@ class Batch {
 };
 
 ct_status Batch::create(int n, const ct_model* const* models, const DeviceBuild* builds) {
+    const TraceRange trace("ct_batch_create");
     if (n < 1) return fail(CT_BAD_ARG, "ct_batch_create: n must be >= 1");
     if (!models && !builds) return fail(CT_BAD_ARG, "ct_batch_create: null model list");
     for (int i = 0; models && i < n; ++i)
@@ -707,6 +709,7 @@ ct_status Batch::record(Bucket& b) {
 // into its control block, then the batched diagonal and factor kernels run
 // the single solver's per-column arithmetic (same bits as Solver::set_dt).
 ct_status Batch::set_dt(const double* dt) {
+    const TraceRange trace("ct_batch_set_dt");
     for (int i = 0; i < ni; ++i) {
         const double v = dt ? dt[i] : 0.0;
         if (!(v >= 0) || !std::isfinite(v)) return fail(CT_BAD_ARG, "ct_batch_set_dt: dt[%d] must be >= 0", i);
@@ -723,6 +726,7 @@ ct_status Batch::set_dt(const double* dt) {
 }
 
 ct_status Batch::solve(double tol, int maxit, ct_stats* out) {
+    const TraceRange trace("ct_batch_solve");
     if (!(tol >= 0)) return fail(CT_BAD_ARG, "ct_batch_solve: tol must be >= 0");
     if (maxit > 100000000) return fail(CT_BAD_ARG, "ct_batch_solve: maxit above 1e8");
     for (int i = 0; i < ni; ++i) {

@@ -28,6 +28,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "trace.h"
 #include "cthermal.h"
 #include "kernels.h"
 #include "solver.h"
@@ -59,6 +60,7 @@ double ms_since(clk::time_point t) {
 // ---- setup ---------------------------------------------------------------
 
 ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec_, const DeviceBuild* build) {
+    const TraceRange trace("ct_solver_create");
     ct_model geo{};  // the geometry when the model is built on the device
     if (build) {
         geo.nx = build->nx;
@@ -318,6 +320,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
 }
 
 ct_status Solver::set_dt(double dt) {
+    const TraceRange trace("ct_set_dt");
     if (!(dt >= 0) || !std::isfinite(dt)) return fail(CT_BAD_ARG, "ct_set_dt: dt must be >= 0");
     inv_dt = dt > 0 ? 1.0 / dt : 0.0;
     launch_diag(st, op(), dface, inv_dt, diag, invd);
@@ -566,6 +569,7 @@ ct_status Solver::record_graphs() {
 }
 
 ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
+    const TraceRange trace("ct_solve");
     if (!(tol >= 0)) return fail(CT_BAD_ARG, "ct_solve: tol must be >= 0");
     if (maxit > 100000000) return fail(CT_BAD_ARG, "ct_solve: maxit above 1e8");
     Ctl c;
