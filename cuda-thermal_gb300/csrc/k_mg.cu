@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(NT)
 // Restriction F -> C fused with C's first sweep (x = 0, red columns). A
 // block is 32 coarse columns x nz planes, one thread per coarse cell as in
 // k_restrict; each thread also stages its cell's b and, for a red column,
-// the cell's Thomas factors and up face in shared memory. After one block
+// the cell's 1/pivot and up face in shared memory (the other Thomas factor
+// is their rounded product). After one block
 // barrier, one thread per red column runs sweep_column<ZERO>'s recurrence on
 // them (same operations, same order) and writes the column's x.
 template <class T, int MZ>
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(32 * MZ)
     k_restrict_sweep0(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
-    __shared__ T sb[MZ][32], sfi[MZ][32], sfc[MZ][32];
+    __shared__ T sb[MZ][32], sfi[MZ][32];
     __shared__ float sgu[MZ][32];
     const Geo& cg = C.g;
     const unsigned q = blockIdx.x * 32u + threadIdx.x;
@@ -134,7 +135,6 @@ __global__ void __launch_bounds__(32 * MZ)
         if (red) {
             sb[l][threadIdx.x] = sum;
             sfi[l][threadIdx.x] = C.finv[id];
-            sfc[l][threadIdx.x] = C.fcp[id];
             sgu[l][threadIdx.x] = C.gU[id];
         }
     }
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(32 * MZ)
             const T lower = k > 0 ? -(T)sgu[k - 1][threadIdx.x] : T(0);
             prev = (sb[k][threadIdx.x] - lower * prev) * sfi[k][threadIdx.x];
             v[k] = prev;
-            fcr[k] = sfc[k][threadIdx.x];
+            fcr[k] = RN<T>::mul(-(T)sgu[k][threadIdx.x], sfi[k][threadIdx.x]);  // fcp, as factor_column rounds it
         }
     }
 #pragma unroll

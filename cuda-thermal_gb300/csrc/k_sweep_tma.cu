@@ -43,10 +43,12 @@ struct Stage {
     static constexpr int ox = round((TJ + 2) * oxw);
     static constexpr int oge = round(TJ * oxw);
     static constexpr int ogn = round((TJ + 1) * TT);
-    static constexpr int full = 6 * own + ox + oge + ogn;
-    static constexpr int zero = 4 * own;
-    static constexpr unsigned tx_full = 4u * (6 * own + (TJ + 2) * oxw + TJ * oxw + (TJ + 1) * TT);
-    static constexpr unsigned tx_zero = 4u * (4 * own);
+    // own boxes: b, finv, gU (and gE, gN unless x = 0); the Thomas factor
+    // fcp is not loaded: it is -gU finv rounded once, recomputed in place
+    static constexpr int full = 5 * own + ox + oge + ogn;
+    static constexpr int zero = 3 * own;
+    static constexpr unsigned tx_full = 4u * (5 * own + (TJ + 2) * oxw + TJ * oxw + (TJ + 1) * TT);
+    static constexpr unsigned tx_zero = 4u * (3 * own);
     static_assert((own * 4) % 128 == 0, "own box must be a multiple of 128 bytes");
 };
 
@@ -81,14 +83,13 @@ __device__ __forceinline__ void issue_plane(const SweepMaps* m, float* sm, uint6
     mbar_arrive_expect_tx(bar, ZERO ? S::tx_zero : S::tx_full);
     load_3d(st, &m->b, t0, j0, l, bar);
     load_3d(st + S::own, &m->fi, t0, j0, l, bar);
-    load_3d(st + 2 * S::own, &m->fc, t0, j0, l, bar);
-    load_3d(st + 3 * S::own, &m->gu, t0, j0, l, bar);
+    load_3d(st + 2 * S::own, &m->gu, t0, j0, l, bar);
     if (!ZERO) {
-        load_3d(st + 4 * S::own, &m->ge, t0, j0, l, bar);
-        load_3d(st + 5 * S::own, &m->gn, t0, j0, l, bar);
-        load_3d(st + 6 * S::own, &m->ox, t0 - 4, j0 - 1, l, bar);
-        load_3d(st + 6 * S::own + S::ox, &m->oge, t0 - 4, j0, l, bar);
-        load_3d(st + 6 * S::own + S::ox + S::oge, &m->ogn, t0, j0 - 1, l, bar);
+        load_3d(st + 3 * S::own, &m->ge, t0, j0, l, bar);
+        load_3d(st + 4 * S::own, &m->gn, t0, j0, l, bar);
+        load_3d(st + 5 * S::own, &m->ox, t0 - 4, j0 - 1, l, bar);
+        load_3d(st + 5 * S::own + S::ox, &m->oge, t0 - 4, j0, l, bar);
+        load_3d(st + 5 * S::own + S::ox + S::oge, &m->ogn, t0, j0 - 1, l, bar);
     }
 }
 
@@ -151,9 +152,10 @@ __device__ __forceinline__ bool sweep_tiles(const SweepMaps* m, const LevelView<
                 const float* st = sm + s * stage_f;
                 if (act && got) {
                     float rhs = st[o];
-                    const float fi = st[S::own + o], fc = st[2 * S::own + o], gu = st[3 * S::own + o];
+                    const float fi = st[S::own + o], gu = st[2 * S::own + o];
+                    const float fc = __fmul_rn(-gu, fi);  // fcp as factor_column rounds it
                     if (!ZERO) {
-                        const float* ox = st + 6 * S::own;
+                        const float* ox = st + 5 * S::own;
                         const float* oge = ox + S::ox;
                         const float* ogn = oge + S::oge;
                         constexpr int W = S::oxw;
@@ -167,7 +169,7 @@ __device__ __forceinline__ bool sweep_tiles(const SweepMaps* m, const LevelView<
                         if (he) {
                             float xv = ox[(ty + 1) * W + tx + 4 + e];
                             if (PRO) xv = xv + ce;
-                            sl += st[4 * S::own + o] * xv;
+                            sl += st[3 * S::own + o] * xv;
                         }
                         if (hs) {
                             float xv = ox[ty * W + tx + 4];
@@ -177,7 +179,7 @@ __device__ __forceinline__ bool sweep_tiles(const SweepMaps* m, const LevelView<
                         if (hn) {
                             float xv = ox[(ty + 2) * W + tx + 4];
                             if (PRO) xv = xv + cn;
-                            sl += st[5 * S::own + o] * xv;
+                            sl += st[4 * S::own + o] * xv;
                         }
                         rhs = rhs + sl;
                     }
@@ -292,9 +294,10 @@ __device__ __forceinline__ bool sweep_tiles_ws(const SweepMaps* m, const LevelVi
                         const float* st = sm + s * stage_f;
                         if (act) {
                             float rhs = st[o];
-                            const float fi = st[S::own + o], fc = st[2 * S::own + o], gu = st[3 * S::own + o];
+                            const float fi = st[S::own + o], gu = st[2 * S::own + o];
+                            const float fc = __fmul_rn(-gu, fi);  // fcp as factor_column rounds it
                             if (!ZERO) {
-                                const float* ox = st + 6 * S::own;
+                                const float* ox = st + 5 * S::own;
                                 const float* oge = ox + S::ox;
                                 const float* ogn = oge + S::oge;
                                 constexpr int W = S::oxw;
@@ -307,7 +310,7 @@ __device__ __forceinline__ bool sweep_tiles_ws(const SweepMaps* m, const LevelVi
                                 if (he) {
                                     float xv = ox[(ty + 1) * W + tx + 4 + e];
                                     if (PRO) xv = xv + ce;
-                                    sl += st[4 * S::own + o] * xv;
+                                    sl += st[3 * S::own + o] * xv;
                                 }
                                 if (hs) {
                                     float xv = ox[ty * W + tx + 4];
@@ -317,7 +320,7 @@ __device__ __forceinline__ bool sweep_tiles_ws(const SweepMaps* m, const LevelVi
                                 if (hn) {
                                     float xv = ox[(ty + 2) * W + tx + 4];
                                     if (PRO) xv = xv + cn;
-                                    sl += st[5 * S::own + o] * xv;
+                                    sl += st[4 * S::own + o] * xv;
                                 }
                                 rhs = rhs + sl;
                             }
@@ -634,7 +637,6 @@ bool make_sweep_maps(const LevelView<float>& L, int color, SweepMaps* m, int til
     bool ok = true;
     ok = ok && encode_rows_map(&m->b, L.b + own, g.hx, g.ny, g.nz, g.plane, T, J);
     ok = ok && encode_rows_map(&m->fi, L.finv + own, g.hx, g.ny, g.nz, g.plane, T, J);
-    ok = ok && encode_rows_map(&m->fc, L.fcp + own, g.hx, g.ny, g.nz, g.plane, T, J);
     ok = ok && encode_rows_map(&m->gu, L.gU + own, g.hx, g.ny, g.nz, g.plane, T, J);
     ok = ok && encode_rows_map(&m->ge, L.gE + own, g.hx, g.ny, g.nz, g.plane, T, J);
     ok = ok && encode_rows_map(&m->gn, L.gN + own, g.hx, g.ny, g.nz, g.plane, T, J);

@@ -167,7 +167,7 @@ constexpr int kSweepStages = 4;  // planes in flight per block
 constexpr int kSweepStagesWs = 6;  // the same with a producer warp (no block barrier per plane)
 constexpr int kSweepWsBlocks = 3;  // resident blocks per SM the producer-warp sweeps are compiled for
 struct SweepMaps {
-    CUtensorMap b, fi, fc, gu, ge, gn;  // the sweep colour's rows, box kTileT x kTileJ
+    CUtensorMap b, fi, gu, ge, gn;      // the sweep colour's rows, box kTileT x kTileJ
     CUtensorMap ox;                     // other colour's x, box (kTileT + 8) x (kTileJ + 2)
     CUtensorMap oge;                    // other colour's gE, box (kTileT + 8) x kTileJ
     CUtensorMap ogn;                    // other colour's gN, box kTileT x (kTileJ + 1)
