@@ -363,3 +363,30 @@ def test_bounded_wait_runs_out_and_context_survives(ct):
     m = workloads.steady_hotspot(64, seed=1)
     st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX_DW)
     assert st.converged and np.isfinite(T).all()
+
+
+@pytest.mark.parametrize("cu_planes,prec", [(16, "MG_FP32_FLEX_DW"), (16, "MG_FP32"), (34, "MG_FP32_FLEX_DW"),
+                                            (34, "MG_FP64")])
+def test_deep_stacks_match_oracle(ct, orc, cu_planes, prec):
+    """Stacks deeper than the common ones: 22 planes (the 32-plane register
+    forms of the staged sweeps, the fused restrictions and the shared-memory
+    bottom) and 40 planes (past 32: the general column path, no staging),
+    on a 160 x 144 grid so level 0 is staged where it can be. Against the
+    FP64 oracle within 5e-4 K and 1e-7 of Tmax, FP64 true residual <= 1e-9."""
+    layers = [ct.Layer("Si tier 2 (bottom)", 50e-6, 130.0, 1.66e6, 2, True),
+              ct.Layer("bond + BEOL", 10e-6, 2.0, 1.70e6, 1, False),
+              ct.Layer("Si tier 1 (top)", 50e-6, 130.0, 1.66e6, 2, True),
+              ct.Layer("TIM", 25e-6, 5.0, 2.00e6, 1, False),
+              ct.Layer("Cu spreader", 1e-3, 400.0, 3.45e6, cu_planes, False)]
+    m = ct.build_model(layers, 160, 144, 10e-3, 9e-3, 2e4, 0.0)
+    ct.add_uniform_power(m, 0, 20.0)
+    ct.add_hotspot(m, 0, 3e-3, 4e-3, 1e-3, 3.0)
+    ct.add_uniform_power(m, 2, 15.0)
+    ct.finalize(m)
+    assert m.nz == 6 + cu_planes
+    ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
+    st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, getattr(ct.Precision, prec))
+    assert st.converged and not st.breakdown
+    tmax = np.abs(ref.T).max()
+    assert np.abs(T - ref.T).max() <= min(5e-4, 1e-7 * tmax)
+    assert orc.true_relres(m, T) <= 1e-9
