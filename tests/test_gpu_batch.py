@@ -283,3 +283,37 @@ def test_batch_from_device_built_specs_bitwise(ct):
     assert out[0][0] == out[1][0]
     for a, c in zip(out[0][1], out[1][1]):
         assert np.array_equal(a, c)
+
+
+def test_batch_deep_stacks_match_oracle(ct, orc):
+    """A batch mixing deep stacks (22 and 40 planes) with a common one:
+    every instance within 1e-7 * Tmax of the FP64 oracle, staged sweeps
+    forced where a level holds a full tile row."""
+    def stack(cu_planes, nx, ny):
+        layers = [ct.Layer("Si tier 2 (bottom)", 50e-6, 130.0, 1.66e6, 2, True),
+                  ct.Layer("bond + BEOL", 10e-6, 2.0, 1.70e6, 1, False),
+                  ct.Layer("Si tier 1 (top)", 50e-6, 130.0, 1.66e6, 2, True),
+                  ct.Layer("TIM", 25e-6, 5.0, 2.00e6, 1, False),
+                  ct.Layer("Cu spreader", 1e-3, 400.0, 3.45e6, cu_planes, False)]
+        m = ct.build_model(layers, nx, ny, 10e-3, 8e-3, 2e4, 0.0)
+        ct.add_uniform_power(m, 0, 20.0)
+        ct.add_hotspot(m, 0, 3e-3, 4e-3, 1e-3, 3.0)
+        ct.add_uniform_power(m, 2, 15.0)
+        ct.finalize(m)
+        return m
+    ms = [stack(16, 128, 96), stack(34, 96, 80), stack(4, 160, 128)]
+    old = _env(CT_BATCH_TMA_TILES="1")
+    try:
+        with ct.GpuBatch(ms) as b:
+            b.set_x_zero()
+            b.set_rhs_steady()
+            st = b.solve(1e-10, 50000)
+            for i, m in enumerate(ms):
+                assert st[i].converged and not st[i].breakdown, (i, st[i])
+                ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
+                T = b.get_x(i)
+                tmax = np.abs(ref.T).max()
+                assert np.abs(T - ref.T).max() <= min(DT_BOUND_K, 1e-7 * tmax), i
+                assert b.true_relres(i) <= 1.5e-10, i
+    finally:
+        _restore(old)
