@@ -32,13 +32,6 @@ __device__ __forceinline__ float2 dw_add(float2 a, float2 b) {
 
 __device__ __forceinline__ float2 dw_neg(float2 a) { return make_float2(-a.x, -a.y); }
 
-__device__ __forceinline__ float2 dw_mul_f(float2 a, float b) {
-    const float p = a.x * b;
-    float e = fmaf(a.x, b, -p);
-    e = fmaf(a.y, b, e);
-    return fast_two_sum(p, e);
-}
-
 __device__ __forceinline__ float2 dw_mul(float2 a, float2 b) {
     const float p = a.x * b.x;
     float e = fmaf(a.x, b.x, -p);
@@ -58,7 +51,8 @@ __device__ __forceinline__ double dw_d(float2 a) { return (double)a.x + (double)
 // (s, c): s collects the products' high parts through TwoSum, c the exact
 // rounding errors of the products and the sums plus the products of the low
 // parts; renormalised once at the end (fast_two_sum(s, c)). Each term costs
-// eleven FP32 operations instead of the seventeen of dw_mul_f + dw_add, with
+// eleven FP32 operations instead of the seventeen of a double-word product
+// and a double-word sum, with
 // an error of the same order (a few units of 2^-48 of the largest term).
 struct DwAcc {
     float s, c;

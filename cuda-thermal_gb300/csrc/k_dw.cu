@@ -150,62 +150,9 @@ __global__ void __launch_bounds__(NT)
 
 // ---- the iteration ------------------------------------------------------------
 
-// Ap = d p - sum G p_nbr, p.Ap, alpha.
-__global__ void __launch_bounds__(NT)
-    k_apply_dw(OpView o, const float2* __restrict__ dgw, const float2* __restrict__ p,
-               float2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
-    if (loop_done(ctl, cond)) return;
-    const Geo& g = o.g;
-    float2 acc = make_float2(0.0f, 0.0f);
-    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
-        const Col c = col_of_slot(g, s);
-        if (!c.valid) {
-            for (int l = 0; l < g.nz; ++l) Ap[(unsigned)l * g.plane + s] = make_float2(0.0f, 0.0f);
-            continue;
-        }
-        float2 p_c = p[c.s], p_b = make_float2(0.0f, 0.0f);
-        float gu_b = 0.0f;
-        for (int l = 0; l < g.nz; ++l) {
-            const unsigned base = (unsigned)l * g.plane, id = base + c.s;
-            const bool up = l < g.nz - 1;
-            const float2 p_a = up ? p[id + g.plane] : make_float2(0.0f, 0.0f);
-            const float gu = o.gU[id];
-            float2 off = make_float2(0.0f, 0.0f);
-            if (c.i > 0) off = dw_add(off, dw_mul_f(p[base + c.sw], o.gE[base + c.sw]));
-            if (c.i < g.nx - 1) off = dw_add(off, dw_mul_f(p[base + c.se], o.gE[id]));
-            if (c.j > 0) off = dw_add(off, dw_mul_f(p[base + c.ss], o.gN[base + c.ss]));
-            if (c.j < g.ny - 1) off = dw_add(off, dw_mul_f(p[base + c.sn], o.gN[id]));
-            if (l > 0) off = dw_add(off, dw_mul_f(p_b, gu_b));
-            if (up) off = dw_add(off, dw_mul_f(p_a, gu));
-            const float2 a = dw_add(dw_mul(dgw[id], p_c), dw_neg(off));
-            Ap[id] = a;
-            acc = dw_add(acc, dw_mul(p_c, a));
-            p_b = p_c;
-            p_c = p_a;
-            gu_b = gu;
-        }
-    }
-    double pap = dw_d(acc), unused = 0.0;
-    block_sum2(pap, unused);
-    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
-        double PAP, U;
-        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
-        if (threadIdx.x == 0) {
-            ctl->pAp = PAP;
-            if (!(PAP > 0.0) || !isfinite(PAP)) {
-                ctl->breakdown = 1;
-                ctl->alpha = 0.0;
-                stop_loop(ctl, cond);
-            } else {
-                ctl->alpha = ctl->rz / PAP;
-                ctl->alpha_w = dw_of(ctl->alpha);
-            }
-        }
-    }
-}
-
-// Same as k_apply_dw, one warp per row of one colour of one plane (no
-// integer division per cell), products summed with DwAcc.
+// Ap = d p - sum G p_nbr (op_apply, src/operator3d.h:108-112), p.Ap and
+// alpha: one warp per row of one colour of one plane (no integer division per
+// cell), two cells per lane, products summed with DwAcc.
 __global__ void __launch_bounds__(NT)
     k_apply_dw_rows(OpView o, const float2* __restrict__ dgw, const float2* __restrict__ p,
                     float2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
@@ -236,56 +183,6 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
-// Same as k_apply_dw, one cell per loop step instead of one column: the steps
-// are independent (no value carried from plane to plane), so consecutive
-// cells' loads overlap; vertical neighbours come from L1/L2.
-__global__ void __launch_bounds__(NT)
-    k_apply_dw_cells(OpView o, const float2* __restrict__ dgw, const float2* __restrict__ p,
-                     float2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
-    if (loop_done(ctl, cond)) return;
-    const Geo& g = o.g;
-    const unsigned n = g.plane * (unsigned)g.nz;
-    float2 acc = make_float2(0.0f, 0.0f);
-#pragma unroll 2
-    for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
-        const unsigned l = k / g.plane;
-        const unsigned s = k - l * g.plane;
-        const Col c = col_of_slot(g, s);
-        if (!c.valid) {
-            Ap[k] = make_float2(0.0f, 0.0f);
-            continue;
-        }
-        const unsigned base = l * g.plane;
-        float2 off = make_float2(0.0f, 0.0f);
-        if (c.i > 0) off = dw_add(off, dw_mul_f(p[base + c.sw], o.gE[base + c.sw]));
-        if (c.i < g.nx - 1) off = dw_add(off, dw_mul_f(p[base + c.se], o.gE[k]));
-        if (c.j > 0) off = dw_add(off, dw_mul_f(p[base + c.ss], o.gN[base + c.ss]));
-        if (c.j < g.ny - 1) off = dw_add(off, dw_mul_f(p[base + c.sn], o.gN[k]));
-        if (l > 0) off = dw_add(off, dw_mul_f(p[k - g.plane], o.gU[k - g.plane]));
-        if ((int)l < g.nz - 1) off = dw_add(off, dw_mul_f(p[k + g.plane], o.gU[k]));
-        const float2 pc = p[k];
-        const float2 a = dw_add(dw_mul(dgw[k], pc), dw_neg(off));
-        Ap[k] = a;
-        acc = dw_add(acc, dw_mul(pc, a));
-    }
-    double pap = dw_d(acc), unused = 0.0;
-    block_sum2(pap, unused);
-    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
-        double PAP, U;
-        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
-        if (threadIdx.x == 0) {
-            ctl->pAp = PAP;
-            if (!(PAP > 0.0) || !isfinite(PAP)) {
-                ctl->breakdown = 1;
-                ctl->alpha = 0.0;
-                stop_loop(ctl, cond);
-            } else {
-                ctl->alpha = ctl->rz / PAP;
-                ctl->alpha_w = dw_of(ctl->alpha);
-            }
-        }
-    }
-}
 
 // x += alpha p, r -= alpha Ap, b0 = r (hi word), ||r||^2, convergence test.
 // Two values per thread and step (float4 = two double words).
@@ -447,28 +344,8 @@ void launch_residual_x(cudaStream_t st, const OpView& o, const double* diag, con
 
 void launch_apply_dw(cudaStream_t st, const OpView& o, const float2* dgw, const float2* p,
                      float2* Ap, Ctl* ctl, const Red& red, Cond cond) {
-    // CT_APPLY=cells / columns selects the earlier forms (one cell or one
-    // column per thread); the default is one warp per row.
-    static const int form = [] {
-        const char* e = std::getenv("CT_APPLY");
-        if (e && e[0] == 'c' && e[1] == 'e') return 1;
-        if (e && e[0] == 'c' && e[1] == 'o') return 2;
-        return 0;
-    }();
-    if (form == 0) {
-        static const int wb = wave_blocks(k_apply_dw_rows, 1 << 30);
-        launch_pdl(k_apply_dw_rows, std::min(red.maxb, wb), NT, 0, st, o, dgw, p, Ap, ctl, red.part, red.maxb,
-                                                              cond);
-        return;
-    }
-    if (form == 1) {
-        static const int wb = wave_blocks(k_apply_dw_cells, 1 << 30);
-        k_apply_dw_cells<<<std::min(red.maxb, wb), NT, 0, st>>>(o, dgw, p, Ap, ctl, red.part,
-                                                               red.maxb, cond);
-        return;
-    }
-    static const int wb = wave_blocks(k_apply_dw, 1 << 30);
-    k_apply_dw<<<std::min(red.blocks, wb), NT, 0, st>>>(o, dgw, p, Ap, ctl, red.part, red.maxb, cond);
+    static const int wb = wave_blocks(k_apply_dw_rows, 1 << 30);
+    launch_pdl(k_apply_dw_rows, std::min(red.maxb, wb), NT, 0, st, o, dgw, p, Ap, ctl, red.part, red.maxb, cond);
 }
 
 void launch_update_dw(cudaStream_t st, unsigned n, const float2* p, const float2* Ap, float2* x,

@@ -14,14 +14,12 @@
 //    the fly, and the red sweep after it overwrites the red cells.
 // The arithmetic of each line solve, restriction and factorisation follows the
 // reference functions named beside them.
-#include <cooperative_groups.h>
 
 #include "kernels.h"
 #include "mg_dev.cuh"
 #include "reduce.cuh"
 #include "setup_dev.cuh"
 
-namespace cg = cooperative_groups;
 
 namespace ct {
 
@@ -160,54 +158,6 @@ __global__ void __launch_bounds__(32 * MZ)
         if (k < nz) C.x[(unsigned)k * cg.plane + cs] = v[k];
 }
 
-// The V-cycle below level k0 (all levels from k0 to the single column) in ONE
-// launch of one thread-block cluster: the phases (sweeps, restrictions, the
-// coarsest solve, prolongation-sweeps back up) are separated by cluster
-// barriers instead of kernel boundaries. Values written by other blocks of
-// the cluster (x, b) are read from L2. Every block runs the same phase
-// sequence, so all of them reach every barrier.
-template <class T, int MZ>
-__global__ void __launch_bounds__(kTailThreads, 1)
-    k_vtail(TailLevels<T> tl, const Ctl* ctl, Cond cond) {
-    if (loop_done(ctl, cond)) return;
-    cg::cluster_group cl = cg::this_cluster();
-    const unsigned tid = cl.block_rank() * kTailThreads + threadIdx.x;
-    const unsigned nth = cl.num_blocks() * kTailThreads;
-    const T inv_dt = (T)ctl->inv_dt;
-    const int last = tl.n - 1;
-    for (int k = 0; k < last; ++k) {
-        const LevelView<T>& L = tl.L[k];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true, true>(L, L, 0, q);
-        cl.sync();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true, true>(L, L, 1, q);
-        cl.sync();
-        const LevelView<T>& C = tl.L[k + 1];
-        const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
-        const unsigned work = ccols * (unsigned)C.g.nz;
-        for (unsigned w = tid; w < work; w += nth) {
-            const int l = (int)(w / ccols);
-            restrict_cell<T, true>(L, C, inv_dt, w - (unsigned)l * ccols, l);
-        }
-        cl.sync();
-    }
-    {
-        const LevelView<T>& L = tl.L[last];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, true, true>(L, L, 0, q);
-        cl.sync();
-    }
-    for (int k = last - 1; k >= 0; --k) {
-        const LevelView<T>& L = tl.L[k];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth)
-            sweep_column<T, MZ, false, true, true, true>(L, tl.L[k + 1], 1, q);
-        cl.sync();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, true, true>(L, L, 0, q);
-        cl.sync();
-    }
-}
-
 // The bottom of the V-cycle in one block from shared memory (mgdev::vsmall_body).
 template <class T, int MZ>
 __global__ void __launch_bounds__(kSmallThreads, 1)
@@ -303,68 +253,6 @@ bool launch_restrict_sweep0(cudaStream_t st, const LevelView<T>& F, const LevelV
     return true;
 }
 
-template <class T>
-int tail_cluster_size() {
-    // Largest cluster this GPU can co-schedule for the tail kernel (16 needs
-    // the non-portable opt-in; 8 is portable).
-    static int cached = 0;
-    if (cached) return cached;
-    int best = 1;
-    for (int cs : {16, 8, 4, 2}) {
-        auto k = k_vtail<T, 12>;
-        if (cs > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(cs);
-        cfg.blockDim = dim3(kTailThreads);
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = cs;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, k, &cfg) == cudaSuccess && nclusters > 0) {
-            best = cs;
-            break;
-        }
-        cudaGetLastError();
-    }
-    cached = best;
-    return best;
-}
-
-template <class T>
-cudaError_t launch_vtail(cudaStream_t st, const TailLevels<T>& tl, int cluster, const Ctl* ctl,
-                         Cond cond) {
-    int mz = 0;
-    for (int k = 0; k < tl.n; ++k) mz = tl.L[k].g.nz;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(cluster);
-    cfg.blockDim = dim3(kTailThreads);
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = cluster;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    auto pick = [&](auto kern) {
-        if (cluster > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        return cudaLaunchKernelEx(&cfg, kern, tl, ctl, cond);
-    };
-    if (mz <= 8) return pick(k_vtail<T, 8>);
-    if (mz <= 12) return pick(k_vtail<T, 12>);
-    if (mz <= 16) return pick(k_vtail<T, 16>);
-    if (mz <= 32) return pick(k_vtail<T, 32>);
-    if (cluster > 8) cudaFuncSetAttribute(k_vtail<T, 0>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    return cudaLaunchKernelEx(&cfg, k_vtail<T, 0>, tl, ctl, cond);
-}
-
 template void launch_factor<float>(cudaStream_t, const LevelView<float>&, float);
 template void launch_factor<double>(cudaStream_t, const LevelView<double>&, double);
 template void launch_sweep<float>(cudaStream_t, const LevelView<float>&, int, bool,
@@ -379,12 +267,6 @@ template bool launch_restrict_sweep0<float>(cudaStream_t, const LevelView<float>
                                             const Ctl*, Cond);
 template bool launch_restrict_sweep0<double>(cudaStream_t, const LevelView<double>&, const LevelView<double>&,
                                              const Ctl*, Cond);
-template int tail_cluster_size<float>();
-template int tail_cluster_size<double>();
-template cudaError_t launch_vtail<float>(cudaStream_t, const TailLevels<float>&, int, const Ctl*,
-                                         Cond);
-template cudaError_t launch_vtail<double>(cudaStream_t, const TailLevels<double>&, int, const Ctl*,
-                                          Cond);
 
 template <class T>
 size_t small_smem_bytes(const TailLevels<T>& tl) {

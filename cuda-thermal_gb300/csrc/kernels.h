@@ -199,16 +199,13 @@ template <class T>
 bool launch_restrict_sweep0(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,
                             Cond cond);
 
-// The levels below a threshold, run by one thread-block cluster in one launch.
+// The levels from some level down to the single column, finest first.
 constexpr int kMaxTail = 24;
-constexpr int kTailThreads = 512;
 template <class T>
 struct TailLevels {
     int n;  // levels in L, the finest of them first, the single column last
     LevelView<T> L[kMaxTail];
 };
-template <class T>
-int tail_cluster_size();
 // The smallest levels (those whose arrays together fit kSmallSmemMax bytes),
 // run by one block out of shared memory.
 constexpr int kSmallThreads = 256;
@@ -217,8 +214,5 @@ template <class T>
 size_t small_smem_bytes(const TailLevels<T>& tl);
 template <class T>
 cudaError_t launch_vsmall(cudaStream_t st, const TailLevels<T>& tl, Ctl* ctl, Cond cond);
-template <class T>
-cudaError_t launch_vtail(cudaStream_t st, const TailLevels<T>& tl, int cluster, const Ctl* ctl,
-                         Cond cond);
 
 }  // namespace ct

@@ -165,20 +165,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
             L = C;
         }
     }
-    // Levels with at most tail_cols columns run inside one thread-block
-    // cluster launch (k_vtail); CT_TAIL_COLS overrides the default.
     {
-        long tail_cols = 0;
-        if (const char* e = std::getenv("CT_TAIL_COLS")) tail_cols = std::atol(e);
-        tail_k0 = lv.size();
-        for (size_t k = 0; k < lv.size(); ++k)
-            if ((long)lv[k].g.nx * lv[k].g.ny <= tail_cols) {
-                tail_k0 = k;
-                break;
-            }
-        if (lv.size() - tail_k0 > (size_t)kMaxTail) tail_k0 = lv.size() - kMaxTail;
-        if (tail_k0 < lv.size())
-            tail_cluster = mt == MG_F64 ? tail_cluster_size<double>() : tail_cluster_size<float>();
         // The smallest levels whose arrays fit one block's shared memory.
         small_k0 = lv.size();
         long small_max = kSmallSmemMax;
@@ -191,7 +178,6 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
             if ((long)acc > small_max || lv.size() - k > (size_t)kMaxTail) break;
             small_k0 = k;
         }
-        if (small_k0 < tail_k0) tail_k0 = lv.size();  // the shared-memory kernel covers it
     }
     bytes = ar.used;
     {
@@ -364,19 +350,6 @@ void Solver::vcycle(size_t k, Cond cond, bool first_sweep_done) {
         });
         return;
     }
-    if (k == tail_k0) {
-        TailLevels<T> tl;
-        tl.n = (int)(lv.size() - k);
-        double b = 0;
-        for (int q = 0; q < tl.n; ++q) {
-            tl.L[q] = view<T>(k + q);
-            const Geo& g = tl.L[q].g;
-            b += (double)g.nx * g.ny * g.nz * (4 * sizeof(T) + 4 + 2 * sizeof(T) + 16);
-        }
-        enq(("mg_tail_l" + std::to_string(k) + "_c" + std::to_string(tail_cluster)).c_str(), b,
-            [&] { launch_vtail<T>(cs, tl, tail_cluster, ctl, cond); });
-        return;
-    }
     const LevelView<T> L = view<T>(k);
     const double cells = (double)L.g.nx * L.g.ny * L.g.nz;
     const double t = (double)sizeof(T);
@@ -394,11 +367,11 @@ void Solver::vcycle(size_t k, Cond cond, bool first_sweep_done) {
         enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
     enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { sweep<T>(k, L, 1, false, nullptr, cond); });
     // The coarse level's first sweep rides along with the restriction unless
-    // a whole-tail kernel (shared-memory bottom, cluster tail) starts there,
+    // the shared-memory bottom starts there,
     // or the restriction is from the finest level: there it is bandwidth
     // bound, and the block's serial line-solve tail costs more (measured at
     // 800 x 800: 78 us fused against 51 + 13 us) than the launch it saves.
-    const bool fuse = fuse_sweep0 && k > 0 && k + 1 != small_k0 && k + 1 != tail_k0 && L.g.nz <= 32;
+    const bool fuse = fuse_sweep0 && k > 0 && k + 1 != small_k0 && L.g.nz <= 32;
     const double b_restrict = cells * (2 * t + 16) + cells / 4 * t;
     const double cc = (double)C.g.nx * C.g.ny * C.g.nz;
     if (fuse)

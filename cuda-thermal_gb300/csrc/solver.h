@@ -81,10 +81,8 @@ class Solver {
     double inv_dt = 0;
     bool use_graphs = true;
     bool have_cond = false;
-    size_t tail_k0 = 0;    // levels from tail_k0 down run in one cluster launch
     size_t small_k0 = 0;   // levels from small_k0 down run in one block from shared memory
     bool fuse_sweep0 = true;  // a level's first (x = 0) sweep rides with the restriction into it
-    int tail_cluster = 1;  // CTAs in that cluster
     cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
     ct_setup_times times{};
     // per-kernel timing (ct_profile_solve)
