@@ -440,35 +440,47 @@ __device__ __forceinline__ bool vsmall_body(const TailLevels<T>& tl, T inv_dt,
     // in shared memory, where the sweeps also store x through generic
     // pointers, so reading them in place would reload every field after
     // every store.
-    for (int k = 0; k < last; ++k) {
-        const LevelView<T> L = sl.L[k];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false, true>(L, L, 0, q);
-        __syncthreads();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false, true>(L, L, 1, q);
-        __syncthreads();
-        const LevelView<T> C = sl.L[k + 1];
-        const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
-        const unsigned work = ccols * (unsigned)C.g.nz;
-        for (unsigned w = tid; w < work; w += nth) {
-            const int l = (int)(w / ccols);
-            restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
+    // The phases in V-cycle order, driven by one loop so that each kind of
+    // phase (x = 0 sweep, sweep, restriction, prolongating sweep) is one
+    // code region, warm in the instruction cache after its first use: down
+    // the levels k < last (red x = 0 sweep, black sweep, restriction), the
+    // single column (x = 0 sweep), back up (black sweep with the coarse
+    // correction, red sweep).
+    const int nph = 3 * last + 1 + 2 * last;
+    for (int ph = 0; ph < nph; ++ph) {
+        int k, kind;  // kind: 0 x = 0 sweep, 1 sweep, 2 restriction, 3 prolongating sweep
+        int color = 0;
+        if (ph < 3 * last) {
+            k = ph / 3;
+            kind = ph - 3 * k;
+            color = kind == 1 ? 1 : 0;
+        } else if (ph == 3 * last) {
+            k = last;
+            kind = 0;
+        } else {
+            const int u = ph - 3 * last - 1;
+            k = last - 1 - u / 2;
+            kind = (u & 1) ? 1 : 3;
+            color = (u & 1) ? 0 : 1;
         }
-        __syncthreads();
-    }
-    {
-        const LevelView<T> L = sl.L[last];
-        const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false, true>(L, L, 0, q);
-        __syncthreads();
-    }
-    for (int k = last - 1; k >= 0; --k) {
         const LevelView<T> L = sl.L[k];
-        const LevelView<T> C = sl.L[k + 1];
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false, true>(L, C, 1, q);
-        __syncthreads();
-        for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false, true>(L, L, 0, q);
+        if (kind == 0) {
+            for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false, true>(L, L, 0, q);
+        } else if (kind == 1) {
+            for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false, true>(L, L, color, q);
+        } else if (kind == 2) {
+            const LevelView<T> C = sl.L[k + 1];
+            const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
+            const unsigned work = ccols * (unsigned)C.g.nz;
+            for (unsigned w = tid; w < work; w += nth) {
+                const int l = (int)(w / ccols);
+                restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
+            }
+        } else {
+            const LevelView<T> C = sl.L[k + 1];
+            for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false, true>(L, C, 1, q);
+        }
         __syncthreads();
     }
     const LevelView<T> S0 = sl.L[0];
