@@ -430,8 +430,9 @@ def bench_transient_batched(ct, np, args, steps):
     for k in range(steps):
         for i, w in enumerate(ws):
             if w.advance(t[i]):
-                b.set_power(i, w.power())
-                ptot[i] = ws[i].power().sum()
+                P = w.power()
+                b.set_power(i, P)
+                ptot[i] = P.sum()
                 dt[i] = TR_DT0
                 switches += 1
         st = b.step_transient(dt, TR_TOL, MAXIT)

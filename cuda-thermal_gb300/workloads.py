@@ -195,12 +195,15 @@ class Switching:
         self.toggles = toggles    # list of sorted toggle times (s), one per block
         self.on = list(on)        # block states at t = 0
         self._next = [0] * len(maps)
+        # each block's nonzero cells: summing only those, block by block in
+        # the same order, gives the dense sum's bits (adding 0.0 changes nothing)
+        self._sparse = [(np.flatnonzero(m), m[np.flatnonzero(m)]) for m in maps]
 
     def power(self) -> np.ndarray:
         P = np.zeros(self.model.ncells())
-        for b, m in enumerate(self.maps):
+        for b, (idx, vals) in enumerate(self._sparse):
             if self.on[b]:
-                P += m
+                P[idx] += vals
         return P
 
     def advance(self, t: float) -> bool:
