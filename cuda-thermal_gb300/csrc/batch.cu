@@ -909,6 +909,11 @@ ct_status ct_batch_set_power(ct_batch* b, int i, const double* P) {
     return ct_set_power(b->impl.sv[(size_t)i].get(), P);
 }
 
+ct_status ct_batch_set_power_device(ct_batch* b, int i, const double* P_dev) {
+    CT_BATCH_INST(b, i);
+    return ct_set_power_device(b->impl.sv[(size_t)i].get(), P_dev);
+}
+
 ct_status ct_batch_set_x(ct_batch* b, int i, const double* T) {
     CT_BATCH_INST(b, i);
     return ct_set_x(b->impl.sv[(size_t)i].get(), T);

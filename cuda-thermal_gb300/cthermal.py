@@ -120,6 +120,7 @@ def _signatures():
         "ct_batch_set_rhs_steady": (i, [vp]),
         "ct_batch_set_rhs_transient": (i, [vp]),
         "ct_batch_set_power": (i, [vp, i, vp]),
+        "ct_batch_set_power_device": (i, [vp, i, vp]),
         "ct_batch_solve": (i, [vp, d, i, vp]),
         "ct_batch_step_transient": (i, [vp, vp, d, i, vp]),
         "ct_batch_get_x": (i, [vp, i, vp]),
@@ -844,6 +845,11 @@ class GpuBatch:
         P = np.ascontiguousarray(P, np.float64)
         assert P.size == self.models[i].ncells()
         _check(lib().ct_batch_set_power(self._h, int(i), _ptr(P)))
+
+    def set_power_device(self, i, ptr: int):
+        """Instance i's power map from device memory (natural layout, ncells
+        doubles), ordered on the batch's stream."""
+        _check(lib().ct_batch_set_power_device(self._h, int(i), C.c_void_p(ptr)))
 
     @staticmethod
     def _stats(arr):

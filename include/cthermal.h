@@ -234,6 +234,9 @@ ct_status ct_batch_set_x(ct_batch* b, int i, const double* T);
 ct_status ct_batch_set_rhs_steady(ct_batch* b);
 ct_status ct_batch_set_rhs_transient(ct_batch* b);
 ct_status ct_batch_set_power(ct_batch* b, int i, const double* P);
+/* The same from device memory (natural layout, ncells doubles), ordered on
+ * the batch's stream (ct_batch_stream). */
+ct_status ct_batch_set_power_device(ct_batch* b, int i, const double* P_dev);
 /* Solves every instance to its own relres < tol (or maxit); stats[i] per
  * instance (stats may be NULL). Returns CT_BREAKDOWN / CT_NOT_CONVERGED if
  * any instance did. */

@@ -317,3 +317,29 @@ def test_batch_deep_stacks_match_oracle(ct, orc):
                 assert b.true_relres(i) <= 1.5e-10, i
     finally:
         _restore(old)
+
+
+def test_batch_power_from_device_memory(ct, mixed):
+    """ct_batch_set_power_device: power maps handed over in device memory
+    give the host-array path's results bit for bit."""
+    import torch
+    out = []
+    for dev in (False, True):
+        with ct.GpuBatch(mixed) as b:
+            keep = []
+            for i, m in enumerate(mixed):
+                P = np.asarray(m.P, np.float64) * 1.25
+                if dev:
+                    t = torch.from_numpy(P).cuda()
+                    keep.append(t)
+                    torch.cuda.synchronize()
+                    b.set_power_device(i, t.data_ptr())
+                else:
+                    b.set_power(i, P)
+            b.set_x_zero()
+            b.set_rhs_steady()
+            st = b.solve(1e-10, 50000)
+            out.append(([s.iters for s in st], [b.get_x(i) for i in range(len(mixed))]))
+    assert out[0][0] == out[1][0]
+    for a, c in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, c)
