@@ -340,6 +340,25 @@ __device__ __forceinline__ T restrict_sum(const LevelView<T>& F, T inv_dt, int I
     return sum;
 }
 
+// Coarse cell q = J cnx + I of the planes l and l + 1 (when it exists):
+// both sums before either store, so the shared vertical operands are loaded
+// once.
+template <class T, bool CG>
+__device__ __forceinline__ void restrict_pair(const LevelView<T>& F, const LevelView<T>& C, T inv_dt,
+                                              unsigned q, int l) {
+    const Geo& cg = C.g;
+    const int J = (int)(q / (unsigned)cg.nx), I = (int)(q - (unsigned)J * cg.nx);
+    const unsigned cs = scol(cg, I, J);
+    const T s0 = restrict_sum<T, CG>(F, inv_dt, I, J, l);
+    if (l + 1 < cg.nz) {
+        const T s1 = restrict_sum<T, CG>(F, inv_dt, I, J, l + 1);
+        C.b[(unsigned)l * cg.plane + cs] = s0;
+        C.b[(unsigned)(l + 1) * cg.plane + cs] = s1;
+    } else {
+        C.b[(unsigned)l * cg.plane + cs] = s0;
+    }
+}
+
 // The same stored as coarse b; q = J cnx + I.
 template <class T, bool CG>
 __device__ __forceinline__ void restrict_cell(const LevelView<T>& F, const LevelView<T>& C,
