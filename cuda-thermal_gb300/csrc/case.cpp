@@ -505,6 +505,25 @@ ct_status ct_case_new(const ct_layer* layers, int nlayers, double Lx, double Ly,
     return CT_OK;
 }
 
+ct_status ct_case_set_name(ct_case* c, int kind, int k, const char* name) {
+    if (!c || !name) return fail(CT_BAD_ARG, "ct_case_set_name: null argument");
+    if (kind == 0 && k >= 0 && k < (int)c->layers.size()) {
+        c->layers[(size_t)k].name = name;
+        return CT_OK;
+    }
+    if (kind == 1 && k >= 0 && k < (int)c->blocks.size()) {
+        c->blocks[(size_t)k].name = name;
+        return CT_OK;
+    }
+    return fail(CT_BAD_ARG, "ct_case_set_name: no %s %d", kind == 0 ? "layer" : "block", k);
+}
+
+ct_status ct_case_set_ambient(ct_case* c, double T_amb) {
+    if (!c) return fail(CT_BAD_ARG, "ct_case_set_ambient: null case");
+    c->T_amb = T_amb;
+    return CT_OK;
+}
+
 ct_status ct_case_add_block(ct_case* c, int layer, double x0, double y0, double w, double h,
                             double watts) {
     if (!c || layer < 0 || layer >= (int)c->layers.size())

@@ -2,7 +2,9 @@
 // C ABI: the classes and functions of src/stack3d.h (model), src/pcg3d.h
 // (GpuPcg, gpu_pcg, true_relres, gpu_use_graphs, gpu_last_setup) and
 // src/transient3d.h (run_transient), with the same names and meaning, so code
-// written against the reference's headers compiles against this one.
+// written against the reference's headers compiles against this one; and the
+// case files of src/case3d.h (CaseSpec, load_case, build_case_model,
+// export_3dice).
 //
 // Differences from the reference, all deliberate:
 //  - errors throw cthermal::Error (a std::runtime_error carrying the
@@ -381,9 +383,121 @@ TransientResult run_transient(const Model3D& m, const TransientOptions& o) {
     return res;
 }
 
+// ---- cases (src/case3d.h) ----------------------------------------------------
+
+struct PowerBlock {
+    std::string name;
+    int layer;
+    double x0, y0, w, h;  // m
+    double watts;
+};
+
+struct TsvRegion {
+    int layer;
+    double x0, y0, w, h;  // m
+    double fraction;
+};
+
+struct CaseSpec {
+    std::vector<Layer> layers;
+    std::vector<PowerBlock> blocks;
+    std::vector<TsvRegion> tsvs;
+    double Lx = 10e-3, Ly = 10e-3;
+    double h_top = 2e4, h_bot = 0.0;
+    double T_amb = 25.0;
+};
+
+namespace detail {
+struct CaseHandle {
+    ct_case* c = nullptr;
+    ~CaseHandle() {
+        if (c) ct_case_destroy(c);
+    }
+};
+}  // namespace detail
+
+// load_case (src/case3d.h:86-156): false with the reference's message in err
+// on a bad case.
+inline bool load_case(const std::string& dir, CaseSpec& cs, std::string& err) {
+    detail::CaseHandle h;
+    if (ct_case_load(dir.c_str(), &h.c) != CT_OK) {
+        err = ct_last_error();
+        return false;
+    }
+    int nl = 0, nb = 0, nt = 0;
+    cs = CaseSpec{};
+    check(ct_case_info(h.c, &nl, &nb, &nt, &cs.Lx, &cs.Ly, &cs.h_top, &cs.h_bot, &cs.T_amb));
+    char name[256];
+    for (int k = 0; k < nl; ++k) {
+        ct_layer v;
+        check(ct_case_layer(h.c, k, &v, name, (int)sizeof name));
+        cs.layers.push_back(Layer{name, v.thickness, v.k, v.rho_c, v.ncells, v.active != 0});
+    }
+    for (int k = 0; k < nb; ++k) {
+        PowerBlock b;
+        double rect[4];
+        check(ct_case_block(h.c, k, &b.layer, rect, &b.watts, name, (int)sizeof name));
+        b.name = name;
+        b.x0 = rect[0], b.y0 = rect[1], b.w = rect[2], b.h = rect[3];
+        cs.blocks.push_back(b);
+    }
+    for (int k = 0; k < nt; ++k) {
+        TsvRegion t;
+        double rect[4];
+        check(ct_case_tsv(h.c, k, &t.layer, rect, &t.fraction));
+        t.x0 = rect[0], t.y0 = rect[1], t.w = rect[2], t.h = rect[3];
+        cs.tsvs.push_back(t);
+    }
+    return true;
+}
+
+// build_case_model (src/case3d.h:158-168).
+inline Model3D build_case_model(const CaseSpec& cs, int nx, int ny, bool with_tsv = true) {
+    Model3D m = build_model(cs.layers, nx, ny, cs.Lx, cs.Ly, cs.h_top, cs.h_bot);
+    m.T_amb = cs.T_amb;
+    for (const PowerBlock& b : cs.blocks) add_power_block(m, b.layer, b.x0, b.y0, b.w, b.h, b.watts);
+    if (with_tsv)
+        for (const TsvRegion& t : cs.tsvs) add_tsv_region(m, t.layer, t.x0, t.y0, t.w, t.h, t.fraction);
+    finalize(m);
+    return m;
+}
+
+// export_3dice (src/case3d.h:266-383): false with the reference's message in
+// err when 3D-ICE cannot express the case.
+inline bool export_3dice(const CaseSpec& cs, double cell_um, const std::string& outdir, std::string& err) {
+    std::vector<ct_layer> ls;
+    for (const Layer& L : cs.layers) ls.push_back(ct_layer{L.thickness, L.k, L.rho_c, L.ncells, L.active ? 1 : 0});
+    detail::CaseHandle h;
+    ct_status s = ct_case_new(ls.data(), (int)ls.size(), cs.Lx, cs.Ly, cs.h_top, cs.h_bot, &h.c);
+    for (size_t k = 0; s == CT_OK && k < cs.layers.size(); ++k)
+        s = ct_case_set_name(h.c, 0, (int)k, cs.layers[k].name.c_str());
+    for (size_t k = 0; s == CT_OK && k < cs.blocks.size(); ++k) {
+        const PowerBlock& b = cs.blocks[k];
+        s = ct_case_add_block(h.c, b.layer, b.x0, b.y0, b.w, b.h, b.watts);
+        if (s == CT_OK) s = ct_case_set_name(h.c, 1, (int)k, b.name.c_str());
+    }
+    for (size_t k = 0; s == CT_OK && k < cs.tsvs.size(); ++k) {
+        const TsvRegion& t = cs.tsvs[k];
+        s = ct_case_add_tsv(h.c, t.layer, t.x0, t.y0, t.w, t.h, t.fraction);
+    }
+    if (s == CT_OK) s = ct_case_set_ambient(h.c, cs.T_amb);
+    if (s == CT_OK) s = ct_case_export_3dice(h.c, cell_um, outdir.c_str());
+    if (s != CT_OK) {
+        err = ct_last_error();
+        return false;
+    }
+    return true;
+}
+
 }  // namespace cthermal
 
 #ifndef CTHERMAL_NO_GLOBAL_NAMES
+using cthermal::build_case_model;
+using cthermal::CaseSpec;
+using cthermal::export_3dice;
+using cthermal::load_case;
+using cthermal::PowerBlock;
+using cthermal::TsvRegion;
 using cthermal::add_hotspot;
 using cthermal::add_power_block;
 using cthermal::add_tsv_region;

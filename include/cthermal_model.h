@@ -96,6 +96,10 @@ ct_status ct_case_add_block(ct_case* c, int layer, double x0, double y0, double 
                             double watts);
 ct_status ct_case_add_tsv(ct_case* c, int layer, double x0, double y0, double w, double h,
                           double fraction);
+/* Names of a case built in code (kind 0: layer k, kind 1: block k; they
+ * appear in the 3D-ICE export) and its ambient temperature (C). */
+ct_status ct_case_set_name(ct_case* c, int kind, int k, const char* name);
+ct_status ct_case_set_ambient(ct_case* c, double T_amb);
 ct_status ct_case_info(const ct_case* c, int* nlayers, int* nblocks, int* ntsvs, double* Lx,
                        double* Ly, double* h_top, double* h_bot, double* T_amb);
 /* Layer k (bottom to top) and its name (at most name_cap bytes with the NUL). */
