@@ -154,6 +154,8 @@ def _signatures():
         "ct_case_block": (i, [vp, i, ip, dp, dp, C.c_char_p, i]),
         "ct_case_tsv": (i, [vp, i, ip, dp, dp]),
         "ct_case_export_3dice": (i, [vp, C.c_double, C.c_char_p]),
+        "ct_case_set_name": (i, [vp, i, i, C.c_char_p]),
+        "ct_case_set_ambient": (i, [vp, C.c_double]),
         "ct_selftest_bounded_wait": (i, [C.c_uint, ip]),
         "ct_eff_kz": (d, [d, d, d]),
         "ct_eff_kxy": (d, [d, d, d]),
@@ -458,13 +460,20 @@ def selftest_bounded_wait(polls: int) -> bool:
     return bool(t.value)
 
 
-def export_3dice(folder: str, cell_um: float, outdir: str) -> None:
-    """export_3dice (src/case3d.h:266-383) of the case in `folder` on a grid of
-    cell_um micrometres: case.stk, L<k>.flp and LT<k>_<p>.lay in the existing
-    folder outdir (3D-ICE 4.0 input). Raises CtError with the reference's
-    message when 3D-ICE cannot express the case."""
+def export_3dice(case, cell_um: float, outdir: str) -> None:
+    """export_3dice (src/case3d.h:266-383) of a case (a folder of CSV files or
+    a CaseSpec) on a grid of cell_um micrometres: case.stk, L<k>.flp and
+    LT<k>_<p>.lay in the existing folder outdir (3D-ICE 4.0 input). Raises
+    CtError with the reference's message when 3D-ICE cannot express the case."""
+    if isinstance(case, CaseSpec):
+        h = _CaseHandle(case)
+        try:
+            _check(lib().ct_case_export_3dice(h.h, float(cell_um), os.fsencode(outdir)))
+        finally:
+            h.close()
+        return
     h = C.c_void_p()
-    _check(lib().ct_case_load(os.fsencode(folder), C.byref(h)))
+    _check(lib().ct_case_load(os.fsencode(case), C.byref(h)))
     try:
         _check(lib().ct_case_export_3dice(h, float(cell_um), os.fsencode(outdir)))
     finally:
@@ -495,10 +504,14 @@ class _CaseHandle:
         h = C.c_void_p()
         _check(lib().ct_case_new(arr, len(cs.layers), cs.Lx, cs.Ly, cs.h_top, cs.h_bot, C.byref(h)))
         self.h = h
-        for b in cs.blocks:
+        for k, L in enumerate(cs.layers):
+            _check(lib().ct_case_set_name(h, 0, k, L.name.encode()))
+        for k, b in enumerate(cs.blocks):
             _check(lib().ct_case_add_block(h, b.layer, b.x0, b.y0, b.w, b.h, b.watts))
+            _check(lib().ct_case_set_name(h, 1, k, b.name.encode()))
         for t in cs.tsvs:
             _check(lib().ct_case_add_tsv(h, t.layer, t.x0, t.y0, t.w, t.h, t.fraction))
+        _check(lib().ct_case_set_ambient(h, cs.T_amb))
 
     def close(self):
         if self.h:

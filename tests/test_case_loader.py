@@ -174,3 +174,17 @@ def test_read_3dice_tmap_and_transient_csv(ct, tmp_path):
     assert lines[0] == "t_s,dt_s,pcg_iters,T_max_C,heat_out_W,heat_stored_W"
     assert lines[1] == "1.000000e-05,1.000000e-05,7,26.250000,10.000000,40.000000"
     assert lines[2] == "2.100000e-05,1.100000e-05,6,27.500000,11.000000,39.000000"
+
+
+def test_export_3dice_from_case_spec(ct, tmp_path):
+    """A CaseSpec (here the one loaded from the folder) exports the same files
+    as the folder itself: names and ambient travel with it."""
+    folder = case_dir("validate_tsv")
+    a, b = tmp_path / "a", tmp_path / "b"
+    a.mkdir()
+    b.mkdir()
+    ct.export_3dice(folder, 100.0, str(a))
+    ct.export_3dice(ct.load_case(folder), 100.0, str(b))
+    assert sorted(os.listdir(a)) == sorted(os.listdir(b))
+    for name in os.listdir(a):
+        assert (a / name).read_text() == (b / name).read_text(), name
