@@ -132,16 +132,18 @@ class ClockSampler:
 
 
 def dist_setup(n_gpus):
+    """One process per GPU (RANK / LOCAL_RANK / WORLD_SIZE from the launcher):
+    NCCL between GPU ranks, gloo when there is no GPU (the host-side logic
+    of the multi-rank path is tested that way)."""
     import torch
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local if world > 1 else 0)
     if world > 1:
         import torch.distributed as td
-        torch.cuda.set_device(local)
-        td.init_process_group("nccl")
-    else:
-        torch.cuda.set_device(0)
+        td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world, local
 
 
@@ -151,24 +153,26 @@ def barrier(world):
         td.barrier()
 
 
-def max_over_ranks(v, world):
+def _reduce(v, world, op):
+    """v reduced over the ranks (a plain float; on the GPU under NCCL)."""
     if world == 1:
         return v
     import torch
     import torch.distributed as td
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    td.all_reduce(t, op=td.ReduceOp.MAX)
+    dev = "cuda" if td.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    td.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(v, world):
+    import torch.distributed as td
+    return _reduce(v, world, td.ReduceOp.MAX)
 
 
 def sum_over_ranks(v, world):
-    if world == 1:
-        return v
-    import torch
     import torch.distributed as td
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    td.all_reduce(t, op=td.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(v, world, td.ReduceOp.SUM)
 
 
 def timed_solves(ct, solver, k, world):
