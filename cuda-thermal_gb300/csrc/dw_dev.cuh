@@ -79,6 +79,86 @@ __device__ __forceinline__ void acc_mul(DwAcc& a, float2 u, float2 v) {
     acc_add(a, h, fmaf(u.x, v.y, fmaf(u.y, v.x, fmaf(u.x, v.x, -h))));
 }
 
+// ---- block and grid sums of accumulators ----------------------------------------
+// The fixed trees of block_sum2 / gather2 (reduce.cuh) on the FP32 pipe: each
+// step adds another thread's (s, c) with acc_add (TwoSum on s, c collecting
+// the errors), and only thread 0 converts the block's or the grid's total to
+// FP64. Summing every thread's value in FP64 instead cost each block about a
+// microsecond of FP64 adds and conversions at its end, with the memory
+// system idle.
+__device__ __forceinline__ void warp_sum_acc(DwAcc& a) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s = __shfl_down_sync(0xffffffffu, a.s, o);
+        const float c = __shfl_down_sync(0xffffffffu, a.c, o);
+        acc_add(a, s, c);
+    }
+}
+
+// Block sum of (a, b) over NTH threads (at most 32 warps); valid in thread 0.
+template <int NTH = NT>
+__device__ __forceinline__ void block_sum_acc2(DwAcc& a, DwAcc& b) {
+    constexpr int NW = NTH / 32;
+    static_assert(NTH % 32 == 0 && NW <= 32, "whole warps, at most 32");
+    __shared__ float2 sa[NW], sb[NW];
+    warp_sum_acc(a);
+    warp_sum_acc(b);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sa[w] = make_float2(a.s, a.c);
+        sb[w] = make_float2(b.s, b.c);
+    }
+    __syncthreads();
+    if (w == 0) {
+        const float2 u = lane < NW ? sa[lane] : make_float2(0.0f, 0.0f);
+        const float2 v = lane < NW ? sb[lane] : make_float2(0.0f, 0.0f);
+        a = DwAcc{u.x, u.y};
+        b = DwAcc{v.x, v.y};
+        warp_sum_acc(a);
+        warp_sum_acc(b);
+    }
+}
+
+__device__ __forceinline__ double acc_value(const DwAcc& a) { return (double)a.s + (double)a.c; }
+
+// Publishes the block's (a, b) (valid in thread 0) as float pairs in slots
+// blockIdx.x and maxb + blockIdx.x of part, takes a ticket, and returns in
+// every thread whether this block arrived last of `count`.
+__device__ __forceinline__ bool publish_acc2(const DwAcc& a, const DwAcc& b, double* part, int maxb,
+                                             unsigned slot, unsigned* ticket, unsigned count) {
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        float2* pp = reinterpret_cast<float2*>(part);
+        pp[slot] = make_float2(a.s, a.c);
+        pp[maxb + slot] = make_float2(b.s, b.c);
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        last = (t == count - 1u) ? 1 : 0;
+    }
+    __syncthreads();
+    return last != 0;
+}
+
+// In the last block: the totals of slots [first, first + count), in slot
+// order through the same tree, as FP64 in thread 0. Resets the ticket.
+template <int NTH = NT>
+__device__ __forceinline__ void gather_acc2(const double* part, int maxb, unsigned first, unsigned count,
+                                            unsigned* ticket, double& A, double& B) {
+    __threadfence();
+    const float2* pp = reinterpret_cast<const float2*>(part);
+    DwAcc a = {0.0f, 0.0f}, b = {0.0f, 0.0f};
+    for (unsigned k = threadIdx.x; k < count; k += NTH) {
+        const float2 u = __ldcg(pp + first + k), v = __ldcg(pp + maxb + first + k);
+        acc_add(a, u.x, u.y);
+        acc_add(b, v.x, v.y);
+    }
+    block_sum_acc2<NTH>(a, b);
+    if (threadIdx.x == 0) {
+        A = acc_value(a);
+        B = acc_value(b);
+        *ticket = 0u;
+    }
+}
+
 // ---- streaming ranges of value pairs ------------------------------------------
 // Items k = k0, k0 + stride, ... < end; each item is a pair of values (float4
 // = two double words). kU items are loaded before any is used, so a thread

@@ -169,11 +169,11 @@ __global__ void __launch_bounds__(AT * AR)
         }
         return;
     }
-    double v = (double)pap.s + (double)pap.c, unused = 0.0;
-    block_sum2(v, unused);
-    if (publish2(v, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
+    DwAcc unused = {0.0f, 0.0f};
+    block_sum_acc2(pap, unused);
+    if (publish_acc2(pap, unused, part, maxb, blockIdx.x, &ctl->ticket[SL_APPLY], gridDim.x)) {
         double PAP, U;
-        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
+        gather_acc2(part, maxb, 0u, gridDim.x, &ctl->ticket[SL_APPLY], PAP, U);
         if (threadIdx.x == 0) {
             ctl->pAp = PAP;
             if (!(PAP > 0.0) || !isfinite(PAP)) {

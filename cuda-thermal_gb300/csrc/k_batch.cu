@@ -64,6 +64,18 @@ __device__ __forceinline__ void gather_inst(const BRed& red, int ntasks, int ins
     }
 }
 
+// The same for double-word accumulators (float pairs in the same slots),
+// summed on the FP32 pipe.
+__device__ __forceinline__ bool publish_inst_acc(const DwAcc& a, const DwAcc& b, const BRed& red, int ntasks,
+                                                 int inst, int count) {
+    return publish_acc2(a, b, red.part, ntasks, blockIdx.x, &red.tickets[inst], (unsigned)count);
+}
+
+__device__ __forceinline__ void gather_inst_acc(const BRed& red, int ntasks, int inst, int first, int count,
+                                                double& A, double& B) {
+    gather_acc2(red.part, ntasks, (unsigned)first, (unsigned)count, &red.tickets[inst], A, B);
+}
+
 // Start of every loop body: ends the loop once no instance is active, and
 // bounds the number of bodies.
 __global__ void kb_guard(BCtl* bc, Cond cond) {
@@ -205,11 +217,11 @@ __global__ void __launch_bounds__(NT)
         else
             apply_row<U>(o, dgw, pv, Ap, R, lane, pacc);
     }
-    double pap = (double)pacc.s + (double)pacc.c, unused = 0.0;
-    block_sum2(pap, unused);
-    if (publish_inst(pap, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
+    DwAcc unused = {0.0f, 0.0f};
+    block_sum_acc2(pacc, unused);
+    if (publish_inst_acc(pacc, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double PAP, unused2;
-        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], PAP, unused2);
+        gather_inst_acc(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], PAP, unused2);
         if (threadIdx.x == 0) {
             c->pAp = PAP;
             if (!(PAP > 0.0) || !isfinite(PAP)) {
@@ -237,11 +249,11 @@ __global__ void __launch_bounds__(NT)
                  reinterpret_cast<const float4*>(bi[t.inst].Ap),
                  reinterpret_cast<float4*>(bi[t.inst].xw), reinterpret_cast<float4*>(bi[t.inst].r),
                  reinterpret_cast<float2*>(bi[t.inst].b0), acc);
-    double rr = (double)acc.s + (double)acc.c, unused = 0.0;
-    block_sum2(rr, unused);
-    if (publish_inst(rr, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
+    DwAcc unused = {0.0f, 0.0f};
+    block_sum_acc2(acc, unused);
+    if (publish_inst_acc(acc, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RR, U;
-        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], RR, U);
+        gather_inst_acc(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], RR, U);
         if (threadIdx.x == 0) {
             c->rr = RR;
             c->iter += 1;
@@ -272,11 +284,10 @@ __global__ void __launch_bounds__(NT)
     dot_range(t.begin + threadIdx.x, t.end, NT, reinterpret_cast<const float4*>(bi[t.inst].r),
               reinterpret_cast<const float2*>(bi[t.inst].z),
               reinterpret_cast<const float4*>(bi[t.inst].Ap), rz, zap);
-    double RZ0 = (double)rz.s + (double)rz.c, ZAP0 = (double)zap.s + (double)zap.c;
-    block_sum2(RZ0, ZAP0);
-    if (publish_inst(RZ0, ZAP0, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
+    block_sum_acc2(rz, zap);
+    if (publish_inst_acc(rz, zap, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RZ, ZAP;
-        gather_inst(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], RZ, ZAP);
+        gather_inst_acc(red, p.ntasks, t.inst, p.inst_first[t.inst], p.inst_count[t.inst], RZ, ZAP);
         if (threadIdx.x == 0) {
             c->beta = c->iter > 0 ? -ZAP / c->pAp : 0.0;
             c->beta_w = dw_of(c->beta);
@@ -433,7 +444,8 @@ __global__ void __launch_bounds__(kSmallThreads, 1)
     Ctl* c = &ctl[i];
     if (inst_done(c)) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    if (!vsmall_body<float, MZ>(small[i], (float)c->inv_dt, smem) && threadIdx.x == 0) {
+    if (vsmall_body<float, MZ>(small[i], &c->inv_dt, smem, [] {}, [] { return true; }) == kSmallTimeout &&
+        threadIdx.x == 0) {
         // a bounded wait ran out: record it and stop this instance
         atomicExch(&c->err, 1);
         c->breakdown = 1;

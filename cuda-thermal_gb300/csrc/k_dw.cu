@@ -9,8 +9,9 @@
 // (TwoSum, Fast2Sum, FMA-based TwoProd; Joldes, Muller and Popescu, "Tight
 // and rigorous error bounds for basic building blocks of double-word
 // arithmetic", 2017), which carry ~48 significant bits. Dot products are
-// accumulated in double words per thread and in FP64 per block; alpha and beta
-// stay FP64 scalars on the device.
+// accumulated in double words per thread, per block and over the grid (on the
+// FP32 pipe; only the grid's total is converted); alpha and beta stay FP64
+// scalars on the device.
 //
 // Two limits of 48 bits, and how they are lifted:
 //  - the recurrence residual drifts from the true residual by ~2^-48 times the
@@ -164,11 +165,11 @@ __global__ void __launch_bounds__(NT)
     DwAcc acc = {0.0f, 0.0f};
     for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows; R += gridDim.x * (NT / 32))
         apply_row<2>(o, dgw, p, Ap, R, lane, acc);
-    double pap = (double)acc.s + (double)acc.c, unused = 0.0;
-    block_sum2(pap, unused);
-    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
+    DwAcc unused = {0.0f, 0.0f};
+    block_sum_acc2(acc, unused);
+    if (publish_acc2(acc, unused, part, maxb, blockIdx.x, &ctl->ticket[SL_APPLY], gridDim.x)) {
         double PAP, U;
-        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
+        gather_acc2(part, maxb, 0u, gridDim.x, &ctl->ticket[SL_APPLY], PAP, U);
         if (threadIdx.x == 0) {
             ctl->pAp = PAP;
             if (!(PAP > 0.0) || !isfinite(PAP)) {
@@ -195,11 +196,11 @@ __global__ void __launch_bounds__(NT)
     DwAcc acc = {0.0f, 0.0f};
     const BlockRange br = block_range(n2);
     update_range(br.begin, br.end, NT, ctl->alpha_w, p, Ap, x, r, b0, acc);
-    double rr = (double)acc.s + (double)acc.c, unused = 0.0;
-    block_sum2(rr, unused);
-    if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
+    DwAcc unused = {0.0f, 0.0f};
+    block_sum_acc2(acc, unused);
+    if (publish_acc2(acc, unused, part, maxb, blockIdx.x, &ctl->ticket[SL_UPDATE], gridDim.x)) {
         double RR, U;
-        gather2(part, maxb, &ctl->ticket[SL_UPDATE], RR, U);
+        gather_acc2(part, maxb, 0u, gridDim.x, &ctl->ticket[SL_UPDATE], RR, U);
         if (threadIdx.x == 0) {
             ctl->rr = RR;
             ctl->iter += 1;
@@ -231,11 +232,10 @@ __global__ void __launch_bounds__(NT)
     DwAcc rz = {0.0f, 0.0f}, zap = {0.0f, 0.0f};
     const BlockRange br = block_range(n2);
     dot_range(br.begin, br.end, NT, r, z, Ap, rz, zap);
-    double RZ0 = (double)rz.s + (double)rz.c, ZAP0 = (double)zap.s + (double)zap.c;
-    block_sum2(RZ0, ZAP0);
-    if (publish2(RZ0, ZAP0, part, maxb, &ctl->ticket[SL_DOT])) {
+    block_sum_acc2(rz, zap);
+    if (publish_acc2(rz, zap, part, maxb, blockIdx.x, &ctl->ticket[SL_DOT], gridDim.x)) {
         double RZ, ZAP;
-        gather2(part, maxb, &ctl->ticket[SL_DOT], RZ, ZAP);
+        gather_acc2(part, maxb, 0u, gridDim.x, &ctl->ticket[SL_DOT], RZ, ZAP);
         if (threadIdx.x == 0) {
             ctl->beta = ctl->iter > 0 ? -ZAP / ctl->pAp : 0.0;
             ctl->beta_w = dw_of(ctl->beta);

@@ -178,10 +178,10 @@ __global__ void __launch_bounds__(32 * MZ)
 template <class T, int MZ>
 __global__ void __launch_bounds__(kSmallThreads, 1)
     k_vsmall(TailLevels<T> tl, Ctl* ctl, Cond cond) {
-    pdl_enter();
-    if (loop_done(ctl, cond)) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    if (!mgdev::vsmall_body<T, MZ>(tl, (T)ctl->inv_dt, smem) && threadIdx.x == 0) {
+    const auto wait = [] { pdl_enter(); };
+    const auto go = [&] { return !loop_done(ctl, cond); };
+    if (mgdev::vsmall_body<T, MZ>(tl, &ctl->inv_dt, smem, wait, go) == mgdev::kSmallTimeout && threadIdx.x == 0) {
         // a bounded wait ran out: record it and stop the solve
         atomicExch(&ctl->err, 1);
         ctl->breakdown = 1;

@@ -208,7 +208,7 @@ struct TailLevels {
 };
 // The smallest levels (those whose arrays together fit kSmallSmemMax bytes),
 // run by one block out of shared memory.
-constexpr int kSmallThreads = 256;
+constexpr int kSmallThreads = 512;
 constexpr int kSmallSmemMax = 200 * 1024;
 template <class T>
 size_t small_smem_bytes(const TailLevels<T>& tl);

@@ -83,6 +83,73 @@ __device__ __forceinline__ T lat_sum(const LevelView<T>& L, const LevelView<T>& 
     return s;
 }
 
+// Right-hand side of plane l of a column in the branch-free form (BF below):
+// b plus the lateral sum in op_lat_sum's order (west, east, south, north),
+// each neighbour value with its parent's coarse correction under PRO; an
+// absent neighbour reads the column itself with weight 0.
+template <class T, bool ZERO, bool PRO, bool CG>
+__device__ __forceinline__ T bf_rhs(const LevelView<T>& L, const LevelView<T>& C, const Nbr& n, unsigned l) {
+    const Geo& g = L.g;
+    const unsigned base = l * g.plane, id = base + n.s;
+    T rhs = ldm<CG>(L.b + id);
+    if (!ZERO) {
+        const unsigned sw = n.w ? n.sw : n.s, se = n.e ? n.se : n.s;
+        const unsigned ss = n.so ? n.ss : n.s, sn = n.no ? n.sn : n.s;
+        T xw = ldm<CG>(L.x + base + sw), xe = ldm<CG>(L.x + base + se);
+        T xs = ldm<CG>(L.x + base + ss), xn = ldm<CG>(L.x + base + sn);
+        if (PRO) {
+            const T* cx = C.x + l * C.g.plane;
+            xw = xw + ldm<CG>(cx + n.pw);
+            xe = xe + ldm<CG>(cx + n.pe);
+            xs = xs + ldm<CG>(cx + n.ps);
+            xn = xn + ldm<CG>(cx + n.pn);
+        }
+        const float ew = L.gE[base + sw], ee = L.gE[id], ns = L.gN[base + ss], nn = L.gN[id];
+        T sum = 0;
+        sum += (n.w ? (T)ew : T(0)) * xw;
+        sum += (n.e ? (T)ee : T(0)) * xe;
+        sum += (n.so ? (T)ns : T(0)) * xs;
+        sum += (n.no ? (T)nn : T(0)) * xn;
+        rhs = rhs + sum;
+    }
+    return rhs;
+}
+
+// The Thomas recurrence of sweep_column on the column at slot s whose
+// right-hand sides are src[l * plane + s] (nz <= MZ): every operand loaded
+// first, the recurrence on registers, x written once.
+template <class T, int MZ>
+__device__ __forceinline__ void column_solve(const LevelView<T>& L, const T* src, unsigned s) {
+    const Geo& g = L.g;
+    T v[MZ], fi[MZ], fc[MZ];
+    float gu[MZ];
+#pragma unroll
+    for (int l = 0; l < MZ; ++l) {
+        if (l < g.nz) {
+            const unsigned id = (unsigned)l * g.plane + s;
+            v[l] = src[id];
+            fi[l] = L.finv[id];
+            fc[l] = L.fcp[id];
+            gu[l] = L.gU[id];
+        }
+    }
+    T prev = 0;
+#pragma unroll
+    for (int l = 0; l < MZ; ++l) {
+        if (l < g.nz) {
+            const T lower = l > 0 ? -(T)gu[l - 1] : T(0);
+            prev = (v[l] - lower * prev) * fi[l];
+            v[l] = prev;
+        }
+    }
+#pragma unroll
+    for (int l = MZ - 2; l >= 0; --l)
+        if (l < g.nz - 1) v[l] -= fc[l] * v[l + 1];
+#pragma unroll
+    for (int l = 0; l < MZ; ++l)
+        if (l < g.nz) L.x[(unsigned)l * g.plane + s] = v[l];
+}
+
 // Line solve of the q-th column of colour `color` (mg_line_solve,
 // src/mg3d.h:179-196). With MZ > 0 (nz <= MZ) the column stays in registers:
 // every plane's right-hand side (b plus the lateral sum) is gathered first,
@@ -104,34 +171,13 @@ __device__ __forceinline__ void sweep_column(const LevelView<T>& L, const LevelV
     if (i >= g.nx) return;
     const Nbr n = neighbours<PRO>(g, C.g, i, j, t, color);
     if constexpr (MZ > 0 && BF) {
-        const unsigned sw = n.w ? n.sw : n.s, se = n.e ? n.se : n.s;
-        const unsigned ss = n.so ? n.ss : n.s, sn = n.no ? n.sn : n.s;
         T v[MZ], fi[MZ], fc[MZ];
         float gu[MZ];
 #pragma unroll
         for (int l = 0; l < MZ; ++l) {
             const unsigned lc = (unsigned)(l < g.nz ? l : g.nz - 1);
-            const unsigned base = lc * g.plane, id = base + n.s;
-            T rhs = ldm<CG>(L.b + id);
-            if (!ZERO) {
-                T xw = ldm<CG>(L.x + base + sw), xe = ldm<CG>(L.x + base + se);
-                T xs = ldm<CG>(L.x + base + ss), xn = ldm<CG>(L.x + base + sn);
-                if (PRO) {
-                    const T* cx = C.x + lc * C.g.plane;
-                    xw = xw + ldm<CG>(cx + n.pw);
-                    xe = xe + ldm<CG>(cx + n.pe);
-                    xs = xs + ldm<CG>(cx + n.ps);
-                    xn = xn + ldm<CG>(cx + n.pn);
-                }
-                const float ew = L.gE[base + sw], ee = L.gE[id], ns = L.gN[base + ss], nn = L.gN[id];
-                T sum = 0;  // op_lat_sum order: west, east, south, north
-                sum += (n.w ? (T)ew : T(0)) * xw;
-                sum += (n.e ? (T)ee : T(0)) * xe;
-                sum += (n.so ? (T)ns : T(0)) * xs;
-                sum += (n.no ? (T)nn : T(0)) * xn;
-                rhs = rhs + sum;
-            }
-            v[l] = rhs;
+            const unsigned id = lc * g.plane + n.s;
+            v[l] = bf_rhs<T, ZERO, PRO, CG>(L, C, n, lc);
             fi[l] = L.finv[id];
             fc[l] = L.fcp[id];
             gu[l] = L.gU[id];
@@ -369,96 +415,154 @@ __device__ __forceinline__ void restrict_cell(const LevelView<T>& F, const Level
 }
 
 
+// Writes the right-hand side (bf_rhs) of every plane of every column of
+// colour `color` into that column's x slots; tasks are (plane, column) pairs
+// strided over the nth threads of the block.
+template <class T, bool PRO>
+__device__ __forceinline__ void gather_rhs(const LevelView<T>& L, const LevelView<T>& C, int color, unsigned tid,
+                                           unsigned nth) {
+    const Geo& g = L.g;
+    const unsigned ncol = (unsigned)g.ny * (unsigned)g.hx;
+    const unsigned work = ncol * (unsigned)g.nz;
+    for (unsigned w = tid; w < work; w += nth) {
+        const unsigned l = w / ncol, q = w - l * ncol;
+        const int j = (int)(q / (unsigned)g.hx), t = (int)(q - (unsigned)j * g.hx);
+        const int i = 2 * t + ((j + color) & 1);
+        if (i >= g.nx) continue;
+        const Nbr n = neighbours<PRO>(g, C.g, i, j, t, color);
+        L.x[l * g.plane + n.s] = bf_rhs<T, false, PRO, false>(L, C, n, l);
+    }
+}
+
+// Level views of the shared-memory bottom: a level's arrays lie at base in
+// the order gE, gN, gU, cap, gB, fcp, finv, x, b, each rounded up to 16 bytes
+// (small_smem_bytes adds the same sizes). The views are rebuilt from the
+// block's base and a byte offset wherever they are used, never stored as
+// pointers, so every pointer visibly points into shared memory and the
+// compiler issues shared-memory loads through them rather than generic ones.
+template <class T>
+__device__ __forceinline__ unsigned small_level_bytes(const Geo& g) {
+    const unsigned ln = g.plane * (unsigned)g.nz;
+    return 4u * ((ln * 4u + 15u) & ~15u) + ((g.plane * 4u + 15u) & ~15u) +
+           4u * ((ln * (unsigned)sizeof(T) + 15u) & ~15u);
+}
+
+template <class T>
+__device__ __forceinline__ LevelView<T> small_view(unsigned char* base, const Geo& g) {
+    const unsigned ln = g.plane * (unsigned)g.nz;
+    unsigned char* p = base;
+    auto take = [&](unsigned bytes) {
+        unsigned char* r = p;
+        p += (bytes + 15u) & ~15u;
+        return r;
+    };
+    LevelView<T> S;
+    S.g = g;
+    S.gE = (const float*)take(ln * 4u);
+    S.gN = (const float*)take(ln * 4u);
+    S.gU = (const float*)take(ln * 4u);
+    S.cap = (const float*)take(ln * 4u);
+    S.gB = (const float*)take(g.plane * 4u);
+    S.fcp = (T*)take(ln * (unsigned)sizeof(T));
+    S.finv = (T*)take(ln * (unsigned)sizeof(T));
+    S.x = (T*)take(ln * (unsigned)sizeof(T));
+    S.b = (T*)take(ln * (unsigned)sizeof(T));
+    return S;
+}
+
 // The bottom of the V-cycle (levels k0 .. single column) in ONE block, with
 // every one of those levels held in shared memory: operator and factors of
-// every level and level k0's b come in by bulk copies (all in flight at once,
-// one mbarrier), x and the coarser b start at zero, the phases run with block
-// barriers, and level k0's x goes back out for the prolongation above it.
-// Same line-solve and restriction code as the grid-wide kernels, pointed at
-// shared memory. Returns false (nothing written) if the bounded wait for the
-// copies ran out.
-template <class T, int MZ>
-__device__ __forceinline__ bool vsmall_body(const TailLevels<T>& tl, T inv_dt,
-                                            unsigned char* smem) {
-    __shared__ TailLevels<T> sl;  // views of the same levels, in shared memory
-    __shared__ uint64_t bar;
+// every level and level k0's b come in by bulk copies (all in flight at once),
+// x and the coarser b start at zero, the phases run with block barriers, and
+// level k0's x goes back out for the prolongation above it. Same line-solve
+// and restriction code as the grid-wide kernels, pointed at shared memory.
+//
+// The operator and factors do not change during a solve, so their copies are
+// issued (one per lane of the first warp) before wait() (every thread calls
+// it: it waits for the preceding kernel); level k0's b, the preceding
+// kernel's output, is copied after it, and go() (called after that copy is
+// issued, so the two latencies overlap) says whether to run the phases at
+// all. Returns kSmallDone, kSmallClosed (go() said no: nothing written once
+// the copies have landed) or kSmallTimeout (a bounded wait for the copies ran
+// out: nothing written).
+constexpr int kSmallDone = 0, kSmallTimeout = 1, kSmallClosed = 2;
+
+template <class T, int MZ, class Wait, class Go>
+__device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double* inv_dt_src,
+                                           unsigned char* smem, Wait wait, Go go) {
+    __shared__ Geo sg[kMaxTail];      // level geometry
+    __shared__ unsigned soff[kMaxTail];  // byte offset of each level in smem
+    __shared__ uint64_t bar, barb;    // operator and factors; level k0's b
+    const int nl = tl.n;
     if (threadIdx.x == 0) {
-        sl.n = tl.n;
+        unsigned off = 0, total = 0;
+        for (int k = 0; k < nl; ++k) {
+            const Geo g = tl.L[k].g;
+            sg[k] = g;
+            soff[k] = off;
+            off += small_level_bytes<T>(g);
+            const unsigned ln = g.plane * (unsigned)g.nz;
+            total += 4u * ln * 4u + g.plane * 4u + 2u * ln * (unsigned)sizeof(T);
+        }
         tma::mbar_init(&bar, 1);
+        tma::mbar_init(&barb, 1);
         tma::fence_barrier_init();
+        tma::mbar_arrive_expect_tx(&bar, total);
     }
     __syncthreads();
-    {
-        unsigned char* q = smem;
-        auto take = [&](size_t bytes) {
-            unsigned char* r = q;
-            q += (bytes + 15) & ~size_t(15);
-            return r;
-        };
-        if (threadIdx.x == 0) {
-            unsigned total = 0;
-            for (int k = 0; k < tl.n; ++k) {
-                const unsigned ln = tl.L[k].g.plane * (unsigned)tl.L[k].g.nz;
-                total += 4u * ln * 4u + tl.L[k].g.plane * 4u + 2u * ln * (unsigned)sizeof(T);
-                if (k == 0) total += ln * (unsigned)sizeof(T);
-            }
-            tma::mbar_arrive_expect_tx(&bar, total);
-        }
-        for (int k = 0; k < tl.n; ++k) {
+    if (threadIdx.x < 32u) {
+        // copy c of level k = c / 7: gE, gN, gU, cap, gB, fcp, finv
+        for (int c = (int)threadIdx.x; c < 7 * nl; c += 32) {
+            const int k = c / 7, a = c - 7 * k;
             const LevelView<T>& G = tl.L[k];
-            LevelView<T> S;
-            const unsigned ln = G.g.plane * (unsigned)G.g.nz;
-            S.g = G.g;
-            float* gE = (float*)take(ln * 4);
-            float* gN = (float*)take(ln * 4);
-            float* gU = (float*)take(ln * 4);
-            float* cap = (float*)take(ln * 4);
-            float* gB = (float*)take(G.g.plane * 4);
-            T* fcp = (T*)take(ln * sizeof(T));
-            T* finv = (T*)take(ln * sizeof(T));
-            T* x = (T*)take(ln * sizeof(T));
-            T* b = (T*)take(ln * sizeof(T));
-            if (threadIdx.x == 0) {
-                tma::bulk_load(gE, G.gE, ln * 4u, &bar);
-                tma::bulk_load(gN, G.gN, ln * 4u, &bar);
-                tma::bulk_load(gU, G.gU, ln * 4u, &bar);
-                tma::bulk_load(cap, G.cap, ln * 4u, &bar);
-                tma::bulk_load(gB, G.gB, G.g.plane * 4u, &bar);
-                tma::bulk_load(fcp, G.fcp, ln * (unsigned)sizeof(T), &bar);
-                tma::bulk_load(finv, G.finv, ln * (unsigned)sizeof(T), &bar);
-                if (k == 0) tma::bulk_load(b, G.b, ln * (unsigned)sizeof(T), &bar);
-            }
-            // Padding slots are never written by the phases below but go back
-            // out with level k0's x: start every slot at zero, as the global
-            // arrays' padding is, so no stale shared-memory value (possibly a
-            // NaN) reaches the outer iteration.
-            for (unsigned i = threadIdx.x; i < ln; i += kSmallThreads) {
-                x[i] = T(0);
-                if (k > 0) b[i] = T(0);
-            }
-            S.gE = gE;
-            S.gN = gN;
-            S.gU = gU;
-            S.cap = cap;
-            S.gB = gB;
-            S.fcp = fcp;
-            S.finv = finv;
-            S.x = x;
-            S.b = b;
-            if (threadIdx.x == 0) sl.L[k] = S;
+            const LevelView<T> S = small_view<T>(smem + soff[k], sg[k]);
+            const unsigned ln = sg[k].plane * (unsigned)sg[k].nz;
+            const unsigned fb = ln * 4u, tb = ln * (unsigned)sizeof(T);
+            if (a == 0) tma::bulk_load((void*)S.gE, G.gE, fb, &bar);
+            else if (a == 1) tma::bulk_load((void*)S.gN, G.gN, fb, &bar);
+            else if (a == 2) tma::bulk_load((void*)S.gU, G.gU, fb, &bar);
+            else if (a == 3) tma::bulk_load((void*)S.cap, G.cap, fb, &bar);
+            else if (a == 4) tma::bulk_load((void*)S.gB, G.gB, sg[k].plane * 4u, &bar);
+            else if (a == 5) tma::bulk_load(S.fcp, G.fcp, tb, &bar);
+            else tma::bulk_load(S.finv, G.finv, tb, &bar);
         }
     }
-    const bool got = tma::mbar_wait(&bar, 0u);
+    // Padding slots are never written by the phases below but go back out
+    // with level k0's x: start every slot at zero, as the global arrays'
+    // padding is, so no stale shared-memory value (possibly a NaN) reaches
+    // the outer iteration.
+    for (int k = 0; k < nl; ++k) {
+        const LevelView<T> S = small_view<T>(smem + soff[k], sg[k]);
+        const unsigned ln = sg[k].plane * (unsigned)sg[k].nz;
+        for (unsigned i = threadIdx.x; i < ln; i += kSmallThreads) {
+            S.x[i] = T(0);
+            if (k > 0) S.b[i] = T(0);
+        }
+    }
+    wait();
+    if (threadIdx.x == 0) {
+        const unsigned bytes = sg[0].plane * (unsigned)sg[0].nz * (unsigned)sizeof(T);
+        tma::mbar_arrive_expect_tx(&barb, bytes);
+        tma::bulk_load(small_view<T>(smem, sg[0]).b, tl.L[0].b, bytes, &barb);
+    }
+    if (!__syncthreads_and(go() ? 1 : 0)) {
+        if (threadIdx.x == 0) {  // let the copies land before leaving
+            tma::mbar_wait(&bar, 0u);
+            tma::mbar_wait(&barb, 0u);
+        }
+        return kSmallClosed;
+    }
+    const T inv_dt = (T)*inv_dt_src;
+    const bool got = tma::mbar_wait(&bar, 0u) && tma::mbar_wait(&barb, 0u);
     if (!__syncthreads_and(got)) {
-        if (threadIdx.x == 0) tma::mbar_wait(&bar, 0u);  // let the copies land before leaving
-        return false;
+        if (threadIdx.x == 0) {  // let the copies land before leaving
+            tma::mbar_wait(&bar, 0u);
+            tma::mbar_wait(&barb, 0u);
+        }
+        return kSmallTimeout;
     }
     const unsigned tid = threadIdx.x, nth = kSmallThreads;
-    const int last = sl.n - 1;
-    // Each phase works on register copies of the level views: the views live
-    // in shared memory, where the sweeps also store x through generic
-    // pointers, so reading them in place would reload every field after
-    // every store.
+    const int last = nl - 1;
     // The phases in V-cycle order, driven by one loop so that each kind of
     // phase (x = 0 sweep, sweep, restriction, prolongating sweep) is one
     // code region, warm in the instruction cache after its first use: down
@@ -482,14 +586,38 @@ __device__ __forceinline__ bool vsmall_body(const TailLevels<T>& tl, T inv_dt,
             kind = (u & 1) ? 1 : 3;
             color = (u & 1) ? 0 : 1;
         }
-        const LevelView<T> L = sl.L[k];
+        const LevelView<T> L = small_view<T>(smem + soff[k], sg[k]);
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        if (kind == 0) {
+        bool swept = false;
+        if constexpr (MZ > 0) {
+          if (kind != 2) {
+            swept = true;
+            // A sweep in two steps: one task per column and plane gathers
+            // that plane's right-hand side into the column's own x slot (the
+            // sweep reads only the other colour's x, so no task reads a slot
+            // another one writes), then one thread per column runs the
+            // recurrence. Same operations as sweep_column, with the gathers
+            // spread over the block instead of one thread walking the planes.
+            if (kind == 1)
+                gather_rhs<T, false>(L, L, color, tid, nth);
+            else if (kind == 3)
+                gather_rhs<T, true>(L, small_view<T>(smem + soff[k + 1], sg[k + 1]), color, tid, nth);
+            if (kind != 0) __syncthreads();
+            const T* src = kind == 0 ? L.b : L.x;
+            for (unsigned q = tid; q < ncol; q += nth) {
+                const int j = (int)(q / (unsigned)L.g.hx), t = (int)(q - (unsigned)j * L.g.hx);
+                if (2 * t + ((j + color) & 1) < L.g.nx)
+                    column_solve<T, MZ>(L, src, (unsigned)(2 * j + color) * (unsigned)L.g.hx + (unsigned)t);
+            }
+          }
+        }
+        if (swept) {
+        } else if (kind == 0) {
             for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false, true>(L, L, 0, q);
         } else if (kind == 1) {
             for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false, true>(L, L, color, q);
         } else if (kind == 2) {
-            const LevelView<T> C = sl.L[k + 1];
+            const LevelView<T> C = small_view<T>(smem + soff[k + 1], sg[k + 1]);
             const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
             const unsigned work = ccols * (unsigned)C.g.nz;
             for (unsigned w = tid; w < work; w += nth) {
@@ -497,16 +625,16 @@ __device__ __forceinline__ bool vsmall_body(const TailLevels<T>& tl, T inv_dt,
                 restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
             }
         } else {
-            const LevelView<T> C = sl.L[k + 1];
+            const LevelView<T> C = small_view<T>(smem + soff[k + 1], sg[k + 1]);
             for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false, true>(L, C, 1, q);
         }
         __syncthreads();
     }
-    const LevelView<T> S0 = sl.L[0];
+    const LevelView<T> S0 = small_view<T>(smem, sg[0]);
     const unsigned ln0 = S0.g.plane * (unsigned)S0.g.nz;
     T* out = tl.L[0].x;
     for (unsigned i = tid; i < ln0; i += nth) out[i] = S0.x[i];
-    return true;
+    return kSmallDone;
 }
 
 

@@ -354,6 +354,46 @@ def test_fused_first_sweep_bitwise(ct, n, prec):
             assert a == b
 
 
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
+@pytest.mark.parametrize("n", [203, 64, 9])
+def test_shared_memory_bottom_bitwise(ct, n, prec):
+    """The bottom levels run by one block out of shared memory (the default;
+    its sweeps gather every plane's right-hand side with one task per column
+    and plane before the recurrences) give the grid-wide launches' results
+    (CT_SMALL_BYTES=0: no shared-memory bottom) bit for bit: steady solve,
+    then two backward-Euler steps."""
+    import os
+    import workloads
+    m = workloads.steady_hotspot(n, seed=17)
+    out = []
+    for flag in ("0", None):
+        old = os.environ.get("CT_SMALL_BYTES")
+        if flag is None:
+            os.environ.pop("CT_SMALL_BYTES", None)
+        else:
+            os.environ["CT_SMALL_BYTES"] = flag  # read when the solver is created
+        try:
+            with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
+                s.set_x_zero()
+                s.set_rhs_steady()
+                res = [s.solve(1e-10, 1000).iters, s.get_x()]
+                s.set_dt(1e-3)
+                for _ in range(2):
+                    s.set_rhs_transient()
+                    res += [s.solve(1e-9, 1000).iters, s.get_x()]
+                out.append(res)
+        finally:
+            if old is None:
+                os.environ.pop("CT_SMALL_BYTES", None)
+            else:
+                os.environ["CT_SMALL_BYTES"] = old
+    for a, b in zip(out[0], out[1]):
+        if isinstance(a, np.ndarray):
+            assert np.array_equal(a, b)
+        else:
+            assert a == b
+
+
 def test_bounded_wait_runs_out_and_context_survives(ct):
     """Failure detection without a fault: a device wait that nothing
     completes runs out after its poll limit, its kernel returns and reports
