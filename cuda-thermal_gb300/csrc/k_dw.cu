@@ -223,15 +223,16 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
-// rz = r.z and z.Ap (flexible beta); beta.
+// rz = r.z and z.Ap (flexible beta); beta. Items strided over the whole grid
+// (4 blocks per SM): 32.9 us at 800 x 800 x 10 against 34.5 us with one
+// contiguous range per block on 6 blocks per SM.
 __global__ void __launch_bounds__(NT)
     k_dot_dw(unsigned n2, const float4* __restrict__ r, const float2* __restrict__ z,
              const float4* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
     DwAcc rz = {0.0f, 0.0f}, zap = {0.0f, 0.0f};
-    const BlockRange br = block_range(n2);
-    dot_range(br.begin, br.end, NT, r, z, Ap, rz, zap);
+    dot_range(blockIdx.x * NT + threadIdx.x, n2, gridDim.x * NT, r, z, Ap, rz, zap);
     block_sum_acc2(rz, zap);
     if (publish_acc2(rz, zap, part, maxb, blockIdx.x, &ctl->ticket[SL_DOT], gridDim.x)) {
         double RZ, ZAP;
@@ -358,8 +359,8 @@ void launch_update_dw(cudaStream_t st, unsigned n, const float2* p, const float2
 void launch_dot_dw(cudaStream_t st, unsigned n, const float2* r, const float* z, const float2* Ap,
                    Ctl* ctl, const Red& red, Cond cond) {
     static const int wb = wave_blocks(k_dot_dw, 1 << 30);
-    launch_pdl(k_dot_dw, std::min(red.blocks, wb), NT, 0, st, n / 2, (const float4*)r, (const float2*)z,
-                                        (const float4*)Ap, ctl, red.part, red.maxb, cond);
+    launch_pdl(k_dot_dw, std::min(std::max(1, red.maxb / 2), wb), NT, 0, st, n / 2, (const float4*)r,
+               (const float2*)z, (const float4*)Ap, ctl, red.part, red.maxb, cond);
 }
 
 void launch_update_p_dw(cudaStream_t st, unsigned n, const float* z, float2* p, Ctl* ctl,

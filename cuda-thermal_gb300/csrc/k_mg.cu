@@ -100,7 +100,10 @@ __global__ void __launch_bounds__(NT)
 // operands, a child's x one plane up being the next plane's own, are loaded
 // once). Pairs pay on large fine levels (800 x 800: 46 us against 49 us),
 // single planes on small ones (25 x 25: 8.8 us against 10.5 us, twice the
-// threads for a latency-bound launch).
+// threads for a latency-bound launch). k_restrict2 is compiled for 4 blocks
+// per SM (64 registers): 38.8 us at 800 x 800, against 39.5 us with 80
+// registers and 46.8 / 53.7 us with 48 / 40; the load round trips of a
+// thread, not the number of resident warps, bound it.
 template <class T>
 __global__ void __launch_bounds__(NT)
     k_restrict(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
@@ -112,7 +115,7 @@ __global__ void __launch_bounds__(NT)
 }
 
 template <class T>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 4)
     k_restrict2(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
