@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(NT)
 
 // Ap = d p - sum G p_nbr over rows [begin, end) of the instance (one warp
 // per row of one colour of one plane, apply_row), p.Ap, alpha.
-template <int U>
-__global__ void __launch_bounds__(NT)
+template <int U, int MINB = 0>
+__global__ void __launch_bounds__(NT, MINB)
     kb_apply(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
@@ -420,7 +420,10 @@ __global__ void __launch_bounds__(NT)
         sweep_column<float, MZ, ZERO, PRO, false>(L, C, color, q);
 }
 
-__global__ void __launch_bounds__(NT)
+// Compiled for 4 blocks per SM (64 registers): level 0 of the 256-instance
+// batch 296 us per launch against 429 us with the compiler's own choice (also
+// 64 registers), as for the single solver's k_restrict2.
+__global__ void __launch_bounds__(NT, 4)
     kb_restrict(Plan p, const LevelView<float>* __restrict__ views,
                 const LevelView<float>* __restrict__ cviews, const Ctl* ctl) {
     const Task t = p.tasks[blockIdx.x];
@@ -471,13 +474,14 @@ void launch_b_apply(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, B
     // one cell per lane, every operand of it gathered at once (measured on the
     // 256-instance floorplan batch: 40.7 ms per solve against 50.0 ms with the
     // operands loaded term by term, CT_BATCH_APPLY=0, and 59.0 ms with two
-    // cells per lane, CT_BATCH_APPLY=2)
+    // cells per lane, CT_BATCH_APPLY=2), compiled for 4 blocks per SM (64
+    // registers: 600 us per launch against 722 us with the compiler's 78)
     static const int form = [] {
         const char* e = std::getenv("CT_BATCH_APPLY");
         return e ? std::atoi(e) : 1;
     }();
     if (form == 1)
-        kb_apply<1><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+        kb_apply<1, 4><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
     else if (form == 2)
         kb_apply<2><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
     else

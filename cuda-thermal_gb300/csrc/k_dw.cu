@@ -224,9 +224,10 @@ __global__ void __launch_bounds__(NT)
 }
 
 // rz = r.z and z.Ap (flexible beta); beta. Items strided over the whole grid
-// (4 blocks per SM): 32.9 us at 800 x 800 x 10 against 34.5 us with one
-// contiguous range per block on 6 blocks per SM.
-__global__ void __launch_bounds__(NT)
+// on 4 blocks per SM, compiled for 4 blocks per SM: 31.7 us at 800 x 800 x 10
+// against 32.9 us with the compiler's own register choice and 34.5 us with
+// one contiguous range per block on 6 blocks per SM.
+__global__ void __launch_bounds__(NT, 4)
     k_dot_dw(unsigned n2, const float4* __restrict__ r, const float2* __restrict__ z,
              const float4* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
     pdl_enter();
