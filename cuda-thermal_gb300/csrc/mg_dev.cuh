@@ -588,10 +588,15 @@ __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double
         }
         const LevelView<T> L = small_view<T>(smem + soff[k], sg[k]);
         const unsigned ncol = (unsigned)L.g.ny * (unsigned)L.g.hx;
-        bool swept = false;
-        if constexpr (MZ > 0) {
-          if (kind != 2) {
-            swept = true;
+        if (kind == 2) {
+            const LevelView<T> C = small_view<T>(smem + soff[k + 1], sg[k + 1]);
+            const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
+            const unsigned work = ccols * (unsigned)C.g.nz;
+            for (unsigned w = tid; w < work; w += nth) {
+                const int l = (int)(w / ccols);
+                restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
+            }
+        } else if constexpr (MZ > 0) {
             // A sweep in two steps: one task per column and plane gathers
             // that plane's right-hand side into the column's own x slot (the
             // sweep reads only the other colour's x, so no task reads a slot
@@ -609,21 +614,10 @@ __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double
                 if (2 * t + ((j + color) & 1) < L.g.nx)
                     column_solve<T, MZ>(L, src, (unsigned)(2 * j + color) * (unsigned)L.g.hx + (unsigned)t);
             }
-          }
-        }
-        if (swept) {
-        } else if (kind == 0) {
+        } else if (kind == 0) {  // deep columns (MZ = 0): x goes through memory
             for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, true, false, false, true>(L, L, 0, q);
         } else if (kind == 1) {
             for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, false, false, true>(L, L, color, q);
-        } else if (kind == 2) {
-            const LevelView<T> C = small_view<T>(smem + soff[k + 1], sg[k + 1]);
-            const unsigned ccols = (unsigned)C.g.nx * (unsigned)C.g.ny;
-            const unsigned work = ccols * (unsigned)C.g.nz;
-            for (unsigned w = tid; w < work; w += nth) {
-                const int l = (int)(w / ccols);
-                restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
-            }
         } else {
             const LevelView<T> C = small_view<T>(smem + soff[k + 1], sg[k + 1]);
             for (unsigned q = tid; q < ncol; q += nth) sweep_column<T, MZ, false, true, false, true>(L, C, 1, q);
