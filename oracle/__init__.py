@@ -1,8 +1,8 @@
 """CPU oracle for the MG-PCG thermal solve (ctypes bindings to liboracle.so).
 
 TEST INFRASTRUCTURE ONLY. Only the tests, ``__graft_entry__.smoke()`` and the
-CPU baseline leg of ``bench.py`` import this package, as the checker. The
-product library never loads it.
+CPU baseline leg of ``bench.py`` import this package, to check results and
+to time the CPU reference arithmetic. The product library never loads it.
 
 ``liboracle.so`` is a plain-C restatement of the reference CPU solver
 (cuda-thermal ``src/pcg3d_cpu.cpp``, ``src/mg3d.h``, ``src/operator3d.h``,

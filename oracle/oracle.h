@@ -3,8 +3,9 @@
  * TEST INFRASTRUCTURE ONLY. This is a plain-C restatement of the reference's
  * CPU solver (cuda-thermal: src/pcg3d_cpu.cpp, src/mg3d.h, src/operator3d.h,
  * src/transient3d.h, src/stack3d.h:252-273). Only the tests, the smoke check
- * and the CPU baseline leg of the benchmark load it, as the checker. The
- * product path (the CUDA library) never links, loads or calls it.
+ * and the CPU baseline leg of the benchmark load it, to check results and to
+ * time the CPU reference arithmetic. The product path (the CUDA library)
+ * never links, loads or calls it.
  *
  * Arithmetic follows the reference operation by operation, in the same order,
  * so that with FMA contraction disabled (-ffp-contract=off) the results are
