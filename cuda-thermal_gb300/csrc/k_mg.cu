@@ -295,13 +295,7 @@ template bool launch_restrict_sweep0<double>(cudaStream_t, const LevelView<doubl
 template <class T>
 size_t small_smem_bytes(const TailLevels<T>& tl) {
     size_t b = 0;
-    auto take = [&](size_t bytes) { b += (bytes + 15) & ~size_t(15); };
-    for (int k = 0; k < tl.n; ++k) {
-        const size_t ln = (size_t)tl.L[k].g.plane * tl.L[k].g.nz;
-        for (int a = 0; a < 4; ++a) take(ln * 4);
-        take((size_t)tl.L[k].g.plane * 4);
-        for (int a = 0; a < 4; ++a) take(ln * sizeof(T));
-    }
+    for (int k = 0; k < tl.n; ++k) b += small_level_bytes(tl.L[k].g, sizeof(T));
     return b;
 }
 

@@ -210,6 +210,15 @@ struct TailLevels {
 // run by one block out of shared memory.
 constexpr int kSmallThreads = 512;
 constexpr int kSmallSmemMax = 200 * 1024;
+// Bytes one level takes there: gE, gN, gU, cap (float), gB (one plane of
+// float), fcp, finv, x, b (elem bytes each), every array rounded up to 16
+// bytes. The device carving of the block's shared memory, its size at launch
+// and the choice of the first level held there all use this one sum.
+__host__ __device__ inline size_t small_round16(size_t b) { return (b + 15) & ~size_t(15); }
+__host__ __device__ inline size_t small_level_bytes(const Geo& g, size_t elem) {
+    const size_t ln = (size_t)g.plane * (size_t)g.nz;
+    return 4 * small_round16(ln * 4) + small_round16((size_t)g.plane * 4) + 4 * small_round16(ln * elem);
+}
 template <class T>
 size_t small_smem_bytes(const TailLevels<T>& tl);
 template <class T>

@@ -436,24 +436,17 @@ __device__ __forceinline__ void gather_rhs(const LevelView<T>& L, const LevelVie
 
 // Level views of the shared-memory bottom: a level's arrays lie at base in
 // the order gE, gN, gU, cap, gB, fcp, finv, x, b, each rounded up to 16 bytes
-// (small_smem_bytes adds the same sizes). The views are rebuilt from the
+// (small_level_bytes adds the same sizes). The views are rebuilt from the
 // block's base and a byte offset wherever they are used, never stored as
 // pointers, so every pointer visibly points into shared memory and the
 // compiler issues shared-memory loads through them rather than generic ones.
-template <class T>
-__device__ __forceinline__ unsigned small_level_bytes(const Geo& g) {
-    const unsigned ln = g.plane * (unsigned)g.nz;
-    return 4u * ((ln * 4u + 15u) & ~15u) + ((g.plane * 4u + 15u) & ~15u) +
-           4u * ((ln * (unsigned)sizeof(T) + 15u) & ~15u);
-}
-
 template <class T>
 __device__ __forceinline__ LevelView<T> small_view(unsigned char* base, const Geo& g) {
     const unsigned ln = g.plane * (unsigned)g.nz;
     unsigned char* p = base;
     auto take = [&](unsigned bytes) {
         unsigned char* r = p;
-        p += (bytes + 15u) & ~15u;
+        p += small_round16(bytes);
         return r;
     };
     LevelView<T> S;
@@ -500,7 +493,7 @@ __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double
             const Geo g = tl.L[k].g;
             sg[k] = g;
             soff[k] = off;
-            off += small_level_bytes<T>(g);
+            off += (unsigned)small_level_bytes(g, sizeof(T));
             const unsigned ln = g.plane * (unsigned)g.nz;
             total += 4u * ln * 4u + g.plane * 4u + 2u * ln * (unsigned)sizeof(T);
         }

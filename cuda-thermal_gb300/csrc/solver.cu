@@ -172,9 +172,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
         if (const char* e = std::getenv("CT_SMALL_BYTES")) small_max = std::atol(e);
         size_t acc = 0;
         for (size_t k = lv.size(); k-- > 0;) {
-            const size_t ln = (size_t)lv[k].g.plane * lv[k].g.nz;
-            acc += 4 * ((ln * 4 + 15) & ~size_t(15)) + ((lv[k].g.plane * 4 + 15) & ~size_t(15)) +
-                   4 * ((ln * tsize + 15) & ~size_t(15));
+            acc += small_level_bytes(lv[k].g, tsize);
             if ((long)acc > small_max || lv.size() - k > (size_t)kMaxTail) break;
             small_k0 = k;
         }
