@@ -6,6 +6,8 @@
 // order with the same fixed tree and finishes the iteration's scalar work
 // (alpha, beta, the convergence test). No floating-point atomics, so the same
 // inputs give the same bits on every run and in graph or direct launches.
+// The double-word kernels (k_dw.cu, k_batch.cu) run the same trees on float
+// pairs instead (block_sum_acc2 / publish_acc2 / gather_acc2 in dw_dev.cuh).
 #pragma once
 #include "device.h"
 
