@@ -1,26 +1,28 @@
 """Benchmark: steady MG-PCG solves per second on the 800 x 800 x 10 stack.
 
 Workload (a "step"): one steady solve from T = 0 to ||r|| / ||P|| < 1e-10 of
-the 800 x 800 x 10 two-tier stack (25 W per Si tier + a seeded 3 W, 1 mm
-hotspot), FP32 V-cycle inside flexible PCG whose outer iteration runs in
-double-word arithmetic on the FP32 pipes with one FP64 residual replacement
-(CT_MG_FP32_FLEX_DW), the operator and multigrid hierarchy resident in HBM
-(built once, outside the timed region, as in a power-map sweep). Inputs are
-larger than L2 (the fine level alone moves > 1 GB per iteration), so no L2
-flush is needed between steps.
+the 800 x 800 x 10 two-tier stack (the reference's default_stack: 25 W per Si
+tier + a seeded 3 W, 1 mm hotspot in the bottom tier), FP32 V-cycle inside a
+flexible PCG whose outer iteration - residual and iterate updates, dot
+products, alpha and beta - is FP64 (CT_MG_FP32_FLEX), with the operator and
+multigrid hierarchy resident in HBM (built once, outside the timed region, as
+in a power-map sweep). Inputs are larger than L2 (the fine level alone moves
+> 1 GB per iteration), so no L2 flush is needed between steps.
 
-Reported beside it, on the same GPU: the 1024 x 1024 x 16 four-tier stack
-(DW, FLEX and FP64 solves/s), the batched backward-Euler run (64
-switching 256 x 256 x 10 stacks, 500 steps, per-instance dt), the batched form
-on a 256-instance
-floorplan sweep (uneven stacks solved together, instance solves/s against
-the plain FP64 MG-PCG solving the same instances one by one), the FP32
-V-cycle in FP64 flexible PCG
-(CT_MG_FP32_FLEX), the plain FP64 MG-PCG (FP64 V-cycle), max|dT| and the
-FP64 true residual of each, the end-to-end rate through the C ABI with the
-power map copied in and the temperatures copied out every step, the
-per-kernel roofline of the dominant kernel, and the CPU oracle (a C
-restatement of the reference CPU solver) timed on this machine's host cores.
+Reported beside it, on the same GPU and the same model: the plain FP64
+MG-PCG (FP64 V-cycle); the same FP32 V-cycle with the outer iteration in
+double-word arithmetic on the FP32 pipes (CT_MG_FP32_FLEX_DW); the
+reference's own GPU solver (src/pcg3d_gpu.cu, compiled for sm_103a from an
+unmodified copy, in its default and -DMG_DOUBLE builds; a child process);
+max|dT| and the FP64 true residual of each; the end-to-end rate through the
+C ABI with the power map copied in and the temperatures copied out every
+step; the per-kernel roofline; the 1024 x 1024 x 16 four-tier stack; the
+batched 256-instance floorplan sweep; the 800 x 800 and batched 64 x 256 x
+256 backward-Euler runs; and the reference CPU solver on the host cores.
+
+--impl reference times the UNMODIFIED reference CPU solver (src/pcg3d_cpu.cpp,
+default build, model built by the reference's own stack3d.h functions) on
+every host core, one steady solve of the same workload per core and step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -53,6 +55,9 @@ TR_N, TR_GRID, TR_SEED = 64, 256, 5   # batched transient: instances, lateral si
 TR_DT0, TR_GROWTH, TR_DT_MAX, TR_TOL = 1e-5, 1.1, 0.05, 1e-9
 TR_CHECK = 4   # instances re-run with the plain FP64 solver for max|dT| and its rate
 FALLBACK_HBM_GBS = 6800.0
+# the workload as both arms name it
+WORKLOAD = (f"steady solve {N_GRID}x{N_GRID}x10 two-tier stack (default_stack), 25 W per Si tier "
+            f"+ 3 W 1 mm hotspot at a seeded position (seed {SEED}), tol {TOL:g}, from T = 0")
 
 
 def log(*a):
@@ -196,36 +201,6 @@ def timed_solves(ct, solver, k, world):
     return ms, stats
 
 
-def cpu_oracle_rate(m, threads, solves_per_thread=1, mg_double=False, flexible=False):
-    """The CPU oracle (reference default build arithmetic) on `threads` host
-    threads, each solving its own copy of the workload; returns solves/s and
-    the seconds the timed phase took."""
-    import oracle
-    solvers = [oracle.Solver(m, "multigrid", mg_double=mg_double, flexible=flexible)
-               for _ in range(threads)]
-    go = threading.Barrier(threads + 1)
-    iters = [0] * threads
-
-    def work(k):
-        s = solvers[k]
-        go.wait()
-        for _ in range(solves_per_thread):
-            s.set_x_zero()
-            s.set_rhs_steady()
-            iters[k] = s.solve(TOL, MAXIT)[0]
-
-    th = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
-    for t in th:
-        t.start()
-    go.wait()
-    t0 = time.perf_counter()
-    for t in th:
-        t.join()
-    sec = time.perf_counter() - t0
-    del solvers
-    return threads * solves_per_thread / sec, sec, iters[0]
-
-
 def host_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -233,25 +208,91 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+class RefCpu:
+    """The reference CPU solver on `threads` host threads, one CpuPcg per
+    thread solving the workload's model from T = 0 (the unmodified reference,
+    kind "reference", when its sources are staged and its build succeeds;
+    otherwise the C oracle, a restatement of the same arithmetic, kind
+    "port"). Set-up (model, levels, factors) happens once, outside timing."""
+
+    def __init__(self, threads):
+        self.threads = threads
+        self.kind = "port"
+        self.why = ""
+        self.model = self.solvers = None
+        try:
+            from oracle import ref
+            if ref.available() or ref.stage():
+                ref.build()
+                self.kind = "reference"
+        except Exception as e:  # noqa: BLE001 - reported in the JSON line
+            self.why = f"reference build unavailable ({e}); C oracle port timed instead"
+        if self.kind == "port":
+            import oracle
+            import workloads
+            oracle.build()
+            m = workloads.steady_hotspot(N_GRID, seed=SEED)
+            self.port = [oracle.Solver(m, "multigrid", mg_double=False) for _ in range(threads)]
+
+    def step(self):
+        """One timed step: every thread solves once. (solves/s, seconds, iterations)"""
+        if self.kind == "reference":
+            from oracle import ref_bench
+            rate, sec, it, self.model, self.solvers = ref_bench.cpu_rate(
+                N_GRID, SEED, self.threads, TOL, MAXIT, model=self.model, solvers=self.solvers)
+            return rate, sec, it
+        go = threading.Barrier(self.threads + 1)
+        iters = [0] * self.threads
+
+        def work(k):
+            s = self.port[k]
+            go.wait()
+            s.set_x_zero()
+            s.set_rhs_steady()
+            iters[k] = s.solve(TOL, MAXIT)[0]
+
+        th = [threading.Thread(target=work, args=(k,)) for k in range(self.threads)]
+        for t in th:
+            t.start()
+        go.wait()
+        t0 = time.perf_counter()
+        for t in th:
+            t.join()
+        sec = time.perf_counter() - t0
+        return self.threads / sec, sec, iters[0]
+
+    def close(self):
+        if self.kind == "reference" and self.solvers:
+            from oracle import ref_bench
+            ref_bench.free_cpu_solvers(self.solvers)
+            self.solvers = None
+
+    def describe(self, sec, it, steps):
+        what = ("unmodified reference src/pcg3d_cpu.cpp (default build: float V-cycle, FP64 PCG), "
+                "model from the reference's stack3d.h" if self.kind == "reference" else
+                "C oracle port of src/pcg3d_cpu.cpp (float V-cycle)")
+        d = (f"{self.threads} threads x {steps} step(s) x 1 steady {N_GRID}x{N_GRID}x10 solve each "
+             f"({sec:.1f} s, {it} iterations); {what}")
+        return d + (f"; {self.why}" if self.why else "")
+
+
 def run_reference(args):
-    """Reference arm: the reference CPU solver's arithmetic (the C oracle, a
-    restatement of src/pcg3d_cpu.cpp in its default float-V-cycle build) on
-    every host thread, each thread solving its own copy of the workload."""
+    """Reference arm: the unmodified reference CPU solver (CpuPcg of
+    src/pcg3d_cpu.cpp, default build) on every host core, each core solving
+    its own copy of the workload once per step. Nothing of this library is
+    loaded. Under torchrun only rank 0 runs."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import oracle
-    import workloads
-    oracle.build()
-    m = workloads.steady_hotspot(N_GRID, seed=SEED)
     threads = host_threads()
+    rc = RefCpu(threads)
     for _ in range(args.warmup):
-        cpu_oracle_rate(m, threads)
-    rates, secs = [], []
+        rc.step()
+    secs, it = [], 0
     for _ in range(args.steps):
-        r, s, it = cpu_oracle_rate(m, threads)
-        rates.append(r)
-        secs.append(s)
+        _, sec, it = rc.step()
+        secs.append(sec)
+    rc.close()
     total = sum(secs)
     value = threads * args.steps / total
     out = {
@@ -259,15 +300,49 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"steady solve {N_GRID}x{N_GRID}x10, tol {TOL:g}",
+        "config": {"workload": WORKLOAD, "cells": N_GRID * N_GRID * 10,
+                   "precision": "reference default build (float V-cycle in FP64 PCG)",
                    "iters": it, "cpu_threads": threads},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": f"{threads} threads x 1 steady {N_GRID}x{N_GRID}x10 solve per step"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": rc.kind,
+                         "sample": rc.describe(total, it, args.steps)},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
     return 0
+
+
+def reference_gpu(np, T, steps, warmup):
+    """The reference's own GPU solver (src/pcg3d_gpu.cu for sm_103a, from an
+    unmodified copy; default and -DMG_DOUBLE builds) on the same model, in a
+    child process: solves/s, iterations, set-up, and max|dT| against this
+    library's solves T[name]."""
+    try:
+        from oracle import ref
+        if not (ref.available() or ref.stage()):
+            return {"unavailable": "reference sources not staged"}
+        ref.build(gpu=True)
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference GPU build failed: {e}"}
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        for name, flag in (("default", []), ("mg_double", ["--mg-double"])):
+            f = os.path.join(td, f"T_{name}.npy")
+            cmd = [sys.executable, "-m", "oracle.ref_bench", "gpu", "--n", str(N_GRID), "--seed",
+                   str(SEED), "--steps", str(steps), "--warmup", str(warmup), "--tol", str(TOL),
+                   "--maxit", str(MAXIT), "--out", f] + flag
+            try:
+                r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=900)
+                res = json.loads(r.stdout.strip().splitlines()[-1])
+            except Exception as e:  # noqa: BLE001
+                out[name] = {"unavailable": f"reference GPU run failed: {e}"}
+                continue
+            if os.path.exists(f):
+                Tr = np.load(f)
+                for k, v in T.items():
+                    res[f"max_dT_K_vs_{k}"] = float(np.abs(Tr - v).max())
+            out[name] = res
+    return out
 
 
 def traffic_from_profiles(kernel_name):
@@ -378,8 +453,8 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
 
 def bench_four_tier(ct, np, torch, args):
     """The 1024 x 1024 x 16 four-tier stack (TSV blocks, log-normal
-    floorplans, 80 W): DW, FLEX and plain FP64 steady solves/s on the same
-    GPU, max|dT|, FP64 true residuals."""
+    floorplans, 80 W): FLEX (the value), DW and plain FP64 steady solves/s
+    on the same GPU, max|dT| against FP64, FP64 true residuals."""
     import workloads
     m = workloads.four_tier(1024, seed=3)
     out = {"workload": "steady solve 1024x1024x16 four-tier stack (Si/bond x4, TIM, Cu), 2 % Cu "
@@ -399,12 +474,13 @@ def bench_four_tier(ct, np, torch, args):
         out[key] = {"value": k / (ms / 1e3), "unit": "solves/s", "iters": st[-1].iters,
                     "ms_per_solve": ms / k, "true_relres": s.true_relres()}
         s.close()
-    out["value"] = out["dw"]["value"]
+    out["value"] = out["flex"]["value"]
     out["unit"] = "solves/s"
-    out["speedup_vs_fp64"] = out["dw"]["value"] / out["fp64"]["value"]
-    out["flex_speedup_vs_fp64"] = out["flex"]["value"] / out["fp64"]["value"]
-    out["max_dT_K"] = float(np.abs(T["dw"] - T["fp64"]).max())
-    out["max_dT_K_flex"] = float(np.abs(T["flex"] - T["fp64"]).max())
+    out["precision"] = "CT_MG_FP32_FLEX"
+    out["speedup_vs_fp64"] = out["flex"]["value"] / out["fp64"]["value"]
+    out["dw_speedup_vs_fp64"] = out["dw"]["value"] / out["fp64"]["value"]
+    out["max_dT_K"] = float(np.abs(T["flex"] - T["fp64"]).max())
+    out["max_dT_K_dw"] = float(np.abs(T["dw"] - T["fp64"]).max())
     return out
 
 
@@ -496,9 +572,10 @@ def bench_transient_800(ct, np, solvers, m, steps):
     with the power on at t = 0 (run_transient, src/transient3d.h:48-90), dt
     10 us growing 10 % per step up to 50 ms, tol 1e-9, each step warm-started
     from the last; per step set_dt, b = P + C/dt T, the solve and the step
-    record (T_max, heat out, heat stored reduced on the device). The double-
-    word solver against the plain FP64 MG-PCG on the same steps; the
-    solvers already hold the operator and hierarchy."""
+    record (T_max, heat out, heat stored reduced on the device). The FP32
+    V-cycle in FP64 flexible PCG (and the double-word form) against the plain
+    FP64 MG-PCG on the same steps; the solvers already hold the operator and
+    hierarchy."""
     ptot = float(np.sum(m.P))
     res = {}
     for name, s in solvers.items():
@@ -517,19 +594,39 @@ def bench_transient_800(ct, np, solvers, m, steps):
         sec = time.perf_counter() - t0
         res[name] = dict(sec=sec, iters=its, eb=eb, T=s.get_x(), T_max=rec.T_max)
         s.set_dt(0.0)
-    dw, f64 = res["dw"], res["fp64"]
-    return {
-        "value": steps / dw["sec"], "unit": "steps/s",
+    fx, f64 = res["flex"], res["fp64"]
+    out = {
+        "value": steps / fx["sec"], "unit": "steps/s", "precision": "CT_MG_FP32_FLEX",
         "workload": f"{N_GRID}x{N_GRID}x10 stack, {steps} backward-Euler steps from T = 0, dt "
                     f"{TR_DT0:g} s x {TR_GROWTH} per step (max {TR_DT_MAX:g}), tol {TR_TOL:g}, "
                     f"device step records",
-        "steps": steps, "iters_total": dw["iters"], "energy_balance_err_max": dw["eb"],
-        "T_max_end_K": dw["T_max"],
+        "steps": steps, "iters_total": fx["iters"], "energy_balance_err_max": fx["eb"],
+        "T_max_end_K": fx["T_max"],
         "fp64_mg_pcg": {"value": steps / f64["sec"], "unit": "steps/s", "iters_total": f64["iters"],
                         "energy_balance_err_max": f64["eb"]},
-        "speedup_vs_fp64": f64["sec"] / dw["sec"],
-        "max_dT_K_vs_fp64": float(np.abs(dw["T"] - f64["T"]).max()),
+        "speedup_vs_fp64": f64["sec"] / fx["sec"],
+        "max_dT_K_vs_fp64": float(np.abs(fx["T"] - f64["T"]).max()),
     }
+    if "dw" in res:
+        dw = res["dw"]
+        out["double_word"] = {"value": steps / dw["sec"], "unit": "steps/s", "iters_total": dw["iters"],
+                              "energy_balance_err_max": dw["eb"],
+                              "max_dT_K_vs_fp64": float(np.abs(dw["T"] - f64["T"]).max())}
+    return out
+
+
+def profile_rows(solver):
+    """Per-kernel CUDA-event times of one solve launched kernel by kernel."""
+    solver.set_x_zero()
+    solver.set_rhs_steady()
+    _, rows = solver.profile_solve(TOL, MAXIT)
+    rows.sort(key=lambda r: -r["total_ms"])
+    return rows
+
+
+def kernel_table(rows, n=10):
+    return [{"name": r["name"], "launches": r["launches"], "ms": round(r["total_ms"], 4),
+             "GBs": round(r["bytes"] / (r["total_ms"] / 1e3) / 1e9, 1)} for r in rows[:n]]
 
 
 def main():
@@ -539,6 +636,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 256-instance run")
     ap.add_argument("--no-four-tier", action="store_true", help="skip the 1024x1024x16 stack")
     ap.add_argument("--transient-steps", type=int, default=500,
@@ -562,31 +660,31 @@ def main():
     m = workloads.steady_hotspot(N_GRID, seed=SEED)
     ncells = m.ncells()
 
-    s32 = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX_DW)
     sfx = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX)
+    sdw = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP32_FLEX_DW)
     s64 = ct.GpuPcg(m, ct.Precond.Multigrid, ct.Precision.MG_FP64)
     for _ in range(args.warmup):
-        for s in (s32, sfx, s64):
+        for s in (sfx, sdw, s64):
             s.set_x_zero()
             s.set_rhs_steady()
             s.solve(TOL, MAXIT)
 
-    # ---- headline: FP32 V-cycle, double-word flexible PCG, device-resident -
+    # ---- headline: FP32 V-cycle in FP64 flexible PCG, device-resident -------
     clocks = ClockSampler(local)
     clocks.start()
-    ms32, st32 = timed_solves(ct, s32, args.steps, world)
-    T32 = s32.get_x()
-    true32 = s32.true_relres()
-    ms32 = max_over_ranks(ms32, world)
-    value = sum_over_ranks(args.steps, world) / (ms32 / 1e3)
-
-    # ---- FP32 V-cycle in FP64 flexible PCG -----------------------------------
-    kfx = max(3, args.steps // 2)
-    msfx, stfx = timed_solves(ct, sfx, kfx, world)
+    msfx, stfx = timed_solves(ct, sfx, args.steps, world)
     Tfx = sfx.get_x()
     truefx = sfx.true_relres()
     msfx = max_over_ranks(msfx, world)
-    valuefx = sum_over_ranks(kfx, world) / (msfx / 1e3)
+    value = sum_over_ranks(args.steps, world) / (msfx / 1e3)
+
+    # ---- the same with the outer iteration in double words (FP32 pipes) -----
+    kdw = max(3, args.steps // 2)
+    msdw, stdw = timed_solves(ct, sdw, kdw, world)
+    Tdw = sdw.get_x()
+    truedw = sdw.true_relres()
+    msdw = max_over_ranks(msdw, world)
+    valuedw = sum_over_ranks(kdw, world) / (msdw / 1e3)
 
     # ---- plain FP64 MG-PCG on the same GPU ---------------------------------
     k64 = max(3, args.steps // 2)
@@ -595,46 +693,40 @@ def main():
     true64 = s64.true_relres()
     ms64 = max_over_ranks(ms64, world)
     value64 = sum_over_ranks(k64, world) / (ms64 / 1e3)
-    max_dT = float(np.abs(T32 - T64).max())
-    max_dT_fx = float(np.abs(Tfx - T64).max())
 
     # ---- end to end through the C ABI: host P in, host T out -------------
     P_host = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
     T_host = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
     P_np, T_np = P_host.numpy(), T_host.numpy()
     P_np[:] = m.P
-    stream = torch.cuda.ExternalStream(s32.stream())
+    stream = torch.cuda.ExternalStream(sfx.stream())
     torch.cuda.synchronize()
     barrier(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record(stream)
     for _ in range(args.steps):
-        s32.set_power(P_np)
-        s32.set_x_zero()
-        s32.set_rhs_steady()
-        s32.solve(TOL, MAXIT)
-        s32.get_x(T_np)
+        sfx.set_power(P_np)
+        sfx.set_x_zero()
+        sfx.set_rhs_steady()
+        sfx.solve(TOL, MAXIT)
+        sfx.get_x(T_np)
     e1.record(stream)
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t0
     ms_e2e = max_over_ranks(e0.elapsed_time(e1), world)
     e2e_value = sum_over_ranks(args.steps, world) / (ms_e2e / 1e3)
-    e2e_same_bits = bool(np.array_equal(T_np, T32))
+    e2e_same_bits = bool(np.array_equal(T_np, Tfx))
 
     # ---- roofline: per-kernel CUDA-event times of one solve ------------------
-    s32.set_x_zero()
-    s32.set_rhs_steady()
-    _, rows = s32.profile_solve(TOL, MAXIT)
-    rows.sort(key=lambda r: -r["total_ms"])
+    rows = profile_rows(sfx)
     tot_ms = sum(r["total_ms"] for r in rows)
     top = rows[0]
     achieved = top["bytes"] / top["launches"] / (top["total_ms"] / top["launches"] / 1e3) / 1e9
     traffic = traffic_from_profiles(top["name"])
     alg_bytes_solve = sum(r["bytes"] for r in rows)
-    iters = st32[-1].iters
-    nlev = s32.num_levels()
     launches_per_solve = sum(r["launches"] for r in rows)
+    rows_dw = profile_rows(sdw)
 
     batched = None
     if not args.no_batch:
@@ -649,55 +741,43 @@ def main():
         transient = bench_transient_batched(ct, np, args, args.transient_steps)
     transient800 = None
     if args.transient_800_steps > 0:
-        transient800 = bench_transient_800(ct, np, {"dw": s32, "fp64": s64}, m, args.transient_800_steps)
-    # clocks sampled over every timed region above (headline, FP64, e2e, batched)
+        transient800 = bench_transient_800(ct, np, {"flex": sfx, "dw": sdw, "fp64": s64}, m,
+                                           args.transient_800_steps)
+    # clocks sampled over every timed region above
     clk = clocks.stop()
+
+    ref_gpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        ref_gpu = reference_gpu(np, {"flex": Tfx, "fp64": T64}, max(3, args.steps // 2),
+                                args.warmup)
+        for k in ("default", "mg_double"):
+            if isinstance(ref_gpu.get(k), dict) and ref_gpu[k].get("value"):
+                ref_gpu[k]["flex_speedup"] = value / ref_gpu[k]["value"]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        threads = host_threads()
-        rate, sec, it = cpu_oracle_rate(m, threads)
-        cpu = {"value": rate, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": f"{threads} threads x 1 steady {N_GRID}x{N_GRID}x10 solve "
-                         f"({sec:.1f} s, {it} iterations, float V-cycle as the reference default)"}
+        rc = RefCpu(host_threads())
+        rate, sec, it = rc.step()
+        rc.close()
+        cpu = {"value": rate, "unit": "solves/s", "cores": rc.threads, "kind": rc.kind,
+               "sample": rc.describe(sec, it, 1)}
 
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": msfx / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64+f32", "data": "synthetic",
-            "config": {"workload": f"steady solve {N_GRID}x{N_GRID}x10 two-tier stack, seeded "
-                                   f"3 W hotspot, tol {TOL:g}, FP32 V-cycle in flexible PCG, "
-                                   f"double-word outer on FP32 pipes + FP64 residual replacement",
-                       "precision": "CT_MG_FP32_FLEX_DW",
-                       "cells": ncells, "levels": nlev, "iters": iters,
+            "config": {"workload": WORKLOAD, "cells": ncells,
+                       "precision": "CT_MG_FP32_FLEX",
+                       "precision_note": "FP32 V-cycle in flexible PCG; FP64 residual and iterate "
+                                         "updates, dot products, alpha, beta",
+                       "levels": sfx.num_levels(), "iters": stfx[-1].iters,
                        "l2": "inputs larger than L2 (fine level ~1.7 GB moved per iteration)",
                        "parallelism": f"replicas x{world}"},
-            "fp64_mg_pcg": {"value": value64, "unit": "solves/s", "iters": st64[-1].iters,
-                            "ms_per_solve": ms64 / k64, "true_relres": true64},
-            "fp32_mg_fp64_outer": {"value": valuefx, "unit": "solves/s", "iters": stfx[-1].iters,
-                                   "ms_per_solve": msfx / kfx, "true_relres": truefx,
-                                   "max_dT_K": max_dT_fx, "speedup_vs_fp64": valuefx / value64},
-            "speedup_vs_fp64": value / value64,
-            "max_dT_K": max_dT,
-            "true_relres": true32,
-            "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved,
-                         "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                         "peak_kind": peak_kind, "traffic": traffic,
-                         "alg_bytes_per_launch": top["bytes"] / top["launches"],
-                         "launch_ms": top["total_ms"] / top["launches"],
-                         "share": top["total_ms"] / tot_ms,
-                         "solve_frac": alg_bytes_solve / (ms32 / args.steps / 1e3) / 1e9 / hbm_peak},
-            "kernels": [{"name": r["name"], "launches": r["launches"],
-                         "ms": round(r["total_ms"], 4),
-                         "GBs": round(r["bytes"] / (r["total_ms"] / 1e3) / 1e9, 1)}
-                        for r in rows[:12]],
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": ncells * 8,
-                    "d2h_bytes_per_step": ncells * 8, "wall_s": wall_e2e,
-                    "same_bits_as_device_run": e2e_same_bits},
             "gpu_launches": launches_per_solve * args.steps,
-            "clocks": clk,
+            "kernels": kernel_table(rows),
+            "double_word_kernels": kernel_table(rows_dw, 6),
         }
         if batched:
             out["batched"] = batched
@@ -707,11 +787,33 @@ def main():
             out["transient_800"] = transient800
         if four:
             out["four_tier"] = four
+        out["e2e"] = {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": ncells * 8,
+                      "d2h_bytes_per_step": ncells * 8, "wall_s": wall_e2e,
+                      "same_bits_as_device_run": e2e_same_bits}
+        out["roofline"] = {"bound": "hbm", "kernel": top["name"], "achieved": achieved,
+                           "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                           "peak_kind": peak_kind, "traffic": traffic,
+                           "alg_bytes_per_launch": top["bytes"] / top["launches"],
+                           "launch_ms": top["total_ms"] / top["launches"],
+                           "share": top["total_ms"] / tot_ms,
+                           "solve_frac": alg_bytes_solve / (msfx / args.steps / 1e3) / 1e9 / hbm_peak}
+        out["true_relres"] = truefx
+        out["double_word"] = {"value": valuedw, "unit": "solves/s", "precision": "CT_MG_FP32_FLEX_DW",
+                              "iters": stdw[-1].iters, "ms_per_solve": msdw / kdw,
+                              "true_relres": truedw, "max_dT_K_vs_fp64": float(np.abs(Tdw - T64).max()),
+                              "speedup_vs_fp64": valuedw / value64}
+        out["fp64_mg_pcg"] = {"value": value64, "unit": "solves/s", "iters": st64[-1].iters,
+                              "ms_per_solve": ms64 / k64, "true_relres": true64}
+        out["max_dT_K"] = float(np.abs(Tfx - T64).max())
+        out["speedup_vs_fp64"] = value / value64
+        if ref_gpu is not None:
+            out["reference_gpu"] = ref_gpu
         if cpu:
             out["cpu_baseline"] = cpu
+        out["clocks"] = clk
         print(json.dumps(out), flush=True)
-    s32.close()
     sfx.close()
+    sdw.close()
     s64.close()
     if world > 1:
         import torch.distributed as td

@@ -10,7 +10,7 @@
 // skipped; '#' lines are comments (settings in stack.csv); fields are trimmed
 // of blanks and double quotes. Numbers are read as leading decimal prefixes
 // (as std::stod / std::stoi read them). The model is then built with the
-// library's stack builder (build_case_model, src/case3d.h:158-168).
+// library's stack builder (build_case_model, src/case3d.h:157-166).
 #include <algorithm>
 #include <cctype>
 #include <cerrno>
@@ -207,7 +207,7 @@ struct ct_case {
 
 namespace ct {
 
-// The device build of build_case_model (src/case3d.h:158-168): planes as
+// The device build of build_case_model (src/case3d.h:157-166): planes as
 // ct_model_planes lays them out, every power block, every TSV region (when
 // wanted), copper TSV material.
 ct_status case_build(const ct_case* c, int nx, int ny, bool with_tsv, DeviceBuild* b) {
@@ -255,7 +255,7 @@ void copy_name(const std::string& s, char* out, int cap) {
 using ct::fail;
 
 // ---- export to 3D-ICE -----------------------------------------------------------
-// export_3dice / export_3dice_layout (src/case3d.h:195-383): the case as 3D-ICE
+// export_3dice / export_3dice_layout (src/case3d.h:192-383): the case as 3D-ICE
 // 4.0 input on a uniform grid of cell_um: <outdir>/case.stk (materials, top
 // heat sink, dimensions, one layer type per plane of a passive layer, one die
 // per active layer with its single source layer, the stack listed top to

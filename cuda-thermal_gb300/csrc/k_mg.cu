@@ -1,7 +1,7 @@
 // k_mg.cu - multigrid V-cycle kernels (x-y semi-coarsening, red-black column
 // line smoother) and the multigrid setup kernels, for T = float or double.
 //
-// Sweeps (mg_line_solve, src/mg3d.h:175-196): one thread per column of the
+// Sweeps (mg_line_solve, src/mg3d.h:67-84): one thread per column of the
 // active colour, so a warp reads one contiguous half-row of the split layout
 // per z-plane. The column is eliminated forward through the planes with the
 // precomputed Thomas factors and substituted back in registers, so x is
@@ -28,7 +28,7 @@ using namespace setupdev;
 
 namespace {
 
-// mg_factor_column (src/mg3d.h:157-173): Thomas factors of every column.
+// mg_factor_column (src/mg3d.h:46-61): Thomas factors of every column.
 template <class T>
 __global__ void k_factor(LevelView<T> L, T inv_dt) {
     const unsigned ncol = (unsigned)L.g.nx * L.g.ny;
@@ -36,7 +36,7 @@ __global__ void k_factor(LevelView<T> L, T inv_dt) {
         factor_column<T>(L, inv_dt, q);
 }
 
-// mg_coarse_cell (src/mg3d.h:206-248) on split layouts: one thread per coarse
+// mg_coarse_cell (src/mg3d.h:100-136) on split layouts: one thread per coarse
 // cell, sums in double in the reference's child order, one cast to float.
 __global__ void k_coarsen(Geo fg, const float* __restrict__ fgE, const float* __restrict__ fgN,
                           const float* __restrict__ fgU, const float* __restrict__ fgB,

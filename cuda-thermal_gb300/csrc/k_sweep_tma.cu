@@ -1,18 +1,19 @@
 // k_sweep_tma.cu - the red-black column line solve of the large multigrid
-// levels (mg_line_solve, src/mg3d.h:179-196), with its operands staged in
+// levels (mg_line_solve, src/mg3d.h:67-84), with its operands staged in
 // shared memory by bulk tensor copies (TMA).
 //
 // Work unit: a tile of 32 x 8 columns of the sweep's colour (32 consecutive
-// slots of 8 rows j), one thread per column, all nz planes. For each plane of
-// the tile one thread issues a handful of TMA box loads (the tile's own b,
-// column factors, gU, gE, gN and, with halos, the other colour's x, gE and gN
-// around it) into one stage of a ring of kStages stages. The block is
-// persistent over its tiles and the ring runs across tile boundaries, so the
-// copies for the next planes (and the next tile) are in flight while the
-// threads run the Thomas recurrence on the current one. Each thread keeps its
-// column's forward values in registers and writes x once after the last
-// plane. The arithmetic is the grid kernel's (k_mg.cu), operation for
-// operation.
+// slots of 8 rows j), one thread per column, all nz planes. A block is 8
+// consumer warps (one tile row each) and one producer warp, whose lane 0
+// issues, for each plane of the tile, a handful of TMA box loads (the tile's
+// own b, column factors, gU, gE, gN and, with halos, the other colour's x, gE
+// and gN around it) into one stage of a ring of kSweepStagesWs stages. The
+// block is persistent over its tiles and the ring runs across tile
+// boundaries, so the copies for the next planes (and the next tile) are in
+// flight while the consumers run the Thomas recurrence on the current one.
+// Each consumer thread keeps its column's forward values in registers and
+// writes x once after the last plane. The arithmetic is the grid kernel's
+// (k_mg.cu), operation for operation.
 //
 // Every mbarrier wait is bounded; a wait that runs out sets ctl->err and ends
 // the solve, and the block leaves after waiting (bounded) for its own copies.
@@ -91,128 +92,6 @@ __device__ __forceinline__ void issue_plane(const SweepMaps* m, float* sm, uint6
         load_3d(st + 5 * S::own + S::ox, &m->oge, t0 - 4, j0, l, bar);
         load_3d(st + 5 * S::own + S::ox + S::oge, &m->ogn, t0, j0 - 1, l, bar);
     }
-}
-
-// The line solves of a block's tiles (all threads of the block call it).
-// Returns false if a wait ran out; the block's copies still in flight have
-// then landed (bounded) and the caller records the failure.
-template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
-__device__ __forceinline__ bool sweep_tiles(const SweepMaps* m, const LevelView<float>& L,
-                                            const LevelView<float>& C, int color,
-                                            const TileList& tl, float* sm, uint64_t* full) {
-    using S = Stage<TT, TJ>;
-    constexpr int stage_f = ZERO ? S::zero : S::full;
-    const Geo& g = L.g;
-    const int nz = g.nz;
-    const int tilesx = (g.hx + TT - 1) / TT;
-    const int nitems = tl.count * nz;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
-        for (int w = 0; w < NS && w < nitems; ++w) issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w, nz, tilesx, tl);
-
-    const int tx = (int)threadIdx.x % TT, ty = (int)threadIdx.x / TT;
-    const int o = ty * TT + tx;
-    int w = 0;
-    bool ok = true;
-    for (int mt = 0; mt < tl.count && ok; ++mt) {
-        const int tile = tl.tile(mt);
-        const int tyi = tile / tilesx;
-        const int t = (tile - tyi * tilesx) * TT + tx, j = tyi * TJ + ty;
-        const int e = (j + color) & 1;
-        const int i = 2 * t + e;
-        const bool act = j < g.ny && i < g.nx;
-        const bool hw = i > 0, he = i < g.nx - 1, hs = j > 0, hn = j < g.ny - 1;
-        unsigned pw = 0, pe = 0, ps = 0, pn = 0;
-        if (PRO && act) {
-            if (hw) pw = scol(C.g, (i - 1) >> 1, j >> 1);
-            if (he) pe = scol(C.g, (i + 1) >> 1, j >> 1);
-            if (hs) ps = scol(C.g, i >> 1, (j - 1) >> 1);
-            if (hn) pn = scol(C.g, i >> 1, (j + 1) >> 1);
-        }
-        float v[MZ], fcr[MZ];
-        float prev = 0.0f, gu_prev = 0.0f;
-#pragma unroll
-        for (int l = 0; l < MZ; ++l) {
-            if (l < nz) {
-                // the coarse corrections come from L2; load them before the wait
-                float cw = 0.0f, ce = 0.0f, cs = 0.0f, cn = 0.0f;
-                if (PRO && act) {
-                    const float* cx = C.x + (unsigned)l * C.g.plane;
-                    if (hw) cw = cx[pw];
-                    if (he) ce = cx[pe];
-                    if (hs) cs = cx[ps];
-                    if (hn) cn = cx[pn];
-                }
-                const int s = w % NS;
-                const bool got = mbar_wait(&full[s], (unsigned)(w / NS) & 1u);
-                const float* st = sm + s * stage_f;
-                if (act && got) {
-                    float rhs = st[o];
-                    const float fi = st[S::own + o], gu = st[2 * S::own + o];
-                    const float fc = __fmul_rn(-gu, fi);  // fcp as factor_column rounds it
-                    if (!ZERO) {
-                        const float* ox = st + 5 * S::own;
-                        const float* oge = ox + S::ox;
-                        const float* ogn = oge + S::oge;
-                        constexpr int W = S::oxw;
-                        // op_lat_sum order: west, east, south, north
-                        float sl = 0.0f;
-                        if (hw) {
-                            float xv = ox[(ty + 1) * W + tx + 3 + e];
-                            if (PRO) xv = xv + cw;
-                            sl += oge[ty * W + tx + 3 + e] * xv;
-                        }
-                        if (he) {
-                            float xv = ox[(ty + 1) * W + tx + 4 + e];
-                            if (PRO) xv = xv + ce;
-                            sl += st[3 * S::own + o] * xv;
-                        }
-                        if (hs) {
-                            float xv = ox[ty * W + tx + 4];
-                            if (PRO) xv = xv + cs;
-                            sl += ogn[ty * TT + tx] * xv;
-                        }
-                        if (hn) {
-                            float xv = ox[(ty + 2) * W + tx + 4];
-                            if (PRO) xv = xv + cn;
-                            sl += st[4 * S::own + o] * xv;
-                        }
-                        rhs = rhs + sl;
-                    }
-                    const float lower = l > 0 ? -gu_prev : 0.0f;
-                    prev = (rhs - lower * prev) * fi;
-                    v[l] = prev;
-                    fcr[l] = fc;
-                    gu_prev = gu;
-                }
-                // every thread is done with stage s: refill it
-                ok = __syncthreads_and(got) != 0;
-                if (!ok) break;
-                if (threadIdx.x == 0 && w + NS < nitems)
-                    issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w + NS, nz, tilesx, tl);
-                ++w;
-            }
-        }
-        if (!ok) break;
-        if (act) {
-#pragma unroll
-            for (int l = MZ - 2; l >= 0; --l)
-                if (l < nz - 1) v[l] -= fcr[l] * v[l + 1];
-            const unsigned s0 = (unsigned)(2 * j + color) * (unsigned)g.hx + (unsigned)t;
-#pragma unroll
-            for (int l = 0; l < MZ; ++l)
-                if (l < nz) L.x[(unsigned)l * g.plane + s0] = v[l];
-        }
-    }
-    if (!ok && threadIdx.x == 0) {
-        // let this block's copies still in flight land before it leaves
-        for (int q = w; q < w + NS && q < nitems; ++q) mbar_wait(&full[q % NS], (unsigned)(q / NS) & 1u);
-    }
-    return ok;
 }
 
 // The same line solves with a producer warp: TJ consumer warps (one tile row
@@ -381,48 +260,8 @@ __global__ void __launch_bounds__(TT * TJ + 32, MZ <= 16 ? kSweepWsBlocks : 2)
         fail_wait(ctl, cond);
 }
 
-// Single solver: the level's tiles spread over a persistent grid.
-template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
-__global__ void __launch_bounds__(TT * TJ, 2)
-    k_sweep_tma(const __grid_constant__ SweepMaps m, LevelView<float> L, LevelView<float> C,
-                int color, Ctl* ctl, Cond cond) {
-    pdl_enter();
-    if (loop_done(ctl, cond)) return;
-    extern __shared__ __align__(128) float sm[];
-    __shared__ uint64_t full[NS];
-    const Geo& g = L.g;
-    const int ntiles = ((g.hx + TT - 1) / TT) * ((g.ny + TJ - 1) / TJ);
-    const int count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const TileList tl{(int)blockIdx.x, (int)gridDim.x, count};
-    if (!sweep_tiles<TT, TJ, NS, MZ, ZERO, PRO>(&m, L, C, color, tl, sm, full) && threadIdx.x == 0)
-        fail_wait(ctl, cond);
-}
-
 // Batch: block b runs task b of the plan (consecutive tiles of one
 // instance's level); maps[i] are instance i's maps for this level and colour.
-template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
-__global__ void __launch_bounds__(TT * TJ, 2)
-    kb_sweep_tma(Plan p, const SweepMaps* __restrict__ maps, const LevelView<float>* __restrict__ views,
-                 const LevelView<float>* __restrict__ cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
-    const Task t = p.tasks[blockIdx.x];
-    Ctl* c = &ctl[t.inst];
-    if (*(volatile const int*)&c->done) return;
-    extern __shared__ __align__(128) float sm[];
-    __shared__ uint64_t full[NS];
-    const LevelView<float> L = views[t.inst];
-    const LevelView<float> C = PRO ? cviews[t.inst] : L;
-    const TileList tl{(int)t.begin, 1, (int)(t.end - t.begin)};
-    if (!sweep_tiles<TT, TJ, NS, MZ, ZERO, PRO>(&maps[t.inst], L, C, color, tl, sm, full) &&
-        threadIdx.x == 0) {
-        // stop this instance (once, whichever of its blocks gets here first)
-        atomicExch(&c->err, 1);
-        *(volatile int*)&c->breakdown = 1;
-        if (atomicExch(&c->done, 1) == 0 && atomicSub(&bc->active, 1) == 1 && cond.use)
-            cudaGraphSetConditional(cond.h, 0u);
-    }
-}
-
-// The batch kernel with a producer warp (sweep_tiles_ws).
 template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(TT * TJ + 32, MZ <= 16 ? kSweepWsBlocks : 2)
     kb_sweep_tma_ws(Plan p, const SweepMaps* __restrict__ maps, const LevelView<float>* __restrict__ views,
@@ -449,14 +288,6 @@ __global__ void __launch_bounds__(TT * TJ + 32, MZ <= 16 ? kSweepWsBlocks : 2)
 template <int TT, int TJ, int NS>
 constexpr size_t stage_bytes(bool zero_x) {
     return (size_t)NS * (zero_x ? Stage<TT, TJ>::zero : Stage<TT, TJ>::full) * sizeof(float);
-}
-
-bool sweep_ws() {
-    static const bool on = [] {
-        const char* e = std::getenv("CT_SWEEP_WS");
-        return !(e && e[0] == '0');
-    }();
-    return on;
 }
 
 template <int NS, int MZ, bool ZERO, bool PRO>
@@ -486,38 +317,9 @@ void go_ws_ns(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L, co
 }
 
 template <int MZ, bool ZERO, bool PRO>
-void go_ws(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L, const LevelView<float>& C,
-           int color, Ctl* ctl, Cond cond) {
-    go_ws_ns<kSweepStagesWs, MZ, ZERO, PRO>(st, m, L, C, color, ctl, cond);
-}
-
-template <int MZ, bool ZERO, bool PRO>
 void go(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L, const LevelView<float>& C,
         int color, Ctl* ctl, Cond cond) {
-    if (sweep_ws()) {
-        go_ws<MZ, ZERO, PRO>(st, m, L, C, color, ctl, cond);
-        return;
-    }
-    constexpr int TT = kTileT, TJ = kTileJ, NS = kSweepStages;
-    auto kern = k_sweep_tma<TT, TJ, NS, MZ, ZERO, PRO>;
-    // persistent grid: SMs x resident blocks of this instantiation, at most one per tile
-    static int full_wave = 0;
-    if (!full_wave) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TT * TJ,
-                                                          stage_bytes<TT, TJ, NS>(ZERO)) != cudaSuccess ||
-            per < 1) {
-            cudaGetLastError();
-            per = 1;
-        }
-        full_wave = std::max(1, sms) * per;
-    }
-    const Geo& g = L.g;
-    const int ntiles = ((g.hx + TT - 1) / TT) * ((g.ny + TJ - 1) / TJ);
-    const int grid = std::max(1, std::min(ntiles, full_wave));
-    launch_pdl(kern, grid, TT * TJ, stage_bytes<TT, TJ, NS>(ZERO), st, m, L, C, color, ctl, cond);
+    go_ws_ns<kSweepStagesWs, MZ, ZERO, PRO>(st, m, L, C, color, ctl, cond);
 }
 
 template <int MZ>
@@ -533,7 +335,7 @@ void go_sweep(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L,
 
 }  // namespace
 
-size_t sweep_tma_smem(bool zero_x) { return stage_bytes<kTileT, kTileJ, kSweepStages>(zero_x); }
+size_t sweep_tma_smem(bool zero_x) { return stage_bytes<kTileT, kTileJ, kSweepStagesWs>(zero_x); }
 
 bool sweep_tma_fits(const Geo& g) { return g.nz <= 32 && g.hx >= kTileT; }
 
@@ -555,18 +357,13 @@ namespace {
 template <int MZ, bool ZERO, bool PRO>
 void go_b(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView<float>* views,
           const LevelView<float>* cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
-    constexpr int TT = kTileT, TJ = kTileJ, NS = kSweepStages;
-    if (sweep_ws()) {
-        constexpr int NW = kSweepStagesWs;
-        auto kern = kb_sweep_tma_ws<TT, TJ, NW, MZ, ZERO, PRO>;
-        static const bool attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      (int)stage_bytes<TT, TJ, NW>(ZERO)) == cudaSuccess;
-        (void)attr;
-        kern<<<p.ntasks, TT * TJ + 32, stage_bytes<TT, TJ, NW>(ZERO), st>>>(p, maps, views, cviews, color, ctl,
-                                                                            bc, cond);
-    } else
-        kb_sweep_tma<TT, TJ, NS, MZ, ZERO, PRO><<<p.ntasks, TT * TJ, stage_bytes<TT, TJ, NS>(ZERO), st>>>(
-            p, maps, views, cviews, color, ctl, bc, cond);
+    constexpr int TT = kTileT, TJ = kTileJ, NW = kSweepStagesWs;
+    auto kern = kb_sweep_tma_ws<TT, TJ, NW, MZ, ZERO, PRO>;
+    static const bool attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)stage_bytes<TT, TJ, NW>(ZERO)) == cudaSuccess;
+    (void)attr;
+    kern<<<p.ntasks, TT * TJ + 32, stage_bytes<TT, TJ, NW>(ZERO), st>>>(p, maps, views, cviews, color, ctl,
+                                                                        bc, cond);
 }
 template <int MZ>
 void go_b_sweep(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView<float>* views,

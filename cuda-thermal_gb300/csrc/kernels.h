@@ -163,8 +163,7 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
 constexpr int kTileT = 32;  // slots per tile row
 constexpr int kTileJ = 8;   // rows per tile
 constexpr int kTileThreads = kTileT * kTileJ;
-constexpr int kSweepStages = 4;  // planes in flight per block
-constexpr int kSweepStagesWs = 6;  // the same with a producer warp (no block barrier per plane)
+constexpr int kSweepStagesWs = 6;  // planes in flight per block (a producer warp, no block barrier per plane)
 constexpr int kSweepWsBlocks = 3;  // resident blocks per SM the producer-warp sweeps are compiled for
 struct SweepMaps {
     CUtensorMap b, fi, gu, ge, gn;      // the sweep colour's rows, box kTileT x kTileJ
@@ -179,15 +178,6 @@ bool make_sweep_maps(const LevelView<float>& L, int color, SweepMaps* m, int til
 void launch_sweep_tma(cudaStream_t st, const SweepMaps& m, const LevelView<float>& L,
                       const LevelView<float>* coarse_for_prolong, int color, bool zero_x, Ctl* ctl,
                       Cond cond);
-// The double-word operator apply staged by bulk tensor copies
-// (k_apply_tma.cu): Ap, p.Ap and alpha like launch_apply_dw, same Ap bits.
-struct ApplyMaps {
-    CUtensorMap p, ge, gn, gu, dg;  // both colours' rows of p, gE, gN, gU and the DW diagonal
-};
-bool apply_tma_fits(const Geo& g);  // at least one full 32-slot half-row
-bool make_apply_maps(const OpView& o, const float2* p, const float2* dgw, ApplyMaps* m);
-cudaError_t launch_apply_tma(cudaStream_t st, const ApplyMaps& m, const OpView& o, float2* Ap,
-                             Ctl* ctl, const Red& red, Cond cond);
 // coarse b = sum over the children of (b - (A + C/dt) x).
 template <class T>
 void launch_restrict(cudaStream_t st, const LevelView<T>& F, const LevelView<T>& C, const Ctl* ctl,

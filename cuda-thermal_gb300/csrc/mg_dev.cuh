@@ -1,7 +1,7 @@
 // mg_dev.cuh - device code of the multigrid V-cycle shared by the single
 // solver (k_mg.cu) and the batched solver (k_batch.cu): neighbour maps of the
 // colour-split layout, the column line solve (mg_line_solve,
-// src/mg3d.h:179-196), the fine residual and restriction
+// src/mg3d.h:67-84), the fine residual and restriction
 // (src/pcg3d_cpu.cpp:87-100), and the shared-memory bottom of the V-cycle.
 #pragma once
 #include "kernels.h"
@@ -151,7 +151,7 @@ __device__ __forceinline__ void column_solve(const LevelView<T>& L, const T* src
 }
 
 // Line solve of the q-th column of colour `color` (mg_line_solve,
-// src/mg3d.h:179-196). With MZ > 0 (nz <= MZ) the column stays in registers:
+// src/mg3d.h:67-84). With MZ > 0 (nz <= MZ) the column stays in registers:
 // every plane's right-hand side (b plus the lateral sum) is gathered first,
 // all loads independent of one another, then the Thomas recurrence runs on
 // registers and x is written once. MZ = 0 is the general path for deep

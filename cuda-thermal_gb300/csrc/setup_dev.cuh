@@ -1,6 +1,6 @@
 // setup_dev.cuh - the per-column set-up arithmetic that depends on dt: the
 // FP64 diagonal of the fine operator (op_diag, src/operator3d.h:80-88) and the
-// Thomas factors of a multigrid level (mg_factor_column, src/mg3d.h:157-173),
+// Thomas factors of a multigrid level (mg_factor_column, src/mg3d.h:46-61),
 // every rounding explicit (no contraction) so both equal the CPU's bit for
 // bit. Shared by the single solver (k_outer.cu, k_mg.cu) and the batched
 // set_dt (k_batch.cu).

@@ -118,7 +118,7 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     CT_CK(cudaMallocHost(&h_ctl, sizeof(Ctl)));
     std::memset(h_ctl, 0, sizeof(Ctl));
 
-    // Level sizes (src/mg3d.h:271-293) and the arena layout.
+    // Level sizes (src/mg3d.h:159-181) and the arena layout.
     Arena ar;
     const size_t o_gE = ar.take(n * 4), o_gN = ar.take(n * 4), o_gU = ar.take(n * 4);
     const size_t o_cap = ar.take(n * 4), o_gB = ar.take((size_t)g0.plane * 4);
@@ -211,12 +211,6 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     CT_CK(cudaStreamSynchronize(st));
     times.alloc_ms = ms_since(t0);
 
-    // The staged DW operator apply (CT_APPLY=rows / cells / columns: the
-    // earlier forms).
-    if (dw && apply_tma_fits(g0)) {
-        const char* e = std::getenv("CT_APPLY");
-        if (e && e[0] == 't') apply_tma = make_apply_maps(op(), pw(), dgw, &amaps);
-    }
     // CT_FUSE_SWEEP0=0 keeps each level's first sweep a launch of its own
     // instead of riding along with the restriction into that level.
     if (const char* e = std::getenv("CT_FUSE_SWEEP0")) fuse_sweep0 = e[0] != '0';
@@ -416,14 +410,8 @@ void Solver::enqueue_body(Cond cond) {
         enq("pcg_dot", N * (8 + 4 + 8),
             [&] { launch_dot_dw(cs, n, rw(), zf, Apw(), ctl, red_vec(SL_DOT), cond); });
         enq("pcg_update_p", N * (4 + 16), [&] { launch_update_p_dw(cs, n, zf, pw(), ctl, cond); });
-        enq("pcg_apply", N * 36, [&] {
-            if (apply_tma) {
-                const cudaError_t e = launch_apply_tma(cs, amaps, op(), Apw(), ctl, red_cols(SL_APPLY), cond);
-                if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
-            } else {
-                launch_apply_dw(cs, op(), dgw, pw(), Apw(), ctl, red_cols(SL_APPLY), cond);
-            }
-        });
+        enq("pcg_apply", N * 36,
+            [&] { launch_apply_dw(cs, op(), dgw, pw(), Apw(), ctl, red_cols(SL_APPLY), cond); });
         enq("pcg_update_xr", N * (48 + 4), [&] {
             launch_update_dw(cs, n, pw(), Apw(), xw(), rw(), b0, ctl, red_vec(SL_UPDATE), cond);
         });

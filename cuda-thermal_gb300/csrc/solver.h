@@ -32,7 +32,7 @@ struct Level {
     SweepMaps maps[2];
 };
 
-// mg_coarse_widths (src/mg3d.h:250-256).
+// mg_coarse_widths (src/mg3d.h:139-144).
 inline std::vector<double> coarse_widths(const std::vector<double>& f) {
     std::vector<double> c;
     const int n = (int)f.size();
@@ -89,8 +89,6 @@ class Solver {
     bool prof = false;
     std::vector<ProfEntry> prof_log;
 
-    bool apply_tma = false;   // the DW apply staged by bulk tensor copies (maps below)
-    ApplyMaps amaps{};
     bool own_stream = true;   // false: st belongs to a batch that owns this solver
     bool skip_graphs = false; // batch members record no graphs of their own
 

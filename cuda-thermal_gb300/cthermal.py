@@ -461,7 +461,7 @@ def selftest_bounded_wait(polls: int) -> bool:
 
 
 def export_3dice(case, cell_um: float, outdir: str) -> None:
-    """export_3dice (src/case3d.h:266-383) of a case (a folder of CSV files or
+    """export_3dice (src/case3d.h:267-383) of a case (a folder of CSV files or
     a CaseSpec) on a grid of cell_um micrometres: case.stk, L<k>.flp and
     LT<k>_<p>.lay in the existing folder outdir (3D-ICE 4.0 input). Raises
     CtError with the reference's message when 3D-ICE cannot express the case."""
@@ -481,7 +481,7 @@ def export_3dice(case, cell_um: float, outdir: str) -> None:
 
 
 def read_3dice_tmap(path: str) -> np.ndarray:
-    """read_3dice_tmap (src/case3d.h:386-401): a 3D-ICE Tmap text file ('%'
+    """read_3dice_tmap (src/case3d.h:385-400): a 3D-ICE Tmap text file ('%'
     lines are comments) as a 2-D array, one row per line."""
     rows = []
     with open(path) as f:
@@ -543,7 +543,7 @@ def case_geometry(cs: CaseSpec, nx: int, ny: int) -> Model3D:
 
 
 def build_case_model(cs: CaseSpec, nx: int, ny: int, with_tsv: bool = True) -> Model3D:
-    """build_case_model (src/case3d.h:158-168)."""
+    """build_case_model (src/case3d.h:157-166)."""
     m = build_model(cs.layers, nx, ny, cs.Lx, cs.Ly, cs.h_top, cs.h_bot)
     m.T_amb = cs.T_amb
     for b in cs.blocks:

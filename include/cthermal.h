@@ -68,7 +68,7 @@ typedef enum ct_precision {
 
 /* A finalized Model3D's arrays (src/stack3d.h:45-79): gE, gN, gU, cap have
  * nx*ny*nz entries, gB nx*ny, P nx*ny*nz. dx, dy (m) are the lateral cell
- * sizes, which the multigrid coarsening needs (src/mg3d.h:259-265). */
+ * sizes, which the multigrid coarsening needs (src/mg3d.h:139-166). */
 typedef struct ct_model {
     int nx, ny, nz;
     double dx, dy;
@@ -130,7 +130,7 @@ ct_status ct_solver_create(const ct_model* m, ct_precond pc, ct_precision prec, 
 /* GpuPcg::~GpuPcg (src/pcg3d_gpu.cu:495-509). */
 ct_status ct_solver_destroy(ct_solver* s);
 /* No single counterpart in the reference: build_case_model
- * (src/case3d.h:158-168) followed by the solver's construction, with the
+ * (src/case3d.h:157-166) followed by the solver's construction, with the
  * model built on the device (power blocks, TSV regions and the face
  * conductances computed by kernels straight into the solver's layout; the
  * same arrays, bit for bit, as ct_model_* on the host), so a floorplan sweep
@@ -178,7 +178,7 @@ ct_status ct_solver_step_record(ct_solver* s, double dt, ct_step_record* out);
 ct_status ct_num_levels(const ct_solver* s, int* n);
 ct_status ct_level_dims(const ct_solver* s, int k, int* nx, int* ny, int* nz);
 /* Level k's operator (natural layout, host arrays as in MgLevelHost,
- * src/mg3d.h:200-204) as built on the device. gB has nx*ny entries. */
+ * src/mg3d.h:88-93) as built on the device. gB has nx*ny entries. */
 ct_status ct_level_operator(ct_solver* s, int k, float* gE, float* gN, float* gU, float* gB,
                             float* cap);
 /* Level k's column factors for the current dt, widened to double. */

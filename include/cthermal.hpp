@@ -451,7 +451,7 @@ inline bool load_case(const std::string& dir, CaseSpec& cs, std::string& err) {
     return true;
 }
 
-// build_case_model (src/case3d.h:158-168).
+// build_case_model (src/case3d.h:157-166).
 inline Model3D build_case_model(const CaseSpec& cs, int nx, int ny, bool with_tsv = true) {
     Model3D m = build_model(cs.layers, nx, ny, cs.Lx, cs.Ly, cs.h_top, cs.h_bot);
     m.T_amb = cs.T_amb;
@@ -462,7 +462,7 @@ inline Model3D build_case_model(const CaseSpec& cs, int nx, int ny, bool with_ts
     return m;
 }
 
-// export_3dice (src/case3d.h:266-383): false with the reference's message in
+// export_3dice (src/case3d.h:267-383): false with the reference's message in
 // err when 3D-ICE cannot express the case.
 inline bool export_3dice(const CaseSpec& cs, double cell_um, const std::string& outdir, std::string& err) {
     std::vector<ct_layer> ls;

@@ -83,7 +83,7 @@ ct_status ct_model_analytic_1d(const ct_grid* g, const ct_layer* layers, const i
  * message) for a malformed one. The model is then built with ct_model_planes,
  * ct_model_add_power_block for every block, ct_model_add_tsv_region for every
  * TSV region (when wanted) and ct_model_finalize, in that order
- * (build_case_model, src/case3d.h:158-168). */
+ * (build_case_model, src/case3d.h:157-166). */
 ct_status ct_case_load(const char* dir, ct_case** out);
 ct_status ct_case_destroy(ct_case* c);
 /* A case built in code (no files): layers bottom to top (named layer0,
@@ -110,7 +110,7 @@ ct_status ct_case_block(const ct_case* c, int k, int* layer, double* rect, doubl
 /* TSV region k: layer index, rect in m, copper fraction. */
 ct_status ct_case_tsv(const ct_case* c, int k, int* layer, double* rect, double* fraction);
 
-/* export_3dice (src/case3d.h:266-383): the case as 3D-ICE 4.0 input on a
+/* export_3dice (src/case3d.h:267-383): the case as 3D-ICE 4.0 input on a
  * uniform grid of cell_um micrometres, written into the existing folder
  * outdir: case.stk, L<k>.flp for every active layer k, LT<k>_<p>.lay for every
  * TSV-carrying plane p of a passive layer k. CT_BAD_ARG (with the reference's

@@ -30,7 +30,7 @@
 #undef SFX
 
 /* Host copy of one level's operator and cell widths (MgLevelHost,
- * src/mg3d.h:200-204). */
+ * src/mg3d.h:88-93). */
 typedef struct hlevel {
     int nx, ny, nz;
     double *dx, *dy;
@@ -50,7 +50,7 @@ struct oracle_solver {
     level_d* ld;    /* double V-cycle state (mg_double == 1) */
 };
 
-/* mg_coarse_cell (src/mg3d.h:206-248): sums in double in a fixed child order,
+/* mg_coarse_cell (src/mg3d.h:100-136): sums in double in a fixed child order,
  * then one cast to float. */
 static void coarse_cell(const hlevel* f, hlevel* c, int I, int J, int l) {
     const size_t fxy = (size_t)f->nx * f->ny, cxy = (size_t)c->nx * c->ny;
@@ -87,7 +87,7 @@ static void coarse_cell(const hlevel* f, hlevel* c, int I, int J, int l) {
     c->gN[cid] = nn;
 }
 
-/* mg_coarse_widths (src/mg3d.h:250-256). */
+/* mg_coarse_widths (src/mg3d.h:139-144). */
 static double* coarse_widths(const double* f, int n, int* cn) {
     *cn = (n + 1) / 2;
     double* c = (double*)malloc(sizeof(double) * (size_t)(*cn));
@@ -101,7 +101,7 @@ static float* fdup(const float* v, size_t n) {
     return o;
 }
 
-/* mg_build_levels (src/mg3d.h:258-295): finest first, down to 1 x 1. */
+/* mg_build_levels (src/mg3d.h:147-183): finest first, down to 1 x 1. */
 static hlevel* build_levels(const oracle_model* m, int* nlev_out) {
     int cap_lev = 64, nlev = 1;
     hlevel* L = (hlevel*)calloc((size_t)cap_lev, sizeof(hlevel));

@@ -55,7 +55,7 @@ void oracle_get_x(const oracle_solver* s, double* T);
  * the reference. */
 void oracle_set_outer_df(oracle_solver* s, int on);
 
-/* Multigrid hierarchy (natural layout, as src/mg3d.h:259-295). */
+/* Multigrid hierarchy (natural layout, as src/mg3d.h:147-183). */
 int oracle_num_levels(const oracle_solver* s);
 void oracle_level_dims(const oracle_solver* s, int k, int* nx, int* ny, int* nz);
 void oracle_level_operator(const oracle_solver* s, int k, float* gE, float* gN, float* gU,

@@ -1,11 +1,16 @@
-"""ctypes bindings to the UNMODIFIED reference CPU solver (oracle/_ref/).
+"""ctypes bindings to the UNMODIFIED reference solvers (oracle/_ref/).
 
-TEST INFRASTRUCTURE ONLY: used to generate tests/golden/ fixtures
-(tests/golden/make_golden.py) and, where the reference sources are present,
-to pin the C oracle against the reference directly. ``oracle/_ref`` is built by
-``make -C oracle ref`` from the reference's own sources (src/pcg3d_cpu.cpp and
-headers); it does not exist where those sources are absent, and nothing on the
-product path needs it.
+TEST AND BASELINE INFRASTRUCTURE ONLY: used to generate tests/golden/
+fixtures (tests/golden/make_golden.py), to pin the C oracle against the
+reference directly, and as the timed reference arm of bench.py (the
+reference CPU solver, and the reference GPU solver on the same inputs).
+
+``oracle/_ref`` is built by ``make -C oracle ref ref-gpu`` from an unmodified
+copy of the reference's own sources (src/pcg3d_cpu.cpp, src/pcg3d_gpu.cu and
+their headers) that ``make -C oracle stage`` places under baseline/_ref/src
+(git-ignored; it travels with the working tree, so machines without a
+checkout of the reference can build it too). Nothing on the product path
+needs any of it.
 """
 from __future__ import annotations
 
@@ -17,17 +22,28 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("CT_REFERENCE_DIR", "/root/reference")
+REPO = os.path.dirname(HERE)
+REF_SRC = os.environ.get("CT_REFERENCE_SRC", os.path.join(REPO, "baseline", "_ref", "src"))
+
+
+def stage() -> bool:
+    """Copies the reference's solver sources into baseline/_ref/src when a
+    checkout of the reference sits beside this repository; True if a staged
+    copy is present afterwards."""
+    subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF_SRC={REF_SRC}"],
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    return available()
 
 
 def available() -> bool:
-    return os.path.exists(os.path.join(REF_SRC, "src", "pcg3d_cpu.cpp"))
+    return os.path.exists(os.path.join(REF_SRC, "pcg3d_cpu.cpp"))
 
 
-def build() -> None:
+def build(gpu: bool = False) -> None:
     if not available():
-        raise RuntimeError("reference sources not present")
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+        raise RuntimeError("reference sources not staged (make -C oracle stage)")
+    targets = ["ref", "ref-gpu"] if gpu else ["ref"]
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, *targets, f"REF_SRC={REF_SRC}"], check=True)
 
 
 class RefLayer(C.Structure):
@@ -48,14 +64,9 @@ class RefTsv(C.Structure):
 _libs = {}
 
 
-def lib(mg_double: bool):
-    key = bool(mg_double)
-    if key in _libs:
-        return _libs[key]
-    path = os.path.join(HERE, "_ref", "libref_mgd.so" if key else "libref_mgf.so")
-    if not os.path.exists(path):
-        build()
-    L = C.CDLL(path)
+def _bind_model(L) -> None:
+    """Argument types of the model, CPU solver and transient entry points
+    (ref_harness.cpp), present in every reference library."""
     vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
     L.ref_model_new.restype = vp
     L.ref_model_new.argtypes = [C.POINTER(RefLayer), C.c_int, C.c_int, C.c_int, C.c_double,
@@ -86,7 +97,53 @@ def lib(mg_double: bool):
     L.ref_run_transient.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_int, vp, C.c_int, vp, C.POINTER(C.c_long), ip]
     L.ref_mg_double.restype = C.c_int
+    L.ref_cpu_solver_new.restype = vp
+    L.ref_cpu_solver_new.argtypes = [vp, C.c_int]
+    L.ref_cpu_solver_free.argtypes = [vp]
+    L.ref_cpu_solver_steady.restype = C.c_int
+    L.ref_cpu_solver_steady.argtypes = [vp, C.c_double, C.c_int, ip, dp]
+    L.ref_cpu_solver_get_x.argtypes = [vp, vp]
+    L.ref_default_model_new.restype = vp
+    L.ref_default_model_new.argtypes = [C.c_int, C.c_int, C.POINTER(RefPower), C.c_int]
+
+
+def lib(mg_double: bool):
+    key = bool(mg_double)
+    if key in _libs:
+        return _libs[key]
+    path = os.path.join(HERE, "_ref", "libref_mgd.so" if key else "libref_mgf.so")
+    if not os.path.exists(path):
+        build()
+    L = C.CDLL(path)
+    _bind_model(L)
     _libs[key] = L
+    return L
+
+
+_gpu_libs = {}
+
+
+def gpu_lib(mg_double: bool):
+    """The reference GPU solver (with the same CPU entry points as lib())."""
+    key = bool(mg_double)
+    if key in _gpu_libs:
+        return _gpu_libs[key]
+    path = os.path.join(HERE, "_ref", "libref_gpu_mgd.so" if key else "libref_gpu_mgf.so")
+    if not os.path.exists(path):
+        build(gpu=True)
+    L = C.CDLL(path)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    _bind_model(L)
+    L.refg_mg_double.restype = C.c_int
+    L.refg_device_count.restype = C.c_int
+    L.refg_use_graphs.argtypes = [C.c_int]
+    L.refg_solver_new.restype = vp
+    L.refg_solver_new.argtypes = [vp, C.c_int, dp]
+    L.refg_solver_free.argtypes = [vp]
+    L.refg_solve_steady.restype = C.c_int
+    L.refg_solve_steady.argtypes = [vp, C.c_double, C.c_int, ip, dp]
+    L.refg_get_x.argtypes = [vp, vp]
+    _gpu_libs[key] = L
     return L
 
 
@@ -109,10 +166,11 @@ class RefModel:
     plane_layer: np.ndarray
     handle: int = 0
     mg_double: bool = True
+    owner: object = None  # the library that built it (frees it)
 
     def __del__(self):
         if self.handle:
-            lib(self.mg_double).ref_model_free(self.handle)
+            (self.owner or lib(self.mg_double)).ref_model_free(self.handle)
             self.handle = 0
 
 
@@ -130,7 +188,7 @@ def _wrap(L, h, mg_double) -> RefModel:
     pl = np.empty(nz.value, np.int32)
     L.ref_model_arrays(h, *(a.ctypes.data for a in (gE, gN, gU, gB, cap, P, dz, tsv, pl)))
     return RefModel(nx.value, ny.value, nz.value, dx.value, dy.value, gE, gN, gU, gB, cap, P, dz,
-                    tsv, pl, h, mg_double)
+                    tsv, pl, h, mg_double, L)
 
 
 def model(layers, nx, ny, Lx, Ly, h_top, h_bot, power=(), tsvs=(), mg_double=True) -> RefModel:
@@ -147,6 +205,18 @@ def model(layers, nx, ny, Lx, Ly, h_top, h_bot, power=(), tsvs=(), mg_double=Tru
     ta = (RefTsv * max(1, len(tv)))(*tv)
     h = L.ref_model_new(la, len(layers), nx, ny, Lx, Ly, h_top, h_bot, pa, len(pw), ta, len(tv))
     return _wrap(L, h, mg_double)
+
+
+def default_model(nx, ny, power=(), mg_double=True, gpu=False) -> RefModel:
+    """default_model(nx, ny) (src/stack3d.h:165-168) with the power operations
+    listed as in model(), then finalize(); gpu: built by the library that also
+    holds the reference GPU solver (models are solved by the library that
+    built them)."""
+    L = gpu_lib(mg_double) if gpu else lib(mg_double)
+    kinds = {"block": 0, "uniform": 1, "hotspot": 2}
+    pw = [RefPower(kinds[p[0]], *p[1:]) for p in power]
+    pa = (RefPower * max(1, len(pw)))(*pw)
+    return _wrap(L, L.ref_default_model_new(nx, ny, pa, len(pw)), mg_double)
 
 
 def case_model(folder, nx, ny, with_tsv=True, mg_double=True) -> RefModel:

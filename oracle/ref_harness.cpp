@@ -1,12 +1,14 @@
 // ref_harness.cpp - C entry points around the UNMODIFIED reference CPU solver,
-// compiled from the reference's own sources where they lie (oracle/Makefile,
-// target `ref`). TEST INFRASTRUCTURE ONLY: it pins the C oracle and generates
-// the golden fixtures under tests/golden/ (make_golden.py). Nothing in the
-// product loads it, and it is not built where the reference sources are absent.
+// compiled from an unmodified copy of the reference's own sources
+// (oracle/Makefile, targets `stage` and `ref`). TEST AND BASELINE
+// INFRASTRUCTURE ONLY: it pins the C oracle, generates the golden fixtures
+// under tests/golden/ (make_golden.py) and is the timed reference CPU solver
+// of the benchmark's reference arm. Nothing in the product loads it, and it is
+// not built where the reference sources are absent.
 //
 // Models are built with the reference's own stack3d.h / case3d.h functions, in
 // the order the caller lists: power operations first, then TSV regions, then
-// finalize(), as build_case_model (src/case3d.h:158-166) does.
+// finalize(), as build_case_model (src/case3d.h:157-166) does.
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -58,6 +60,24 @@ void* ref_model_new(const ref_layer* L, int nl, int nx, int ny, double Lx, doubl
     }
     for (int k = 0; k < nt; ++k)
         add_tsv_region(*m, tv[k].layer, tv[k].x0, tv[k].y0, tv[k].w, tv[k].h, tv[k].f);
+    finalize(*m);
+    return m;
+}
+
+// default_model(nx, ny) (src/stack3d.h:165-168: the two-tier stack of
+// default_stack, 10 x 10 mm, h_top 2e4) with the listed power operations,
+// then finalize().
+void* ref_default_model_new(int nx, int ny, const ref_power* pw, int np) {
+    Model3D* m = new Model3D(default_model(nx, ny));
+    for (int k = 0; k < np; ++k) {
+        const ref_power& p = pw[k];
+        if (p.kind == 0)
+            add_power_block(*m, p.layer, p.x0, p.y0, p.w, p.h, p.watts);
+        else if (p.kind == 1)
+            add_uniform_power(*m, p.layer, p.watts);
+        else
+            add_hotspot(*m, p.layer, p.x0, p.y0, p.w, p.watts);
+    }
     finalize(*m);
     return m;
 }
@@ -121,6 +141,31 @@ int ref_cpu_pcg(void* h, double tol, int maxit, int precond, double* T, int* ite
     return r.converged ? 1 : 0;
 }
 
+// A CpuPcg (src/pcg3d.h:71-99) kept across solves, so a steady solve can be
+// timed without the set-up (levels, factors) that cpu_pcg includes.
+void* ref_cpu_solver_new(void* model, int precond) {
+    return new CpuPcg(*static_cast<Model3D*>(model), precond ? Precond::Multigrid : Precond::Jacobi);
+}
+
+void ref_cpu_solver_free(void* s) { delete static_cast<CpuPcg*>(s); }
+
+// set_x_zero, set_rhs_steady, solve (src/pcg3d_cpu.cpp:126-185); 1 if converged.
+int ref_cpu_solver_steady(void* h, double tol, int maxit, int* iters, double* relres) {
+    CpuPcg* s = static_cast<CpuPcg*>(h);
+    s->set_x_zero();
+    s->set_rhs_steady();
+    const PcgStats st = s->solve(tol, maxit);
+    *iters = st.iters;
+    *relres = st.relres;
+    return st.converged ? 1 : 0;
+}
+
+void ref_cpu_solver_get_x(void* h, double* T) {
+    std::vector<Real> x;
+    static_cast<CpuPcg*>(h)->get_x(x);
+    for (size_t k = 0; k < x.size(); ++k) T[k] = (double)x[k];
+}
+
 double ref_true_relres(void* h, const double* T) {
     const Model3D& m = *static_cast<Model3D*>(h);
     std::vector<Real> t(T, T + m.ncells());
@@ -137,7 +182,7 @@ int ref_num_levels(void* h) {
     return (int)mg_build_levels(*static_cast<Model3D*>(h)).size();
 }
 
-// Level k of mg_build_levels (src/mg3d.h:258-295), natural layout.
+// Level k of mg_build_levels (src/mg3d.h:147-183), natural layout.
 void ref_level(void* h, int k, int* nx, int* ny, float* gE, float* gN, float* gU, float* gB,
                float* cap) {
     std::vector<MgLevelHost> L = mg_build_levels(*static_cast<Model3D*>(h));
@@ -183,7 +228,7 @@ int ref_run_transient(void* h, int precond, double dt0, double growth, double dt
     return (int)r.steps.size();
 }
 
-// export_3dice (src/case3d.h:266-383) of the case folder on a grid of cell_um:
+// export_3dice (src/case3d.h:267-383) of the case folder on a grid of cell_um:
 // 1 on success, else 0 with the reference's message in err.
 int ref_export_3dice(const char* folder, double cell_um, const char* outdir, char* err, int errcap) {
     CaseSpec cs;

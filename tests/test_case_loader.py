@@ -1,4 +1,4 @@
-"""Case loader (load_case / build_case_model, src/case3d.h:86-168) against
+"""Case loader (load_case / build_case_model, src/case3d.h:84-166) against
 the reference's own loader: the four example cases (tests/golden/cases, the
 reference's CSV inputs) built on a 40 x 40 grid with and without TSVs give
 the same model arrays bit for bit (SHA-256 from the reference, golden.json)
@@ -137,7 +137,7 @@ def _content_lines(path):
 
 @pytest.mark.parametrize("key", sorted(_export_index()))
 def test_export_3dice_matches_reference(ct, key, tmp_path):
-    """export_3dice (src/case3d.h:266-383) against the reference's own export
+    """export_3dice (src/case3d.h:267-383) against the reference's own export
     of the same case folder and cell size: the same files with the same
     contents line for line (comments aside), or the same refusal message."""
     rec = _export_index()[key]

@@ -270,35 +270,11 @@ def test_staged_sweeps_bitwise(ct, prec):
     assert np.array_equal(out[0][1], out[1][1])
 
 
-@pytest.mark.parametrize("n", [203, 96])
-def test_staged_apply_matches_row_apply(ct, n, tmp_path):
-    """The operator apply staged by bulk tensor copies computes the row
-    kernel's Ap bit for bit (p.Ap is summed in another order): the same
-    iteration count and temperatures to 1e-9 of Tmax."""
-    import os
-    import subprocess
-    import sys
-    code = ("import sys, numpy as np; sys.path[:0]=['.', 'cuda-thermal_gb300']; import cthermal as ct, "
-            "workloads; m=workloads.steady_hotspot(%d, seed=5); s=ct.GpuPcg(m, ct.Precond.Multigrid, "
-            "ct.Precision.MG_FP32_FLEX_DW); s.set_x_zero(); s.set_rhs_steady(); st=s.solve(1e-10, 1000); "
-            "np.save(sys.argv[1], np.concatenate([[st.iters], s.get_x()]))" % n)
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    out = []
-    for form in ("rows", "tma"):
-        f = str(tmp_path / f"apply_{form}_{n}.npy")
-        env = dict(os.environ, CT_APPLY=form)  # the apply form is fixed per process
-        subprocess.run([sys.executable, "-c", code, f], check=True, cwd=root, env=env, timeout=300)
-        out.append(np.load(f))
-    assert out[0][0] == out[1][0]
-    T0, T1 = out[0][1:], out[1][1:]
-    assert np.abs(T0 - T1).max() <= 1e-9 * np.abs(T0).max()
-
-
 @pytest.mark.parametrize("n,prec", [(203, "MG_FP32_FLEX_DW"), (130, "MG_FP32_FLEX"), (203, "MG_FP32")])
-def test_producer_warp_sweeps_bitwise(ct, n, prec, tmp_path):
-    """The staged sweeps with a producer warp and per-stage release barriers
-    (the default) give the block-barrier form's results bit for bit, single
-    solver and batch (the form is fixed per process: one child each)."""
+def test_staged_sweeps_bitwise_single_and_batch(ct, n, prec, tmp_path):
+    """The staged sweeps (producer warp, per-stage release barriers) give the
+    grid sweeps' results bit for bit, single solver and batch (the form is
+    read when a solver or batch is created: one child process each)."""
     import os
     import subprocess
     import sys
@@ -312,8 +288,8 @@ def test_producer_warp_sweeps_bitwise(ct, n, prec, tmp_path):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     out = []
     for flag in ("0", "1"):
-        f = str(tmp_path / f"ws_{flag}.npy")
-        env = dict(os.environ, CT_SWEEP_WS=flag, CT_SWEEP_TMA="1")
+        f = str(tmp_path / f"staged_{flag}.npy")
+        env = dict(os.environ, CT_SWEEP_TMA=flag)
         subprocess.run([sys.executable, "-c", code, f], check=True, cwd=root, env=env, timeout=300)
         out.append(np.load(f))
     assert np.array_equal(out[0], out[1])

@@ -2,7 +2,7 @@
 golden case it must reproduce the reference's temperatures bit for bit (same
 SHA-256 of the T bytes), iteration counts and residuals, in both V-cycle
 precisions, with Jacobi, through transients, and its multigrid hierarchy must
-equal mg_build_levels (src/mg3d.h:258-295) bit for bit."""
+equal mg_build_levels (src/mg3d.h:147-183) bit for bit."""
 import hashlib
 
 import numpy as np
