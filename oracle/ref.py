@@ -5,7 +5,7 @@ fixtures (tests/golden/make_golden.py), to pin the C oracle against the
 reference directly, and as the timed reference arm of bench.py (the
 reference CPU solver, and the reference GPU solver on the same inputs).
 
-``oracle/_ref`` is built by ``make -C oracle ref ref-gpu`` from an unmodified
+``oracle/_ref/<machine>/`` is built by ``make -C oracle ref ref-gpu`` from an unmodified
 copy of the reference's own sources (src/pcg3d_cpu.cpp, src/pcg3d_gpu.cu and
 their headers) that ``make -C oracle stage`` places under baseline/_ref/src
 (git-ignored; it travels with the working tree, so machines without a
@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import subprocess
 from dataclasses import dataclass
 
@@ -23,6 +24,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_ref", platform.machine())
 REF_SRC = os.environ.get("CT_REFERENCE_SRC", os.path.join(REPO, "baseline", "_ref", "src"))
 
 
@@ -111,7 +113,7 @@ def lib(mg_double: bool):
     key = bool(mg_double)
     if key in _libs:
         return _libs[key]
-    path = os.path.join(HERE, "_ref", "libref_mgd.so" if key else "libref_mgf.so")
+    path = os.path.join(OUT, "libref_mgd.so" if key else "libref_mgf.so")
     if not os.path.exists(path):
         build()
     L = C.CDLL(path)
@@ -128,7 +130,7 @@ def gpu_lib(mg_double: bool):
     key = bool(mg_double)
     if key in _gpu_libs:
         return _gpu_libs[key]
-    path = os.path.join(HERE, "_ref", "libref_gpu_mgd.so" if key else "libref_gpu_mgf.so")
+    path = os.path.join(OUT, "libref_gpu_mgd.so" if key else "libref_gpu_mgf.so")
     if not os.path.exists(path):
         build(gpu=True)
     L = C.CDLL(path)
