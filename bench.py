@@ -180,6 +180,22 @@ def sum_over_ranks(v, world):
     return _reduce(v, world, td.ReduceOp.SUM)
 
 
+def partition_instances(costs, world):
+    """A cost-balanced share of the batched instances for each rank: the
+    largest remaining instance goes to the rank with the least cost so far
+    (longest-processing-time first). Instances are independent, so ranks
+    exchange nothing but their timing. Returns one sorted index list per
+    rank; every instance is in exactly one."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
 def timed_solves(ct, solver, k, world):
     """k steady solves, timed with CUDA events on the solver's stream."""
     import torch
@@ -363,13 +379,19 @@ def traffic_from_profiles(kernel_name):
     return None
 
 
-def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
+def bench_batched(ct, np, torch, args, hbm_peak, peak_kind, rank=0, world=1):
     """The batched form on the 256-instance floorplan sweep: uneven stacks
     (nx, ny in 64..512, 6-16 planes), all solved to 1e-10 together, against
-    the plain FP64 MG-PCG solving the same instances one after another."""
+    the plain FP64 MG-PCG solving the same instances one after another. With
+    several ranks each solves a cost-balanced share (cells per instance; the
+    iteration counts hardly vary) and the rate is all instances over the
+    slowest rank's time."""
     import workloads
     t0 = time.perf_counter()
-    specs = workloads.batch_instance_specs(BATCH_N, seed=BATCH_SEED)
+    specs_all = workloads.batch_instance_specs(BATCH_N, seed=BATCH_SEED)
+    costs = [nx * ny * sum(l.ncells for l in cs.layers) for cs, nx, ny in specs_all]
+    mine = partition_instances(costs, world)[rank]
+    specs = [specs_all[i] for i in mine]
     # every instance's model is built on the device from its description
     b = ct.GpuBatch.from_specs([s[0] for s in specs], [s[1] for s in specs], [s[2] for s in specs],
                                False)
@@ -383,6 +405,7 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
     stream = torch.cuda.ExternalStream(b.stream())
     kb = max(3, args.steps // 3)
     torch.cuda.synchronize()
+    barrier(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(kb):
@@ -391,7 +414,7 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
         st = b.solve(TOL, MAXIT)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / kb
+    ms = max_over_ranks(e0.elapsed_time(e1) / kb, world)
     iters = [s.iters for s in st]
     conv = sum(1 for s in st if s.converged)
     Tb = [b.get_x(i) for i in range(len(models))]
@@ -426,13 +449,16 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
             ms64 += a0.elapsed_time(a1)
             it64.append(r.iters)
             max_dT = max(max_dT, float(np.abs(s.get_x() - Tb[i]).max()))
-    value = len(models) / (ms / 1e3)
-    value64 = len(models) / (ms64 / 1e3)
+    ms64 = max_over_ranks(ms64, world)
+    max_dT = max_over_ranks(max_dT, world)
+    value = len(specs_all) / (ms / 1e3)
+    value64 = len(specs_all) / (ms64 / 1e3)
     return {
         "value": value, "unit": "instance solves/s",
-        "workload": f"{len(models)} seeded stacks, nx, ny in 64..512 step 32, 6-16 planes, "
+        "workload": f"{len(specs_all)} seeded stacks, nx, ny in 64..512 step 32, 6-16 planes, "
                     f"12 log-normal floorplan blocks per tier, tol {TOL:g} per instance",
-        "instances": len(models), "cells": cells, "ms_per_batch_solve": ms, "batch_solves": kb,
+        "instances": len(specs_all), "instances_rank0": len(models), "cells_rank0": cells,
+        "ms_per_batch_solve": ms, "batch_solves": kb,
         "iters_min": min(iters), "iters_max": max(iters), "converged": conv,
         "true_relres_max": true_max, "max_dT_K_vs_fp64": max_dT,
         "fp64_mg_pcg_sequential": {"value": value64, "unit": "instance solves/s",
@@ -440,6 +466,7 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind):
         "speedup_vs_fp64": value / value64,
         "setup_s": setup_s,
         "setup": "models described on the host, built on the device (ct_batch_create_cases)",
+        "sharding": f"{world} rank(s), cost-balanced by cells, no collective",
         "buckets": [{"instances": k["instances"], "depth": k["depth"], "staged": k["staged"],
                      "sweep_tiles": k["sweep_tiles"]} for k in buckets],
         "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved,
@@ -624,9 +651,24 @@ def profile_rows(solver):
     return rows
 
 
-def kernel_table(rows, n=10):
-    return [{"name": r["name"], "launches": r["launches"], "ms": round(r["total_ms"], 4),
-             "GBs": round(r["bytes"] / (r["total_ms"] / 1e3) / 1e9, 1)} for r in rows[:n]]
+# FP64 instructions per cell of the FP64 outer kernels (CT_MG_FP32_FLEX;
+# k_fp64.cu): 7 DFMA for (A + C/dt) p and 1 for p.Ap; x, r and ||r||^2; r.z
+# and z.Ap; p = z + beta p; ||b||^2 of a start from x = 0. Conversions are
+# integer operations.
+FP64_OPS = {"pcg_apply": 8, "pcg_update_xr": 3, "pcg_dot": 2, "pcg_update_p": 1, "pcg_residual": 1}
+
+
+def kernel_table(rows, n=10, cells=None, dfma=None):
+    out = []
+    for r in rows[:n]:
+        e = {"name": r["name"], "launches": r["launches"], "ms": round(r["total_ms"], 4),
+             "GBs": round(r["bytes"] / (r["total_ms"] / 1e3) / 1e9, 1)}
+        if cells and dfma and r["name"] in FP64_OPS:
+            rate = FP64_OPS[r["name"]] * cells * r["launches"] / (r["total_ms"] / 1e3)
+            e["fp64_ops_per_cell"] = FP64_OPS[r["name"]]
+            e["fp64_frac"] = round(rate / dfma, 3)
+        out.append(e)
+    return out
 
 
 def main():
@@ -720,6 +762,7 @@ def main():
 
     # ---- roofline: per-kernel CUDA-event times of one solve ------------------
     rows = profile_rows(sfx)
+    dfma = ct.probe_fp64_rate()
     tot_ms = sum(r["total_ms"] for r in rows)
     top = rows[0]
     achieved = top["bytes"] / top["launches"] / (top["total_ms"] / top["launches"] / 1e3) / 1e9
@@ -730,9 +773,7 @@ def main():
 
     batched = None
     if not args.no_batch:
-        batched = bench_batched(ct, np, torch, args, hbm_peak, peak_kind)
-        if world > 1:
-            batched["value"] = sum_over_ranks(batched["value"], world)
+        batched = bench_batched(ct, np, torch, args, hbm_peak, peak_kind, rank, world)
     four = None
     if not args.no_four_tier:
         four = bench_four_tier(ct, np, torch, args)
@@ -776,7 +817,7 @@ def main():
                        "l2": "inputs larger than L2 (fine level ~1.7 GB moved per iteration)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_solve * args.steps,
-            "kernels": kernel_table(rows),
+            "kernels": kernel_table(rows, 12, ncells, dfma),
             "double_word_kernels": kernel_table(rows_dw, 6),
         }
         if batched:
@@ -797,6 +838,14 @@ def main():
                            "launch_ms": top["total_ms"] / top["launches"],
                            "share": top["total_ms"] / tot_ms,
                            "solve_frac": alg_bytes_solve / (msfx / args.steps / 1e3) / 1e9 / hbm_peak}
+        ap = next((r for r in rows if r["name"] == "pcg_apply"), None)
+        if ap:
+            rate = FP64_OPS["pcg_apply"] * ncells * ap["launches"] / (ap["total_ms"] / 1e3)
+            out["roofline"]["fp64_pipe"] = {
+                "kernel": "pcg_apply", "bound": "fp64", "achieved": rate, "peak": dfma,
+                "unit": "DFMA/s", "frac": rate / dfma,
+                "peak_kind": "measured (ct_probe_fp64_rate: independent DFMA chains on every SM)",
+                "hbm_frac": ap["bytes"] / (ap["total_ms"] / 1e3) / 1e9 / hbm_peak}
         out["true_relres"] = truefx
         out["double_word"] = {"value": valuedw, "unit": "solves/s", "precision": "CT_MG_FP32_FLEX_DW",
                               "iters": stdw[-1].iters, "ms_per_solve": msdw / kdw,

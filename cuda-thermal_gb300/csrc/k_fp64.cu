@@ -1,0 +1,589 @@
+// k_fp64.cu - the FP64 outer PCG of the multigrid modes (CT_MG_FP32_FLEX,
+// CT_MG_FP32, CT_MG_FP64): residual, operator apply, x/r update, dot
+// products and p update, all in IEEE double arithmetic as the reference's
+// outer iteration is (Real = double, src/pcg3d.h:18-22; k_residual,
+// k_apply, k_update_xr, k_mg_dot, k_update_p_mg, src/pcg3d_gpu.cu:159-256).
+//
+// On GB300 these kernels are bound by the FP64 pipe, not by HBM: a DFMA
+// issues at ~1/70 of the FFMA rate (0.53 T/s on 152 SMs), so at 800 x 800 x
+// 10 every FP64 instruction per cell costs ~12 us while an 8-byte stream
+// costs ~7.5 us at the measured copy bandwidth. So each kernel does the
+// fewest FP64 instructions the algorithm needs: the float face conductances
+// and V-cycle values are widened to double, and the residual narrowed to the
+// V-cycle's float, with exact integer conversions (f64_dev.cuh) instead of
+// the FP64-rate hardware conversions, and every multiply-add is one DFMA.
+// Per cell: apply 8 (7 for Ap, 1 for p.Ap), update 3, dot 2, p update 1.
+// The memory side follows the double-word kernels (k_dw.cu): the apply runs
+// one warp per row of one colour and plane (no index division per cell),
+// the streaming kernels keep several items in flight per thread, and every
+// kernel is launched with programmatic dependent launch.
+#include <algorithm>
+#include <cmath>
+
+#include "f64_dev.cuh"
+#include "kernels.h"
+#include "reduce.cuh"
+
+namespace ct {
+
+using namespace f64dev;
+
+namespace {
+
+// ---- the operator apply, one warp per row ----------------------------------
+
+// Operands of one cell, loaded before any is used (absent neighbours stay
+// zero and are skipped by the same guards).
+struct Cell64 {
+    double pc, dg, pw, pe, ps, pn, pd, pu;
+    float gw, ge, gs, gn, gd, gu;
+};
+
+__device__ __forceinline__ void load64(const OpView& o, const double* __restrict__ diag,
+                                       const double* __restrict__ v, unsigned k, unsigned t,
+                                       unsigned orow, int i, int e, bool hs, bool hn, bool hd, bool hu,
+                                       Cell64& a) {
+    const Geo& g = o.g;
+    const unsigned hx = (unsigned)g.hx;
+    a.pc = v[k];
+    a.dg = diag[k];
+    a.pw = a.pe = a.ps = a.pn = a.pd = a.pu = 0.0;
+    a.gw = a.ge = a.gs = a.gn = a.gd = a.gu = 0.0f;
+    if (i > 0) {
+        const unsigned w = orow + t - 1u + (unsigned)e;
+        a.pw = v[w];
+        a.gw = o.gE[w];
+    }
+    if (i < g.nx - 1) {
+        a.pe = v[orow + t + (unsigned)e];
+        a.ge = o.gE[k];
+    }
+    if (hs) {
+        const unsigned sl = orow - 2u * hx + t;
+        a.ps = v[sl];
+        a.gs = o.gN[sl];
+    }
+    if (hn) {
+        a.pn = v[orow + 2u * hx + t];
+        a.gn = o.gN[k];
+    }
+    if (hd) {
+        a.pd = v[k - g.plane];
+        a.gd = o.gU[k - g.plane];
+    }
+    if (hu) {
+        a.pu = v[k + g.plane];
+        a.gu = o.gU[k];
+    }
+}
+
+// (A + C/dt) v at the cell: the stored diagonal times v minus the west, east,
+// south, north, down and up terms, in op_apply's order (src/operator3d.h:
+// 100-112), each a DFMA: 7 FP64 instructions.
+__device__ __forceinline__ double compute64(const Cell64& a, bool w, bool e, bool s, bool n, bool d,
+                                            bool u) {
+    double off = 0.0;
+    if (w) off = __fma_rn(widen(a.gw), a.pw, off);
+    if (e) off = __fma_rn(widen(a.ge), a.pe, off);
+    if (s) off = __fma_rn(widen(a.gs), a.ps, off);
+    if (n) off = __fma_rn(widen(a.gn), a.pn, off);
+    if (d) off = __fma_rn(widen(a.gd), a.pd, off);
+    if (u) off = __fma_rn(widen(a.gu), a.pu, off);
+    return __fma_rn(a.dg, a.pc, -off);
+}
+
+// Row R = l * 2 ny + 2 j + colour: the calling warp strides over the row's hx
+// slots, U cells per lane and step (32 slots apart) with every operand of all
+// U loaded first, and hands f(slot, valid, (A + C/dt) v, v) for each slot in
+// order (padding slots: valid = false, zeros).
+template <int U, class F>
+__device__ __forceinline__ void row64(const OpView& o, const double* __restrict__ diag,
+                                      const double* __restrict__ v, unsigned R, int lane, F&& f) {
+    const Geo& g = o.g;
+    const unsigned rows = 2u * (unsigned)g.ny;
+    const unsigned l = R / rows;
+    const unsigned r = R - l * rows;
+    const int j = (int)(r >> 1), c = (int)(r & 1u), e = (j + c) & 1;
+    const unsigned hx = (unsigned)g.hx;
+    const unsigned base = l * g.plane;
+    const unsigned row = base + r * hx;
+    const unsigned orow = base + (unsigned)(2 * j + (c ^ 1)) * hx;  // other colour, same j
+    const bool hs = j > 0, hn = j < g.ny - 1, hd = l > 0, hu = (int)l < g.nz - 1;
+    for (unsigned t0 = (unsigned)lane; t0 < hx; t0 += 32u * U) {
+        Cell64 a[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const unsigned t = t0 + 32u * u;
+            const int i = 2 * (int)t + e;
+            if (t < hx && i < g.nx) load64(o, diag, v, row + t, t, orow, i, e, hs, hn, hd, hu, a[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const unsigned t = t0 + 32u * u;
+            const int i = 2 * (int)t + e;
+            if (t < hx) {
+                if (i < g.nx)
+                    f(row + t, true, compute64(a[u], i > 0, i < g.nx - 1, hs, hn, hd, hu), a[u].pc);
+                else
+                    f(row + t, false, 0.0, 0.0);
+            }
+        }
+    }
+}
+
+constexpr int kRowU = 2;
+
+// Ap = (A + C/dt) p, p.Ap and alpha = rz / p.Ap.
+__global__ void __launch_bounds__(NT)
+    k_apply64(OpView o, const double* __restrict__ diag, const double* __restrict__ p,
+              double* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    pdl_enter();
+    if (loop_done(ctl, cond)) return;
+    const Geo& g = o.g;
+    const unsigned rows = 2u * (unsigned)g.ny * (unsigned)g.nz;
+    const int lane = (int)(threadIdx.x & 31u);
+    double pap = 0.0, unused = 0.0;
+    for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows; R += gridDim.x * (NT / 32))
+        row64<kRowU>(o, diag, p, R, lane, [&](unsigned k, bool valid, double av, double pc) {
+            Ap[k] = av;
+            if (valid) pap = __fma_rn(pc, av, pap);
+        });
+    block_sum2(pap, unused);
+    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
+        double PAP, U;
+        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
+        if (threadIdx.x == 0) {
+            ctl->pAp = PAP;
+            if (!(PAP > 0.0) || !isfinite(PAP)) {  // A is SPD: p.Ap > 0 unless p = 0
+                ctl->breakdown = 1;
+                ctl->alpha = 0.0;
+                stop_loop(ctl, cond);
+            } else {
+                ctl->alpha = ctl->rz / PAP;
+            }
+        }
+    }
+}
+
+// The start test of a solve from its residual sums (src/pcg3d_cpu.cpp:142-150).
+__device__ __forceinline__ void start_test(Ctl* ctl, Cond cond, double RR, double BB) {
+    ctl->rr = RR;
+    ctl->bb = BB;
+    if (BB == 0.0) {  // no heat in: x = 0 (src/pcg3d_cpu.cpp:146)
+        ctl->bb_zero = 1;
+        ctl->converged = 1;
+        ctl->relres = 0.0;
+        stop_loop(ctl, cond);
+        return;
+    }
+    const double rel = sqrt(RR / BB);
+    ctl->relres = rel;
+    if (rel < ctl->tol) {
+        ctl->converged = 1;
+        stop_loop(ctl, cond);
+    } else if (!isfinite(rel)) {
+        ctl->breakdown = 1;
+        stop_loop(ctl, cond);
+    } else if (ctl->maxit <= 0) {
+        stop_loop(ctl, cond);
+    }
+}
+
+// r = b - (A + C/dt) x, b0 = r in the V-cycle precision, ||r||^2, ||b||^2 and
+// the start test. A solve that starts from x = 0 (every steady solve) has
+// r = b exactly and streams b once.
+template <class T>
+__global__ void __launch_bounds__(NT)
+    k_residual64(OpView o, unsigned n, const double* __restrict__ diag, const double* __restrict__ b,
+                 const double* __restrict__ x, double* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
+                 double* part, int maxb, Cond cond) {
+    pdl_enter();
+    const Geo& g = o.g;
+    double rr = 0.0, bb = 0.0;
+    if (ctl->x_zero) {
+        for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
+            const double bi = b[k];
+            r[k] = bi;
+            b0[k] = from_d<T>(bi);
+            bb = __fma_rn(bi, bi, bb);
+        }
+        rr = bb;
+    } else {
+        const unsigned rows = 2u * (unsigned)g.ny * (unsigned)g.nz;
+        const int lane = (int)(threadIdx.x & 31u);
+        for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows;
+             R += gridDim.x * (NT / 32))
+            row64<kRowU>(o, diag, x, R, lane, [&](unsigned k, bool valid, double ax, double) {
+                if (!valid) {
+                    r[k] = 0.0;
+                    b0[k] = T(0);
+                    return;
+                }
+                const double bi = b[k];
+                const double ri = bi - ax;
+                r[k] = ri;
+                b0[k] = from_d<T>(ri);
+                rr = __fma_rn(ri, ri, rr);
+                bb = __fma_rn(bi, bi, bb);
+            });
+    }
+    block_sum2(rr, bb);
+    if (publish2(rr, bb, part, maxb, &ctl->ticket[SL_INIT])) {
+        double RR, BB;
+        gather2(part, maxb, &ctl->ticket[SL_INIT], RR, BB);
+        if (threadIdx.x == 0) start_test(ctl, cond, RR, BB);
+    }
+}
+
+// ---- streaming kernels ---------------------------------------------------------
+
+// Block b streams the contiguous items [begin, end), NT apart, in chunks of
+// NT * U items.
+struct Range {
+    unsigned begin, end;
+};
+template <int U>
+__device__ __forceinline__ Range block_range(unsigned n) {
+    const unsigned per = ((n + gridDim.x - 1) / gridDim.x + NT * U - 1) / (NT * U) * (NT * U);
+    const unsigned b = blockIdx.x * per;
+    return Range{b + threadIdx.x, b + per < n ? b + per : n};
+}
+
+// Two values of the V-cycle's precision at pair index k, as doubles.
+__device__ __forceinline__ double2 load_pair(const float* z, unsigned k) {
+    const float2 v = reinterpret_cast<const float2*>(z)[k];
+    return make_double2(widen(v.x), widen(v.y));
+}
+__device__ __forceinline__ double2 load_pair(const double* z, unsigned k) {
+    return reinterpret_cast<const double2*>(z)[k];
+}
+__device__ __forceinline__ void store_pair(float* b0, unsigned k, double a, double b) {
+    reinterpret_cast<float2*>(b0)[k] = make_float2(narrow(a), narrow(b));
+}
+__device__ __forceinline__ void store_pair(double* b0, unsigned k, double a, double b) {
+    reinterpret_cast<double2*>(b0)[k] = make_double2(a, b);
+}
+
+// x += alpha p, r -= alpha Ap, b0 = r in the V-cycle precision, ||r||^2 and
+// the convergence test (src/pcg3d_gpu.cu:218-233). Pairs of values (double2).
+constexpr int kUpdU = 2;
+template <class T>
+__global__ void __launch_bounds__(NT)
+    k_update64(unsigned n2, const double2* __restrict__ p, const double2* __restrict__ Ap,
+               double2* __restrict__ x, double2* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
+               double* part, int maxb, Cond cond) {
+    pdl_enter();
+    if (loop_done(ctl, cond)) return;
+    const double alpha = ctl->alpha, malpha = -alpha;
+    double rr = 0.0, unused = 0.0;
+    const Range br = block_range<kUpdU>(n2);
+    auto one = [&](unsigned k, const double2& pv, const double2& av, double2 xv, double2 rv) {
+        xv.x = __fma_rn(alpha, pv.x, xv.x);
+        xv.y = __fma_rn(alpha, pv.y, xv.y);
+        rv.x = __fma_rn(malpha, av.x, rv.x);
+        rv.y = __fma_rn(malpha, av.y, rv.y);
+        x[k] = xv;
+        r[k] = rv;
+        store_pair(b0, k, rv.x, rv.y);
+        rr = __fma_rn(rv.x, rv.x, rr);
+        rr = __fma_rn(rv.y, rv.y, rr);
+    };
+    unsigned k = br.begin;
+    for (; k + (kUpdU - 1) * NT < br.end; k += kUpdU * NT) {
+        double2 pv[kUpdU], av[kUpdU], xv[kUpdU], rv[kUpdU];
+#pragma unroll
+        for (int u = 0; u < kUpdU; ++u) {
+            pv[u] = p[k + u * NT];
+            av[u] = Ap[k + u * NT];
+            xv[u] = x[k + u * NT];
+            rv[u] = r[k + u * NT];
+        }
+#pragma unroll
+        for (int u = 0; u < kUpdU; ++u) one(k + u * NT, pv[u], av[u], xv[u], rv[u]);
+    }
+    for (; k < br.end; k += NT) one(k, p[k], Ap[k], x[k], r[k]);
+    block_sum2(rr, unused);
+    if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
+        double RR, U;
+        gather2(part, maxb, &ctl->ticket[SL_UPDATE], RR, U);
+        if (threadIdx.x == 0) {
+            ctl->rr = RR;
+            ctl->iter += 1;
+            const double rel = sqrt(RR / ctl->bb);
+            ctl->relres = rel;
+            if (rel < ctl->tol) {
+                ctl->converged = 1;
+                stop_loop(ctl, cond);
+            } else if (!isfinite(rel)) {
+                ctl->breakdown = 1;
+                stop_loop(ctl, cond);
+            } else if (ctl->iter >= ctl->maxit) {
+                stop_loop(ctl, cond);
+            }
+        }
+    }
+}
+
+// rz = r.z (and z.Ap for the flexible beta); beta (src/pcg3d_gpu.cu:239-247,
+// 121-126). Pairs strided over the whole grid, kDotU in flight per thread.
+constexpr int kDotU = 4;
+template <class T, bool FLEX>
+__global__ void __launch_bounds__(NT, 4)
+    k_dot64(unsigned n2, const double2* __restrict__ r, const T* __restrict__ z,
+            const double2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
+    pdl_enter();
+    if (loop_done(ctl, cond)) return;
+    double rz = 0.0, zap = 0.0;
+    const unsigned stride = gridDim.x * NT;
+    auto one = [&](const double2& rv, const double2& zv, const double2& av) {
+        rz = __fma_rn(rv.x, zv.x, rz);
+        rz = __fma_rn(rv.y, zv.y, rz);
+        if (FLEX) {
+            zap = __fma_rn(zv.x, av.x, zap);
+            zap = __fma_rn(zv.y, av.y, zap);
+        }
+    };
+    unsigned k = blockIdx.x * NT + threadIdx.x;
+    for (; k + (kDotU - 1) * stride < n2; k += kDotU * stride) {
+        double2 rv[kDotU], zv[kDotU], av[kDotU];
+#pragma unroll
+        for (int u = 0; u < kDotU; ++u) {
+            rv[u] = r[k + u * stride];
+            zv[u] = load_pair(z, k + u * stride);
+            if (FLEX) av[u] = Ap[k + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kDotU; ++u) one(rv[u], zv[u], av[u]);
+    }
+    for (; k < n2; k += stride) one(r[k], load_pair(z, k), FLEX ? Ap[k] : make_double2(0.0, 0.0));
+    block_sum2(rz, zap);
+    if (publish2(rz, zap, part, maxb, &ctl->ticket[SL_DOT])) {
+        double RZ, ZAP;
+        gather2(part, maxb, &ctl->ticket[SL_DOT], RZ, ZAP);
+        if (threadIdx.x == 0) {
+            if (ctl->iter > 0) {
+                // Fletcher-Reeves (src/pcg3d_cpu.cpp:179) or flexible
+                // Polak-Ribiere: z_new.(r_new - r_old) / (z_old . r_old)
+                // = -(z_new . Ap) / (p . Ap).
+                ctl->beta = FLEX ? -ZAP / ctl->pAp : RZ / ctl->rz;
+            } else {
+                ctl->beta = 0.0;
+            }
+            ctl->rz = RZ;
+            ctl->zAp = ZAP;
+            if (!isfinite(RZ) || !isfinite(ctl->beta)) {
+                ctl->breakdown = 1;
+                stop_loop(ctl, cond);
+            }
+        }
+    }
+}
+
+// p = z + beta p (p = z on the first iteration; src/pcg3d_gpu.cu:249-256).
+constexpr int kPU = 4;
+template <class T>
+__global__ void __launch_bounds__(NT)
+    k_update_p64(unsigned n2, const T* __restrict__ z, double2* __restrict__ p, const Ctl* ctl,
+                 Cond cond) {
+    pdl_enter();
+    if (loop_done(ctl, cond)) return;
+    const double beta = ctl->beta;
+    const Range br = block_range<kPU>(n2);
+    if (ctl->iter == 0) {
+        for (unsigned k = br.begin; k < br.end; k += NT) p[k] = load_pair(z, k);
+        return;
+    }
+    unsigned k = br.begin;
+    for (; k + (kPU - 1) * NT < br.end; k += kPU * NT) {
+        double2 zv[kPU], pv[kPU];
+#pragma unroll
+        for (int u = 0; u < kPU; ++u) {
+            zv[u] = load_pair(z, k + u * NT);
+            pv[u] = p[k + u * NT];
+        }
+#pragma unroll
+        for (int u = 0; u < kPU; ++u)
+            p[k + u * NT] = make_double2(__fma_rn(beta, pv[u].x, zv[u].x), __fma_rn(beta, pv[u].y, zv[u].y));
+    }
+    for (; k < br.end; k += NT) {
+        const double2 zv = load_pair(z, k), pv = p[k];
+        p[k] = make_double2(__fma_rn(beta, pv.x, zv.x), __fma_rn(beta, pv.y, zv.y));
+    }
+}
+
+// ---- self-test of the integer conversions -----------------------------------
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// Item q tests widen() on a float bit pattern and narrow() on a double bit
+// pattern against the hardware conversions; the first 2^18 items sweep every
+// float exponent and every double exponent near the float range (with
+// mantissas at, just below and just above the rounding tie), the rest are
+// hashed. NaN results compare by NaN-ness.
+__global__ void k_conv_selftest(unsigned long long n, unsigned long long seed,
+                                unsigned long long* mismatches) {
+    unsigned long long bad = 0;
+    for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+         q += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long h = mix64(q ^ seed);
+        unsigned fb;
+        unsigned long long db;
+        if (q < (1ull << 18)) {
+            const unsigned sel = (unsigned)(q & 15u), ex = (unsigned)(q >> 4) & 0x7ffu;
+            fb = ((unsigned)(h >> 32) & 0x807fffffu) | ((ex & 0xffu) << 23);
+            const unsigned long long tie = 1ull << 28, low = (h & 0xffffffe0000000ull);
+            const unsigned long long tail = sel < 4 ? tie : sel < 8 ? tie - 1 : sel < 12 ? tie + 1 : (h & 0x1fffffffull);
+            db = (h & 0x8000000000000000ull) | ((unsigned long long)ex << 52) | (low & 0xfffffe0000000ull) | tail;
+        } else {
+            fb = (unsigned)h;
+            db = mix64(h);
+        }
+        const float f = __uint_as_float(fb);
+        const double wd = widen(f), hd = (double)f;
+        const bool wok = (isnan(hd) && isnan(wd)) || __double_as_longlong(wd) == __double_as_longlong(hd);
+        const double d = __longlong_as_double((long long)db);
+        const float nf = narrow(d), hf = (float)d;
+        const bool nok = (isnan(hf) && isnan(nf)) || __float_as_uint(nf) == __float_as_uint(hf);
+        bad += (wok ? 0u : 1u) + (nok ? 0u : 1u);
+    }
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+// FP64-pipe peak probe: kDfmaChains independent DFMA chains per thread, kDfmaSteps
+// steps each (no memory traffic but one store per thread).
+constexpr int kDfmaChains = 8, kDfmaSteps = 2048;
+__global__ void k_dfma_probe(double a, double* out) {
+    double v[kDfmaChains];
+#pragma unroll
+    for (int c = 0; c < kDfmaChains; ++c) v[c] = threadIdx.x * 1e-3 + c;
+    for (int k = 0; k < kDfmaSteps; ++k)
+#pragma unroll
+        for (int c = 0; c < kDfmaChains; ++c) v[c] = __fma_rn(v[c], a, 1e-9);
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kDfmaChains; ++c) s += v[c];
+    out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+// ---- launchers ------------------------------------------------------------------
+
+void launch_apply64(cudaStream_t st, const OpView& o, const double* diag, const double* p,
+                    double* Ap, Ctl* ctl, const Red& red, Cond cond) {
+    static const int wb = wave_blocks(k_apply64, 1 << 30);
+    launch_pdl(k_apply64, std::min(red.maxb, wb), NT, 0, st, o, diag, p, Ap, ctl, red.part, red.maxb, cond);
+}
+
+void launch_residual64(cudaStream_t st, MgType mt, const OpView& o, unsigned n, const double* diag,
+                       const double* b, const double* x, double* r, void* b0, Ctl* ctl, const Red& red,
+                       Cond cond) {
+    if (mt == MG_F64) {
+        static const int wb = wave_blocks(k_residual64<double>, 1 << 30);
+        launch_pdl(k_residual64<double>, std::min(red.maxb, wb), NT, 0, st, o, n, diag, b, x, r, (double*)b0,
+                   ctl, red.part, red.maxb, cond);
+    } else {
+        static const int wb = wave_blocks(k_residual64<float>, 1 << 30);
+        launch_pdl(k_residual64<float>, std::min(red.maxb, wb), NT, 0, st, o, n, diag, b, x, r, (float*)b0,
+                   ctl, red.part, red.maxb, cond);
+    }
+}
+
+void launch_update64(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap, double* x,
+                     double* r, void* b0, Ctl* ctl, const Red& red, Cond cond) {
+    const unsigned n2 = n / 2;
+    const auto* p2 = reinterpret_cast<const double2*>(p);
+    const auto* a2 = reinterpret_cast<const double2*>(Ap);
+    auto* x2 = reinterpret_cast<double2*>(x);
+    auto* r2 = reinterpret_cast<double2*>(r);
+    if (mt == MG_F64) {
+        static const int wb = wave_blocks(k_update64<double>, 1 << 30);
+        launch_pdl(k_update64<double>, std::min(red.blocks, wb), NT, 0, st, n2, p2, a2, x2, r2, (double*)b0, ctl,
+                   red.part, red.maxb, cond);
+    } else {
+        static const int wb = wave_blocks(k_update64<float>, 1 << 30);
+        launch_pdl(k_update64<float>, std::min(red.blocks, wb), NT, 0, st, n2, p2, a2, x2, r2, (float*)b0, ctl,
+                   red.part, red.maxb, cond);
+    }
+}
+
+void launch_dot64(cudaStream_t st, MgType mt, bool flexible, unsigned n, const double* r, const void* z,
+                  const double* Ap, Ctl* ctl, const Red& red, Cond cond) {
+    const unsigned n2 = n / 2;
+    const auto* r2 = reinterpret_cast<const double2*>(r);
+    const auto* a2 = reinterpret_cast<const double2*>(Ap);
+    const int nb = std::min(red.maxb, std::max(1, red.maxb / 2));
+    if (mt == MG_F64) {
+        if (flexible)
+            launch_pdl(k_dot64<double, true>, nb, NT, 0, st, n2, r2, (const double*)z, a2, ctl, red.part,
+                       red.maxb, cond);
+        else
+            launch_pdl(k_dot64<double, false>, nb, NT, 0, st, n2, r2, (const double*)z, a2, ctl, red.part,
+                       red.maxb, cond);
+    } else {
+        if (flexible)
+            launch_pdl(k_dot64<float, true>, nb, NT, 0, st, n2, r2, (const float*)z, a2, ctl, red.part,
+                       red.maxb, cond);
+        else
+            launch_pdl(k_dot64<float, false>, nb, NT, 0, st, n2, r2, (const float*)z, a2, ctl, red.part,
+                       red.maxb, cond);
+    }
+}
+
+void launch_update_p64(cudaStream_t st, MgType mt, unsigned n, const void* z, double* p, Ctl* ctl,
+                       Cond cond) {
+    const unsigned n2 = n / 2;
+    auto* p2 = reinterpret_cast<double2*>(p);
+    const unsigned want = std::max(1u, (n2 + NT * kPU - 1) / (NT * kPU));
+    if (mt == MG_F64) {
+        static const int wb = wave_blocks(k_update_p64<double>, 1 << 30);
+        launch_pdl(k_update_p64<double>, (int)std::min(want, (unsigned)wb), NT, 0, st, n2, (const double*)z, p2,
+                   ctl, cond);
+    } else {
+        static const int wb = wave_blocks(k_update_p64<float>, 1 << 30);
+        launch_pdl(k_update_p64<float>, (int)std::min(want, (unsigned)wb), NT, 0, st, n2, (const float*)z, p2,
+                   ctl, cond);
+    }
+}
+
+cudaError_t measure_dfma_rate(double* per_s) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int blocks = std::max(1, sms) * 8;
+    double* out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    e = cudaMalloc(&out, (size_t)blocks * NT * sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float ms = 0.0f;
+    constexpr int kReps = 5;
+    if (e == cudaSuccess) {
+        for (int w = 0; w < 2; ++w) k_dfma_probe<<<blocks, NT>>>(0.999999, out);
+        cudaEventRecord(e0);
+        for (int r = 0; r < kReps; ++r) k_dfma_probe<<<blocks, NT>>>(0.999999, out);
+        cudaEventRecord(e1);
+        e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (out) cudaFree(out);
+    if (e == cudaSuccess)
+        *per_s = (double)blocks * NT * kDfmaChains * kDfmaSteps * kReps / (ms * 1e-3);
+    return e;
+}
+
+cudaError_t launch_conv_selftest(cudaStream_t st, unsigned long long n, unsigned long long seed,
+                                 unsigned long long* mismatches) {
+    k_conv_selftest<<<1024, NT, 0, st>>>(n, seed, mismatches);
+    return cudaGetLastError();
+}
+
+}  // namespace ct

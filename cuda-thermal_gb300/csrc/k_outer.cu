@@ -1,10 +1,12 @@
 // k_outer.cu - FP64 outer-PCG kernels, setup and bookkeeping kernels.
 //
-// The outer iteration is FP64 (residual, iterate updates, dot products,
-// alpha, beta), as in the reference (src/pcg3d_gpu.cu:134-264). Its stencil
-// kernels walk one column per thread through the z-planes, so the vertical
-// neighbours and the face below come from registers and every z-plane access
-// of a warp is one contiguous run of the split layout.
+// The Jacobi-preconditioned outer iteration (FP64, as in the reference,
+// src/pcg3d_gpu.cu:134-264; the multigrid modes run k_fp64.cu), the set-up
+// kernels (diagonal, layout changes) and the bookkeeping reductions (true
+// residual, step records). Their stencil kernels walk one column per thread
+// through the z-planes, so the vertical neighbours and the face below come
+// from registers and every z-plane access of a warp is one contiguous run of
+// the split layout.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -75,27 +77,27 @@ __device__ __forceinline__ void apply_column(const OpView& o, const double* __re
     }
 }
 
-template <class T>
+// ---- the Jacobi-preconditioned iteration (src/pcg3d_gpu.cu:134-264) ---------
+// The multigrid modes run the FP64 kernels of k_fp64.cu; these serve the
+// Jacobi preconditioner, kept for drop-in completeness.
+
+// r = b - (A + C/dt) x, ||r||^2, ||b||^2 and the start test.
 __global__ void __launch_bounds__(NT)
     k_residual(OpView o, const double* __restrict__ diag, const double* __restrict__ b,
-               const double* __restrict__ x, double* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
-               double* part, int maxb, Cond cond) {
+               const double* __restrict__ x, double* __restrict__ r, Ctl* ctl, double* part,
+               int maxb, Cond cond) {
     const Geo& g = o.g;
     double rr = 0.0, bb = 0.0;
     for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
         const Col c = col_of_slot(g, s);
         if (!c.valid) {
-            for (int l = 0; l < g.nz; ++l) {
-                r[(unsigned)l * g.plane + s] = 0.0;
-                if (b0) b0[(unsigned)l * g.plane + s] = T(0);
-            }
+            for (int l = 0; l < g.nz; ++l) r[(unsigned)l * g.plane + s] = 0.0;
             continue;
         }
         apply_column(o, diag, x, c, [&](int, unsigned id, double, double ax) {
             const double bi = b[id];
             const double ri = bi - ax;
             r[id] = ri;
-            if (b0) b0[id] = (T)ri;
             rr += ri * ri;
             bb += bi * bi;
         });
@@ -129,57 +131,11 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
-__global__ void __launch_bounds__(NT)
-    k_apply(OpView o, const double* __restrict__ diag, const double* __restrict__ p,
-            double* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
-    if (loop_done(ctl, cond)) return;
-    const Geo& g = o.g;
-    double pap = 0.0, unused = 0.0;
-    for (unsigned s = blockIdx.x * NT + threadIdx.x; s < g.plane; s += gridDim.x * NT) {
-        const Col c = col_of_slot(g, s);
-        if (!c.valid) {
-            for (int l = 0; l < g.nz; ++l) Ap[(unsigned)l * g.plane + s] = 0.0;
-            continue;
-        }
-        apply_column(o, diag, p, c, [&](int, unsigned id, double pc, double a) {
-            Ap[id] = a;
-            pap += pc * a;
-        });
-    }
-    block_sum2(pap, unused);
-    if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
-        double PAP, U;
-        gather2(part, maxb, &ctl->ticket[SL_APPLY], PAP, U);
-        if (threadIdx.x == 0) {
-            ctl->pAp = PAP;
-            if (!(PAP > 0.0) || !isfinite(PAP)) {  // A is SPD: p.Ap > 0 unless p = 0
-                ctl->breakdown = 1;
-                ctl->alpha = 0.0;
-                stop_loop(ctl, cond);
-            } else {
-                ctl->alpha = ctl->rz / PAP;
-            }
-        }
-    }
-}
-
-template <class T>
-__device__ __forceinline__ void store2(T* b0, unsigned k, double a, double b);
-template <>
-__device__ __forceinline__ void store2<float>(float* b0, unsigned k, double a, double b) {
-    reinterpret_cast<float2*>(b0)[k] = make_float2((float)a, (float)b);
-}
-template <>
-__device__ __forceinline__ void store2<double>(double* b0, unsigned k, double a, double b) {
-    reinterpret_cast<double2*>(b0)[k] = make_double2(a, b);
-}
-
-// n2 = n / 2 pairs (n, the slots of all planes, is even).
-template <class T, bool MG>
+// x += alpha p, r -= alpha Ap; ||r||^2; convergence test. n2 = n / 2 pairs.
 __global__ void __launch_bounds__(NT)
     k_update(unsigned n2, const double* __restrict__ p, const double* __restrict__ Ap,
-             double* __restrict__ x, double* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
-             double* part, int maxb, Cond cond) {
+             double* __restrict__ x, double* __restrict__ r, Ctl* ctl, double* part, int maxb,
+             Cond cond) {
     if (loop_done(ctl, cond)) return;
     const double alpha = ctl->alpha;
     const double2* p2 = reinterpret_cast<const double2*>(p);
@@ -196,7 +152,6 @@ __global__ void __launch_bounds__(NT)
         rv.y -= alpha * av.y;
         x2[k] = xv;
         r2[k] = rv;
-        if (MG) store2<T>(b0, k, rv.x, rv.y);
         rr += rv.x * rv.x;
         rr += rv.y * rv.y;
     }
@@ -222,71 +177,26 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
-template <class T>
-__device__ __forceinline__ void load2(const T* z, unsigned k, double& a, double& b);
-template <>
-__device__ __forceinline__ void load2<float>(const float* z, unsigned k, double& a, double& b) {
-    const float2 v = reinterpret_cast<const float2*>(z)[k];
-    a = (double)v.x;
-    b = (double)v.y;
-}
-template <>
-__device__ __forceinline__ void load2<double>(const double* z, unsigned k, double& a, double& b) {
-    const double2 v = reinterpret_cast<const double2*>(z)[k];
-    a = v.x;
-    b = v.y;
-}
-
-// z = the V-cycle result (T) or, with JAC, r * invd.
-template <class T, bool JAC>
-__device__ __forceinline__ void z_pair(const T* z, const double2* r2, const double2* d2, unsigned k,
-                                       double& za, double& zb) {
-    if (JAC) {
-        const double2 rv = r2[k], dv = d2[k];
-        za = rv.x * dv.x;
-        zb = rv.y * dv.y;
-    } else {
-        load2<T>(z, k, za, zb);
-    }
-}
-
-template <class T, bool JAC, bool FLEX>
+// rz = r.z with z = r * invd; beta = rz_new / rz (src/pcg3d_gpu.cu:121-126).
 __global__ void __launch_bounds__(NT)
-    k_dot(unsigned n2, const double* __restrict__ r, const T* __restrict__ z,
-          const double* __restrict__ invd, const double* __restrict__ Ap, Ctl* ctl, double* part,
-          int maxb, Cond cond) {
+    k_dot(unsigned n2, const double* __restrict__ r, const double* __restrict__ invd, Ctl* ctl,
+          double* part, int maxb, Cond cond) {
     if (loop_done(ctl, cond)) return;
     const double2* r2 = reinterpret_cast<const double2*>(r);
     const double2* d2 = reinterpret_cast<const double2*>(invd);
-    const double2* a2 = reinterpret_cast<const double2*>(Ap);
-    double rz = 0.0, zap = 0.0;
+    double rz = 0.0, unused = 0.0;
     for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
-        double za, zb;
-        z_pair<T, JAC>(z, r2, d2, k, za, zb);
-        const double2 rv = r2[k];
-        rz += rv.x * za;
-        rz += rv.y * zb;
-        if (FLEX) {
-            const double2 av = a2[k];
-            zap += za * av.x;
-            zap += zb * av.y;
-        }
+        const double2 rv = r2[k], dv = d2[k];
+        rz += rv.x * (rv.x * dv.x);
+        rz += rv.y * (rv.y * dv.y);
     }
-    block_sum2(rz, zap);
-    if (publish2(rz, zap, part, maxb, &ctl->ticket[SL_DOT])) {
-        double RZ, ZAP;
-        gather2(part, maxb, &ctl->ticket[SL_DOT], RZ, ZAP);
+    block_sum2(rz, unused);
+    if (publish2(rz, unused, part, maxb, &ctl->ticket[SL_DOT])) {
+        double RZ, U;
+        gather2(part, maxb, &ctl->ticket[SL_DOT], RZ, U);
         if (threadIdx.x == 0) {
-            if (ctl->iter > 0) {
-                // Fletcher-Reeves (src/pcg3d_cpu.cpp:179) or flexible
-                // Polak-Ribiere: z_new.(r_new - r_old) / (z_old . r_old)
-                // = -(z_new . Ap) / (p . Ap).
-                ctl->beta = FLEX ? -ZAP / ctl->pAp : RZ / ctl->rz;
-            } else {
-                ctl->beta = 0.0;
-            }
+            ctl->beta = ctl->iter > 0 ? RZ / ctl->rz : 0.0;
             ctl->rz = RZ;
-            ctl->zAp = ZAP;
             if (!isfinite(RZ) || !isfinite(ctl->beta)) {
                 ctl->breakdown = 1;
                 stop_loop(ctl, cond);
@@ -295,10 +205,10 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
-template <class T, bool JAC>
+// p = z + beta p with z = r * invd (p = z on the first iteration).
 __global__ void __launch_bounds__(NT)
-    k_update_p(unsigned n2, const T* __restrict__ z, const double* __restrict__ r,
-               const double* __restrict__ invd, double* __restrict__ p, const Ctl* ctl, Cond cond) {
+    k_update_p(unsigned n2, const double* __restrict__ r, const double* __restrict__ invd,
+               double* __restrict__ p, const Ctl* ctl, Cond cond) {
     if (loop_done(ctl, cond)) return;
     const double beta = ctl->beta;
     const bool first = ctl->iter == 0;
@@ -306,8 +216,8 @@ __global__ void __launch_bounds__(NT)
     const double2* d2 = reinterpret_cast<const double2*>(invd);
     double2* p2 = reinterpret_cast<double2*>(p);
     for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n2; k += gridDim.x * NT) {
-        double za, zb;
-        z_pair<T, JAC>(z, r2, d2, k, za, zb);
+        const double2 rv = r2[k], dv = d2[k];
+        const double za = rv.x * dv.x, zb = rv.y * dv.y;
         if (first) {
             p2[k] = make_double2(za, zb);
         } else {
@@ -515,75 +425,48 @@ bool pdl_enabled() {
 void launch_residual(cudaStream_t st, MgType mt, const OpView& o, const double* diag,
                      const double* b, const double* x, double* r, void* b0, Ctl* ctl,
                      const Red& red, Cond cond) {
-    static const int wb = wave_blocks(k_residual<float>, 1 << 30);
-    const int nb = std::min(red.blocks, wb);
-    if (mt == MG_F64)
-        k_residual<double><<<nb, NT, 0, st>>>(o, diag, b, x, r, (double*)b0, ctl, red.part,
-                                              red.maxb, cond);
-    else
-        k_residual<float><<<nb, NT, 0, st>>>(o, diag, b, x, r,
-                                                     mt == MG_F32 ? (float*)b0 : nullptr, ctl,
-                                                     red.part, red.maxb, cond);
+    if (mt != MG_NONE) {
+        launch_residual64(st, mt, o, o.g.plane * (unsigned)o.g.nz, diag, b, x, r, b0, ctl, red, cond);
+        return;
+    }
+    static const int wb = wave_blocks(k_residual, 1 << 30);
+    k_residual<<<std::min(red.blocks, wb), NT, 0, st>>>(o, diag, b, x, r, ctl, red.part, red.maxb, cond);
 }
 
 void launch_apply(cudaStream_t st, const OpView& o, const double* diag, const double* p,
                   double* Ap, Ctl* ctl, const Red& red, Cond cond) {
-    static const int wb = wave_blocks(k_apply, 1 << 30);
-    k_apply<<<std::min(red.blocks, wb), NT, 0, st>>>(o, diag, p, Ap, ctl, red.part, red.maxb, cond);
+    launch_apply64(st, o, diag, p, Ap, ctl, red, cond);
 }
 
 void launch_update(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap,
                    double* x, double* r, void* b0, Ctl* ctl, const Red& red, Cond cond) {
-    const unsigned n2 = n / 2;
-    static const int wb = wave_blocks(k_update<double, true>, 1 << 30);
-    Red rb = red;
-    rb.blocks = std::min(red.blocks, wb);
-    if (mt == MG_F32)
-        k_update<float, true><<<rb.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (float*)b0, ctl, red.part,
-                                                         red.maxb, cond);
-    else if (mt == MG_F64)
-        k_update<double, true><<<rb.blocks, NT, 0, st>>>(n2, p, Ap, x, r, (double*)b0, ctl,
-                                                          red.part, red.maxb, cond);
-    else
-        k_update<float, false><<<rb.blocks, NT, 0, st>>>(n2, p, Ap, x, r, nullptr, ctl, red.part,
-                                                          red.maxb, cond);
+    if (mt != MG_NONE) {
+        launch_update64(st, mt, n, p, Ap, x, r, b0, ctl, red, cond);
+        return;
+    }
+    static const int wb = wave_blocks(k_update, 1 << 30);
+    k_update<<<std::min(red.blocks, wb), NT, 0, st>>>(n / 2, p, Ap, x, r, ctl, red.part, red.maxb, cond);
 }
 
 void launch_dot(cudaStream_t st, MgType mt, bool flexible, unsigned n, const double* r,
                 const void* z, const double* invd, const double* Ap, Ctl* ctl, const Red& red,
                 Cond cond) {
-    const unsigned n2 = n / 2;
-    static const int wb = wave_blocks(k_dot<double, false, true>, 1 << 30);
-    Red rb = red;
-    rb.blocks = std::min(red.blocks, wb);
-    if (mt == MG_NONE)
-        k_dot<float, true, false><<<rb.blocks, NT, 0, st>>>(n2, r, nullptr, invd, Ap, ctl,
-                                                             red.part, red.maxb, cond);
-    else if (mt == MG_F32 && flexible)
-        k_dot<float, false, true><<<rb.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap, ctl,
-                                                             red.part, red.maxb, cond);
-    else if (mt == MG_F32)
-        k_dot<float, false, false><<<rb.blocks, NT, 0, st>>>(n2, r, (const float*)z, invd, Ap,
-                                                              ctl, red.part, red.maxb, cond);
-    else if (flexible)
-        k_dot<double, false, true><<<rb.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
-                                                              ctl, red.part, red.maxb, cond);
-    else
-        k_dot<double, false, false><<<rb.blocks, NT, 0, st>>>(n2, r, (const double*)z, invd, Ap,
-                                                               ctl, red.part, red.maxb, cond);
+    if (mt != MG_NONE) {
+        launch_dot64(st, mt, flexible, n, r, z, Ap, ctl, red, cond);
+        return;
+    }
+    static const int wb = wave_blocks(k_dot, 1 << 30);
+    k_dot<<<std::min(red.blocks, wb), NT, 0, st>>>(n / 2, r, invd, ctl, red.part, red.maxb, cond);
 }
 
 void launch_update_p(cudaStream_t st, MgType mt, unsigned n, const void* z, const double* r,
                      const double* invd, double* p, Ctl* ctl, Cond cond) {
-    const unsigned n2 = n / 2;
-    static const int wb = wave_blocks(k_update_p<double, false>, 1 << 30);
-    const unsigned grid = std::min(grid_for(n2), (unsigned)wb);
-    if (mt == MG_NONE)
-        k_update_p<float, true><<<grid, NT, 0, st>>>(n2, nullptr, r, invd, p, ctl, cond);
-    else if (mt == MG_F32)
-        k_update_p<float, false><<<grid, NT, 0, st>>>(n2, (const float*)z, r, invd, p, ctl, cond);
-    else
-        k_update_p<double, false><<<grid, NT, 0, st>>>(n2, (const double*)z, r, invd, p, ctl, cond);
+    if (mt != MG_NONE) {
+        launch_update_p64(st, mt, n, z, p, ctl, cond);
+        return;
+    }
+    static const int wb = wave_blocks(k_update_p, 1 << 30);
+    k_update_p<<<std::min(grid_for(n / 2), (unsigned)wb), NT, 0, st>>>(n / 2, r, invd, p, ctl, cond);
 }
 
 void launch_to_split_f(cudaStream_t st, const Geo& g, int planes, const float* nat, float* split) {

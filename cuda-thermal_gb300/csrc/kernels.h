@@ -92,6 +92,29 @@ void launch_dot(cudaStream_t st, MgType mt, bool flexible, unsigned n, const dou
 void launch_update_p(cudaStream_t st, MgType mt, unsigned n, const void* z, const double* r,
                      const double* invd, double* p, Ctl* ctl, Cond cond);
 
+// ---- FP64 outer PCG of the multigrid modes, k_fp64.cu --------------------------
+// The same operations for mt = MG_F32 / MG_F64 with the fewest FP64
+// instructions (integer float <-> double conversions); the launchers above
+// hand the multigrid modes to these.
+void launch_residual64(cudaStream_t st, MgType mt, const OpView& o, unsigned n, const double* diag,
+                       const double* b, const double* x, double* r, void* b0, Ctl* ctl, const Red& red,
+                       Cond cond);
+void launch_apply64(cudaStream_t st, const OpView& o, const double* diag, const double* p,
+                    double* Ap, Ctl* ctl, const Red& red, Cond cond);
+void launch_update64(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap, double* x,
+                     double* r, void* b0, Ctl* ctl, const Red& red, Cond cond);
+void launch_dot64(cudaStream_t st, MgType mt, bool flexible, unsigned n, const double* r, const void* z,
+                  const double* Ap, Ctl* ctl, const Red& red, Cond cond);
+void launch_update_p64(cudaStream_t st, MgType mt, unsigned n, const void* z, double* p, Ctl* ctl,
+                       Cond cond);
+// The GPU's DFMA issue rate (instructions per second, independent chains on
+// every SM; synchronises the device): the FP64-pipe roofline's denominator.
+cudaError_t measure_dfma_rate(double* per_s);
+// Integer conversions against the hardware on n bit patterns (adds the
+// mismatch count to *mismatches).
+cudaError_t launch_conv_selftest(cudaStream_t st, unsigned long long n, unsigned long long seed,
+                                 unsigned long long* mismatches);
+
 // ---- setup and auxiliary kernels, k_outer.cu ------------------------------
 void launch_to_split_f(cudaStream_t st, const Geo& g, int planes, const float* nat, float* split);
 void launch_to_split_d(cudaStream_t st, const Geo& g, const double* nat, double* split);

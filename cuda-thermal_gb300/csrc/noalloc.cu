@@ -40,28 +40,59 @@ static_assert((size_t)kThreads * kMaxBlocks == CT_NOALLOC_MAX_COLUMNS, "column l
 
 static __device__ __align__(256) double g_scratch[kScratchDoubles];
 
-// The device address of g_scratch, looked up once per device. In host code
-// the name g_scratch is only a host-side stand-in for the symbol, not a
-// device address, so it must never be passed to a kernel.
+// The device address of g_scratch, looked up once per device and context.
+// In host code the name g_scratch is only a host-side stand-in for the
+// symbol, not a device address, so it must never be passed to a kernel. The
+// address is cached with the context it was looked up in: after a device
+// reset the library's module is loaded again into a new context, where the
+// array may sit elsewhere, so a new context means a new lookup.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
+struct ScratchAddr {
+    void* ctx;
+    double* ptr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices] = {};
+
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<CtxGetCurrentFn>(p);
+    }();
+    return fn;
+}
 
 ct_status scratch_for_current_device(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return ct::fail(CT_CUDA_ERROR, "cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return ct::fail(CT_BAD_ARG, "device %d out of range", dev);
+    const CtxGetCurrentFn get = ctx_get_current();
+    if (!get) return ct::fail(CT_CUDA_ERROR, "cuCtxGetCurrent not available");
+    void* ctx = nullptr;  // null until the runtime has made a context current
+    if (get(&ctx) != 0) ctx = nullptr;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    ScratchAddr& a = g_scratch_addr[dev];
+    if (!ctx || !a.ptr || a.ctx != ctx) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_scratch);
+        e = cudaGetSymbolAddress(&p, g_scratch);  // also makes the device's context current
         if (e != cudaSuccess || !p)
             return ct::fail(CT_CUDA_ERROR, "cudaGetSymbolAddress(scratch) on device %d: %s", dev,
                             cudaGetErrorString(e));
-        g_scratch_ptr[dev] = static_cast<double*>(p);
+        if (get(&ctx) != 0 || !ctx)
+            return ct::fail(CT_CUDA_ERROR, "no current CUDA context on device %d", dev);
+        a.ctx = ctx;
+        a.ptr = static_cast<double*>(p);
     }
-    *out = g_scratch_ptr[dev];
+    *out = a.ptr;
     return CT_OK;
 }
 

@@ -168,8 +168,18 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     {
         // The smallest levels whose arrays fit one block's shared memory.
         small_k0 = lv.size();
-        long small_max = kSmallSmemMax;
-        if (const char* e = std::getenv("CT_SMALL_BYTES")) small_max = std::atol(e);
+        // CT_SMALL_BYTES lowers the budget (a diagnostics knob); it can never
+        // exceed what one block may hold on this device
+        int optin = 0;
+        CT_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        long small_max = std::min<long>(kSmallSmemMax, optin);
+        if (const char* e = std::getenv("CT_SMALL_BYTES")) {
+            char* end = nullptr;
+            const long v = std::strtol(e, &end, 10);
+            if (end == e || *end != '\0' || v < 0)
+                return fail(CT_BAD_ARG, "CT_SMALL_BYTES=%s is not a byte count", e);
+            small_max = std::min(small_max, v);
+        }
         size_t acc = 0;
         for (size_t k = lv.size(); k-- > 0;) {
             acc += small_level_bytes(lv[k].g, tsize);
@@ -652,6 +662,39 @@ ct_status ct_selftest_bounded_wait(unsigned polls, int* timed_out) {
     if (e != cudaSuccess) return fail(CT_CUDA_ERROR, "ct_selftest_bounded_wait: %s", cudaGetErrorString(e));
     if (h != 1 && h != 2) return fail(CT_CUDA_ERROR, "ct_selftest_bounded_wait: status %d", h);
     *timed_out = h == 1 ? 1 : 0;
+    return CT_OK;
+}
+
+ct_status ct_selftest_conversions(unsigned long long n, unsigned long long seed,
+                                  unsigned long long* mismatches) {
+    if (!mismatches) return fail(CT_BAD_ARG, "ct_selftest_conversions: null");
+    if (n == 0 || n > (1ull << 32)) return fail(CT_BAD_ARG, "ct_selftest_conversions: n in 1..2^32");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CT_NO_DEVICE, "no CUDA device");
+    }
+    unsigned long long* d = nullptr;
+    unsigned long long h = 0;
+    cudaError_t e = cudaMalloc(&d, sizeof(*d));
+    if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(*d));
+    if (e == cudaSuccess) e = ct::launch_conv_selftest(nullptr, n, seed, d);
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return fail(CT_CUDA_ERROR, "ct_selftest_conversions: %s", cudaGetErrorString(e));
+    *mismatches = h;
+    return CT_OK;
+}
+
+ct_status ct_probe_fp64_rate(double* dfma_per_s) {
+    if (!dfma_per_s) return fail(CT_BAD_ARG, "ct_probe_fp64_rate: null");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CT_NO_DEVICE, "no CUDA device");
+    }
+    const cudaError_t e = ct::measure_dfma_rate(dfma_per_s);
+    if (e != cudaSuccess) return fail(CT_CUDA_ERROR, "ct_probe_fp64_rate: %s", cudaGetErrorString(e));
     return CT_OK;
 }
 

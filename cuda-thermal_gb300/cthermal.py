@@ -157,6 +157,8 @@ def _signatures():
         "ct_case_set_name": (i, [vp, i, i, C.c_char_p]),
         "ct_case_set_ambient": (i, [vp, C.c_double]),
         "ct_selftest_bounded_wait": (i, [C.c_uint, ip]),
+        "ct_selftest_conversions": (i, [C.c_ulonglong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]),
+        "ct_probe_fp64_rate": (i, [C.POINTER(C.c_double)]),
         "ct_eff_kz": (d, [d, d, d]),
         "ct_eff_kxy": (d, [d, d, d]),
     }
@@ -458,6 +460,22 @@ def selftest_bounded_wait(polls: int) -> bool:
     t = C.c_int(0)
     _check(lib().ct_selftest_bounded_wait(int(polls), C.byref(t)))
     return bool(t.value)
+
+
+def selftest_conversions(n: int, seed: int = 1) -> int:
+    """The integer float <-> double conversions of the FP64 outer kernels
+    against the hardware conversions on n bit patterns: the mismatch count."""
+    bad = C.c_ulonglong(0)
+    _check(lib().ct_selftest_conversions(int(n), int(seed), C.byref(bad)))
+    return int(bad.value)
+
+
+def probe_fp64_rate() -> float:
+    """The device's DFMA rate (instructions per second): the denominator of
+    the FP64-pipe roofline."""
+    r = C.c_double(0.0)
+    _check(lib().ct_probe_fp64_rate(C.byref(r)))
+    return float(r.value)
 
 
 def export_3dice(case, cell_um: float, outdir: str) -> None:

@@ -119,6 +119,20 @@ void ct_use_graphs(int on);
  * the kernel returned (as it must; the solvers then report CT_TIMEOUT). The
  * context stays usable. */
 ct_status ct_selftest_bounded_wait(unsigned polls, int* timed_out);
+/* No counterpart in the reference. The FP64 outer kernels convert between
+ * float and double with integer operations instead of the hardware
+ * conversions, which issue at the FP64 rate on GB300; this runs both on n
+ * bit patterns (every float exponent, doubles around the float range with
+ * mantissas at and beside the rounding tie, then hashed patterns) and
+ * returns the number of results that differ in *mismatches (0 expected).
+ * n in 1..2^32; synchronises the device. */
+ct_status ct_selftest_conversions(unsigned long long n, unsigned long long seed,
+                                  unsigned long long* mismatches);
+/* No counterpart in the reference. The device's FP64 fused multiply-add
+ * rate (instructions per second over every SM, independent chains; about
+ * 0.53e12 on GB300): the denominator of the FP64-pipe roofline reported for
+ * the FP64 outer kernels. Synchronises the device. */
+ct_status ct_probe_fp64_rate(double* dfma_per_s);
 /* gpu_last_setup (src/pcg3d_gpu.cu:87-88): setup times of the last solver
  * created on any thread. */
 ct_status ct_last_setup(ct_setup_times* out);
@@ -200,7 +214,9 @@ ct_status ct_level_factors(ct_solver* s, int k, double* fcp, double* finv);
  * limits a model to CT_NOALLOC_MAX_COLUMNS columns (nx * ny); larger models
  * get CT_BAD_ARG. The first call on each device looks up that array's device
  * address (cudaGetSymbolAddress, no allocation), so make the first call on a
- * device before any stream capture. All calls share the one scratch array:
+ * device before any stream capture; the address is kept per CUDA context,
+ * and the first call in a new context (after a device reset) looks it up
+ * again, so make that call before any capture too. All calls share the one scratch array:
  * calls whose work can overlap on the GPU (other streams, other threads)
  * race on it and must be serialised by the caller. */
 #define CT_NOALLOC_SCRATCH_BYTES 131072

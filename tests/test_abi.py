@@ -61,3 +61,19 @@ def test_unfinalized_model_rejected(ctlib, ct):
     with pytest.raises(ct.CtError) as e:
         ct.GpuPcg(m)
     assert e.value.status == 6
+
+
+def test_noalloc_argument_checks_without_gpu(ctlib, ct):
+    """ct_true_relres_noalloc rejects bad arguments before any device call:
+    too many planes, a null model array, a null output."""
+    import ctypes as C
+    dummy = C.c_void_p(256)  # never dereferenced
+    deep = ct.CtModel(8, 8, 65, 1e-5, 1e-5, dummy, dummy, dummy, dummy, dummy, dummy)
+    assert ctlib.ct_true_relres_noalloc(C.byref(deep), dummy, dummy, None) == 5
+    assert b"bad size" in ctlib.ct_last_error()
+    no_gb = ct.CtModel(8, 8, 10, 1e-5, 1e-5, dummy, dummy, dummy, None, dummy, dummy)
+    assert ctlib.ct_true_relres_noalloc(C.byref(no_gb), dummy, dummy, None) == 5
+    assert b"null model array" in ctlib.ct_last_error()
+    ok = ct.CtModel(8, 8, 10, 1e-5, 1e-5, dummy, dummy, dummy, dummy, dummy, dummy)
+    assert ctlib.ct_true_relres_noalloc(C.byref(ok), dummy, None, None) == 5
+    assert b"null argument" in ctlib.ct_last_error()

@@ -406,3 +406,19 @@ def test_deep_stacks_match_oracle(ct, orc, cu_planes, prec):
     tmax = np.abs(ref.T).max()
     assert np.abs(T - ref.T).max() <= min(5e-4, 1e-7 * tmax)
     assert orc.true_relres(m, T) <= 1e-9
+
+
+def test_integer_conversions_equal_hardware(ct):
+    """The FP64 outer kernels widen floats and narrow doubles with integer
+    operations (the hardware conversions issue at the FP64 rate); on 2^24 bit
+    patterns, every float exponent and doubles around the float range with
+    mantissas at and beside the rounding tie included, they give the
+    hardware's results bit for bit."""
+    assert ct.selftest_conversions(1 << 24, seed=7) == 0
+
+
+def test_fp64_rate_probe(ct):
+    """The FP64-pipe roofline's denominator: a DFMA rate between 0.1e12 and
+    1e14 per second (GB300: about 0.53e12)."""
+    r = ct.probe_fp64_rate()
+    assert 1e11 < r < 1e14

@@ -5,8 +5,10 @@ caller's device arrays with a fixed scratch array inside the library.
 
 Checked through the C ABI against the existing entry point (ct_true_relres on
 a solver holding the same temperatures), on two calls in a row, with a call on
-a different model in between (the calls share one scratch array), and for the
-size limit. This file is named to be collected last.
+a different model in between (the calls share one scratch array), on a
+stream other than the current one, on a model of exactly the largest size
+the scratch allows, and for the size limit. This file is named to be
+collected last.
 Tolerance: relative 1e-12 (both compute the same per-cell residuals in FP64;
 only the grouping of the two sums differs).
 """
@@ -30,11 +32,13 @@ def device_model(ct, torch, m):
     return cm, t
 
 
-def noalloc_relres(ct, torch, cm, T_dev):
+def noalloc_relres(ct, torch, cm, T_dev, stream=None):
     out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
-    stream = torch.cuda.current_stream().cuda_stream
+    s = stream if stream is not None else torch.cuda.current_stream()
+    if stream is not None:
+        s.wait_stream(torch.cuda.current_stream())  # inputs were written on the current stream
     st = ct.lib().ct_true_relres_noalloc(C.byref(cm), C.c_void_p(T_dev.data_ptr()),
-                                         C.c_void_p(out.data_ptr()), C.c_void_p(stream))
+                                         C.c_void_p(out.data_ptr()), C.c_void_p(s.cuda_stream))
     assert st == 0, ct.lib().ct_last_error().decode()
     torch.cuda.synchronize()
     return float(out.item())
@@ -68,6 +72,30 @@ def test_noalloc_matches_existing_entry_point(ct):
     assert abs(a1 - refA) <= REL_TOL * refA
     assert a2 == a1 and a3 == a1
     assert abs(b1 - refB) <= REL_TOL * refB
+    # the same on a stream of its own
+    side = torch.cuda.Stream()
+    a4 = noalloc_relres(ct, torch, cmA, TA_dev, stream=side)
+    assert a4 == a1
+
+
+def test_noalloc_at_its_column_limit(ct):
+    """A model of exactly CT_NOALLOC_MAX_COLUMNS columns (1536 x 1365, two
+    planes): every scratch slot is used, and the result matches the solver's."""
+    torch = pytest.importorskip("torch")
+    nx, ny = 1536, 1365
+    assert nx * ny == 2096640  # CT_NOALLOC_MAX_COLUMNS
+    layers = [ct.Layer("Si", 50e-6, 130.0, 1.66e6, 1, True), ct.Layer("Cu", 1e-3, 400.0, 3.45e6, 1, False)]
+    m = ct.build_model(layers, nx, ny, 10e-3, 10e-3, 2e4, 0.0)
+    ct.add_uniform_power(m, 0, 10.0)
+    ct.add_hotspot(m, 0, 4e-3, 6e-3, 1e-3, 2.0)
+    ct.finalize(m)
+    T, ref = solved_field(ct, m, 1e-4)
+    cm, keep = device_model(ct, torch, m)
+    T_dev = torch.from_numpy(T).cuda()
+    r1 = noalloc_relres(ct, torch, cm, T_dev)
+    r2 = noalloc_relres(ct, torch, cm, T_dev)
+    assert abs(r1 - ref) <= REL_TOL * ref
+    assert r2 == r1
 
 
 def test_noalloc_rejects_models_beyond_its_scratch(ct):
