@@ -532,7 +532,7 @@ def bench_transient_batched(ct, np, args, steps):
     t = np.zeros(n)
     ptot = np.array([w.power().sum() for w in ws])
     eb, its, switches = [], [], 0
-    dts = []
+    dts, eb_inst = [], []
     t0 = time.perf_counter()
     for k in range(steps):
         for i, w in enumerate(ws):
@@ -545,8 +545,10 @@ def bench_transient_batched(ct, np, args, steps):
         st = b.step_transient(dt, TR_TOL, MAXIT)
         rec = b.step_records(dt)
         on = ptot > 0
+        ebk = np.where(on, np.abs(rec[:, 1] + rec[:, 2] - ptot) / np.where(on, ptot, 1.0), np.nan)
+        eb_inst.append(ebk[:TR_CHECK].copy())
         if on.any():
-            eb.append(float(np.max(np.abs(rec[on, 1] + rec[on, 2] - ptot[on]) / ptot[on])))
+            eb.append(float(np.nanmax(ebk)))
         its.append(max(s.iters for s in st))
         dts.append(dt.copy())
         t += dt
@@ -557,6 +559,7 @@ def bench_transient_batched(ct, np, args, steps):
     # the same steps for the first instances with the plain FP64 MG-PCG, one by one
     ref = workloads.switching_instances(TR_CHECK, TR_GRID, seed=TR_SEED)
     sec64, max_dT = 0.0, 0.0
+    eb64, eb_same = [], []  # the FP64 solver's balance per step; the batch's on the same instances
     for i, w in enumerate(ref):
         s = ct.GpuPcg(w.model, ct.Precond.Multigrid, ct.Precision.MG_FP64)
         s.set_power(w.power())
@@ -564,15 +567,24 @@ def bench_transient_batched(ct, np, args, steps):
         s.set_rhs_steady()
         s.solve(TOL, MAXIT)
         tt = 0.0
-        a0 = time.perf_counter()
+        sec = 0.0
+        pt = float(w.power().sum())
         for k in range(steps):
+            a0 = time.perf_counter()
             if w.advance(tt):
-                s.set_power(w.power())
+                P = w.power()
+                s.set_power(P)
+                pt = float(P.sum())
             s.set_dt(float(dts[k][i]))
             s.set_rhs_transient()
             s.solve(TR_TOL, MAXIT)
+            sec += time.perf_counter() - a0
+            if pt > 0:  # bookkeeping outside the timed part
+                r = s.step_record(float(dts[k][i]))
+                eb64.append(abs(r.q_out + r.q_stored - pt) / pt)
+                eb_same.append(eb_inst[k][i])
             tt += float(dts[k][i])
-        sec64 += time.perf_counter() - a0
+        sec64 += sec
         max_dT = max(max_dT, float(np.abs(s.get_x() - Tb[i]).max()))
         s.close()
     value = n * steps / sec
@@ -588,7 +600,12 @@ def bench_transient_batched(ct, np, args, steps):
         "energy_balance_err_max": max(eb) if eb else None,
         "energy_balance_err_median": float(np.median(eb)) if eb else None,
         "fp64_mg_pcg_sequential": {"value": value64, "unit": "instance steps/s",
-                                   "instances": TR_CHECK},
+                                   "instances": TR_CHECK,
+                                   "energy_balance_err_max": max(eb64) if eb64 else None,
+                                   "energy_balance_err_median": float(np.median(eb64)) if eb64 else None},
+        "energy_balance_same_instances": {"batch_max": float(np.nanmax(eb_same)) if eb_same else None,
+                                          "fp64_max": max(eb64) if eb64 else None,
+                                          "note": "tol is relative to ||b|| = ||P + C/dt T_old||"},
         "speedup_vs_fp64": value / value64,
         "max_dT_K_vs_fp64": max_dT,
     }
