@@ -31,6 +31,71 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
+def deep_stack(ct, nx, cu_planes, ny=None):
+    """The default stack with a copper spreader of cu_planes planes (6 +
+    cu_planes planes in all), 10 x 9 mm, 35 W with a hotspot."""
+    layers = [ct.Layer("Si tier 2 (bottom)", 50e-6, 130.0, 1.66e6, 2, True),
+              ct.Layer("bond + BEOL", 10e-6, 2.0, 1.70e6, 1, False),
+              ct.Layer("Si tier 1 (top)", 50e-6, 130.0, 1.66e6, 2, True),
+              ct.Layer("TIM", 25e-6, 5.0, 2.00e6, 1, False),
+              ct.Layer("Cu spreader", 1e-3, 400.0, 3.45e6, cu_planes, False)]
+    m = ct.build_model(layers, nx, ny or nx, 10e-3, 9e-3, 2e4, 0.0)
+    ct.add_uniform_power(m, 0, 20.0)
+    ct.add_hotspot(m, 0, 3e-3, 4e-3, 1e-3, 3.0)
+    ct.add_uniform_power(m, 2, 15.0)
+    ct.finalize(m)
+    return m
+
+
+class env_vars:
+    """Sets environment variables (None: unset) while a solver is created
+    (the solver reads its switches then), and restores them after."""
+
+    def __init__(self, **kw):
+        self.kw = kw
+        self.old = {}
+
+    def __enter__(self):
+        import os
+        for k, v in self.kw.items():
+            self.old[k] = os.environ.get(k)
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        return self
+
+    def __exit__(self, *a):
+        import os
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def steady_then_steps(ct, m, prec):
+    """A steady solve, then two backward-Euler steps: iteration counts and
+    fields, in order."""
+    with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
+        s.set_x_zero()
+        s.set_rhs_steady()
+        res = [s.solve(1e-10, 1000).iters, s.get_x()]
+        s.set_dt(1e-3)
+        for _ in range(2):
+            s.set_rhs_transient()
+            res += [s.solve(1e-9, 1000).iters, s.get_x()]
+        return res
+
+
+def assert_same_results(a, b):
+    for x, y in zip(a, b):
+        if isinstance(x, np.ndarray):
+            assert np.array_equal(x, y)
+        else:
+            assert x == y
+
+
 def gpu_solve(ct, m, tol, pc, prec):
     with ct.GpuPcg(m, pc, prec) as s:
         s.set_x_zero()
@@ -300,74 +365,52 @@ def test_staged_sweeps_bitwise_single_and_batch(ct, n, prec, tmp_path):
 def test_fused_first_sweep_bitwise(ct, n, prec):
     """Each level's first (x = 0) sweep run inside the restriction into that
     level (the default) gives the separate launches' results bit for bit:
-    steady solve, then two backward-Euler steps."""
-    import os
+    steady solve, then two backward-Euler steps (cluster tail off, so every
+    level runs as grid launches)."""
     import workloads
     m = workloads.steady_hotspot(n, seed=13)
     out = []
     for flag in ("0", "1"):
-        old = os.environ.get("CT_FUSE_SWEEP0")
-        os.environ["CT_FUSE_SWEEP0"] = flag  # read when the solver is created
-        try:
-            with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
-                s.set_x_zero()
-                s.set_rhs_steady()
-                res = [s.solve(1e-10, 1000).iters, s.get_x()]
-                s.set_dt(1e-3)
-                for _ in range(2):
-                    s.set_rhs_transient()
-                    res += [s.solve(1e-9, 1000).iters, s.get_x()]
-                out.append(res)
-        finally:
-            if old is None:
-                os.environ.pop("CT_FUSE_SWEEP0", None)
-            else:
-                os.environ["CT_FUSE_SWEEP0"] = old
-    for a, b in zip(out[0], out[1]):
-        if isinstance(a, np.ndarray):
-            assert np.array_equal(a, b)
-        else:
-            assert a == b
+        with env_vars(CT_FUSE_SWEEP0=flag, CT_TAIL_COLS="0"):
+            out.append(steady_then_steps(ct, m, prec))
+    assert_same_results(out[0], out[1])
 
 
 @pytest.mark.parametrize("prec", ["MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
 @pytest.mark.parametrize("n", [203, 64, 9])
 def test_shared_memory_bottom_bitwise(ct, n, prec):
-    """The bottom levels run by one block out of shared memory (the default;
-    its sweeps gather every plane's right-hand side with one task per column
-    and plane before the recurrences) give the grid-wide launches' results
+    """The bottom levels run by one block out of shared memory (its sweeps
+    gather every plane's right-hand side with one task per column and plane
+    before the recurrences) give the grid-wide launches' results
     (CT_SMALL_BYTES=0: no shared-memory bottom) bit for bit: steady solve,
-    then two backward-Euler steps."""
-    import os
+    then two backward-Euler steps (cluster tail off in both)."""
     import workloads
     m = workloads.steady_hotspot(n, seed=17)
     out = []
     for flag in ("0", None):
-        old = os.environ.get("CT_SMALL_BYTES")
-        if flag is None:
-            os.environ.pop("CT_SMALL_BYTES", None)
-        else:
-            os.environ["CT_SMALL_BYTES"] = flag  # read when the solver is created
-        try:
-            with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
-                s.set_x_zero()
-                s.set_rhs_steady()
-                res = [s.solve(1e-10, 1000).iters, s.get_x()]
-                s.set_dt(1e-3)
-                for _ in range(2):
-                    s.set_rhs_transient()
-                    res += [s.solve(1e-9, 1000).iters, s.get_x()]
-                out.append(res)
-        finally:
-            if old is None:
-                os.environ.pop("CT_SMALL_BYTES", None)
-            else:
-                os.environ["CT_SMALL_BYTES"] = old
-    for a, b in zip(out[0], out[1]):
-        if isinstance(a, np.ndarray):
-            assert np.array_equal(a, b)
-        else:
-            assert a == b
+        with env_vars(CT_SMALL_BYTES=flag, CT_TAIL_COLS="0"):
+            out.append(steady_then_steps(ct, m, prec))
+    assert_same_results(out[0], out[1])
+
+
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
+@pytest.mark.parametrize("n,cu_planes", [(203, 4), (130, 4), (96, 4), (96, 16), (72, 34)])
+def test_cluster_tail_bitwise(ct, n, cu_planes, prec):
+    """The coarse end of the V-cycle in one thread-block cluster launch (the
+    default: levels of at most 64 x 64 columns, the restriction into the first
+    of them included) gives the separate launches' results (CT_TAIL_COLS=0)
+    bit for bit: steady solve, then two backward-Euler steps. Sizes put the
+    tail's first level at 51 x 51 (level 2), 33 x 33 (level 2, after a
+    65 x 65 level just over the limit) and 48 x 48 (level 1: the restriction
+    from the fine level); plane counts 10, 22 and 40 (register columns of 12
+    and 32 planes, and the general column path)."""
+    import workloads
+    m = workloads.steady_hotspot(n, seed=19) if cu_planes == 4 else deep_stack(ct, n, cu_planes)
+    out = []
+    for flag in ("0", None):
+        with env_vars(CT_TAIL_COLS=flag):
+            out.append(steady_then_steps(ct, m, prec))
+    assert_same_results(out[0], out[1])
 
 
 def test_bounded_wait_runs_out_and_context_survives(ct):
@@ -389,16 +432,7 @@ def test_deep_stacks_match_oracle(ct, orc, cu_planes, prec):
     bottom) and 40 planes (past 32: the general column path, no staging),
     on a 160 x 144 grid so level 0 is staged where it can be. Against the
     FP64 oracle within 5e-4 K and 1e-7 of Tmax, FP64 true residual <= 1e-9."""
-    layers = [ct.Layer("Si tier 2 (bottom)", 50e-6, 130.0, 1.66e6, 2, True),
-              ct.Layer("bond + BEOL", 10e-6, 2.0, 1.70e6, 1, False),
-              ct.Layer("Si tier 1 (top)", 50e-6, 130.0, 1.66e6, 2, True),
-              ct.Layer("TIM", 25e-6, 5.0, 2.00e6, 1, False),
-              ct.Layer("Cu spreader", 1e-3, 400.0, 3.45e6, cu_planes, False)]
-    m = ct.build_model(layers, 160, 144, 10e-3, 9e-3, 2e4, 0.0)
-    ct.add_uniform_power(m, 0, 20.0)
-    ct.add_hotspot(m, 0, 3e-3, 4e-3, 1e-3, 3.0)
-    ct.add_uniform_power(m, 2, 15.0)
-    ct.finalize(m)
+    m = deep_stack(ct, 160, cu_planes, 144)
     assert m.nz == 6 + cu_planes
     ref = orc.solve_steady(m, 1e-10, 50000, "multigrid", mg_double=True)
     st, T = gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, getattr(ct.Precision, prec))
