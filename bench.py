@@ -381,40 +381,54 @@ def traffic_from_profiles(kernel_name):
 
 def bench_batched(ct, np, torch, args, hbm_peak, peak_kind, rank=0, world=1):
     """The batched form on the 256-instance floorplan sweep: uneven stacks
-    (nx, ny in 64..512, 6-16 planes), all solved to 1e-10 together, against
-    the plain FP64 MG-PCG solving the same instances one after another. With
+    (nx, ny in 64..512, 6-16 planes), all solved to 1e-10 together with the
+    FP32 V-cycle in FP64 flexible PCG (and, beside it, with the outer
+    iteration in double words), against the plain FP64 MG-PCG solving the
+    same instances one after another. With
     several ranks each solves a cost-balanced share (cells per instance; the
     iteration counts hardly vary) and the rate is all instances over the
     slowest rank's time."""
     import workloads
-    t0 = time.perf_counter()
     specs_all = workloads.batch_instance_specs(BATCH_N, seed=BATCH_SEED)
     costs = [nx * ny * sum(l.ncells for l in cs.layers) for cs, nx, ny in specs_all]
     mine = partition_instances(costs, world)[rank]
     specs = [specs_all[i] for i in mine]
-    # every instance's model is built on the device from its description
-    b = ct.GpuBatch.from_specs([s[0] for s in specs], [s[1] for s in specs], [s[2] for s in specs],
-                               False)
+    kb = max(3, args.steps // 3)
+
+    def make(prec):
+        # every instance's model is built on the device from its description
+        return ct.GpuBatch.from_specs([q[0] for q in specs], [q[1] for q in specs], [q[2] for q in specs],
+                                      False, precision=prec)
+
+    def timed(bt):
+        for _ in range(args.warmup):
+            bt.set_x_zero()
+            bt.set_rhs_steady()
+            bt.solve(TOL, MAXIT)
+        stream = torch.cuda.ExternalStream(bt.stream())
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(kb):
+            bt.set_x_zero()
+            bt.set_rhs_steady()
+            stats = bt.solve(TOL, MAXIT)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / kb, world), stats
+
+    # the same instances with the outer iteration in double words
+    bdw = make(ct.Precision.MG_FP32_FLEX_DW)
+    ms_dw, st_dw = timed(bdw)
+    Tdw = [bdw.get_x(i) for i in range(len(specs))]
+    bdw.close()
+    t0 = time.perf_counter()
+    b = make(ct.Precision.MG_FP32_FLEX)
     models = b.models
     cells = sum(m.ncells() for m in models)
     setup_s = time.perf_counter() - t0
-    for _ in range(args.warmup):
-        b.set_x_zero()
-        b.set_rhs_steady()
-        b.solve(TOL, MAXIT)
-    stream = torch.cuda.ExternalStream(b.stream())
-    kb = max(3, args.steps // 3)
-    torch.cuda.synchronize()
-    barrier(world)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(kb):
-        b.set_x_zero()
-        b.set_rhs_steady()
-        st = b.solve(TOL, MAXIT)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = max_over_ranks(e0.elapsed_time(e1) / kb, world)
+    ms, st = timed(b)
     iters = [s.iters for s in st]
     conv = sum(1 for s in st if s.converged)
     Tb = [b.get_x(i) for i in range(len(models))]
@@ -451,10 +465,11 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind, rank=0, world=1):
             max_dT = max(max_dT, float(np.abs(s.get_x() - Tb[i]).max()))
     ms64 = max_over_ranks(ms64, world)
     max_dT = max_over_ranks(max_dT, world)
+    max_dT_dw = max_over_ranks(max(float(np.abs(a - c).max()) for a, c in zip(Tdw, Tb)), world)
     value = len(specs_all) / (ms / 1e3)
     value64 = len(specs_all) / (ms64 / 1e3)
     return {
-        "value": value, "unit": "instance solves/s",
+        "value": value, "unit": "instance solves/s", "precision": "CT_MG_FP32_FLEX",
         "workload": f"{len(specs_all)} seeded stacks, nx, ny in 64..512 step 32, 6-16 planes, "
                     f"12 log-normal floorplan blocks per tier, tol {TOL:g} per instance",
         "instances": len(specs_all), "instances_rank0": len(models), "cells_rank0": cells,
@@ -464,6 +479,9 @@ def bench_batched(ct, np, torch, args, hbm_peak, peak_kind, rank=0, world=1):
         "fp64_mg_pcg_sequential": {"value": value64, "unit": "instance solves/s",
                                    "ms_total": ms64, "iters_max": max(it64)},
         "speedup_vs_fp64": value / value64,
+        "double_word": {"value": len(specs_all) / (ms_dw / 1e3), "unit": "instance solves/s",
+                        "precision": "CT_MG_FP32_FLEX_DW", "ms_per_batch_solve": ms_dw,
+                        "iters_max": max(s.iters for s in st_dw), "max_dT_K_vs_flex": max_dT_dw},
         "setup_s": setup_s,
         "setup": "models described on the host, built on the device (ct_batch_create_cases)",
         "sharding": f"{world} rank(s), cost-balanced by cells, no collective",
@@ -512,7 +530,8 @@ def bench_four_tier(ct, np, torch, args):
 
 
 def bench_transient_batched(ct, np, args, steps):
-    """The batched transient: 64 instances of the 256 x 256 x 10 stack, each
+    """The batched transient (FP32 V-cycle in FP64 flexible PCG; the
+    double-word form beside it): 64 instances of the 256 x 256 x 10 stack, each
     with 9 blocks switching at Poisson times (mean 5 ms), backward-Euler steps
     with per-instance dt (10 us growing 10 % per step, capped at 50 ms, reset
     to 10 us on a switch), warm-started from the steady field of the initial
@@ -520,42 +539,48 @@ def bench_transient_batched(ct, np, args, steps):
     (power maps uploaded), set_dt, b = P + C/dt T, the batched solve and the
     batched step records of every step."""
     import workloads
-    ws = workloads.switching_instances(TR_N, TR_GRID, seed=TR_SEED)
-    n = len(ws)
-    b = ct.GpuBatch([w.model for w in ws])
-    for i, w in enumerate(ws):
-        b.set_power(i, w.power())
-    b.set_x_zero()
-    b.set_rhs_steady()
-    b.solve(TOL, MAXIT)
-    dt = np.full(n, TR_DT0)
-    t = np.zeros(n)
-    ptot = np.array([w.power().sum() for w in ws])
-    eb, its, switches = [], [], 0
-    dts, eb_inst = [], []
-    t0 = time.perf_counter()
-    for k in range(steps):
+
+    def run(prec):
+        ws = workloads.switching_instances(TR_N, TR_GRID, seed=TR_SEED)
+        n = len(ws)
+        b = ct.GpuBatch([w.model for w in ws], precision=prec)
         for i, w in enumerate(ws):
-            if w.advance(t[i]):
-                P = w.power()
-                b.set_power(i, P)
-                ptot[i] = P.sum()
-                dt[i] = TR_DT0
-                switches += 1
-        st = b.step_transient(dt, TR_TOL, MAXIT)
-        rec = b.step_records(dt)
-        on = ptot > 0
-        ebk = np.where(on, np.abs(rec[:, 1] + rec[:, 2] - ptot) / np.where(on, ptot, 1.0), np.nan)
-        eb_inst.append(ebk[:TR_CHECK].copy())
-        if on.any():
-            eb.append(float(np.nanmax(ebk)))
-        its.append(max(s.iters for s in st))
-        dts.append(dt.copy())
-        t += dt
-        dt = np.minimum(dt * TR_GROWTH, TR_DT_MAX)
-    sec = time.perf_counter() - t0
-    Tb = [b.get_x(i) for i in range(TR_CHECK)]
-    b.close()
+            b.set_power(i, w.power())
+        b.set_x_zero()
+        b.set_rhs_steady()
+        b.solve(TOL, MAXIT)
+        dt = np.full(n, TR_DT0)
+        t = np.zeros(n)
+        ptot = np.array([w.power().sum() for w in ws])
+        eb, its, switches = [], [], 0
+        dts, eb_inst = [], []
+        t0 = time.perf_counter()
+        for k in range(steps):
+            for i, w in enumerate(ws):
+                if w.advance(t[i]):
+                    P = w.power()
+                    b.set_power(i, P)
+                    ptot[i] = P.sum()
+                    dt[i] = TR_DT0
+                    switches += 1
+            st = b.step_transient(dt, TR_TOL, MAXIT)
+            rec = b.step_records(dt)
+            on = ptot > 0
+            ebk = np.where(on, np.abs(rec[:, 1] + rec[:, 2] - ptot) / np.where(on, ptot, 1.0), np.nan)
+            eb_inst.append(ebk[:TR_CHECK].copy())
+            if on.any():
+                eb.append(float(np.nanmax(ebk)))
+            its.append(max(s.iters for s in st))
+            dts.append(dt.copy())
+            t += dt
+            dt = np.minimum(dt * TR_GROWTH, TR_DT_MAX)
+        sec = time.perf_counter() - t0
+        Tb = [b.get_x(i) for i in range(TR_CHECK)]
+        b.close()
+        return n, sec, eb, its, switches, dts, eb_inst, Tb
+
+    n, sec_dw, eb_dw, _, _, _, _, Tb_dw = run(ct.Precision.MG_FP32_FLEX_DW)
+    n, sec, eb, its, switches, dts, eb_inst, Tb = run(ct.Precision.MG_FP32_FLEX)
     # the same steps for the first instances with the plain FP64 MG-PCG, one by one
     ref = workloads.switching_instances(TR_CHECK, TR_GRID, seed=TR_SEED)
     sec64, max_dT = 0.0, 0.0
@@ -567,7 +592,7 @@ def bench_transient_batched(ct, np, args, steps):
         s.set_rhs_steady()
         s.solve(TOL, MAXIT)
         tt = 0.0
-        sec = 0.0
+        sec_i = 0.0  # this instance's solving time
         pt = float(w.power().sum())
         for k in range(steps):
             a0 = time.perf_counter()
@@ -578,19 +603,23 @@ def bench_transient_batched(ct, np, args, steps):
             s.set_dt(float(dts[k][i]))
             s.set_rhs_transient()
             s.solve(TR_TOL, MAXIT)
-            sec += time.perf_counter() - a0
+            sec_i += time.perf_counter() - a0
             if pt > 0:  # bookkeeping outside the timed part
                 r = s.step_record(float(dts[k][i]))
                 eb64.append(abs(r.q_out + r.q_stored - pt) / pt)
                 eb_same.append(eb_inst[k][i])
             tt += float(dts[k][i])
-        sec64 += sec
+        sec64 += sec_i
         max_dT = max(max_dT, float(np.abs(s.get_x() - Tb[i]).max()))
         s.close()
     value = n * steps / sec
     value64 = TR_CHECK * steps / sec64
     return {
-        "value": value, "unit": "instance steps/s",
+        "value": value, "unit": "instance steps/s", "precision": "CT_MG_FP32_FLEX",
+        "double_word": {"value": n * steps / sec_dw, "unit": "instance steps/s",
+                        "precision": "CT_MG_FP32_FLEX_DW",
+                        "energy_balance_err_max": max(eb_dw) if eb_dw else None,
+                        "max_dT_K_vs_flex": max(float(np.abs(a - c).max()) for a, c in zip(Tb_dw, Tb))},
         "workload": f"{n} x {TR_GRID}x{TR_GRID}x10 default stack, 9 blocks per instance toggled at "
                     f"Poisson times (mean 5 ms), {steps} backward-Euler steps, per-instance dt "
                     f"{TR_DT0:g} s x {TR_GROWTH} per step (max {TR_DT_MAX:g}), reset on a switch, "

@@ -9,14 +9,19 @@
 // arrays (BInst per instance, LevelView per instance and depth, the small-level
 // descriptors) and block tables (batch.h) per stage.
 //
+// Precision: the FP32 V-cycle inside flexible PCG with the outer iteration
+// in FP64 (CT_MG_FP32_FLEX, k_batch64.cu) or in double words on the FP32
+// pipes with an FP64 residual replacement (CT_MG_FP32_FLEX_DW, k_batch.cu).
+//
 // Size buckets. Instances are grouped by the number of levels their V-cycle
 // runs as separate sweeps (the rest run in the one-block shared-memory kernel),
 // which follows their lateral size. Each bucket has its own stream and ONE
 // captured CUDA graph per solve:
-//     fold x;  r = b - A x (FP64);  WHILE (any instance active) {
+//     [fold x];  r = b - A x (FP64);  WHILE (any instance active) {
 //         guard;  V-cycle stages per depth;  small levels;  dot;  p;  Ap;
-//         x, r update and test;  residual replacement of instances whose
-//         first phase ended }
+//         x, r update and test;  [residual replacement of instances whose
+//         first phase ended] }
+// (the bracketed steps in the double-word mode only)
 // so instances converge one by one (their blocks return at entry) and the
 // loop ends when the bucket's last one does. Buckets run concurrently.
 //
@@ -92,6 +97,8 @@ class Batch {
     std::vector<std::unique_ptr<ct_solver>> sv;  // the instances (ct_solver wraps a Solver)
     cudaStream_t st = nullptr;  // set-up, copies, per-instance calls
     int sms = 0;
+    ct_precision prec = CT_MG_FP32_FLEX_DW;
+    bool dw = true;  // double-word outer iteration (else FP64)
     double rr_thr = 1e-5;
     bool use_cond = true;
     bool prof = false;
@@ -225,7 +232,7 @@ class Batch {
     }
     int small_k0(int i) const { return (int)inst(i).small_k0; }
 
-    ct_status create(int n, const ct_model* const* models, const DeviceBuild* builds = nullptr);
+    ct_status create(int n, const ct_model* const* models, const DeviceBuild* builds, ct_precision pr);
     ct_status build_bucket(Bucket& b);
     ct_status tune_bucket(Bucket& b);
     ct_status record(Bucket& b);
@@ -239,9 +246,13 @@ class Batch {
     void sweep(Bucket& b, cudaStream_t s, int d, int color, bool zero_x, bool prolong, Cond cond);
 };
 
-ct_status Batch::create(int n, const ct_model* const* models, const DeviceBuild* builds) {
+ct_status Batch::create(int n, const ct_model* const* models, const DeviceBuild* builds, ct_precision pr) {
     const TraceRange trace("ct_batch_create");
     if (n < 1) return fail(CT_BAD_ARG, "ct_batch_create: n must be >= 1");
+    if (pr != CT_MG_FP32_FLEX && pr != CT_MG_FP32_FLEX_DW)
+        return fail(CT_BAD_ARG, "ct_batch_create: precision must be CT_MG_FP32_FLEX or CT_MG_FP32_FLEX_DW");
+    prec = pr;
+    dw = pr == CT_MG_FP32_FLEX_DW;
     if (!models && !builds) return fail(CT_BAD_ARG, "ct_batch_create: null model list");
     for (int i = 0; models && i < n; ++i)
         if (!models[i]) return fail(CT_BAD_ARG, "ct_batch_create: null model %d", i);
@@ -269,8 +280,8 @@ ct_status Batch::create(int n, const ct_model* const* models, const DeviceBuild*
         s->st = st;
         s->skip_graphs = true;
         s->rr_thr = rr_thr;
-        const ct_status cs = builds ? s->create(nullptr, CT_MULTIGRID, CT_MG_FP32_FLEX_DW, &builds[i])
-                                    : s->create(models[i], CT_MULTIGRID, CT_MG_FP32_FLEX_DW);
+        const ct_status cs = builds ? s->create(nullptr, CT_MULTIGRID, prec, &builds[i])
+                                    : s->create(models[i], CT_MULTIGRID, prec);
         if (cs != CT_OK) {
             const std::string why = ct_last_error();
             return fail(cs, "ct_batch_create: instance %d: %s", i, why.c_str());
@@ -300,6 +311,9 @@ ct_status Batch::create(int n, const ct_model* const* models, const DeviceBuild*
         I.b0 = s.at<float>(s.lv[0].o_b);
         I.z = s.at<float>(s.lv[0].o_x);
         I.xold = s.xold;
+        I.r64 = s.r;
+        I.p64 = s.p;
+        I.Ap64 = s.Ap;
         I.n = s.n;
     }
     ct_status s;
@@ -424,7 +438,8 @@ ct_status Batch::build_bucket(Bucket& b) {
     if ((s = upload_plan(make_plan(ni, b.inst, pairs, kVecChunk), &b.vec)) != CT_OK) return s;
     if ((s = upload_plan(make_plan(ni, b.inst, cols, kColChunk), &b.cols)) != CT_OK) return s;
     if ((s = upload_plan(make_plan(ni, b.inst, rows, kRowChunk), &b.rows)) != CT_OK) return s;
-    if ((s = make_red(b.cols, &b.r_res)) != CT_OK) return s;
+    // the start residual walks columns (double words) or rows (FP64)
+    if ((s = make_red(dw ? b.cols : b.rows, &b.r_res)) != CT_OK) return s;
     if ((s = make_red(b.rows, &b.r_apply)) != CT_OK) return s;
     if ((s = make_red(b.vec, &b.r_update)) != CT_OK) return s;
     if ((s = make_red(b.vec, &b.r_dot)) != CT_OK) return s;
@@ -632,6 +647,10 @@ void Batch::vcycle(Bucket& b, cudaStream_t s, Cond cond) {
 
 void Batch::enqueue_init(Bucket& b, cudaStream_t s, Cond cond) {
     const double N = cells_of(b, -1);
+    if (!dw) {
+        enq(s, "b_residual", N * 56, [&] { launch_b_residual64(s, b.rows, bi, ctl, b.r_res, b.bc, cond); });
+        return;
+    }
     enq(s, "b_fold", N * 32, [&] { launch_b_fold(s, b.vec, bi, ctl, 0); });
     enq(s, "b_residual", N * 56,
         [&] { launch_b_residual(s, b.cols, bi, ctl, b.r_res, 1, b.bc, cond); });
@@ -641,6 +660,14 @@ void Batch::enqueue_body(Bucket& b, cudaStream_t s, Cond cond) {
     const double N = cells_of(b, -1);
     launch_b_guard(s, b.bc, cond);
     vcycle(b, s, cond);
+    if (!dw) {
+        enq(s, "b_dot", N * 20, [&] { launch_b_dot64(s, b.vec, bi, ctl, b.r_dot, b.bc, cond); });
+        enq(s, "b_update_p", N * 20, [&] { launch_b_update_p64(s, b.vec, bi, ctl); });
+        enq(s, "b_apply", N * 36, [&] { launch_b_apply64(s, b.rows, bi, ctl, b.r_apply, b.bc, cond); });
+        enq(s, "b_update_xr", N * 52,
+            [&] { launch_b_update64(s, b.vec, bi, ctl, b.r_update, b.bc, cond); });
+        return;
+    }
     enq(s, "b_dot", N * 20, [&] { launch_b_dot(s, b.vec, bi, ctl, b.r_dot, b.bc, cond); });
     enq(s, "b_update_p", N * 20, [&] { launch_b_update_p(s, b.vec, bi, ctl); });
     enq(s, "b_apply", N * 36, [&] { launch_b_apply(s, b.rows, bi, ctl, b.r_apply, b.bc, cond); });
@@ -780,7 +807,7 @@ ct_status Batch::solve(double tol, int maxit, ct_stats* out) {
         Solver& v = inst(i);
         if (c.bb_zero) {  // no heat in: x = 0 (src/pcg3d_cpu.cpp:146)
             CT_BK(cudaMemsetAsync(v.x, 0, (size_t)v.n * 8, st));
-            CT_BK(cudaMemsetAsync(v.xwc, 0, (size_t)v.n * 8, st));
+            if (v.xwc) CT_BK(cudaMemsetAsync(v.xwc, 0, (size_t)v.n * 8, st));
         }
         if (out) {
             out[i].iters = c.iter;
@@ -822,11 +849,15 @@ using ct::fail;
 extern "C" {
 
 ct_status ct_batch_create(int n, const ct_model* const* models, ct_batch** out) {
+    return ct_batch_create_prec(n, models, CT_MG_FP32_FLEX_DW, out);
+}
+
+ct_status ct_batch_create_prec(int n, const ct_model* const* models, ct_precision prec, ct_batch** out) {
     if (!out) return fail(CT_BAD_ARG, "ct_batch_create: null output");
     *out = nullptr;
     ct_batch* b = new (std::nothrow) ct_batch();
     if (!b) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
-    const ct_status s = b->impl.create(n, models);
+    const ct_status s = b->impl.create(n, models, nullptr, prec);
     if (s != CT_OK) {
         delete b;
         return s;
@@ -837,6 +868,11 @@ ct_status ct_batch_create(int n, const ct_model* const* models, ct_batch** out) 
 
 ct_status ct_batch_create_cases(int n, const ct_case* const* cases, const int* nx, const int* ny,
                                 const int* with_tsv, ct_batch** out) {
+    return ct_batch_create_cases_prec(n, cases, nx, ny, with_tsv, CT_MG_FP32_FLEX_DW, out);
+}
+
+ct_status ct_batch_create_cases_prec(int n, const ct_case* const* cases, const int* nx, const int* ny,
+                                     const int* with_tsv, ct_precision prec, ct_batch** out) {
     if (!out) return fail(CT_BAD_ARG, "ct_batch_create_cases: null output");
     *out = nullptr;
     if (n < 1 || !cases || !nx || !ny) return fail(CT_BAD_ARG, "ct_batch_create_cases: bad arguments");
@@ -848,7 +884,7 @@ ct_status ct_batch_create_cases(int n, const ct_case* const* cases, const int* n
     }
     ct_batch* b = new (std::nothrow) ct_batch();
     if (!b) return fail(CT_OUT_OF_MEMORY, "host allocation failed");
-    const ct_status s = b->impl.create(n, nullptr, builds.data());
+    const ct_status s = b->impl.create(n, nullptr, builds.data(), prec);
     if (s != CT_OK) {
         delete b;
         return s;
@@ -896,7 +932,7 @@ ct_status ct_batch_set_rhs_transient(ct_batch* b) {
     CT_BATCH_OK(b);
     ct::Batch& B = b->impl;
     for (ct::Batch::Bucket& k : B.bk) {
-        ct::launch_b_fold(B.st, k.vec, B.bi, B.ctl, 0);
+        if (B.dw) ct::launch_b_fold(B.st, k.vec, B.bi, B.ctl, 0);
         ct::launch_b_rhs_transient(B.st, k.vec, B.bi, B.ctl);
     }
     const cudaError_t e = cudaGetLastError();
@@ -994,7 +1030,8 @@ ct_status ct_batch_step_records(ct_batch* b, const double* dt, ct_step_record* o
     CT_BATCH_OK(b);
     if (!dt || !out) return fail(CT_BAD_ARG, "ct_batch_step_records: null");
     ct::Batch& B = b->impl;
-    for (ct::Batch::Bucket& k : B.bk) ct::launch_b_fold(B.st, k.vec, B.bi, B.ctl, 0);
+    if (B.dw)
+        for (ct::Batch::Bucket& k : B.bk) ct::launch_b_fold(B.st, k.vec, B.bi, B.ctl, 0);
     ct::launch_b_step_record(B.st, B.rec_plan, B.bi, B.rec_red, B.rec_mx, B.rec_dev);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess)

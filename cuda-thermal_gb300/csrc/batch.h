@@ -30,7 +30,10 @@ struct Plan {
     const int* inst_count;  // per instance: number of its blocks (0 = not in this stage)
 };
 
-// One instance's fine-level arrays (split layout, double-word outer mode).
+// One instance's fine-level arrays (split layout). The double-word mode
+// (CT_MG_FP32_FLEX_DW) reads r, p, Ap as float pairs and keeps x as an FP64
+// base plus xw; the FP64 mode (CT_MG_FP32_FLEX) reads the same storage as
+// doubles (r64, p64, Ap64) and x is the whole iterate (xw, dgw null).
 struct BInst {
     OpView o;
     const double* P;
@@ -46,6 +49,9 @@ struct BInst {
     float* b0;      // V-cycle input (level 0 b)
     const float* z; // V-cycle result (level 0 x)
     double* xold;   // x at the last set_rhs_transient (step bookkeeping)
+    double* r64;    // r, p, Ap as doubles (the FP64 outer mode)
+    double* p64;
+    double* Ap64;
     unsigned n;     // slots of all planes
 };
 
@@ -75,6 +81,19 @@ void launch_b_update(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, 
 void launch_b_dot(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
                   Cond cond);
 void launch_b_update_p(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl);
+
+// ---- outer PCG in FP64 (CT_MG_FP32_FLEX), one launch for the batch, k_batch64.cu
+// Items: residual and apply, rows of one colour and plane; the others, value
+// pairs.
+void launch_b_residual64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
+                         Cond cond);
+void launch_b_apply64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
+                      Cond cond);
+void launch_b_update64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
+                       Cond cond);
+void launch_b_dot64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
+                    Cond cond);
+void launch_b_update_p64(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl);
 
 // ---- multigrid, one launch per stage and depth for the batch ----------------
 // views / cviews: this depth's and the next coarser depth's LevelView per

@@ -30,107 +30,6 @@ using namespace f64dev;
 
 namespace {
 
-// ---- the operator apply, one warp per row ----------------------------------
-
-// Operands of one cell, loaded before any is used (absent neighbours stay
-// zero and are skipped by the same guards).
-struct Cell64 {
-    double pc, dg, pw, pe, ps, pn, pd, pu;
-    float gw, ge, gs, gn, gd, gu;
-};
-
-__device__ __forceinline__ void load64(const OpView& o, const double* __restrict__ diag,
-                                       const double* __restrict__ v, unsigned k, unsigned t,
-                                       unsigned orow, int i, int e, bool hs, bool hn, bool hd, bool hu,
-                                       Cell64& a) {
-    const Geo& g = o.g;
-    const unsigned hx = (unsigned)g.hx;
-    a.pc = v[k];
-    a.dg = diag[k];
-    a.pw = a.pe = a.ps = a.pn = a.pd = a.pu = 0.0;
-    a.gw = a.ge = a.gs = a.gn = a.gd = a.gu = 0.0f;
-    if (i > 0) {
-        const unsigned w = orow + t - 1u + (unsigned)e;
-        a.pw = v[w];
-        a.gw = o.gE[w];
-    }
-    if (i < g.nx - 1) {
-        a.pe = v[orow + t + (unsigned)e];
-        a.ge = o.gE[k];
-    }
-    if (hs) {
-        const unsigned sl = orow - 2u * hx + t;
-        a.ps = v[sl];
-        a.gs = o.gN[sl];
-    }
-    if (hn) {
-        a.pn = v[orow + 2u * hx + t];
-        a.gn = o.gN[k];
-    }
-    if (hd) {
-        a.pd = v[k - g.plane];
-        a.gd = o.gU[k - g.plane];
-    }
-    if (hu) {
-        a.pu = v[k + g.plane];
-        a.gu = o.gU[k];
-    }
-}
-
-// (A + C/dt) v at the cell: the stored diagonal times v minus the west, east,
-// south, north, down and up terms, in op_apply's order (src/operator3d.h:
-// 100-112), each a DFMA: 7 FP64 instructions.
-__device__ __forceinline__ double compute64(const Cell64& a, bool w, bool e, bool s, bool n, bool d,
-                                            bool u) {
-    double off = 0.0;
-    if (w) off = __fma_rn(widen(a.gw), a.pw, off);
-    if (e) off = __fma_rn(widen(a.ge), a.pe, off);
-    if (s) off = __fma_rn(widen(a.gs), a.ps, off);
-    if (n) off = __fma_rn(widen(a.gn), a.pn, off);
-    if (d) off = __fma_rn(widen(a.gd), a.pd, off);
-    if (u) off = __fma_rn(widen(a.gu), a.pu, off);
-    return __fma_rn(a.dg, a.pc, -off);
-}
-
-// Row R = l * 2 ny + 2 j + colour: the calling warp strides over the row's hx
-// slots, U cells per lane and step (32 slots apart) with every operand of all
-// U loaded first, and hands f(slot, valid, (A + C/dt) v, v) for each slot in
-// order (padding slots: valid = false, zeros).
-template <int U, class F>
-__device__ __forceinline__ void row64(const OpView& o, const double* __restrict__ diag,
-                                      const double* __restrict__ v, unsigned R, int lane, F&& f) {
-    const Geo& g = o.g;
-    const unsigned rows = 2u * (unsigned)g.ny;
-    const unsigned l = R / rows;
-    const unsigned r = R - l * rows;
-    const int j = (int)(r >> 1), c = (int)(r & 1u), e = (j + c) & 1;
-    const unsigned hx = (unsigned)g.hx;
-    const unsigned base = l * g.plane;
-    const unsigned row = base + r * hx;
-    const unsigned orow = base + (unsigned)(2 * j + (c ^ 1)) * hx;  // other colour, same j
-    const bool hs = j > 0, hn = j < g.ny - 1, hd = l > 0, hu = (int)l < g.nz - 1;
-    for (unsigned t0 = (unsigned)lane; t0 < hx; t0 += 32u * U) {
-        Cell64 a[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const unsigned t = t0 + 32u * u;
-            const int i = 2 * (int)t + e;
-            if (t < hx && i < g.nx) load64(o, diag, v, row + t, t, orow, i, e, hs, hn, hd, hu, a[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const unsigned t = t0 + 32u * u;
-            const int i = 2 * (int)t + e;
-            if (t < hx) {
-                if (i < g.nx)
-                    f(row + t, true, compute64(a[u], i > 0, i < g.nx - 1, hs, hn, hd, hu), a[u].pc);
-                else
-                    f(row + t, false, 0.0, 0.0);
-            }
-        }
-    }
-}
-
 constexpr int kRowU = 2;
 
 // Ap = (A + C/dt) p, p.Ap and alpha = rz / p.Ap.

@@ -232,19 +232,6 @@ __host__ __device__ inline size_t small_level_bytes(const Geo& g, size_t elem) {
     const size_t ln = (size_t)g.plane * (size_t)g.nz;
     return 4 * small_round16(ln * 4) + small_round16((size_t)g.plane * 4) + 4 * small_round16(ln * elem);
 }
-// The coarse end of the V-cycle in one launch of one thread-block cluster
-// (k_tail.cu): the restriction from F into tl.L[0], then every phase of the
-// levels tl.L[0 .. n-1] down to the single column and back up, the phases
-// separated by the cluster barrier; level arrays in global memory. Levels of
-// at most kTailColumns columns (nx * ny) go there when the device can place
-// a cluster; tail_cluster_size gives the cluster size (16 or 8 CTAs, 0 when
-// no cluster fits).
-constexpr long kTailColumns = 64L * 64L;
-template <class T>
-int tail_cluster_size(int mz);
-template <class T>
-cudaError_t launch_vtail(cudaStream_t st, int csize, const LevelView<T>& F, const TailLevels<T>& tl, Ctl* ctl,
-                         Cond cond);
 template <class T>
 size_t small_smem_bytes(const TailLevels<T>& tl);
 template <class T>

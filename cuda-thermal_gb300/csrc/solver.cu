@@ -187,33 +187,6 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
             small_k0 = k;
         }
     }
-    {
-        // The coarse end of the V-cycle in one cluster launch: from the first
-        // level of at most kTailColumns columns (CT_TAIL_COLS; 0 turns it
-        // off), when it starts at or above the shared-memory bottom and the
-        // device can place the cluster.
-        long tail_cols = kTailColumns;
-        if (const char* e = std::getenv("CT_TAIL_COLS")) {
-            char* end = nullptr;
-            const long v = std::strtol(e, &end, 10);
-            if (end == e || *end != '\0' || v < 0)
-                return fail(CT_BAD_ARG, "CT_TAIL_COLS=%s is not a column count", e);
-            tail_cols = v;
-        }
-        tail_k0 = 0;
-        if (pc == CT_MULTIGRID && tail_cols > 0) {
-            size_t k1 = 0;
-            for (size_t k = 1; k < lv.size(); ++k)
-                if ((long)lv[k].g.nx * lv[k].g.ny <= tail_cols) {
-                    k1 = k;
-                    break;
-                }
-            if (k1 > 0 && k1 <= small_k0 && lv.size() - k1 <= (size_t)kMaxTail) {
-                tail_cs = mt == MG_F64 ? tail_cluster_size<double>(g0.nz) : tail_cluster_size<float>(g0.nz);
-                if (tail_cs > 0) tail_k0 = k1;
-            }
-        }
-    }
     bytes = ar.used;
     {
         const cudaError_t e = cudaMalloc(&base, bytes);
@@ -395,25 +368,6 @@ void Solver::vcycle(size_t k, Cond cond, bool first_sweep_done) {
     if (!first_sweep_done)
         enq(("mg_sweep0" + lvl).c_str(), b_zero, [&] { sweep<T>(k, L, 0, true, nullptr, cond); });
     enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { sweep<T>(k, L, 1, false, nullptr, cond); });
-    if (tail_k0 > 0 && k + 1 == tail_k0) {
-        // the restriction into level k + 1 and everything below it, one launch
-        TailLevels<T> tl;
-        tl.n = (int)(lv.size() - tail_k0);
-        double b = cells * (2 * t + 16) + cells / 4 * t;
-        for (int q = 0; q < tl.n; ++q) {
-            tl.L[q] = view<T>(tail_k0 + q);
-            const Geo& g = tl.L[q].g;
-            b += (double)g.nx * g.ny * g.nz * (4 * sizeof(T) + 4 + 2 * sizeof(T) + 16);
-        }
-        enq(("mg_tail_l" + std::to_string(k + 1)).c_str(), b, [&] {
-            const cudaError_t e = launch_vtail<T>(cs, tail_cs, L, tl, ctl, cond);
-            if (e != cudaSuccess && launch_error == cudaSuccess) launch_error = e;
-        });
-        enq(("mg_sweep" + lvl).c_str(), b_sweep + cells / 4 * t,
-            [&] { sweep<T>(k, L, 1, false, &C, cond); });
-        enq(("mg_sweep" + lvl).c_str(), b_sweep, [&] { sweep<T>(k, L, 0, false, nullptr, cond); });
-        return;
-    }
     // The coarse level's first sweep rides along with the restriction unless
     // the shared-memory bottom starts there,
     // or the restriction is from the finest level: there it is bandwidth

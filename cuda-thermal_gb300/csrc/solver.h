@@ -82,8 +82,6 @@ class Solver {
     bool use_graphs = true;
     bool have_cond = false;
     size_t small_k0 = 0;   // levels from small_k0 down run in one block from shared memory
-    size_t tail_k0 = 0;    // > 0: levels from tail_k0 down run in one cluster launch (k_tail.cu)
-    int tail_cs = 0;       // its cluster size
     bool fuse_sweep0 = true;  // a level's first (x = 0) sweep rides with the restriction into it
     cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
     ct_setup_times times{};

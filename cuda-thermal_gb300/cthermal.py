@@ -112,6 +112,7 @@ def _signatures():
         "ct_profile_solve": (i, [vp, d, i, C.POINTER(CtStats), C.POINTER(CtKernelTime), i, ip]),
         "ct_true_relres_noalloc": (i, [C.POINTER(CtModel), vp, vp, vp]),
         "ct_batch_create": (i, [i, vp, C.POINTER(vp)]),
+        "ct_batch_create_prec": (i, [i, vp, i, C.POINTER(vp)]),
         "ct_batch_destroy": (i, [vp]),
         "ct_batch_size": (i, [vp, ip]),
         "ct_batch_set_dt": (i, [vp, vp]),
@@ -149,6 +150,7 @@ def _signatures():
         "ct_case_add_block": (i, [vp, i, d, d, d, d, d]),
         "ct_case_add_tsv": (i, [vp, i, d, d, d, d, d]),
         "ct_batch_create_cases": (i, [i, vp, vp, vp, vp, C.POINTER(vp)]),
+        "ct_batch_create_cases_prec": (i, [i, vp, vp, vp, vp, i, C.POINTER(vp)]),
         "ct_case_info": (i, [vp, ip, ip, ip, dp, dp, dp, dp, dp]),
         "ct_case_layer": (i, [vp, i, C.POINTER(CtLayer), C.c_char_p, i]),
         "ct_case_block": (i, [vp, i, ip, dp, dp, C.c_char_p, i]),
@@ -798,18 +800,21 @@ class GpuPcg:
 class GpuBatch:
     """Many independent stacks solved together (ct_batch_*): one launch per
     stage for all instances, per-instance scalars and convergence, one graph
-    per size bucket. Instance i is models[i]."""
+    per size bucket. Instance i is models[i]. precision: Precision.MG_FP32_FLEX
+    (FP64 outer iteration) or MG_FP32_FLEX_DW (double words on the FP32
+    pipes, the default)."""
 
-    def __init__(self, models):
+    def __init__(self, models, precision=None):
         self.models = list(models)
         self._cms = [m.ct_model() for m in self.models]
         arr = (C.POINTER(CtModel) * len(self._cms))(*[C.pointer(c) for c in self._cms])
         h = C.c_void_p()
-        _check(lib().ct_batch_create(len(self._cms), C.cast(arr, C.c_void_p), C.byref(h)))
+        prec = Precision.MG_FP32_FLEX_DW if precision is None else precision
+        _check(lib().ct_batch_create_prec(len(self._cms), C.cast(arr, C.c_void_p), int(prec), C.byref(h)))
         self._h = h
 
     @classmethod
-    def from_specs(cls, specs, nx, ny, with_tsv=True) -> "GpuBatch":
+    def from_specs(cls, specs, nx, ny, with_tsv=True, precision=None) -> "GpuBatch":
         """A batch whose instance i is CaseSpec specs[i] on an nx[i] x ny[i]
         grid, every model built on the device (ct_batch_create_cases)."""
         n = len(specs)
@@ -820,8 +825,9 @@ class GpuBatch:
         try:
             arr = (C.c_void_p * n)(*[hd.h.value for hd in handles])
             h = C.c_void_p()
-            _check(lib().ct_batch_create_cases(n, C.cast(arr, C.c_void_p), _ptr(nxs), _ptr(nys), _ptr(wt),
-                                               C.byref(h)))
+            prec = Precision.MG_FP32_FLEX_DW if precision is None else precision
+            _check(lib().ct_batch_create_cases_prec(n, C.cast(arr, C.c_void_p), _ptr(nxs), _ptr(nys), _ptr(wt),
+                                                    int(prec), C.byref(h)))
         finally:
             for hd in handles:
                 hd.close()

@@ -230,17 +230,23 @@ ct_status ct_true_relres_noalloc(const ct_model* m_dev, const double* T_dev, dou
  * stacks of uneven size (nx, ny, nz per instance), advanced together: every
  * stage of the iteration is one launch for all instances, each instance with
  * its own scalars and convergence test, and the loop of each size bucket is
- * one CUDA graph. Precision is fixed: FP32 V-cycle inside the flexible PCG
- * with FP64 residuals (CT_MG_FP32_FLEX_DW). Instances are numbered 0..n-1 in
- * the order of `models`, which are copied at creation. Per-instance calls
- * mirror the single-solver calls (ct_set_power, ct_get_x, ...). */
+ * one CUDA graph. The V-cycle is FP32 inside the flexible PCG; the outer
+ * iteration is FP64 (CT_MG_FP32_FLEX) or double words on the FP32 pipes with
+ * an FP64 residual replacement (CT_MG_FP32_FLEX_DW). Instances are numbered
+ * 0..n-1 in the order of `models`, which are copied at creation.
+ * Per-instance calls mirror the single-solver calls (ct_set_power, ct_get_x,
+ * ...). ct_batch_create: CT_MG_FP32_FLEX_DW; ct_batch_create_prec: either,
+ * anything else is CT_BAD_ARG. */
 typedef struct ct_batch ct_batch;
 ct_status ct_batch_create(int n, const ct_model* const* models, ct_batch** out);
+ct_status ct_batch_create_prec(int n, const ct_model* const* models, ct_precision prec, ct_batch** out);
 /* The same with every instance's model built on the device from a case on
  * an nx[i] x ny[i] grid (with_tsv may be NULL: all with TSVs), as
  * ct_solver_create_case builds it. */
 ct_status ct_batch_create_cases(int n, const ct_case* const* cases, const int* nx, const int* ny,
                                 const int* with_tsv, ct_batch** out);
+ct_status ct_batch_create_cases_prec(int n, const ct_case* const* cases, const int* nx, const int* ny,
+                                     const int* with_tsv, ct_precision prec, ct_batch** out);
 ct_status ct_batch_destroy(ct_batch* b);
 ct_status ct_batch_size(const ct_batch* b, int* n);
 /* Per-instance time step (dt[i] = 0: steady); NULL: all steady. */

@@ -365,13 +365,12 @@ def test_staged_sweeps_bitwise_single_and_batch(ct, n, prec, tmp_path):
 def test_fused_first_sweep_bitwise(ct, n, prec):
     """Each level's first (x = 0) sweep run inside the restriction into that
     level (the default) gives the separate launches' results bit for bit:
-    steady solve, then two backward-Euler steps (cluster tail off, so every
-    level runs as grid launches)."""
+    steady solve, then two backward-Euler steps."""
     import workloads
     m = workloads.steady_hotspot(n, seed=13)
     out = []
     for flag in ("0", "1"):
-        with env_vars(CT_FUSE_SWEEP0=flag, CT_TAIL_COLS="0"):
+        with env_vars(CT_FUSE_SWEEP0=flag):
             out.append(steady_then_steps(ct, m, prec))
     assert_same_results(out[0], out[1])
 
@@ -383,32 +382,12 @@ def test_shared_memory_bottom_bitwise(ct, n, prec):
     gather every plane's right-hand side with one task per column and plane
     before the recurrences) give the grid-wide launches' results
     (CT_SMALL_BYTES=0: no shared-memory bottom) bit for bit: steady solve,
-    then two backward-Euler steps (cluster tail off in both)."""
+    then two backward-Euler steps."""
     import workloads
     m = workloads.steady_hotspot(n, seed=17)
     out = []
     for flag in ("0", None):
-        with env_vars(CT_SMALL_BYTES=flag, CT_TAIL_COLS="0"):
-            out.append(steady_then_steps(ct, m, prec))
-    assert_same_results(out[0], out[1])
-
-
-@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
-@pytest.mark.parametrize("n,cu_planes", [(203, 4), (130, 4), (96, 4), (96, 16), (72, 34)])
-def test_cluster_tail_bitwise(ct, n, cu_planes, prec):
-    """The coarse end of the V-cycle in one thread-block cluster launch (the
-    default: levels of at most 64 x 64 columns, the restriction into the first
-    of them included) gives the separate launches' results (CT_TAIL_COLS=0)
-    bit for bit: steady solve, then two backward-Euler steps. Sizes put the
-    tail's first level at 51 x 51 (level 2), 33 x 33 (level 2, after a
-    65 x 65 level just over the limit) and 48 x 48 (level 1: the restriction
-    from the fine level); plane counts 10, 22 and 40 (register columns of 12
-    and 32 planes, and the general column path)."""
-    import workloads
-    m = workloads.steady_hotspot(n, seed=19) if cu_planes == 4 else deep_stack(ct, n, cu_planes)
-    out = []
-    for flag in ("0", None):
-        with env_vars(CT_TAIL_COLS=flag):
+        with env_vars(CT_SMALL_BYTES=flag):
             out.append(steady_then_steps(ct, m, prec))
     assert_same_results(out[0], out[1])
 
