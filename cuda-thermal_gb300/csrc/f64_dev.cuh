@@ -65,6 +65,43 @@ __device__ __forceinline__ double from_d<double>(double v) {
     return v;
 }
 
+// Streams the items k = first, first + stride, ... below end, U per step,
+// with the next step's loads issued before the current step's arithmetic (two
+// register sets): the FP64 pipe, at ~1/70 of the FP32 rate, would otherwise
+// hold each warp between its loads, and the memory traffic and the FP64
+// instructions of these kernels would not overlap (measured: the dot took the
+// sum of its DRAM time and its DFMA time, 42 us at 800 x 800 x 10).
+// Single solver (k_fp64.cu) and batch (k_batch64.cu).
+template <int U, class Item, class Load, class Use>
+__device__ __forceinline__ void stream_pipelined(unsigned first, unsigned end, unsigned stride, Load load,
+                                                 Use use) {
+    Item a[U], b[U];
+    bool va[U], vb[U];
+    auto fetch = [&](unsigned k0, Item* it, bool* v) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const unsigned k = k0 + (unsigned)u * stride;
+            v[u] = k < end;
+            if (v[u]) it[u] = load(k);
+        }
+    };
+    unsigned k0 = first;
+    fetch(k0, a, va);
+    while (k0 < end) {
+        const unsigned k1 = k0 + (unsigned)U * stride;
+        fetch(k1, b, vb);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (va[u]) use(k0 + (unsigned)u * stride, a[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            a[u] = b[u];
+            va[u] = vb[u];
+        }
+        k0 = k1;
+    }
+}
+
 // ---- the FP64 operator apply, one warp per row (single solver and batch) ----
 
 // Operands of one cell, loaded before any is used (absent neighbours stay

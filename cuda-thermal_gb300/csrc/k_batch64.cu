@@ -134,19 +134,22 @@ __global__ void __launch_bounds__(NT)
     double2* __restrict__ r2 = reinterpret_cast<double2*>(I.r64);
     float2* __restrict__ b02 = reinterpret_cast<float2*>(I.b0);
     double rr = 0.0, unused = 0.0;
-    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
-        const double2 pv = p2[k], av = a2[k];
-        double2 xv = x2[k], rv = r2[k];
-        xv.x = __fma_rn(alpha, pv.x, xv.x);
-        xv.y = __fma_rn(alpha, pv.y, xv.y);
-        rv.x = __fma_rn(malpha, av.x, rv.x);
-        rv.y = __fma_rn(malpha, av.y, rv.y);
-        x2[k] = xv;
-        r2[k] = rv;
-        b02[k] = make_float2(narrow(rv.x), narrow(rv.y));
-        rr = __fma_rn(rv.x, rv.x, rr);
-        rr = __fma_rn(rv.y, rv.y, rr);
-    }
+    struct Item {
+        double2 p, a, x, r;
+    };
+    stream_pipelined<1, Item>(
+        t.begin + threadIdx.x, t.end, NT, [&](unsigned k) { return Item{p2[k], a2[k], x2[k], r2[k]}; },
+        [&](unsigned k, Item it) {
+            it.x.x = __fma_rn(alpha, it.p.x, it.x.x);
+            it.x.y = __fma_rn(alpha, it.p.y, it.x.y);
+            it.r.x = __fma_rn(malpha, it.a.x, it.r.x);
+            it.r.y = __fma_rn(malpha, it.a.y, it.r.y);
+            x2[k] = it.x;
+            r2[k] = it.r;
+            b02[k] = make_float2(narrow(it.r.x), narrow(it.r.y));
+            rr = __fma_rn(it.r.x, it.r.x, rr);
+            rr = __fma_rn(it.r.y, it.r.y, rr);
+        });
     block_sum2(rr, unused);
     if (publish_inst(rr, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RR, U;
@@ -180,15 +183,19 @@ __global__ void __launch_bounds__(NT)
     const double2* __restrict__ a2 = reinterpret_cast<const double2*>(I.Ap64);
     const float2* __restrict__ z2 = reinterpret_cast<const float2*>(I.z);
     double rz = 0.0, zap = 0.0;
-    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
-        const double2 rv = r2[k], av = a2[k];
-        const float2 zf = z2[k];
-        const double za = widen(zf.x), zb = widen(zf.y);
-        rz = __fma_rn(rv.x, za, rz);
-        rz = __fma_rn(rv.y, zb, rz);
-        zap = __fma_rn(za, av.x, zap);
-        zap = __fma_rn(zb, av.y, zap);
-    }
+    struct Item {
+        double2 r, a;
+        float2 z;
+    };
+    stream_pipelined<2, Item>(
+        t.begin + threadIdx.x, t.end, NT, [&](unsigned k) { return Item{r2[k], a2[k], z2[k]}; },
+        [&](unsigned, const Item& it) {
+            const double za = widen(it.z.x), zb = widen(it.z.y);
+            rz = __fma_rn(it.r.x, za, rz);
+            rz = __fma_rn(it.r.y, zb, rz);
+            zap = __fma_rn(za, it.a.x, zap);
+            zap = __fma_rn(zb, it.a.y, zap);
+        });
     block_sum2(rz, zap);
     if (publish_inst(rz, zap, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RZ, ZAP;
@@ -216,16 +223,22 @@ __global__ void __launch_bounds__(NT)
     const bool first = c->iter == 0;
     const float2* __restrict__ z2 = reinterpret_cast<const float2*>(I.z);
     double2* __restrict__ p2 = reinterpret_cast<double2*>(I.p64);
-    for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
-        const float2 zf = z2[k];
-        const double za = widen(zf.x), zb = widen(zf.y);
-        if (first) {
-            p2[k] = make_double2(za, zb);
-        } else {
-            const double2 pv = p2[k];
-            p2[k] = make_double2(__fma_rn(beta, pv.x, za), __fma_rn(beta, pv.y, zb));
+    if (first) {
+        for (unsigned k = t.begin + threadIdx.x; k < t.end; k += NT) {
+            const float2 zf = z2[k];
+            p2[k] = make_double2(widen(zf.x), widen(zf.y));
         }
+        return;
     }
+    struct Item {
+        double2 p;
+        float2 z;
+    };
+    stream_pipelined<2, Item>(
+        t.begin + threadIdx.x, t.end, NT, [&](unsigned k) { return Item{p2[k], z2[k]}; },
+        [&](unsigned k, const Item& it) {
+            p2[k] = make_double2(__fma_rn(beta, it.p.x, widen(it.z.x)), __fma_rn(beta, it.p.y, widen(it.z.y)));
+        });
 }
 
 }  // namespace

@@ -164,8 +164,12 @@ __device__ __forceinline__ void store_pair(double* b0, unsigned k, double a, dou
 }
 
 // x += alpha p, r -= alpha Ap, b0 = r in the V-cycle precision, ||r||^2 and
-// the convergence test (src/pcg3d_gpu.cu:218-233). Pairs of values (double2).
-constexpr int kUpdU = 2;
+// the convergence test (src/pcg3d_gpu.cu:218-233). Pairs of values (double2),
+// each block a contiguous range.
+constexpr int kUpdU = 1;
+struct UpdItem {
+    double2 p, a, x, r;
+};
 template <class T>
 __global__ void __launch_bounds__(NT)
     k_update64(unsigned n2, const double2* __restrict__ p, const double2* __restrict__ Ap,
@@ -175,32 +179,21 @@ __global__ void __launch_bounds__(NT)
     if (loop_done(ctl, cond)) return;
     const double alpha = ctl->alpha, malpha = -alpha;
     double rr = 0.0, unused = 0.0;
-    const Range br = block_range<kUpdU>(n2);
-    auto one = [&](unsigned k, const double2& pv, const double2& av, double2 xv, double2 rv) {
-        xv.x = __fma_rn(alpha, pv.x, xv.x);
-        xv.y = __fma_rn(alpha, pv.y, xv.y);
-        rv.x = __fma_rn(malpha, av.x, rv.x);
-        rv.y = __fma_rn(malpha, av.y, rv.y);
-        x[k] = xv;
-        r[k] = rv;
-        store_pair(b0, k, rv.x, rv.y);
-        rr = __fma_rn(rv.x, rv.x, rr);
-        rr = __fma_rn(rv.y, rv.y, rr);
-    };
-    unsigned k = br.begin;
-    for (; k + (kUpdU - 1) * NT < br.end; k += kUpdU * NT) {
-        double2 pv[kUpdU], av[kUpdU], xv[kUpdU], rv[kUpdU];
-#pragma unroll
-        for (int u = 0; u < kUpdU; ++u) {
-            pv[u] = p[k + u * NT];
-            av[u] = Ap[k + u * NT];
-            xv[u] = x[k + u * NT];
-            rv[u] = r[k + u * NT];
-        }
-#pragma unroll
-        for (int u = 0; u < kUpdU; ++u) one(k + u * NT, pv[u], av[u], xv[u], rv[u]);
-    }
-    for (; k < br.end; k += NT) one(k, p[k], Ap[k], x[k], r[k]);
+    const Range br = block_range<2>(n2);
+    stream_pipelined<kUpdU, UpdItem>(
+        br.begin, br.end, NT,
+        [&](unsigned k) { return UpdItem{p[k], Ap[k], x[k], r[k]}; },
+        [&](unsigned k, UpdItem it) {
+            it.x.x = __fma_rn(alpha, it.p.x, it.x.x);
+            it.x.y = __fma_rn(alpha, it.p.y, it.x.y);
+            it.r.x = __fma_rn(malpha, it.a.x, it.r.x);
+            it.r.y = __fma_rn(malpha, it.a.y, it.r.y);
+            x[k] = it.x;
+            r[k] = it.r;
+            store_pair(b0, k, it.r.x, it.r.y);
+            rr = __fma_rn(it.r.x, it.r.x, rr);
+            rr = __fma_rn(it.r.y, it.r.y, rr);
+        });
     block_sum2(rr, unused);
     if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
         double RR, U;
@@ -224,37 +217,31 @@ __global__ void __launch_bounds__(NT)
 }
 
 // rz = r.z (and z.Ap for the flexible beta); beta (src/pcg3d_gpu.cu:239-247,
-// 121-126). Pairs strided over the whole grid, kDotU in flight per thread.
-constexpr int kDotU = 4;
+// 121-126). Pairs strided over the whole grid.
+constexpr int kDotU = 2;
+struct DotItem {
+    double2 r, z, a;
+};
 template <class T, bool FLEX>
-__global__ void __launch_bounds__(NT, 4)
+__global__ void __launch_bounds__(NT)
     k_dot64(unsigned n2, const double2* __restrict__ r, const T* __restrict__ z,
             const double2* __restrict__ Ap, Ctl* ctl, double* part, int maxb, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
     double rz = 0.0, zap = 0.0;
-    const unsigned stride = gridDim.x * NT;
-    auto one = [&](const double2& rv, const double2& zv, const double2& av) {
-        rz = __fma_rn(rv.x, zv.x, rz);
-        rz = __fma_rn(rv.y, zv.y, rz);
-        if (FLEX) {
-            zap = __fma_rn(zv.x, av.x, zap);
-            zap = __fma_rn(zv.y, av.y, zap);
-        }
-    };
-    unsigned k = blockIdx.x * NT + threadIdx.x;
-    for (; k + (kDotU - 1) * stride < n2; k += kDotU * stride) {
-        double2 rv[kDotU], zv[kDotU], av[kDotU];
-#pragma unroll
-        for (int u = 0; u < kDotU; ++u) {
-            rv[u] = r[k + u * stride];
-            zv[u] = load_pair(z, k + u * stride);
-            if (FLEX) av[u] = Ap[k + u * stride];
-        }
-#pragma unroll
-        for (int u = 0; u < kDotU; ++u) one(rv[u], zv[u], av[u]);
-    }
-    for (; k < n2; k += stride) one(r[k], load_pair(z, k), FLEX ? Ap[k] : make_double2(0.0, 0.0));
+    stream_pipelined<kDotU, DotItem>(
+        blockIdx.x * NT + threadIdx.x, n2, gridDim.x * NT,
+        [&](unsigned k) {
+            return DotItem{r[k], load_pair(z, k), FLEX ? Ap[k] : make_double2(0.0, 0.0)};
+        },
+        [&](unsigned, const DotItem& it) {
+            rz = __fma_rn(it.r.x, it.z.x, rz);
+            rz = __fma_rn(it.r.y, it.z.y, rz);
+            if (FLEX) {
+                zap = __fma_rn(it.z.x, it.a.x, zap);
+                zap = __fma_rn(it.z.y, it.a.y, zap);
+            }
+        });
     block_sum2(rz, zap);
     if (publish2(rz, zap, part, maxb, &ctl->ticket[SL_DOT])) {
         double RZ, ZAP;
@@ -279,7 +266,10 @@ __global__ void __launch_bounds__(NT, 4)
 }
 
 // p = z + beta p (p = z on the first iteration; src/pcg3d_gpu.cu:249-256).
-constexpr int kPU = 4;
+constexpr int kPU = 2;
+struct PItem {
+    double2 z, p;
+};
 template <class T>
 __global__ void __launch_bounds__(NT)
     k_update_p64(unsigned n2, const T* __restrict__ z, double2* __restrict__ p, const Ctl* ctl,
@@ -287,27 +277,16 @@ __global__ void __launch_bounds__(NT)
     pdl_enter();
     if (loop_done(ctl, cond)) return;
     const double beta = ctl->beta;
-    const Range br = block_range<kPU>(n2);
+    const Range br = block_range<2 * kPU>(n2);
     if (ctl->iter == 0) {
         for (unsigned k = br.begin; k < br.end; k += NT) p[k] = load_pair(z, k);
         return;
     }
-    unsigned k = br.begin;
-    for (; k + (kPU - 1) * NT < br.end; k += kPU * NT) {
-        double2 zv[kPU], pv[kPU];
-#pragma unroll
-        for (int u = 0; u < kPU; ++u) {
-            zv[u] = load_pair(z, k + u * NT);
-            pv[u] = p[k + u * NT];
-        }
-#pragma unroll
-        for (int u = 0; u < kPU; ++u)
-            p[k + u * NT] = make_double2(__fma_rn(beta, pv[u].x, zv[u].x), __fma_rn(beta, pv[u].y, zv[u].y));
-    }
-    for (; k < br.end; k += NT) {
-        const double2 zv = load_pair(z, k), pv = p[k];
-        p[k] = make_double2(__fma_rn(beta, pv.x, zv.x), __fma_rn(beta, pv.y, zv.y));
-    }
+    stream_pipelined<kPU, PItem>(
+        br.begin, br.end, NT, [&](unsigned k) { return PItem{load_pair(z, k), p[k]}; },
+        [&](unsigned k, const PItem& it) {
+            p[k] = make_double2(__fma_rn(beta, it.p.x, it.z.x), __fma_rn(beta, it.p.y, it.z.y));
+        });
 }
 
 // ---- self-test of the integer conversions -----------------------------------
@@ -438,7 +417,7 @@ void launch_update_p64(cudaStream_t st, MgType mt, unsigned n, const void* z, do
                        Cond cond) {
     const unsigned n2 = n / 2;
     auto* p2 = reinterpret_cast<double2*>(p);
-    const unsigned want = std::max(1u, (n2 + NT * kPU - 1) / (NT * kPU));
+    const unsigned want = std::max(1u, (n2 + NT * 2 * kPU - 1) / (NT * 2 * kPU));
     if (mt == MG_F64) {
         static const int wb = wave_blocks(k_update_p64<double>, 1 << 30);
         launch_pdl(k_update_p64<double>, (int)std::min(want, (unsigned)wb), NT, 0, st, n2, (const double*)z, p2,
