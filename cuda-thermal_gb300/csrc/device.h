@@ -18,6 +18,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdint>
 
 namespace ct {
@@ -64,14 +65,18 @@ struct Ctl {
     float2 alpha_w, beta_w;   // alpha, beta as float pairs (double-word mode)
     int iter;                 // completed iterations
     int body;                 // loop bodies entered (bounds the graph loop)
-    int done;                 // stop flag: every kernel of the loop body exits early
+    // done and phase_end sit side by side on an 8-byte boundary: every kernel
+    // of the loop body reads both with one load at entry (loop_done)
+    int done;       // stop flag: every kernel of the loop body exits early
+    int phase_end;  // double-word mode: phase 1 done, residual replacement next
     int converged;
     int breakdown;
     int bb_zero;
-    int phase_end;  // double-word mode: phase 1 done, residual replacement next
     int x_zero;     // set by the host: x = 0 at the start of this solve (r = b)
     unsigned ticket[NSLOT];
 };
+static_assert(offsetof(Ctl, phase_end) == offsetof(Ctl, done) + sizeof(int) && offsetof(Ctl, done) % 8 == 0,
+              "loop_done reads done and phase_end with one 8-byte load");
 
 // Graph while-loop handle: kernels that decide the loop's fate set it.
 struct Cond {

@@ -15,6 +15,8 @@
 // The arithmetic of each line solve, restriction and factorisation follows the
 // reference functions named beside them.
 
+#include <cstdlib>
+
 #include "kernels.h"
 #include "mg_dev.cuh"
 #include "reduce.cuh"
@@ -94,6 +96,70 @@ __global__ void __launch_bounds__(NT)
     sweep_column<T, MZ, ZERO, PRO, false, BF>(L, C, color, q);
 }
 
+// Sweep of a small level (L2-resident, latency-bound) with one thread per
+// column and plane: a block is 32 columns of the active colour x nz planes.
+// Each thread gathers its plane's right-hand side (b plus lat_sum, the same
+// operations as sweep_column) and the column's factors into shared memory;
+// after one block barrier, one thread per column runs sweep_column's
+// recurrence there, and after a second the block writes x plane by plane.
+// Same operations in the same order as k_sweep, so the same bits, but a
+// thread issues one plane's loads instead of nz planes' (k_sweep: 6.5-7.8 us
+// per launch on the 100 x 100 to 25 x 25 levels of an 800 x 800 stack).
+template <class T, int MZ, bool ZERO, bool PRO>
+__global__ void __launch_bounds__(32 * MZ)
+    k_sweep_split(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
+    pdl_enter();
+    const int2 flags = loop_flags(ctl);  // tested after the gathers are issued
+    __shared__ T sv[MZ][32], sfi[MZ][32], sfc[MZ][32];
+    __shared__ float sgu[MZ][32];
+    const Geo& g = L.g;
+    const unsigned tx = threadIdx.x;
+    const int l = (int)threadIdx.y;
+    const unsigned q = blockIdx.x * 32u + tx;
+    const int j = (int)(q / (unsigned)g.hx), t = (int)(q - (unsigned)j * g.hx);
+    const int i = 2 * t + ((j + color) & 1);
+    const bool on = q < (unsigned)g.ny * (unsigned)g.hx && i < g.nx;
+    unsigned s = 0;
+    T rhs = 0, fi = 0, fc = 0;
+    float gu = 0.0f;
+    if (on) {
+        const Nbr n = neighbours<PRO>(g, C.g, i, j, t, color);
+        s = n.s;
+        const unsigned id = (unsigned)l * g.plane + n.s;
+        rhs = L.b[id];
+        if (!ZERO) rhs = rhs + lat_sum<T, PRO, false>(L, C, n, l);
+        fi = L.finv[id];
+        fc = L.fcp[id];
+        gu = L.gU[id];
+    }
+    if (loop_done(flags, cond)) return;  // the same for every thread of the grid
+    if (on) {
+        sv[l][tx] = rhs;
+        sfi[l][tx] = fi;
+        sfc[l][tx] = fc;
+        sgu[l][tx] = gu;
+    }
+    __syncthreads();
+    const int nz = g.nz;
+    if (on && l == 0) {
+        // the recurrence of sweep_column, on shared memory
+        T prev = 0;
+#pragma unroll 4
+        for (int k = 0; k < nz; ++k) {
+            const T lower = k > 0 ? -(T)sgu[k - 1][tx] : T(0);
+            prev = (sv[k][tx] - lower * prev) * sfi[k][tx];
+            sv[k][tx] = prev;
+        }
+#pragma unroll 4
+        for (int k = nz - 2; k >= 0; --k) {
+            prev = sv[k][tx] - sfc[k][tx] * prev;
+            sv[k][tx] = prev;
+        }
+    }
+    __syncthreads();
+    if (on) L.x[(unsigned)l * g.plane + s] = sv[l][tx];
+}
+
 // Restriction F -> C, one thread per coarse cell and plane (blockIdx.y is
 // the plane; k_restrict), or per coarse cell and pair of consecutive planes
 // (k_restrict2: both sums before either store, so the planes' shared
@@ -108,10 +174,15 @@ template <class T>
 __global__ void __launch_bounds__(NT)
     k_restrict(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
     pdl_enter();
-    if (loop_done(ctl, cond)) return;
+    const int2 flags = loop_flags(ctl);  // tested after the sums' loads are issued
     const unsigned q = blockIdx.x * NT + threadIdx.x;
-    if (q >= (unsigned)C.g.nx * (unsigned)C.g.ny) return;
-    restrict_cell<T, false>(F, C, (T)ctl->inv_dt, q, (int)blockIdx.y);
+    const Geo& cg = C.g;
+    const bool on = q < (unsigned)cg.nx * (unsigned)cg.ny;
+    const int J = on ? (int)(q / (unsigned)cg.nx) : 0, I = on ? (int)(q - (unsigned)J * cg.nx) : 0;
+    const int l = (int)blockIdx.y;
+    const T sum = on ? restrict_sum<T, false>(F, (T)ctl->inv_dt, I, J, l) : T(0);
+    if (loop_done(flags, cond) || !on) return;
+    C.b[(unsigned)l * cg.plane + scol(cg, I, J)] = sum;
 }
 
 template <class T>
@@ -135,7 +206,7 @@ template <class T, int MZ>
 __global__ void __launch_bounds__(32 * MZ)
     k_restrict_sweep0(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
     pdl_enter();
-    if (loop_done(ctl, cond)) return;
+    const int2 flags = loop_flags(ctl);  // tested after the sums' loads are issued
     __shared__ T sb[MZ][32], sfi[MZ][32];
     __shared__ float sgu[MZ][32];
     const Geo& cg = C.g;
@@ -145,14 +216,23 @@ __global__ void __launch_bounds__(32 * MZ)
     const int J = on ? (int)(q / (unsigned)cg.nx) : 0, I = on ? (int)(q - (unsigned)J * cg.nx) : 0;
     const bool red = on && ((I + J) & 1) == 0;
     const unsigned cs = scol(cg, I, J);
+    const unsigned id = (unsigned)l * cg.plane + cs;
+    T sum = 0, fi = 0;
+    float gu = 0.0f;
     if (on) {
-        const unsigned id = (unsigned)l * cg.plane + cs;
-        const T sum = restrict_sum<T, false>(F, (T)ctl->inv_dt, I, J, l);
+        sum = restrict_sum<T, false>(F, (T)ctl->inv_dt, I, J, l);
+        if (red) {
+            fi = C.finv[id];
+            gu = C.gU[id];
+        }
+    }
+    if (loop_done(flags, cond)) return;  // the same for every thread of the grid
+    if (on) {
         C.b[id] = sum;
         if (red) {
             sb[l][threadIdx.x] = sum;
-            sfi[l][threadIdx.x] = C.finv[id];
-            sgu[l][threadIdx.x] = C.gU[id];
+            sfi[l][threadIdx.x] = fi;
+            sgu[l][threadIdx.x] = gu;
         }
     }
     __syncthreads();
@@ -216,8 +296,32 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
     const unsigned grid = blocks_for((unsigned)L.g.ny * (unsigned)L.g.hx);
     const LevelView<T> C = coarse ? *coarse : L;
     const int nz = L.g.nz;
-    // small levels (L2-resident, latency-bound): the branch-free gather
+    // small levels (L2-resident, latency-bound): one thread per column and
+    // plane (CT_SWEEP_SPLIT=0: one thread per column, the branch-free gather)
     const bool bf = (unsigned)L.g.nx * (unsigned)L.g.ny <= kSweepBfColumns;
+    const char* split_env = std::getenv("CT_SWEEP_SPLIT");
+    if ((unsigned)L.g.nx * (unsigned)L.g.ny <= kSweepSplitColumns && nz <= 32 &&
+        !(split_env && split_env[0] == '0')) {
+        const unsigned sgrid = ((unsigned)L.g.ny * (unsigned)L.g.hx + 31u) / 32u;
+        const dim3 block(32, (unsigned)nz);
+#define CT_SPLIT(MZ)                                                                                 \
+    do {                                                                                             \
+        if (zero_x)                                                                                  \
+            launch_pdl(k_sweep_split<T, MZ, true, false>, sgrid, block, 0, st, L, color, C, ctl, cond);  \
+        else if (coarse)                                                                             \
+            launch_pdl(k_sweep_split<T, MZ, false, true>, sgrid, block, 0, st, L, color, C, ctl, cond);  \
+        else                                                                                         \
+            launch_pdl(k_sweep_split<T, MZ, false, false>, sgrid, block, 0, st, L, color, C, ctl, cond); \
+    } while (0)
+        if (nz <= 8)
+            CT_SPLIT(8);
+        else if (nz <= 16)
+            CT_SPLIT(16);
+        else
+            CT_SPLIT(32);
+#undef CT_SPLIT
+        return;
+    }
 #define CT_SWEEP2(MZ, BF)                                                                          \
     do {                                                                                           \
         if (zero_x)                                                                                \

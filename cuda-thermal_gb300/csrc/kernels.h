@@ -176,6 +176,11 @@ void launch_factor(cudaStream_t st, const LevelView<T>& L, T inv_dt);
 // Levels of at most this many columns use the branch-free gather
 // (mgdev::sweep_column, BF).
 constexpr unsigned kSweepBfColumns = 128u * 128u;
+// Levels of at most this many columns sweep with one thread per column and
+// plane (k_sweep_split); larger FP32 levels are staged by bulk tensor copies
+// (at 800 x 800: the 200 x 200 level split 6.96 ms per solve against 7.07 ms
+// staged, the 400 x 400 level split 7.11 ms).
+constexpr unsigned kSweepSplitColumns = 256u * 256u;
 template <class T>
 void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x,
                   const LevelView<T>* coarse_for_prolong, const Ctl* ctl, Cond cond);

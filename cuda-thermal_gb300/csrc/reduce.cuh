@@ -86,12 +86,21 @@ __device__ __forceinline__ void stop_loop(Ctl* c, const Cond& cond) {
 // Entry test of every loop-body kernel: once the solve is done (or, in the
 // double-word mode, once its first phase is), the rest of the body is a
 // no-op, and (inside a graph loop) the loop is told to end.
-__device__ __forceinline__ bool loop_done(const Ctl* c, const Cond& cond) {
-    if (*(volatile const int*)&c->done || *(volatile const int*)&c->phase_end) {
+// loop_flags loads the two flags it tests (done, phase_end) on their own,
+// so that a short kernel can issue its first loads before it waits for them
+// and test them before its first store.
+__device__ __forceinline__ int2 loop_flags(const Ctl* c) {
+    return __ldcv(reinterpret_cast<const int2*>(&c->done));
+}
+__device__ __forceinline__ bool loop_done(int2 f, const Cond& cond) {
+    if (f.x | f.y) {
         if (cond.use && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond.h, 0u);
         return true;
     }
     return false;
+}
+__device__ __forceinline__ bool loop_done(const Ctl* c, const Cond& cond) {
+    return loop_done(loop_flags(c), cond);
 }
 
 }  // namespace ct

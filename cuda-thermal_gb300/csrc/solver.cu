@@ -226,14 +226,15 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     if (const char* e = std::getenv("CT_FUSE_SWEEP0")) fuse_sweep0 = e[0] != '0';
     // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
     // (FP32 levels with at least one full tile row, above the shared-memory
-    // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernel. Levels of
-    // at most kSweepBfColumns columns stay on the grid kernel too: they sit in
-    // L2, and a tile pipeline of a few tiles per block costs more latency than
-    // it hides (CT_SWEEP_TMA_COLS sets the smallest staged level instead).
+    // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernels. Levels of
+    // at most kSweepSplitColumns columns stay on the grid kernel too: they sit
+    // in L2, and a tile pipeline of a few tiles per block costs more latency
+    // than one thread per column and plane (CT_SWEEP_TMA_COLS sets the
+    // smallest staged level instead).
     {
         const char* e = std::getenv("CT_SWEEP_TMA");
         const bool want = mt == MG_F32 && !(e && e[0] == '0');
-        long min_cols = (long)kSweepBfColumns + 1;
+        long min_cols = (long)kSweepSplitColumns + 1;
         if (const char* c = std::getenv("CT_SWEEP_TMA_COLS")) min_cols = std::atol(c);
         for (size_t k = 0; want && k < lv.size() && k < small_k0; ++k) {
             Level& L = lv[k];

@@ -375,6 +375,33 @@ def test_fused_first_sweep_bitwise(ct, n, prec):
     assert_same_results(out[0], out[1])
 
 
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
+@pytest.mark.parametrize("n", [203, 130, 37])
+def test_small_level_split_sweeps_bitwise(ct, n, prec):
+    """Sweeps of the small grid levels with one thread per column and plane
+    (the default) give the one-thread-per-column sweeps' results
+    (CT_SWEEP_SPLIT=0) bit for bit: steady solve, then two backward-Euler
+    steps."""
+    import workloads
+    m = workloads.steady_hotspot(n, seed=19)
+    out = []
+    for flag in ("0", None):
+        with env_vars(CT_SWEEP_SPLIT=flag):
+            out.append(steady_then_steps(ct, m, prec))
+    assert_same_results(out[0], out[1])
+
+
+@pytest.mark.parametrize("cu_planes", [2, 16])
+def test_small_level_split_sweeps_bitwise_deep(ct, cu_planes):
+    """The same on 8- and 22-plane stacks (the 8- and 32-plane forms)."""
+    m = deep_stack(ct, 90, cu_planes, ny=70)
+    out = []
+    for flag in ("0", None):
+        with env_vars(CT_SWEEP_SPLIT=flag):
+            out.append(steady_then_steps(ct, m, "MG_FP32_FLEX"))
+    assert_same_results(out[0], out[1])
+
+
 @pytest.mark.parametrize("prec", ["MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
 @pytest.mark.parametrize("n", [203, 64, 9])
 def test_shared_memory_bottom_bitwise(ct, n, prec):
