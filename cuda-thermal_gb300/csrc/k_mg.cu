@@ -86,14 +86,14 @@ __global__ void k_coarsen(Geo fg, const float* __restrict__ fgE, const float* __
     }
 }
 
-template <class T, int MZ, bool ZERO, bool PRO, bool BF>
+template <class T, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(NT)
     k_sweep(LevelView<T> L, int color, LevelView<T> C, const Ctl* ctl, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
     const unsigned q = blockIdx.x * NT + threadIdx.x;
     if (q >= (unsigned)L.g.ny * (unsigned)L.g.hx) return;
-    sweep_column<T, MZ, ZERO, PRO, false, BF>(L, C, color, q);
+    sweep_column<T, MZ, ZERO, PRO, false>(L, C, color, q);
 }
 
 // Sweep of a small level (L2-resident, latency-bound) with one thread per
@@ -129,8 +129,10 @@ __global__ void __launch_bounds__(32 * MZ)
         rhs = L.b[id];
         if (!ZERO) rhs = rhs + lat_sum<T, PRO, false>(L, C, n, l);
         fi = L.finv[id];
-        fc = L.fcp[id];
         gu = L.gU[id];
+        // the x = 0 sweep recomputes fcp as factor_column rounded it (one
+        // operand stream less); the others load it
+        fc = ZERO ? RN<T>::mul(-(T)gu, fi) : L.fcp[id];
     }
     if (loop_done(flags, cond)) return;  // the same for every thread of the grid
     if (on) {
@@ -296,21 +298,23 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
     const unsigned grid = blocks_for((unsigned)L.g.ny * (unsigned)L.g.hx);
     const LevelView<T> C = coarse ? *coarse : L;
     const int nz = L.g.nz;
-    // small levels (L2-resident, latency-bound): one thread per column and
-    // plane (CT_SWEEP_SPLIT=0: one thread per column, the branch-free gather)
-    const bool bf = (unsigned)L.g.nx * (unsigned)L.g.ny <= kSweepBfColumns;
+    // One thread per column and plane on levels of at most split_cols columns
+    // (FP64 levels: all) with at most 32 planes; otherwise one thread per
+    // column (CT_SWEEP_SPLIT=0 forces it; CT_SWEEP_SPLIT_COLS moves the
+    // threshold). Both give the same bits.
     const char* split_env = std::getenv("CT_SWEEP_SPLIT");
-    if ((unsigned)L.g.nx * (unsigned)L.g.ny <= kSweepSplitColumns && nz <= 32 &&
-        !(split_env && split_env[0] == '0')) {
+    long long split_cols = sizeof(T) == 8 ? kSweepSplitColumns64 : kSweepSplitColumns;
+    if (const char* c = std::getenv("CT_SWEEP_SPLIT_COLS")) split_cols = std::atoll(c);
+    if ((long long)L.g.nx * L.g.ny <= split_cols && nz <= 32 && !(split_env && split_env[0] == '0')) {
         const unsigned sgrid = ((unsigned)L.g.ny * (unsigned)L.g.hx + 31u) / 32u;
         const dim3 block(32, (unsigned)nz);
-#define CT_SPLIT(MZ)                                                                                 \
-    do {                                                                                             \
-        if (zero_x)                                                                                  \
+#define CT_SPLIT(MZ)                                                                                     \
+    do {                                                                                                 \
+        if (zero_x)                                                                                      \
             launch_pdl(k_sweep_split<T, MZ, true, false>, sgrid, block, 0, st, L, color, C, ctl, cond);  \
-        else if (coarse)                                                                             \
+        else if (coarse)                                                                                 \
             launch_pdl(k_sweep_split<T, MZ, false, true>, sgrid, block, 0, st, L, color, C, ctl, cond);  \
-        else                                                                                         \
+        else                                                                                             \
             launch_pdl(k_sweep_split<T, MZ, false, false>, sgrid, block, 0, st, L, color, C, ctl, cond); \
     } while (0)
         if (nz <= 8)
@@ -322,21 +326,14 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
 #undef CT_SPLIT
         return;
     }
-#define CT_SWEEP2(MZ, BF)                                                                          \
+#define CT_SWEEP(MZ)                                                                               \
     do {                                                                                           \
         if (zero_x)                                                                                \
-            launch_pdl(k_sweep<T, MZ, true, false, BF>, grid, NT, 0, st, L, color, C, ctl, cond);  \
+            launch_pdl(k_sweep<T, MZ, true, false>, grid, NT, 0, st, L, color, C, ctl, cond);      \
         else if (coarse)                                                                           \
-            launch_pdl(k_sweep<T, MZ, false, true, BF>, grid, NT, 0, st, L, color, C, ctl, cond);  \
+            launch_pdl(k_sweep<T, MZ, false, true>, grid, NT, 0, st, L, color, C, ctl, cond);      \
         else                                                                                       \
-            launch_pdl(k_sweep<T, MZ, false, false, BF>, grid, NT, 0, st, L, color, C, ctl, cond); \
-    } while (0)
-#define CT_SWEEP(MZ)              \
-    do {                          \
-        if (bf)                   \
-            CT_SWEEP2(MZ, true);  \
-        else                      \
-            CT_SWEEP2(MZ, false); \
+            launch_pdl(k_sweep<T, MZ, false, false>, grid, NT, 0, st, L, color, C, ctl, cond);     \
     } while (0)
     if (nz <= 8)
         CT_SWEEP(8);
@@ -349,7 +346,6 @@ void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x
     else
         CT_SWEEP(0);
 #undef CT_SWEEP
-#undef CT_SWEEP2
 }
 
 template <class T>

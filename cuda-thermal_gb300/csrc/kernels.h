@@ -173,14 +173,18 @@ void launch_factor(cudaStream_t st, const LevelView<T>& L, T inv_dt);
 // V-cycle), so lateral neighbours are not read. xc: when not null, the
 // coarser level's x is added to every neighbour value read (prolongation
 // fused into the sweep).
-// Levels of at most this many columns use the branch-free gather
-// (mgdev::sweep_column, BF).
+// Fine levels of more than this many columns restrict by pairs of planes
+// (k_restrict2), smaller ones by single planes (k_restrict).
 constexpr unsigned kSweepBfColumns = 128u * 128u;
 // Levels of at most this many columns sweep with one thread per column and
 // plane (k_sweep_split); larger FP32 levels are staged by bulk tensor copies
 // (at 800 x 800: the 200 x 200 level split 6.96 ms per solve against 7.07 ms
 // staged, the 400 x 400 level split 7.11 ms).
 constexpr unsigned kSweepSplitColumns = 256u * 256u;
+// FP64 levels (the plain FP64 MG-PCG) are never staged and sweep this way at
+// every size (800 x 800: 56.6 solves/s, against 52.4 with the one-thread-per-
+// column sweep above 512 x 512 columns and 50.7 above 256 x 256).
+constexpr unsigned kSweepSplitColumns64 = 0xffffffffu;
 template <class T>
 void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x,
                   const LevelView<T>* coarse_for_prolong, const Ctl* ctl, Cond cond);
