@@ -820,6 +820,12 @@ def main():
     batched = None
     if not args.no_batch:
         batched = bench_batched(ct, np, torch, args, hbm_peak, peak_kind, rank, world)
+        # what separates the batched iteration's stages: a grid-wide barrier in
+        # one persistent kernel against a dependent launch in a graph
+        batched["stage_separation_probe"] = {
+            "per_phase_us": [ct.probe_sync_costs(2000, bps) for bps in (1, 4, 8)],
+            "note": "dependent phases over SMs x blocks/SM blocks of 256 threads: grid barrier in one "
+                    "cooperative kernel vs one PDL launch per phase in a CUDA graph"}
     four = None
     if not args.no_four_tier:
         four = bench_four_tier(ct, np, torch, args)

@@ -30,7 +30,7 @@ CU_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
             "-Xcompiler", "-fPIC,-ffp-contract=off"]
 
 CPP_SOURCES = ["status.cpp", "model.cpp", "case.cpp"]
-CU_SOURCES = ["k_outer.cu", "k_fp64.cu", "k_batch64.cu", "k_mg.cu", "k_dw.cu", "k_batch.cu", "k_sweep_tma.cu", "k_fields.cu", "k_build.cu", "solver.cu", "batch.cu", "noalloc.cu"]
+CU_SOURCES = ["k_outer.cu", "k_fp64.cu", "k_batch64.cu", "k_mg.cu", "k_dw.cu", "k_batch.cu", "k_sweep_tma.cu", "k_fields.cu", "k_build.cu", "solver.cu", "batch.cu", "noalloc.cu", "k_probe.cu"]
 
 
 def nvcc() -> str:

@@ -110,6 +110,12 @@ void launch_update_p64(cudaStream_t st, MgType mt, unsigned n, const void* z, do
 // The GPU's DFMA issue rate (instructions per second, independent chains on
 // every SM; synchronises the device): the FP64-pipe roofline's denominator.
 cudaError_t measure_dfma_rate(double* per_s);
+// k_probe.cu: microseconds per phase of `phases` dependent phases on
+// SMs x blocks_per_sm blocks (capped at the resident limit), separated by a
+// grid barrier inside one cooperative kernel and by dependent launches in a
+// graph; gave_up: a barrier wait ran out of polls.
+cudaError_t measure_sync_costs(int phases, int blocks_per_sm, double* us_barrier, double* us_launch,
+                               int* blocks, int* gave_up);
 // Integer conversions against the hardware on n bit patterns (adds the
 // mismatch count to *mismatches).
 cudaError_t launch_conv_selftest(cudaStream_t st, unsigned long long n, unsigned long long seed,

@@ -699,6 +699,23 @@ ct_status ct_probe_fp64_rate(double* dfma_per_s) {
     return CT_OK;
 }
 
+ct_status ct_probe_sync_costs(int phases, int blocks_per_sm, double* us_grid_barrier,
+                              double* us_dependent_launch, int* blocks) {
+    if (!us_grid_barrier || !us_dependent_launch || !blocks) return fail(CT_BAD_ARG, "ct_probe_sync_costs: null");
+    if (phases < 1 || phases > 100000) return fail(CT_BAD_ARG, "ct_probe_sync_costs: phases in 1..100000");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CT_NO_DEVICE, "no CUDA device");
+    }
+    int gave_up = 0;
+    const cudaError_t e =
+        ct::measure_sync_costs(phases, blocks_per_sm, us_grid_barrier, us_dependent_launch, blocks, &gave_up);
+    if (e != cudaSuccess) return fail(CT_CUDA_ERROR, "ct_probe_sync_costs: %s", cudaGetErrorString(e));
+    if (gave_up) return fail(CT_TIMEOUT, "ct_probe_sync_costs: a grid barrier wait ran out");
+    return CT_OK;
+}
+
 ct_status ct_last_setup(ct_setup_times* out) {
     if (!out) return fail(CT_BAD_ARG, "ct_last_setup: null");
     std::lock_guard<std::mutex> lk(ct::g_setup_mu);

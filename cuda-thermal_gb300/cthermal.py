@@ -161,6 +161,7 @@ def _signatures():
         "ct_selftest_bounded_wait": (i, [C.c_uint, ip]),
         "ct_selftest_conversions": (i, [C.c_ulonglong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]),
         "ct_probe_fp64_rate": (i, [C.POINTER(C.c_double)]),
+        "ct_probe_sync_costs": (i, [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), ip]),
         "ct_eff_kz": (d, [d, d, d]),
         "ct_eff_kxy": (d, [d, d, d]),
     }
@@ -478,6 +479,16 @@ def probe_fp64_rate() -> float:
     r = C.c_double(0.0)
     _check(lib().ct_probe_fp64_rate(C.byref(r)))
     return float(r.value)
+
+
+def probe_sync_costs(phases: int = 2000, blocks_per_sm: int = 1) -> dict:
+    """Microseconds per dependent phase over SMs x blocks_per_sm blocks: a
+    grid-wide barrier inside one persistent cooperative kernel against one
+    dependently launched kernel per phase in a CUDA graph."""
+    bar, lau, nb = C.c_double(0.0), C.c_double(0.0), C.c_int(0)
+    _check(lib().ct_probe_sync_costs(int(phases), int(blocks_per_sm), C.byref(bar), C.byref(lau), C.byref(nb)))
+    return {"grid_barrier_us": float(bar.value), "dependent_launch_us": float(lau.value), "blocks": int(nb.value),
+            "phases": int(phases)}
 
 
 def export_3dice(case, cell_um: float, outdir: str) -> None:

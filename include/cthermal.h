@@ -133,6 +133,15 @@ ct_status ct_selftest_conversions(unsigned long long n, unsigned long long seed,
  * 0.53e12 on GB300): the denominator of the FP64-pipe roofline reported for
  * the FP64 outer kernels. Synchronises the device. */
 ct_status ct_probe_fp64_rate(double* dfma_per_s);
+/* No counterpart in the reference. Microseconds per phase of `phases`
+ * dependent phases run over SMs x blocks_per_sm blocks of 256 threads (capped
+ * at what can be resident; *blocks returns the count), separated (a) by a
+ * grid-wide barrier inside one persistent cooperative kernel and (b) by one
+ * dependently launched kernel per phase in a CUDA graph, the way the solver's
+ * graphs separate stages. CT_TIMEOUT if a barrier wait gave up (bounded).
+ * Synchronises the device. */
+ct_status ct_probe_sync_costs(int phases, int blocks_per_sm, double* us_grid_barrier,
+                              double* us_dependent_launch, int* blocks);
 /* gpu_last_setup (src/pcg3d_gpu.cu:87-88): setup times of the last solver
  * created on any thread. */
 ct_status ct_last_setup(ct_setup_times* out);

@@ -457,6 +457,15 @@ def test_integer_conversions_equal_hardware(ct):
     assert ct.selftest_conversions(1 << 24, seed=7) == 0
 
 
+@pytest.mark.parametrize("blocks_per_sm", [1, 8])
+def test_sync_cost_probe(ct, blocks_per_sm):
+    """The stage-separation probe runs to completion on a full grid: both
+    costs are positive and below a millisecond per phase."""
+    r = ct.probe_sync_costs(500, blocks_per_sm)
+    assert r["blocks"] >= 1
+    assert 0 < r["grid_barrier_us"] < 1e3 and 0 < r["dependent_launch_us"] < 1e3
+
+
 def test_fp64_rate_probe(ct):
     """The FP64-pipe roofline's denominator: a DFMA rate between 0.1e12 and
     1e14 per second (GB300: about 0.53e12)."""
