@@ -330,51 +330,6 @@ __device__ __forceinline__ float2 apply_compute(const ApplyCell& a, bool w, bool
     return av;
 }
 
-// The same row with each neighbour term loaded and accumulated in turn: fewer
-// registers (more resident warps), one load latency per term.
-__device__ __forceinline__ void apply_row_seq(const OpView& o, const float2* __restrict__ dgw,
-                                              const float2* __restrict__ p, float2* __restrict__ Ap,
-                                              unsigned R, int lane, DwAcc& pap) {
-    const Geo& g = o.g;
-    const unsigned rows = 2u * (unsigned)g.ny;
-    const unsigned l = R / rows;
-    const unsigned r = R - l * rows;
-    const int j = (int)(r >> 1), c = (int)(r & 1u), e = (j + c) & 1;
-    const unsigned hx = (unsigned)g.hx;
-    const unsigned base = l * g.plane;
-    const unsigned row = base + r * hx;
-    const unsigned orow = base + (unsigned)(2 * j + (c ^ 1)) * hx;
-    const bool hs = j > 0, hn = j < g.ny - 1, hd = l > 0, hu = (int)l < g.nz - 1;
-    for (unsigned t = (unsigned)lane; t < hx; t += 32u) {
-        const unsigned k = row + t;
-        const int i = 2 * (int)t + e;
-        if (i >= g.nx) {
-            Ap[k] = make_float2(0.0f, 0.0f);
-            continue;
-        }
-        DwAcc off = {0.0f, 0.0f};
-        if (i > 0) {
-            const unsigned w = orow + t - 1u + (unsigned)e;
-            acc_mul_f(off, p[w], o.gE[w]);
-        }
-        if (i < g.nx - 1) acc_mul_f(off, p[orow + t + (unsigned)e], o.gE[k]);
-        if (hs) {
-            const unsigned sl = orow - 2u * hx + t;
-            acc_mul_f(off, p[sl], o.gN[sl]);
-        }
-        if (hn) acc_mul_f(off, p[orow + 2u * hx + t], o.gN[k]);
-        if (hd) acc_mul_f(off, p[k - g.plane], o.gU[k - g.plane]);
-        if (hu) acc_mul_f(off, p[k + g.plane], o.gU[k]);
-        const float2 pc = p[k], dg = dgw[k];
-        const float h = dg.x * pc.x;
-        DwAcc a = {h, fmaf(dg.x, pc.y, fmaf(dg.y, pc.x, fmaf(dg.x, pc.x, -h)))};
-        acc_add(a, -off.s, -off.c);
-        const float2 av = fast_two_sum(a.s, a.c);
-        Ap[k] = av;
-        acc_mul(pap, pc, av);
-    }
-}
-
 // Ap = (A + C/dt) p on one row of one plane (hx slots of one colour of row j).
 // The calling warp strides over the row, U cells per lane and step (32 slots
 // apart) with every operand of all U loaded first; p.Ap of its cells is added

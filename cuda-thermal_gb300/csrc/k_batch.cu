@@ -157,9 +157,12 @@ __global__ void __launch_bounds__(NT)
 }
 
 // Ap = d p - sum G p_nbr over rows [begin, end) of the instance (one warp
-// per row of one colour of one plane, apply_row), p.Ap, alpha.
-template <int U, int MINB = 0>
-__global__ void __launch_bounds__(NT, MINB)
+// per row of one colour of one plane, apply_row with one cell per lane, every
+// operand of it gathered at once), p.Ap, alpha. Measured on the 256-instance
+// floorplan batch: 40.7 ms per solve against 50.0 ms with the operands loaded
+// term by term and 59.0 ms with two cells per lane; compiled for 4 blocks per
+// SM (64 registers: 600 us per launch against 722 us with the compiler's 78).
+__global__ void __launch_bounds__(NT, 4)
     kb_apply(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
@@ -170,12 +173,8 @@ __global__ void __launch_bounds__(NT, MINB)
     float2* __restrict__ Ap = bi[t.inst].Ap;
     const int lane = (int)(threadIdx.x & 31u);
     DwAcc pacc = {0.0f, 0.0f};
-    for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32) {
-        if constexpr (U == 0)
-            apply_row_seq(o, dgw, pv, Ap, R, lane, pacc);
-        else
-            apply_row<U>(o, dgw, pv, Ap, R, lane, pacc);
-    }
+    for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32)
+        apply_row<1>(o, dgw, pv, Ap, R, lane, pacc);
     DwAcc unused = {0.0f, 0.0f};
     block_sum_acc2(pacc, unused);
     if (publish_inst_acc(pacc, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
@@ -430,21 +429,7 @@ void launch_b_residual(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl
 
 void launch_b_apply(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
                     BCtl* bc, Cond cond) {
-    // one cell per lane, every operand of it gathered at once (measured on the
-    // 256-instance floorplan batch: 40.7 ms per solve against 50.0 ms with the
-    // operands loaded term by term, CT_BATCH_APPLY=0, and 59.0 ms with two
-    // cells per lane, CT_BATCH_APPLY=2), compiled for 4 blocks per SM (64
-    // registers: 600 us per launch against 722 us with the compiler's 78)
-    static const int form = [] {
-        const char* e = std::getenv("CT_BATCH_APPLY");
-        return e ? std::atoi(e) : 1;
-    }();
-    if (form == 1)
-        kb_apply<1, 4><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
-    else if (form == 2)
-        kb_apply<2><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
-    else
-        kb_apply<0><<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    kb_apply<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_update(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
