@@ -38,6 +38,27 @@ __global__ void k_factor(LevelView<T> L, T inv_dt) {
         factor_column<T>(L, inv_dt, q);
 }
 
+// set_dt in one launch: the Thomas factors of every column of every level
+// (factor_column, mg_factor_column's arithmetic) and, on the finest level's
+// columns, the FP64 diagonal (diag_column: d, 1/d for Jacobi, the
+// double-word copy). One thread per column of the levels' columns laid end
+// to end; each column's operations are those of k_factor and k_diag, so the
+// same bits, without a launch per level (ten of the eleven levels of an
+// 800 x 800 stack are a few blocks of latency each).
+template <class T>
+__global__ void __launch_bounds__(NT)
+    k_factor_levels(FactorLevels<T> fl, T inv_dt, OpView o, const double* __restrict__ dface, double inv_dt64,
+                    double* __restrict__ diag, double* __restrict__ invd, float2* __restrict__ dgw) {
+    const unsigned total = fl.first[fl.n];
+    for (unsigned q = blockIdx.x * NT + threadIdx.x; q < total; q += gridDim.x * NT) {
+        int k = 0;
+        while (k + 1 < fl.n && q >= fl.first[k + 1]) ++k;
+        const unsigned c = q - fl.first[k];
+        factor_column<T>(fl.L[k], inv_dt, c);
+        if (k == 0 && diag) diag_column(o, dface, inv_dt64, c, diag, invd, dgw);
+    }
+}
+
 // mg_coarse_cell (src/mg3d.h:100-136) on split layouts: one thread per coarse
 // cell, sums in double in the reference's child order, one cast to float.
 __global__ void k_coarsen(Geo fg, const float* __restrict__ fgE, const float* __restrict__ fgN,
@@ -293,6 +314,13 @@ void launch_factor(cudaStream_t st, const LevelView<T>& L, T inv_dt) {
 }
 
 template <class T>
+void launch_factor_levels(cudaStream_t st, const FactorLevels<T>& fl, T inv_dt, const OpView& o,
+                          const double* dface, double inv_dt64, double* diag, double* invd, float2* dgw) {
+    const unsigned total = fl.first[fl.n];
+    k_factor_levels<T><<<blocks_for(total), NT, 0, st>>>(fl, inv_dt, o, dface, inv_dt64, diag, invd, dgw);
+}
+
+template <class T>
 void launch_sweep(cudaStream_t st, const LevelView<T>& L, int color, bool zero_x,
                   const LevelView<T>* coarse, const Ctl* ctl, Cond cond) {
     const unsigned grid = blocks_for((unsigned)L.g.ny * (unsigned)L.g.hx);
@@ -377,6 +405,10 @@ bool launch_restrict_sweep0(cudaStream_t st, const LevelView<T>& F, const LevelV
     return true;
 }
 
+template void launch_factor_levels<float>(cudaStream_t, const FactorLevels<float>&, float, const OpView&,
+                                          const double*, double, double*, double*, float2*);
+template void launch_factor_levels<double>(cudaStream_t, const FactorLevels<double>&, double, const OpView&,
+                                           const double*, double, double*, double*, float2*);
 template void launch_factor<float>(cudaStream_t, const LevelView<float>&, float);
 template void launch_factor<double>(cudaStream_t, const LevelView<double>&, double);
 template void launch_sweep<float>(cudaStream_t, const LevelView<float>&, int, bool,

@@ -229,6 +229,21 @@ bool launch_restrict_sweep0(cudaStream_t st, const LevelView<T>& F, const LevelV
 
 // The levels from some level down to the single column, finest first.
 constexpr int kMaxTail = 24;
+// Every level of a hierarchy (at most kMaxTail) with the first index of each
+// level's columns when they are laid end to end (first[n] = all columns).
+template <class T>
+struct FactorLevels {
+    int n;
+    unsigned first[kMaxTail + 1];
+    LevelView<T> L[kMaxTail];
+};
+// set_dt in one launch: every level's column factors for 1/dt and, when diag
+// is not null, the fine operator's FP64 diagonal (and 1/d, the double-word
+// copy where invd, dgw are not null); the same bits as launch_factor per
+// level and launch_diag (+ the double-word copy).
+template <class T>
+void launch_factor_levels(cudaStream_t st, const FactorLevels<T>& fl, T inv_dt, const OpView& o,
+                          const double* dface, double inv_dt64, double* diag, double* invd, float2* dgw);
 template <class T>
 struct TailLevels {
     int n;  // levels in L, the finest of them first, the single column last

@@ -312,12 +312,25 @@ ct_status Solver::set_dt(double dt) {
     const TraceRange trace("ct_set_dt");
     if (!(dt >= 0) || !std::isfinite(dt)) return fail(CT_BAD_ARG, "ct_set_dt: dt must be >= 0");
     inv_dt = dt > 0 ? 1.0 / dt : 0.0;
-    launch_diag(st, op(), dface, inv_dt, diag, invd);
-    if (dw) launch_to_dw(st, n, diag, dgw);
-    if (mt == MG_F32)
-        for (size_t k = 0; k < lv.size(); ++k) launch_factor<float>(st, view<float>(k), (float)inv_dt);
-    else if (mt == MG_F64)
-        for (size_t k = 0; k < lv.size(); ++k) launch_factor<double>(st, view<double>(k), inv_dt);
+    // one launch for the diagonal and every level's factors (CT_FACTOR_LEVELS=0:
+    // a launch for the diagonal and one per level)
+    const char* fl_env = std::getenv("CT_FACTOR_LEVELS");
+    const bool one_launch = !(fl_env && fl_env[0] == '0');
+    if (one_launch && mt != MG_NONE && lv.size() <= (size_t)kMaxTail) {
+        if (mt == MG_F32)
+            launch_factor_levels<float>(st, factor_levels<float>(), (float)inv_dt, op(), dface, inv_dt, diag, invd,
+                                        dw ? dgw : nullptr);
+        else
+            launch_factor_levels<double>(st, factor_levels<double>(), inv_dt, op(), dface, inv_dt, diag, invd,
+                                         nullptr);
+    } else {
+        launch_diag(st, op(), dface, inv_dt, diag, invd);
+        if (dw) launch_to_dw(st, n, diag, dgw);
+        if (mt == MG_F32)
+            for (size_t k = 0; k < lv.size(); ++k) launch_factor<float>(st, view<float>(k), (float)inv_dt);
+        else if (mt == MG_F64)
+            for (size_t k = 0; k < lv.size(); ++k) launch_factor<double>(st, view<double>(k), inv_dt);
+    }
     CT_CK(cudaGetLastError());
     return CT_OK;
 }

@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -122,6 +123,20 @@ class Solver {
         v.x = at<T>(L.o_x);
         v.b = at<T>(L.o_b);
         return v;
+    }
+
+    // Every level with its columns' first index laid end to end (at most
+    // kMaxTail levels; the caller checks).
+    template <class T>
+    FactorLevels<T> factor_levels() const {
+        FactorLevels<T> fl;
+        fl.n = (int)std::min(lv.size(), (size_t)kMaxTail);
+        fl.first[0] = 0;
+        for (size_t k = 0; k < (size_t)fl.n; ++k) {
+            fl.L[k] = view<T>(k);
+            fl.first[k + 1] = fl.first[k] + (unsigned)lv[k].g.nx * (unsigned)lv[k].g.ny;
+        }
+        return fl;
     }
 
     Red red(int blocks_wanted, Slot sl) const {

@@ -391,6 +391,21 @@ def test_small_level_split_sweeps_bitwise(ct, n, prec):
     assert_same_results(out[0], out[1])
 
 
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
+@pytest.mark.parametrize("n", [203, 37])
+def test_factor_levels_one_launch_bitwise(ct, n, prec):
+    """set_dt with every level's factors and the FP64 diagonal in one launch
+    (the default) gives the per-level launches' results (CT_FACTOR_LEVELS=0)
+    bit for bit: steady solve, then two backward-Euler steps."""
+    import workloads
+    m = workloads.steady_hotspot(n, seed=29)
+    out = []
+    for flag in ("0", None):
+        with env_vars(CT_FACTOR_LEVELS=flag):
+            out.append(steady_then_steps(ct, m, prec))
+    assert_same_results(out[0], out[1])
+
+
 @pytest.mark.parametrize("cu_planes", [2, 16])
 def test_small_level_split_sweeps_bitwise_deep(ct, cu_planes):
     """The same on 8- and 22-plane stacks (the 8- and 32-plane forms)."""
