@@ -166,6 +166,7 @@ __global__ void __launch_bounds__(NT)
     for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows; R += gridDim.x * (NT / 32))
         apply_row<2>(o, dgw, p, Ap, R, lane, acc);
     DwAcc unused = {0.0f, 0.0f};
+    pdl_trigger();
     block_sum_acc2(acc, unused);
     if (publish_acc2(acc, unused, part, maxb, blockIdx.x, &ctl->ticket[SL_APPLY], gridDim.x)) {
         double PAP, U;
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(NT)
     const BlockRange br = block_range(n2);
     update_range(br.begin, br.end, NT, ctl->alpha_w, p, Ap, x, r, b0, acc);
     DwAcc unused = {0.0f, 0.0f};
+    pdl_trigger();
     block_sum_acc2(acc, unused);
     if (publish_acc2(acc, unused, part, maxb, blockIdx.x, &ctl->ticket[SL_UPDATE], gridDim.x)) {
         double RR, U;
@@ -234,6 +236,7 @@ __global__ void __launch_bounds__(NT, 4)
     if (loop_done(ctl, cond)) return;
     DwAcc rz = {0.0f, 0.0f}, zap = {0.0f, 0.0f};
     dot_range(blockIdx.x * NT + threadIdx.x, n2, gridDim.x * NT, r, z, Ap, rz, zap);
+    pdl_trigger();
     block_sum_acc2(rz, zap);
     if (publish_acc2(rz, zap, part, maxb, blockIdx.x, &ctl->ticket[SL_DOT], gridDim.x)) {
         double RZ, ZAP;

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(NT)
             Ap[k] = av;
             if (valid) pap = __fma_rn(pc, av, pap);
         });
+    pdl_trigger();
     block_sum2(pap, unused);
     if (publish2(pap, unused, part, maxb, &ctl->ticket[SL_APPLY])) {
         double PAP, U;
@@ -194,6 +195,7 @@ __global__ void __launch_bounds__(NT)
             rr = __fma_rn(it.r.x, it.r.x, rr);
             rr = __fma_rn(it.r.y, it.r.y, rr);
         });
+    pdl_trigger();
     block_sum2(rr, unused);
     if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
         double RR, U;
@@ -242,6 +244,7 @@ __global__ void __launch_bounds__(NT)
                 zap = __fma_rn(it.z.y, it.a.y, zap);
             }
         });
+    pdl_trigger();
     block_sum2(rz, zap);
     if (publish2(rz, zap, part, maxb, &ctl->ticket[SL_DOT])) {
         double RZ, ZAP;

@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(32 * MZ)
         fc = ZERO ? RN<T>::mul(-(T)gu, fi) : L.fcp[id];
     }
     if (loop_done(flags, cond)) return;  // the same for every thread of the grid
+    pdl_trigger();
     if (on) {
         sv[l][tx] = rhs;
         sfi[l][tx] = fi;
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(NT)
     const int l = (int)blockIdx.y;
     const T sum = on ? restrict_sum<T, false>(F, (T)ctl->inv_dt, I, J, l) : T(0);
     if (loop_done(flags, cond) || !on) return;
+    pdl_trigger();
     C.b[(unsigned)l * cg.plane + scol(cg, I, J)] = sum;
 }
 
@@ -250,6 +252,7 @@ __global__ void __launch_bounds__(32 * MZ)
         }
     }
     if (loop_done(flags, cond)) return;  // the same for every thread of the grid
+    pdl_trigger();
     if (on) {
         C.b[id] = sum;
         if (red) {

@@ -132,6 +132,7 @@ __device__ __forceinline__ bool sweep_tiles_ws(const SweepMaps* m, const LevelVi
                 issue_plane<TT, TJ, NS, ZERO>(m, sm, full, w, nz, tilesx, tl);
                 *issued = w + 1;
             }
+            pdl_trigger();  // every copy of this block issued
         }
     } else {  // consumers: warp = tile row
         const int tx = lane, ty = warp;

@@ -56,6 +56,19 @@ bool pdl_enabled();
 __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
+// Called by a block once its main work is issued (before a reduction's tail,
+// a sweep's last stores): the dependent kernel may be scheduled once every
+// block has called it or exited, so its launch overlaps this kernel's tail.
+// It still waits (pdl_enter) for this whole grid to complete and its memory
+// to be visible, so where the call sits changes timing, never results.
+#ifndef CT_PDL_TRIGGER
+#define CT_PDL_TRIGGER 1
+#endif
+__device__ __forceinline__ void pdl_trigger() {
+#if CT_PDL_TRIGGER
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
 template <class... KArgs, class... Args>
 inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
                        Args&&... args) {

@@ -617,6 +617,7 @@ __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double
         }
         __syncthreads();
     }
+    pdl_trigger();
     const LevelView<T> S0 = small_view<T>(smem, sg[0]);
     const unsigned ln0 = S0.g.plane * (unsigned)S0.g.nz;
     T* out = tl.L[0].x;
