@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(NT, 4)
     k_restrict2(LevelView<T> F, LevelView<T> C, const Ctl* ctl, Cond cond) {
     pdl_enter();
     if (loop_done(ctl, cond)) return;
+    pdl_trigger();  // several waves: the dependent launches as the last one starts
     const unsigned q = blockIdx.x * NT + threadIdx.x;
     if (q >= (unsigned)C.g.nx * (unsigned)C.g.ny) return;
     restrict_pair<T, false>(F, C, (T)ctl->inv_dt, q, 2 * (int)blockIdx.y);
