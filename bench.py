@@ -197,10 +197,14 @@ def partition_instances(costs, world):
 
 
 def timed_solves(ct, solver, k, world):
-    """k steady solves, timed with CUDA events on the solver's stream."""
+    """k steady solves, timed with CUDA events on the solver's stream. The
+    solves are queued one after another (ct_solve_async) and waited for once
+    (ct_solve_wait), as a power-map sweep would run them, so the device time
+    does not include host pauses between solves (a driver call held up by the
+    clock sampler's nvidia-smi queries once stalled a blocking loop by about
+    0.1 s)."""
     import torch
     stream = torch.cuda.ExternalStream(solver.stream())
-    stats = []
     torch.cuda.synchronize()
     barrier(world)
     torch.cuda.synchronize()
@@ -209,12 +213,13 @@ def timed_solves(ct, solver, k, world):
     for _ in range(k):
         solver.set_x_zero()
         solver.set_rhs_steady()
-        stats.append(solver.solve(TOL, MAXIT))
+        solver.solve_async(TOL, MAXIT)
     e1.record(stream)
+    st = solver.solve_wait()
     torch.cuda.synchronize()
     barrier(world)
     ms = e0.elapsed_time(e1)
-    return ms, stats
+    return ms, [st]
 
 
 def host_threads():

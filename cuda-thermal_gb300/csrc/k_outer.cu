@@ -284,6 +284,20 @@ __global__ void k_faces(OpView o, double* __restrict__ dface) {
         setupdev::faces_column(o, (unsigned)q, dface);
 }
 
+// The control block of a solve, set from the launch's own arguments (so
+// that solves queued one after another never share a host buffer), and the
+// zeroing of x that a solve with no heat in asks for (bb_zero), done on the
+// device after the solve so that queued solves need no host step between
+// them.
+__global__ void k_ctl_set(Ctl* ctl, Ctl c) { *ctl = c; }
+__global__ void k_zero_if_no_heat(const Ctl* ctl, unsigned n, double* x, float2* xw) {
+    if (!*(volatile const int*)&ctl->bb_zero) return;
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        x[k] = 0.0;
+        if (xw) xw[k] = make_float2(0.0f, 0.0f);
+    }
+}
+
 __global__ void k_rhs_transient(unsigned n, const float* __restrict__ cap, double inv_dt,
                                 const double* __restrict__ P, const double* __restrict__ x,
                                 double* __restrict__ b, double* __restrict__ xold) {
@@ -510,6 +524,12 @@ void launch_faces(cudaStream_t st, const OpView& o, double* dface) {
 void launch_diag(cudaStream_t st, const OpView& o, const double* dface, double inv_dt, double* diag,
                  double* invd) {
     k_diag<<<grid_for((size_t)o.g.nx * o.g.ny), NT, 0, st>>>(o, dface, inv_dt, diag, invd);
+}
+
+void launch_ctl_set(cudaStream_t st, Ctl* ctl, const Ctl& c) { k_ctl_set<<<1, 1, 0, st>>>(ctl, c); }
+
+void launch_zero_if_no_heat(cudaStream_t st, const Ctl* ctl, unsigned n, double* x, float2* xw) {
+    k_zero_if_no_heat<<<grid_for(n), NT, 0, st>>>(ctl, n, x, xw);
 }
 
 void launch_rhs_transient(cudaStream_t st, unsigned n, const float* cap, double inv_dt,

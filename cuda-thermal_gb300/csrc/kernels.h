@@ -148,6 +148,11 @@ void launch_faces(cudaStream_t st, const OpView& o, double* dface);
 void launch_diag(cudaStream_t st, const OpView& o, const double* dface, double inv_dt, double* diag,
                  double* invd);
 // b = P + cap * inv_dt * x; xold = x.
+// *ctl = c on the stream (a queued solve's control block).
+void launch_ctl_set(cudaStream_t st, Ctl* ctl, const Ctl& c);
+// x (and the double-word correction xw, when not null) = 0 if the solve just
+// run found no heat in (ctl->bb_zero); otherwise it does nothing.
+void launch_zero_if_no_heat(cudaStream_t st, const Ctl* ctl, unsigned n, double* x, float2* xw);
 void launch_rhs_transient(cudaStream_t st, unsigned n, const float* cap, double inv_dt,
                           const double* P, const double* x, double* b, double* xold);
 // ctl->aux0 = ||P - A x||^2, aux1 = ||P||^2 (steady operator, FP64).

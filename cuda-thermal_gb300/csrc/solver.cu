@@ -602,6 +602,49 @@ ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
         }
     }
     CT_CK(cudaGetLastError());
+    return finish_solve(out);
+}
+
+ct_status Solver::solve_async(double tol, int maxit) {
+    const TraceRange trace("ct_solve_async");
+    if (!(tol >= 0)) return fail(CT_BAD_ARG, "ct_solve_async: tol must be >= 0");
+    if (maxit > 100000000) return fail(CT_BAD_ARG, "ct_solve_async: maxit above 1e8");
+    if (!(have_cond && !prof)) {
+        // no single-graph solve here: run it now and keep its result
+        async_status = solve(tol, maxit, &async_done);
+        async_pending = 2;
+        return async_status == CT_NOT_CONVERGED || async_status == CT_BREAKDOWN ? CT_OK : async_status;
+    }
+    Ctl c;
+    std::memset(&c, 0, sizeof c);
+    c.tol = tol;
+    c.maxit = maxit;
+    c.inv_dt = inv_dt;
+    c.stop = dw ? std::max(tol, rr_thr) : tol;
+    c.x_zero = x_zero ? 1 : 0;
+    x_zero = false;
+    cs = st;
+    launch_ctl_set(st, ctl, c);
+    CT_CK(cudaGraphLaunch(gx_solve, st));
+    launch_zero_if_no_heat(st, ctl, n, x, xwc);
+    CT_CK(cudaGetLastError());
+    async_pending = 1;
+    return CT_OK;
+}
+
+ct_status Solver::solve_wait(ct_stats* out) {
+    const TraceRange trace("ct_solve_wait");
+    const int pending = async_pending;
+    async_pending = 0;
+    if (pending == 0) return fail(CT_BAD_ARG, "ct_solve_wait: no solve queued");
+    if (pending == 2) {
+        if (out) *out = async_done;
+        return async_status;
+    }
+    return finish_solve(out);
+}
+
+ct_status Solver::finish_solve(ct_stats* out) {
     CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     CT_CK(cudaStreamSynchronize(st));
     if (h_ctl->bb_zero) {  // no heat in: x = 0 (src/pcg3d_cpu.cpp:146)
@@ -837,7 +880,18 @@ ct_status ct_set_power_device(ct_solver* s, const double* P_dev) {
 
 ct_status ct_solve(ct_solver* s, double tol, int maxit, ct_stats* st) {
     CT_SOLVER_OK(s);
+    s->impl.async_pending = 0;
     return s->impl.solve(tol, maxit, st);
+}
+
+ct_status ct_solve_async(ct_solver* s, double tol, int maxit) {
+    CT_SOLVER_OK(s);
+    return s->impl.solve_async(tol, maxit);
+}
+
+ct_status ct_solve_wait(ct_solver* s, ct_stats* st) {
+    CT_SOLVER_OK(s);
+    return s->impl.solve_wait(st);
 }
 
 ct_status ct_get_x(ct_solver* s, double* T) {

@@ -155,6 +155,15 @@ class Solver {
                      const DeviceBuild* build = nullptr);
     ct_status set_dt(double dt);
     ct_status solve(double tol, int maxit, ct_stats* out);
+    // A solve queued on the stream without waiting for it (the graph path;
+    // otherwise solve_async runs solve() and keeps its result), and the wait
+    // that returns the last queued solve's result.
+    ct_status solve_async(double tol, int maxit);
+    ct_status solve_wait(ct_stats* out);
+    ct_status finish_solve(ct_stats* out);  // reads the control block after a solve
+    int async_pending = 0;                   // 1: a queued solve; 2: a finished one kept in async_done
+    ct_status async_status = CT_OK;
+    ct_stats async_done{};
     ct_status record_graphs();
 
     // Enqueues one kernel launch; in profiling mode brackets it with events.

@@ -99,6 +99,8 @@ def _signatures():
         "ct_set_power": (i, [vp, vp]),
         "ct_set_power_device": (i, [vp, vp]),
         "ct_solve": (i, [vp, d, i, C.POINTER(CtStats)]),
+        "ct_solve_async": (i, [vp, d, i]),
+        "ct_solve_wait": (i, [vp, C.POINTER(CtStats)]),
         "ct_get_x": (i, [vp, vp]),
         "ct_device_x": (i, [vp, C.POINTER(vp)]),
         "ct_solver_setup_times": (i, [vp, C.POINTER(CtSetupTimes)]),
@@ -721,6 +723,16 @@ class GpuPcg:
         st = CtStats()
         _check(lib().ct_solve(self._h, float(tol), int(maxit), C.byref(st)),
                allow=(CT_OK, CT_NOT_CONVERGED, CT_BREAKDOWN))
+        return PcgStats(st.iters, st.relres, bool(st.converged), bool(st.breakdown))
+
+    def solve_async(self, tol, maxit) -> None:
+        """Queues a solve on the solver's stream and returns (ct_solve_async);
+        solve_wait() returns the last queued solve's statistics."""
+        _check(lib().ct_solve_async(self._h, float(tol), int(maxit)))
+
+    def solve_wait(self) -> PcgStats:
+        st = CtStats()
+        _check(lib().ct_solve_wait(self._h, C.byref(st)), allow=(CT_OK, CT_NOT_CONVERGED, CT_BREAKDOWN))
         return PcgStats(st.iters, st.relres, bool(st.converged), bool(st.breakdown))
 
     def get_x(self, out: Optional[np.ndarray] = None) -> np.ndarray:

@@ -180,6 +180,18 @@ ct_status ct_set_power_device(ct_solver* s, const double* P_dev);
  * ||r|| / ||b|| < tol or maxit. Blocks until done. Returns CT_OK,
  * CT_NOT_CONVERGED or CT_BREAKDOWN, with the statistics in *st. */
 ct_status ct_solve(ct_solver* s, double tol, int maxit, ct_stats* st);
+/* No counterpart in the reference (its solve always blocks). Queues the same
+ * solve on the solver's stream and returns at once, so that a caller running
+ * many solves in a row (a power-map sweep: ct_set_power_device or
+ * ct_set_rhs_steady, then ct_solve_async, again and again) keeps the GPU busy
+ * while the host does other work or is held up. Each queued solve overwrites
+ * the previous one's statistics; ct_solve_wait blocks until the last queued
+ * solve is done and returns its status and statistics as ct_solve would. A
+ * solve that finds no heat in still sets x = 0. Where the solver has no
+ * single-graph solve (ct_use_graphs(0)), the solve runs before the call
+ * returns and ct_solve_wait reports it. */
+ct_status ct_solve_async(ct_solver* s, double tol, int maxit);
+ct_status ct_solve_wait(ct_solver* s, ct_stats* st);
 /* GpuPcg::get_x (src/pcg3d_gpu.cu:548-552): x to host memory. */
 ct_status ct_get_x(ct_solver* s, double* T);
 /* GpuPcg::device_x (src/pcg3d.h:130): device pointer to x in the natural

@@ -391,6 +391,41 @@ def test_small_level_split_sweeps_bitwise(ct, n, prec):
     assert_same_results(out[0], out[1])
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
+def test_queued_solves_match_blocking_solve(ct, prec, graphs):
+    """Solves queued with solve_async (x = 0 and b = P set before each) and
+    one solve_wait give the blocking solve's field and statistics bit for
+    bit; a queued solve with no heat in leaves x = 0; a wait with nothing
+    queued is refused."""
+    import workloads
+    m = workloads.steady_hotspot(96, seed=31)
+    pr = getattr(ct.Precision, prec)
+    ct.gpu_use_graphs(graphs)
+    try:
+        with ct.GpuPcg(m, ct.Precond.Multigrid, pr) as s:
+            s.set_x_zero()
+            s.set_rhs_steady()
+            ref = s.solve(1e-10, 200)
+            Tref = s.get_x()
+            for _ in range(3):
+                s.set_x_zero()
+                s.set_rhs_steady()
+                s.solve_async(1e-10, 200)
+            st = s.solve_wait()
+            assert (st.iters, st.converged, st.relres) == (ref.iters, ref.converged, ref.relres)
+            assert np.array_equal(s.get_x(), Tref)
+            with pytest.raises(ct.CtError):
+                s.solve_wait()
+            s.set_power(np.zeros(m.ncells()))
+            s.set_rhs_steady()
+            s.solve_async(1e-10, 200)
+            st = s.solve_wait()
+            assert st.converged and not np.any(s.get_x())
+    finally:
+        ct.gpu_use_graphs(True)
+
+
 @pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
 @pytest.mark.parametrize("n", [203, 37])
 def test_factor_levels_one_launch_bitwise(ct, n, prec):
