@@ -38,6 +38,8 @@ __device__ __forceinline__ void gather_inst_acc(const BRed& red, int ntasks, int
 // Start of every loop body: ends the loop once no instance is active, and
 // bounds the number of bodies.
 __global__ void kb_guard(BCtl* bc, Cond cond) {
+    pdl_enter();
+    pdl_trigger();
     if (threadIdx.x != 0) return;
     bc->body += 1;
     if (bc->active <= 0 || bc->body > bc->maxbody) {
@@ -47,6 +49,7 @@ __global__ void kb_guard(BCtl* bc, Cond cond) {
 
 __global__ void __launch_bounds__(NT)
     kb_fold(Plan p, const BInst* __restrict__ bi, const Ctl* ctl, int only_phase_end) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     const Ctl* c = &ctl[t.inst];
     if (only_phase_end && (inst_done(c) || !c->phase_end)) return;
@@ -69,6 +72,7 @@ __global__ void __launch_bounds__(NT)
 __global__ void __launch_bounds__(NT)
     kb_residual(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, int start, BCtl* bc,
                 Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c) || (!start && !c->phase_end)) return;
@@ -164,6 +168,7 @@ __global__ void __launch_bounds__(NT)
 // SM (64 registers: 600 us per launch against 722 us with the compiler's 78).
 __global__ void __launch_bounds__(NT, 4)
     kb_apply(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -175,6 +180,7 @@ __global__ void __launch_bounds__(NT, 4)
     DwAcc pacc = {0.0f, 0.0f};
     for (unsigned R = t.begin + (threadIdx.x >> 5); R < t.end; R += NT / 32)
         apply_row<1>(o, dgw, pv, Ap, R, lane, pacc);
+    pdl_trigger();
     DwAcc unused = {0.0f, 0.0f};
     block_sum_acc2(pacc, unused);
     if (publish_inst_acc(pacc, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
@@ -198,6 +204,7 @@ __global__ void __launch_bounds__(NT, 4)
 // test. Items are value pairs.
 __global__ void __launch_bounds__(NT)
     kb_update(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -207,6 +214,7 @@ __global__ void __launch_bounds__(NT)
                  reinterpret_cast<const float4*>(bi[t.inst].Ap),
                  reinterpret_cast<float4*>(bi[t.inst].xw), reinterpret_cast<float4*>(bi[t.inst].r),
                  reinterpret_cast<float2*>(bi[t.inst].b0), acc);
+    pdl_trigger();
     DwAcc unused = {0.0f, 0.0f};
     block_sum_acc2(acc, unused);
     if (publish_inst_acc(acc, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
@@ -235,6 +243,7 @@ __global__ void __launch_bounds__(NT)
 // rz = r.z, z.Ap, flexible beta.
 __global__ void __launch_bounds__(NT)
     kb_dot(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -242,6 +251,7 @@ __global__ void __launch_bounds__(NT)
     dot_range(t.begin + threadIdx.x, t.end, NT, reinterpret_cast<const float4*>(bi[t.inst].r),
               reinterpret_cast<const float2*>(bi[t.inst].z),
               reinterpret_cast<const float4*>(bi[t.inst].Ap), rz, zap);
+    pdl_trigger();
     block_sum_acc2(rz, zap);
     if (publish_inst_acc(rz, zap, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RZ, ZAP;
@@ -261,6 +271,7 @@ __global__ void __launch_bounds__(NT)
 
 __global__ void __launch_bounds__(NT)
     kb_update_p(Plan p, const BInst* __restrict__ bi, const Ctl* ctl) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     const Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -370,6 +381,7 @@ template <int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(NT)
     kb_sweep(Plan p, const LevelView<float>* __restrict__ views,
              const LevelView<float>* __restrict__ cviews, int color, const Ctl* ctl) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     if (inst_done(&ctl[t.inst])) return;
     const LevelView<float> L = views[t.inst];
@@ -384,6 +396,7 @@ __global__ void __launch_bounds__(NT)
 __global__ void __launch_bounds__(NT, 4)
     kb_restrict(Plan p, const LevelView<float>* __restrict__ views,
                 const LevelView<float>* __restrict__ cviews, const Ctl* ctl) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     const Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -403,9 +416,12 @@ __global__ void __launch_bounds__(kSmallThreads, 1)
              Ctl* ctl, BCtl* bc, Cond cond) {
     const int i = insts[blockIdx.x];
     Ctl* c = &ctl[i];
-    if (inst_done(c)) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    if (vsmall_body<float, MZ>(small[i], &c->inv_dt, smem, [] {}, [] { return true; }) == kSmallTimeout &&
+    // the levels' operators and factors (not written inside the loop) are
+    // copied before the dependent-launch wait, b and the done flag after it
+    const auto wait = [] { pdl_enter(); };
+    const auto go = [&] { return !inst_done(c); };
+    if (vsmall_body<float, MZ>(small[i], &c->inv_dt, smem, wait, go) == kSmallTimeout &&
         threadIdx.x == 0) {
         // a bounded wait ran out: record it and stop this instance
         atomicExch(&c->err, 1);
@@ -416,34 +432,34 @@ __global__ void __launch_bounds__(kSmallThreads, 1)
 
 }  // namespace
 
-void launch_b_guard(cudaStream_t st, BCtl* bc, Cond cond) { kb_guard<<<1, 32, 0, st>>>(bc, cond); }
+void launch_b_guard(cudaStream_t st, BCtl* bc, Cond cond) { launch_pdl(kb_guard, 1, 32, 0, st, bc, cond); }
 
 void launch_b_fold(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, int only_phase_end) {
-    kb_fold<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, only_phase_end);
+    launch_pdl(kb_fold, p.ntasks, NT, 0, st, p, bi, ctl, only_phase_end);
 }
 
 void launch_b_residual(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
                        int start, BCtl* bc, Cond cond) {
-    kb_residual<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, start, bc, cond);
+    launch_pdl(kb_residual, p.ntasks, NT, 0, st, p, bi, ctl, red, start, bc, cond);
 }
 
 void launch_b_apply(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
                     BCtl* bc, Cond cond) {
-    kb_apply<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    launch_pdl(kb_apply, p.ntasks, NT, 0, st, p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_update(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red,
                      BCtl* bc, Cond cond) {
-    kb_update<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    launch_pdl(kb_update, p.ntasks, NT, 0, st, p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_dot(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
                   Cond cond) {
-    kb_dot<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    launch_pdl(kb_dot, p.ntasks, NT, 0, st, p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_update_p(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl) {
-    kb_update_p<<<p.ntasks, NT, 0, st>>>(p, bi, ctl);
+    launch_pdl(kb_update_p, p.ntasks, NT, 0, st, p, bi, ctl);
 }
 
 void launch_b_step_record(cudaStream_t st, const Plan& p, const BInst* bi, BRed red, double* mx,
@@ -469,11 +485,11 @@ void launch_b_sweep(cudaStream_t st, const Plan& p, const LevelView<float>* view
 #define CT_BSWEEP(MZ)                                                                          \
     do {                                                                                       \
         if (zero_x)                                                                            \
-            kb_sweep<MZ, true, false><<<p.ntasks, NT, 0, st>>>(p, views, cviews, color, ctl);  \
+            launch_pdl(kb_sweep<MZ, true, false>, p.ntasks, NT, 0, st, p, views, cviews, color, ctl);  \
         else if (prolong)                                                                      \
-            kb_sweep<MZ, false, true><<<p.ntasks, NT, 0, st>>>(p, views, cviews, color, ctl);  \
+            launch_pdl(kb_sweep<MZ, false, true>, p.ntasks, NT, 0, st, p, views, cviews, color, ctl);  \
         else                                                                                   \
-            kb_sweep<MZ, false, false><<<p.ntasks, NT, 0, st>>>(p, views, cviews, color, ctl); \
+            launch_pdl(kb_sweep<MZ, false, false>, p.ntasks, NT, 0, st, p, views, cviews, color, ctl); \
     } while (0)
     if (mz <= 8)
         CT_BSWEEP(8);
@@ -490,7 +506,7 @@ void launch_b_sweep(cudaStream_t st, const Plan& p, const LevelView<float>* view
 
 void launch_b_restrict(cudaStream_t st, const Plan& p, const LevelView<float>* views,
                        const LevelView<float>* cviews, const Ctl* ctl) {
-    kb_restrict<<<p.ntasks, NT, 0, st>>>(p, views, cviews, ctl);
+    launch_pdl(kb_restrict, p.ntasks, NT, 0, st, p, views, cviews, ctl);
 }
 
 cudaError_t launch_b_small(cudaStream_t st, const int* insts, int n,
@@ -500,7 +516,7 @@ cudaError_t launch_b_small(cudaStream_t st, const int* insts, int n,
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              kSmallSmemMax);
         if (e != cudaSuccess) return e;
-        kern<<<n, kSmallThreads, smem, st>>>(insts, small, ctl, bc, cond);
+        launch_pdl(kern, n, kSmallThreads, smem, st, insts, small, ctl, bc, cond);
         return cudaGetLastError();
     };
     if (mz <= 8) return go(kb_small<8>);

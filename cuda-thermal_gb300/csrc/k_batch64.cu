@@ -24,6 +24,7 @@ constexpr int kRowU = 2;
 // x = 0 copies b).
 __global__ void __launch_bounds__(NT)
     kb_residual64(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -91,6 +92,7 @@ __global__ void __launch_bounds__(NT)
 // Ap = (A + C/dt) p, p.Ap, alpha; items = rows of one colour and plane.
 __global__ void __launch_bounds__(NT)
     kb_apply64(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -102,6 +104,7 @@ __global__ void __launch_bounds__(NT)
             I.Ap64[k] = av;
             if (valid) pap = __fma_rn(pc, av, pap);
         });
+    pdl_trigger();
     block_sum2(pap, unused);
     if (publish_inst(pap, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double PAP, U;
@@ -123,6 +126,7 @@ __global__ void __launch_bounds__(NT)
 // convergence test; items = value pairs.
 __global__ void __launch_bounds__(NT)
     kb_update64(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -150,6 +154,7 @@ __global__ void __launch_bounds__(NT)
             rr = __fma_rn(it.r.x, it.r.x, rr);
             rr = __fma_rn(it.r.y, it.r.y, rr);
         });
+    pdl_trigger();
     block_sum2(rr, unused);
     if (publish_inst(rr, unused, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RR, U;
@@ -175,6 +180,7 @@ __global__ void __launch_bounds__(NT)
 // rz = r.z, z.Ap, flexible beta; items = value pairs.
 __global__ void __launch_bounds__(NT)
     kb_dot64(Plan p, const BInst* __restrict__ bi, Ctl* ctl, BRed red, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -196,6 +202,7 @@ __global__ void __launch_bounds__(NT)
             zap = __fma_rn(za, it.a.x, zap);
             zap = __fma_rn(zb, it.a.y, zap);
         });
+    pdl_trigger();
     block_sum2(rz, zap);
     if (publish_inst(rz, zap, red, p.ntasks, t.inst, p.inst_count[t.inst])) {
         double RZ, ZAP;
@@ -215,6 +222,7 @@ __global__ void __launch_bounds__(NT)
 // p = z + beta p (p = z on the first iteration); items = value pairs.
 __global__ void __launch_bounds__(NT)
     kb_update_p64(Plan p, const BInst* __restrict__ bi, const Ctl* ctl) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     const Ctl* c = &ctl[t.inst];
     if (inst_done(c)) return;
@@ -245,26 +253,26 @@ __global__ void __launch_bounds__(NT)
 
 void launch_b_residual64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
                          Cond cond) {
-    kb_residual64<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    launch_pdl(kb_residual64, p.ntasks, NT, 0, st, p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_apply64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
                       Cond cond) {
-    kb_apply64<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    launch_pdl(kb_apply64, p.ntasks, NT, 0, st, p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_update64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
                        Cond cond) {
-    kb_update64<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    launch_pdl(kb_update64, p.ntasks, NT, 0, st, p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_dot64(cudaStream_t st, const Plan& p, const BInst* bi, Ctl* ctl, BRed red, BCtl* bc,
                     Cond cond) {
-    kb_dot64<<<p.ntasks, NT, 0, st>>>(p, bi, ctl, red, bc, cond);
+    launch_pdl(kb_dot64, p.ntasks, NT, 0, st, p, bi, ctl, red, bc, cond);
 }
 
 void launch_b_update_p64(cudaStream_t st, const Plan& p, const BInst* bi, const Ctl* ctl) {
-    kb_update_p64<<<p.ntasks, NT, 0, st>>>(p, bi, ctl);
+    launch_pdl(kb_update_p64, p.ntasks, NT, 0, st, p, bi, ctl);
 }
 
 }  // namespace ct

@@ -267,6 +267,7 @@ template <int TT, int TJ, int NS, int MZ, bool ZERO, bool PRO>
 __global__ void __launch_bounds__(TT * TJ + 32, MZ <= 16 ? kSweepWsBlocks : 2)
     kb_sweep_tma_ws(Plan p, const SweepMaps* __restrict__ maps, const LevelView<float>* __restrict__ views,
                     const LevelView<float>* __restrict__ cviews, int color, Ctl* ctl, BCtl* bc, Cond cond) {
+    pdl_enter();
     const Task t = p.tasks[blockIdx.x];
     Ctl* c = &ctl[t.inst];
     if (*(volatile const int*)&c->done) return;
@@ -363,8 +364,8 @@ void go_b(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView
     static const bool attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   (int)stage_bytes<TT, TJ, NW>(ZERO)) == cudaSuccess;
     (void)attr;
-    kern<<<p.ntasks, TT * TJ + 32, stage_bytes<TT, TJ, NW>(ZERO), st>>>(p, maps, views, cviews, color, ctl,
-                                                                        bc, cond);
+    launch_pdl(kern, p.ntasks, TT * TJ + 32, stage_bytes<TT, TJ, NW>(ZERO), st, p, maps, views, cviews, color,
+               ctl, bc, cond);
 }
 template <int MZ>
 void go_b_sweep(cudaStream_t st, const Plan& p, const SweepMaps* maps, const LevelView<float>* views,
