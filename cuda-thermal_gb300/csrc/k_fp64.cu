@@ -89,52 +89,6 @@ __device__ __forceinline__ void start_test(Ctl* ctl, Cond cond, double RR, doubl
     }
 }
 
-// r = b - (A + C/dt) x, b0 = r in the V-cycle precision, ||r||^2, ||b||^2 and
-// the start test. A solve that starts from x = 0 (every steady solve) has
-// r = b exactly and streams b once.
-template <class T>
-__global__ void __launch_bounds__(NT)
-    k_residual64(OpView o, unsigned n, const double* __restrict__ diag, const double* __restrict__ b,
-                 const double* __restrict__ x, double* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
-                 double* part, int maxb, Cond cond) {
-    pdl_enter();
-    const Geo& g = o.g;
-    double rr = 0.0, bb = 0.0;
-    if (ctl->x_zero) {
-        for (unsigned k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
-            const double bi = b[k];
-            r[k] = bi;
-            b0[k] = from_d<T>(bi);
-            bb = __fma_rn(bi, bi, bb);
-        }
-        rr = bb;
-    } else {
-        const unsigned rows = 2u * (unsigned)g.ny * (unsigned)g.nz;
-        const int lane = (int)(threadIdx.x & 31u);
-        for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows;
-             R += gridDim.x * (NT / 32))
-            row64<kRowU>(o, diag, x, R, lane, [&](unsigned k, bool valid, double ax, double) {
-                if (!valid) {
-                    r[k] = 0.0;
-                    b0[k] = T(0);
-                    return;
-                }
-                const double bi = b[k];
-                const double ri = bi - ax;
-                r[k] = ri;
-                b0[k] = from_d<T>(ri);
-                rr = __fma_rn(ri, ri, rr);
-                bb = __fma_rn(bi, bi, bb);
-            });
-    }
-    block_sum2(rr, bb);
-    if (publish2(rr, bb, part, maxb, &ctl->ticket[SL_INIT])) {
-        double RR, BB;
-        gather2(part, maxb, &ctl->ticket[SL_INIT], RR, BB);
-        if (threadIdx.x == 0) start_test(ctl, cond, RR, BB);
-    }
-}
-
 // ---- streaming kernels ---------------------------------------------------------
 
 // Block b streams the contiguous items [begin, end), NT apart, in chunks of
@@ -162,6 +116,58 @@ __device__ __forceinline__ void store_pair(float* b0, unsigned k, double a, doub
 }
 __device__ __forceinline__ void store_pair(double* b0, unsigned k, double a, double b) {
     reinterpret_cast<double2*>(b0)[k] = make_double2(a, b);
+}
+
+// r = b - (A + C/dt) x, b0 = r in the V-cycle precision, ||r||^2, ||b||^2 and
+// the start test. A solve that starts from x = 0 (every steady solve) has
+// r = b exactly and streams b once.
+template <class T>
+__global__ void __launch_bounds__(NT)
+    k_residual64(OpView o, unsigned n, const double* __restrict__ diag, const double* __restrict__ b,
+                 const double* __restrict__ x, double* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
+                 double* part, int maxb, Cond cond) {
+    pdl_enter();
+    const Geo& g = o.g;
+    double rr = 0.0, bb = 0.0;
+    if (ctl->x_zero) {
+        // r = b, streamed in pairs with the next items' loads issued before
+        // the current ones are stored (n is even: whole rows of both colours)
+        const double2* b2 = reinterpret_cast<const double2*>(b);
+        double2* r2 = reinterpret_cast<double2*>(r);
+        stream_pipelined<2, double2>(
+            blockIdx.x * NT + threadIdx.x, n / 2, gridDim.x * NT, [&](unsigned k) { return b2[k]; },
+            [&](unsigned k, const double2& v) {
+                r2[k] = v;
+                store_pair(b0, k, v.x, v.y);
+                bb = __fma_rn(v.x, v.x, bb);
+                bb = __fma_rn(v.y, v.y, bb);
+            });
+        rr = bb;
+    } else {
+        const unsigned rows = 2u * (unsigned)g.ny * (unsigned)g.nz;
+        const int lane = (int)(threadIdx.x & 31u);
+        for (unsigned R = blockIdx.x * (NT / 32) + (threadIdx.x >> 5); R < rows;
+             R += gridDim.x * (NT / 32))
+            row64<kRowU>(o, diag, x, R, lane, [&](unsigned k, bool valid, double ax, double) {
+                if (!valid) {
+                    r[k] = 0.0;
+                    b0[k] = T(0);
+                    return;
+                }
+                const double bi = b[k];
+                const double ri = bi - ax;
+                r[k] = ri;
+                b0[k] = from_d<T>(ri);
+                rr = __fma_rn(ri, ri, rr);
+                bb = __fma_rn(bi, bi, bb);
+            });
+    }
+    block_sum2(rr, bb);
+    if (publish2(rr, bb, part, maxb, &ctl->ticket[SL_INIT])) {
+        double RR, BB;
+        gather2(part, maxb, &ctl->ticket[SL_INIT], RR, BB);
+        if (threadIdx.x == 0) start_test(ctl, cond, RR, BB);
+    }
 }
 
 // x += alpha p, r -= alpha Ap, b0 = r in the V-cycle precision, ||r||^2 and
