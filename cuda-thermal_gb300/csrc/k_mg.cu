@@ -1,11 +1,13 @@
 // k_mg.cu - multigrid V-cycle kernels (x-y semi-coarsening, red-black column
 // line smoother) and the multigrid setup kernels, for T = float or double.
 //
-// Sweeps (mg_line_solve, src/mg3d.h:67-84): one thread per column of the
-// active colour, so a warp reads one contiguous half-row of the split layout
-// per z-plane. The column is eliminated forward through the planes with the
-// precomputed Thomas factors and substituted back in registers, so x is
-// written once per cell. Two fusions remove whole passes over the level:
+// Sweeps (mg_line_solve, src/mg3d.h:67-84) of the levels that are not staged
+// by bulk tensor copies (k_sweep_tma.cu): one thread per column and plane
+// gathers that plane's right-hand side, then one thread per column of the
+// active colour runs the Thomas recurrence (k_sweep_split), or one thread per
+// column does both for columns deeper than 32 planes (k_sweep). A warp reads
+// one contiguous half-row of the split layout per z-plane, and x is written
+// once per cell. Two fusions remove whole passes over the level:
 //  - the first sweep of a V-cycle starts from x = 0, so it reads no lateral
 //    neighbours and needs no memset of x (src/pcg3d_cpu.cpp:71);
 //  - prolongation (fine x += coarse parent x, src/pcg3d_cpu.cpp:105-109) is
