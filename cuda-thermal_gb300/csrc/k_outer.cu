@@ -529,7 +529,8 @@ void launch_diag(cudaStream_t st, const OpView& o, const double* dface, double i
 void launch_ctl_set(cudaStream_t st, Ctl* ctl, const Ctl& c) { k_ctl_set<<<1, 1, 0, st>>>(ctl, c); }
 
 void launch_zero_if_no_heat(cudaStream_t st, const Ctl* ctl, unsigned n, double* x, float2* xw) {
-    k_zero_if_no_heat<<<grid_for(n), NT, 0, st>>>(ctl, n, x, xw);
+    // a few blocks striding over x: almost always they read the flag and leave
+    k_zero_if_no_heat<<<std::min(grid_for(n), 256u), NT, 0, st>>>(ctl, n, x, xw);
 }
 
 void launch_rhs_transient(cudaStream_t st, unsigned n, const float* cap, double inv_dt,
