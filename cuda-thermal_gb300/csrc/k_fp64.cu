@@ -230,6 +230,12 @@ constexpr int kDotU = 2;
 struct DotItem {
     double2 r, z, a;
 };
+template <class T>
+struct DotItemN {
+    double2 r;
+    float2 z;
+    double2 a;
+};
 template <class T, bool FLEX>
 __global__ void __launch_bounds__(NT)
     k_dot64(unsigned n2, const double2* __restrict__ r, const T* __restrict__ z,
@@ -237,19 +243,39 @@ __global__ void __launch_bounds__(NT)
     pdl_enter();
     if (loop_done(ctl, cond)) return;
     double rz = 0.0, zap = 0.0;
-    stream_pipelined<kDotU, DotItem>(
-        blockIdx.x * NT + threadIdx.x, n2, gridDim.x * NT,
-        [&](unsigned k) {
-            return DotItem{r[k], load_pair(z, k), FLEX ? Ap[k] : make_double2(0.0, 0.0)};
-        },
-        [&](unsigned, const DotItem& it) {
-            rz = __fma_rn(it.r.x, it.z.x, rz);
-            rz = __fma_rn(it.r.y, it.z.y, rz);
-            if (FLEX) {
-                zap = __fma_rn(it.z.x, it.a.x, zap);
-                zap = __fma_rn(it.z.y, it.a.y, zap);
-            }
-        });
+    if constexpr (sizeof(T) == 4) {
+        // z kept as loaded (a float pair) until it is used: 2 registers an item
+        // fewer than widening it at the load (42.7 -> 38.7 us at 800 x 800)
+        const float2* z2 = reinterpret_cast<const float2*>(z);
+        stream_pipelined<kDotU, DotItemN<T>>(
+            blockIdx.x * NT + threadIdx.x, n2, gridDim.x * NT,
+            [&](unsigned k) {
+                return DotItemN<T>{r[k], z2[k], FLEX ? Ap[k] : make_double2(0.0, 0.0)};
+            },
+            [&](unsigned, const DotItemN<T>& it) {
+                const double zx = widen(it.z.x), zy = widen(it.z.y);
+                rz = __fma_rn(it.r.x, zx, rz);
+                rz = __fma_rn(it.r.y, zy, rz);
+                if (FLEX) {
+                    zap = __fma_rn(zx, it.a.x, zap);
+                    zap = __fma_rn(zy, it.a.y, zap);
+                }
+            });
+    } else {
+        stream_pipelined<kDotU, DotItem>(
+            blockIdx.x * NT + threadIdx.x, n2, gridDim.x * NT,
+            [&](unsigned k) {
+                return DotItem{r[k], load_pair(z, k), FLEX ? Ap[k] : make_double2(0.0, 0.0)};
+            },
+            [&](unsigned, const DotItem& it) {
+                rz = __fma_rn(it.r.x, it.z.x, rz);
+                rz = __fma_rn(it.r.y, it.z.y, rz);
+                if (FLEX) {
+                    zap = __fma_rn(it.z.x, it.a.x, zap);
+                    zap = __fma_rn(it.z.y, it.a.y, zap);
+                }
+            });
+    }
     pdl_trigger();
     block_sum2(rz, zap);
     if (publish2(rz, zap, part, maxb, &ctl->ticket[SL_DOT])) {
@@ -291,11 +317,25 @@ __global__ void __launch_bounds__(NT)
         for (unsigned k = br.begin; k < br.end; k += NT) p[k] = load_pair(z, k);
         return;
     }
-    stream_pipelined<kPU, PItem>(
-        br.begin, br.end, NT, [&](unsigned k) { return PItem{load_pair(z, k), p[k]}; },
-        [&](unsigned k, const PItem& it) {
-            p[k] = make_double2(__fma_rn(beta, it.p.x, it.z.x), __fma_rn(beta, it.p.y, it.z.y));
-        });
+    if constexpr (sizeof(T) == 4) {
+        // z kept as loaded (a float pair) until it is used, as in k_dot64
+        struct Item {
+            float2 z;
+            double2 p;
+        };
+        const float2* z2 = reinterpret_cast<const float2*>(z);
+        stream_pipelined<kPU, Item>(
+            br.begin, br.end, NT, [&](unsigned k) { return Item{z2[k], p[k]}; },
+            [&](unsigned k, const Item& it) {
+                p[k] = make_double2(__fma_rn(beta, it.p.x, widen(it.z.x)), __fma_rn(beta, it.p.y, widen(it.z.y)));
+            });
+    } else {
+        stream_pipelined<kPU, PItem>(
+            br.begin, br.end, NT, [&](unsigned k) { return PItem{load_pair(z, k), p[k]}; },
+            [&](unsigned k, const PItem& it) {
+                p[k] = make_double2(__fma_rn(beta, it.p.x, it.z.x), __fma_rn(beta, it.p.y, it.z.y));
+            });
+    }
 }
 
 // ---- self-test of the integer conversions -----------------------------------
