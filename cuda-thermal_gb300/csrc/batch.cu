@@ -62,10 +62,11 @@ constexpr unsigned kVecChunk = 4096;   // value pairs (fold, update, dot, p, rhs
 constexpr unsigned kColChunk = 512;    // fine columns (FP64 residual)
 // fine rows of one colour and plane per block of the operator apply: the
 // FP64 apply is FP64-pipe-bound, and per-block reduction overhead weighs less
-// on longer tables (256 instances: 16 / 32 / 64 / 128 rows per block, 73.6 /
-// 63.4 / 59.4 / 58.8 ms of apply per batched solve; double words 1463 / 1477
-// / 1485 / 1479 instance solves/s)
-constexpr unsigned kRowChunk64 = 128;
+// on longer tables (256 instances, two cells per lane: 16 / 32 / 64 / 128 rows
+// per block, 73.6 / 63.4 / 59.4 / 58.8 ms of apply per batched solve; one cell
+// per lane: 64 / 128 / 256 rows, 47.1 / 48.5 / 53.4 ms; double words 1463 /
+// 1477 / 1485 / 1479 instance solves/s at 16 / 32 / 64 / 128)
+constexpr unsigned kRowChunk64 = 64;
 constexpr unsigned kRowChunkDw = 64;
 // Candidate tiles of the autotuner (columns per block for the sweeps, coarse
 // cells per block for the restriction).
