@@ -415,14 +415,6 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 }  // namespace
 
-CUtensorMapL2promotion l2_promotion() {
-    const char* e = std::getenv("CT_TMA_L2");
-    const int v = e ? std::atoi(e) : 128;
-    return v == 256 ? CU_TENSOR_MAP_L2_PROMOTION_L2_256B
-                    : v == 64 ? CU_TENSOR_MAP_L2_PROMOTION_L2_64B
-                              : v == 0 ? CU_TENSOR_MAP_L2_PROMOTION_NONE : CU_TENSOR_MAP_L2_PROMOTION_L2_128B;
-}
-
 bool encode_rows_map(CUtensorMap* out, const float* base, int hx, int ny, int nz, unsigned plane,
                      unsigned bx, unsigned by) {
     PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
@@ -433,7 +425,7 @@ bool encode_rows_map(CUtensorMap* out, const float* base, int hx, int ny, int nz
     const cuuint32_t estr[3] = {1u, 1u, 1u};
     return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box,
               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-              l2_promotion(), CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 bool make_sweep_maps(const LevelView<float>& L, int color, SweepMaps* m, int tile_t, int tile_j) {
