@@ -874,7 +874,7 @@ def main():
                        "l2": "inputs larger than L2 (fine level ~1.7 GB moved per iteration)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_solve * args.steps,
-            "kernels": kernel_table(rows, 12, ncells, dfma),
+            "kernels": kernel_table(rows, 16, ncells, dfma),
             "double_word_kernels": kernel_table(rows_dw, 6),
         }
         if batched:

@@ -130,6 +130,10 @@ class Batch {
         std::vector<char> tma;
         std::vector<Plan> sweep_grid;
         std::vector<unsigned> sweep_grid_tile;
+        // per depth: the x = 0 sweep on the grid kernel over every instance
+        // (sweep0) where that times faster than the staged form
+        std::vector<char> sweep0_grid;
+        std::vector<Plan> sweep0;
         int* small_insts = nullptr;
     };
     std::vector<Bucket> bk;
@@ -453,6 +457,8 @@ ct_status Batch::build_bucket(Bucket& b) {
     if ((s = upload(&b.small_insts, b.inst)) != CT_OK) return s;
     b.sweep.assign((size_t)b.depth, Plan{});
     b.sweep_grid.assign((size_t)b.depth, Plan{});
+    b.sweep0.assign((size_t)b.depth, Plan{});
+    b.sweep0_grid.assign((size_t)b.depth, 0);
     b.restr.assign((size_t)b.depth, Plan{});
     b.sweep_tile.assign((size_t)b.depth, 512);
     b.sweep_grid_tile.assign((size_t)b.depth, 0);
@@ -574,6 +580,43 @@ ct_status Batch::tune_bucket(Bucket& b) {
                 }
             }
         }
+        // the x = 0 sweep, where the level stays staged: it has no
+        // neighbour values to stage, and the grid kernel (every plane's loads
+        // of a column in flight at once) may move its three operand streams
+        // faster
+        // (CT_SWEEP0_GRID=0 keeps it staged, =1 takes the grid kernel)
+        const char* e0 = std::getenv("CT_SWEEP0_GRID");
+        const int mode0 = !e0 ? 1 : e0[0] == '0' ? 0 : 2;  // staged, timed, grid
+        if (s == CT_OK && b.tma[(size_t)d] != 0 && (mode0 == 2 || (mode0 == 1 && !fixed_tma))) {
+            std::vector<unsigned> items;
+            for (int i : b.inst) {
+                const Geo& g = inst(i).lv[(size_t)d].g;
+                items.push_back((unsigned)g.ny * (unsigned)g.hx);
+            }
+            float best = mode0 == 2 ? 1e30f : time_of([&] {
+                launch_b_sweep_tma(b.st, b.sweep[(size_t)d], bmaps[(size_t)(2 * d)], views[(size_t)d],
+                                   views[(size_t)d], 0, true, false, b.mz, ctl, b.bc, Cond{0, 0});
+                if (b.tma[(size_t)d] == 2)
+                    launch_b_sweep(b.st, b.sweep_grid[(size_t)d], views[(size_t)d], views[(size_t)d], 0, true,
+                                   false, b.mz, ctl);
+            });
+            std::vector<unsigned> cands;
+            if (fixed) cands.push_back(fixed);
+            else cands.assign(std::begin(kSweepTiles), std::end(kSweepTiles));
+            for (unsigned tile : cands) {
+                Plan p;
+                if ((s = upload_plan(make_plan(ni, b.inst, items, tile), &p)) != CT_OK) break;
+                CT_BK(cudaStreamSynchronize(st));
+                const float t = time_of([&] {
+                    launch_b_sweep(b.st, p, views[(size_t)d], views[(size_t)d], 0, true, false, b.mz, ctl);
+                });
+                if (t < best) {
+                    best = t;
+                    b.sweep0[(size_t)d] = p;
+                    b.sweep0_grid[(size_t)d] = 1;
+                }
+            }
+        }
         // restriction
         {
             std::vector<unsigned> cands;
@@ -606,6 +649,10 @@ ct_status Batch::tune_bucket(Bucket& b) {
 void Batch::sweep(Bucket& b, cudaStream_t s, int d, int color, bool zero_x, bool prolong, Cond cond) {
     const LevelView<float>* L = views[(size_t)d];
     const LevelView<float>* C = views[(size_t)d + 1];
+    if (zero_x && b.sweep0_grid[(size_t)d]) {
+        launch_b_sweep(s, b.sweep0[(size_t)d], L, C, color, true, prolong, b.mz, ctl);
+        return;
+    }
     if (b.tma[(size_t)d]) {
         launch_b_sweep_tma(s, b.sweep[(size_t)d], bmaps[(size_t)(2 * d + color)], L, C, color, zero_x,
                            prolong, b.mz, ctl, b.bc, cond);

@@ -42,6 +42,11 @@ __device__ __forceinline__ Nbr neighbours(const Geo& g, const Geo& cg, int i, in
     return n;
 }
 
+// The Thomas factor fcp of a cell from its up face and 1/pivot, rounded as
+// factor_column rounds it: -gU * finv, one rounding.
+__device__ __forceinline__ float fcp_of(float gu, float fi) { return __fmul_rn(-gu, fi); }
+__device__ __forceinline__ double fcp_of(float gu, double fi) { return __dmul_rn(-(double)gu, fi); }
+
 // Loads of values that other blocks of the same kernel may have written
 // (x and b inside the cluster tail kernel) go to L2 (CG = true); everything
 // else may use the L1 path.
@@ -210,8 +215,13 @@ __device__ __forceinline__ void sweep_column(const LevelView<T>& L, const LevelV
                 if (!ZERO) rhs = rhs + lat_sum<T, PRO, CG>(L, C, n, l);
                 v[l] = rhs;
                 fi[l] = L.finv[id];
-                fc[l] = L.fcp[id];
                 gu[l] = L.gU[id];
+                // the x = 0 sweep recomputes fcp as factor_column rounded it
+                // (one operand stream less)
+                if (ZERO)
+                    fc[l] = fcp_of(gu[l], fi[l]);
+                else
+                    fc[l] = L.fcp[id];
             }
         }
         // Thomas recurrence on registers.

@@ -224,6 +224,12 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     // CT_FUSE_SWEEP0=0 keeps each level's first sweep a launch of its own
     // instead of riding along with the restriction into that level.
     if (const char* e = std::getenv("CT_FUSE_SWEEP0")) fuse_sweep0 = e[0] != '0';
+    // The x = 0 sweeps of the staged levels run on the grid kernel: with no
+    // neighbour values to share there is nothing to stage, and one thread per
+    // column with every plane's loads in flight at once moves the level's
+    // three operand streams faster than the tile ring (800 x 800 x 10 FLEX
+    // solve 6.52 -> 6.46 ms). CT_SWEEP0_GRID=0 stages them too.
+    if (const char* e = std::getenv("CT_SWEEP0_GRID")) sweep0_grid = e[0] != '0';
     // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
     // (FP32 levels with at least one full tile row, above the shared-memory
     // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernels. Levels of
@@ -341,7 +347,7 @@ template <class T>
 void Solver::sweep(size_t k, const LevelView<T>& L, int color, bool zero_x, const LevelView<T>* coarse,
                    Cond cond) {
     if constexpr (std::is_same<T, float>::value) {
-        if (lv[k].tma) {
+        if (lv[k].tma && !(zero_x && sweep0_grid)) {
             launch_sweep_tma(cs, lv[k].maps[color], L, coarse, color, zero_x, ctl, cond);
             return;
         }

@@ -84,6 +84,7 @@ class Solver {
     bool have_cond = false;
     size_t small_k0 = 0;   // levels from small_k0 down run in one block from shared memory
     bool fuse_sweep0 = true;  // a level's first (x = 0) sweep rides with the restriction into it
+    bool sweep0_grid = true;  // x = 0 sweeps of the staged levels on the grid kernel
     cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
     ct_setup_times times{};
     // per-kernel timing (ct_profile_solve)

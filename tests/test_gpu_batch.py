@@ -232,7 +232,10 @@ def test_batch_transient_matches_single(ct, golden):
 def _env(**kv):
     old = {k: os.environ.get(k) for k in kv}
     for k, v in kv.items():
-        os.environ[k] = v
+        if v is None:
+            os.environ.pop(k, None)
+        else:
+            os.environ[k] = v
     return old
 
 
@@ -248,10 +251,11 @@ def test_batch_staged_sweeps_bitwise(ct, mixed):
     """The sweeps staged by bulk tensor copies (forced on every level that
     holds a full tile row; mixed depths run the rest on the grid kernel)
     compute exactly what the grid sweeps compute: same iterations, same
-    bits."""
+    bits; and so do the x = 0 sweeps on the grid kernel beside staged
+    others (CT_SWEEP0_GRID=1)."""
     out = []
-    for flag in ("0", "1"):
-        old = _env(CT_SWEEP_TMA=flag, CT_BATCH_TMA_TILES="1")
+    for flag, grid0 in (("0", None), ("1", None), ("1", "1")):
+        old = _env(CT_SWEEP_TMA=flag, CT_BATCH_TMA_TILES="1", CT_SWEEP0_GRID=grid0)
         try:
             with ct.GpuBatch(mixed) as b:
                 b.set_x_zero()
@@ -260,9 +264,10 @@ def test_batch_staged_sweeps_bitwise(ct, mixed):
                 out.append(([s.iters for s in st], [b.get_x(i) for i in range(len(mixed))]))
         finally:
             _restore(old)
-    assert out[0][0] == out[1][0]
-    for a, c in zip(out[0][1], out[1][1]):
-        assert np.array_equal(a, c)
+    for o in out[1:]:
+        assert o[0] == out[0][0]
+        for a, c in zip(out[0][1], o[1]):
+            assert np.array_equal(a, c)
 
 
 def test_batch_from_device_built_specs_bitwise(ct):

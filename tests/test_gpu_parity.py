@@ -316,23 +316,21 @@ def test_dw_true_residual_meets_tol_on_larger_grid(ct, orc):
 @pytest.mark.parametrize("prec", ["MG_FP32", "MG_FP32_FLEX", "MG_FP32_FLEX_DW"])
 def test_staged_sweeps_bitwise(ct, prec):
     """Sweeps staged in shared memory by bulk tensor copies give the grid
-    sweeps' results bit for bit (odd sizes: partial tiles, padded half-rows)."""
-    import os
+    sweeps' results bit for bit (odd sizes: partial tiles, padded half-rows),
+    with the x = 0 sweeps of the staged levels on the grid kernel (the
+    default) or staged too. CT_SWEEP_TMA_COLS=1 stages every level with a
+    full tile row (by default only levels of more than 256 x 256 columns)."""
     import workloads
     m = workloads.steady_hotspot(203, seed=7)
     out = []
-    for flag in ("0", "1"):
-        old = os.environ.get("CT_SWEEP_TMA")
-        os.environ["CT_SWEEP_TMA"] = flag
-        try:
+    for flags in ({"CT_SWEEP_TMA": "0"},
+                  {"CT_SWEEP_TMA": "1", "CT_SWEEP_TMA_COLS": "1"},
+                  {"CT_SWEEP_TMA": "1", "CT_SWEEP_TMA_COLS": "1", "CT_SWEEP0_GRID": "0"}):
+        with env_vars(**flags):
             out.append(gpu_solve(ct, m, 1e-10, ct.Precond.Multigrid, getattr(ct.Precision, prec)))
-        finally:
-            if old is None:
-                os.environ.pop("CT_SWEEP_TMA", None)
-            else:
-                os.environ["CT_SWEEP_TMA"] = old
-    assert out[0][0].iters == out[1][0].iters
-    assert np.array_equal(out[0][1], out[1][1])
+    for o in out[1:]:
+        assert o[0].iters == out[0][0].iters
+        assert np.array_equal(o[1], out[0][1])
 
 
 @pytest.mark.parametrize("n,prec", [(203, "MG_FP32_FLEX_DW"), (130, "MG_FP32_FLEX"), (203, "MG_FP32")])
@@ -354,7 +352,7 @@ def test_staged_sweeps_bitwise_single_and_batch(ct, n, prec, tmp_path):
     out = []
     for flag in ("0", "1"):
         f = str(tmp_path / f"staged_{flag}.npy")
-        env = dict(os.environ, CT_SWEEP_TMA=flag)
+        env = dict(os.environ, CT_SWEEP_TMA=flag, CT_SWEEP_TMA_COLS="1")
         subprocess.run([sys.executable, "-c", code, f], check=True, cwd=root, env=env, timeout=300)
         out.append(np.load(f))
     assert np.array_equal(out[0], out[1])
