@@ -703,10 +703,11 @@ def profile_rows(solver):
 
 
 # FP64 instructions per cell of the FP64 outer kernels (CT_MG_FP32_FLEX;
-# k_fp64.cu): 7 DFMA for (A + C/dt) p and 1 for p.Ap; x, r and ||r||^2; r.z
-# and z.Ap; p = z + beta p; ||b||^2 of a start from x = 0. Conversions are
-# integer operations.
-FP64_OPS = {"pcg_apply": 8, "pcg_update_xr": 3, "pcg_dot": 2, "pcg_update_p": 1, "pcg_residual": 1}
+# k_fp64.cu): 7 DFMA for (A + C/dt) p and 1 for p.Ap; r and ||r||^2 (x
+# += alpha p runs beside the next V-cycle: pcg_update_x); r.z and z.Ap; p = z
+# + beta p; ||b||^2 of a start from x = 0. Conversions are integer operations.
+FP64_OPS = {"pcg_apply": 8, "pcg_update_xr": 2, "pcg_update_x": 1, "pcg_dot": 2, "pcg_update_p": 1,
+            "pcg_residual": 1}
 
 
 def kernel_table(rows, n=10, cells=None, dfma=None):

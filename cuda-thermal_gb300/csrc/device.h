@@ -60,6 +60,7 @@ struct Ctl {
     // scalars of the iteration
     double inv_dt;
     double bb, rr, rz, pAp, zAp, alpha, beta, relres;
+    double alpha_x;           // alpha of an x update still to apply (0: none; FP64 outer loop)
     double aux0, aux1, aux2;  // results of the auxiliary reductions
     double stop;              // relres at which the current loop ends (double-word mode: phase 1)
     float2 alpha_w, beta_w;   // alpha, beta as float pairs (double-word mode)

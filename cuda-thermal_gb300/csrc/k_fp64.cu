@@ -177,7 +177,12 @@ constexpr int kUpdU = 1;
 struct UpdItem {
     double2 p, a, x, r;
 };
-template <class T>
+struct UpdItemR {
+    double2 a, r;
+};
+// WX = false: x is left to k_update_x64 (x += alpha p off the critical path,
+// beside the next V-cycle); alpha is kept in ctl->alpha_x for it.
+template <class T, bool WX>
 __global__ void __launch_bounds__(NT)
     k_update64(unsigned n2, const double2* __restrict__ p, const double2* __restrict__ Ap,
                double2* __restrict__ x, double2* __restrict__ r, T* __restrict__ b0, Ctl* ctl,
@@ -187,20 +192,35 @@ __global__ void __launch_bounds__(NT)
     const double alpha = ctl->alpha, malpha = -alpha;
     double rr = 0.0, unused = 0.0;
     const Range br = block_range<2>(n2);
-    stream_pipelined<kUpdU, UpdItem>(
-        br.begin, br.end, NT,
-        [&](unsigned k) { return UpdItem{p[k], Ap[k], x[k], r[k]}; },
-        [&](unsigned k, UpdItem it) {
-            it.x.x = __fma_rn(alpha, it.p.x, it.x.x);
-            it.x.y = __fma_rn(alpha, it.p.y, it.x.y);
-            it.r.x = __fma_rn(malpha, it.a.x, it.r.x);
-            it.r.y = __fma_rn(malpha, it.a.y, it.r.y);
-            x[k] = it.x;
-            r[k] = it.r;
-            store_pair(b0, k, it.r.x, it.r.y);
-            rr = __fma_rn(it.r.x, it.r.x, rr);
-            rr = __fma_rn(it.r.y, it.r.y, rr);
-        });
+    if constexpr (WX) {
+        stream_pipelined<kUpdU, UpdItem>(
+            br.begin, br.end, NT,
+            [&](unsigned k) { return UpdItem{p[k], Ap[k], x[k], r[k]}; },
+            [&](unsigned k, UpdItem it) {
+                it.x.x = __fma_rn(alpha, it.p.x, it.x.x);
+                it.x.y = __fma_rn(alpha, it.p.y, it.x.y);
+                it.r.x = __fma_rn(malpha, it.a.x, it.r.x);
+                it.r.y = __fma_rn(malpha, it.a.y, it.r.y);
+                x[k] = it.x;
+                r[k] = it.r;
+                store_pair(b0, k, it.r.x, it.r.y);
+                rr = __fma_rn(it.r.x, it.r.x, rr);
+                rr = __fma_rn(it.r.y, it.r.y, rr);
+            });
+    } else {
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha_x = alpha;
+        stream_pipelined<2 * kUpdU, UpdItemR>(
+            br.begin, br.end, NT,
+            [&](unsigned k) { return UpdItemR{Ap[k], r[k]}; },
+            [&](unsigned k, UpdItemR it) {
+                it.r.x = __fma_rn(malpha, it.a.x, it.r.x);
+                it.r.y = __fma_rn(malpha, it.a.y, it.r.y);
+                r[k] = it.r;
+                store_pair(b0, k, it.r.x, it.r.y);
+                rr = __fma_rn(it.r.x, it.r.x, rr);
+                rr = __fma_rn(it.r.y, it.r.y, rr);
+            });
+    }
     pdl_trigger();
     block_sum2(rr, unused);
     if (publish2(rr, unused, part, maxb, &ctl->ticket[SL_UPDATE])) {
@@ -222,6 +242,24 @@ __global__ void __launch_bounds__(NT)
             }
         }
     }
+}
+
+// x += alpha p with the alpha k_update64<T, false> left in ctl->alpha_x (0:
+// nothing pending), the same rounding as the fused update. It runs beside the
+// V-cycle of the next iteration (or after the loop for the last one) and
+// before the p update of that iteration, which clears alpha_x.
+struct XItem {
+    double2 p, x;
+};
+__global__ void __launch_bounds__(NT)
+    k_update_x64(unsigned n2, const double2* __restrict__ p, double2* __restrict__ x, const Ctl* ctl) {
+    const double alpha = *(volatile const double*)&ctl->alpha_x;
+    if (alpha == 0.0) return;
+    stream_pipelined<4, XItem>(
+        blockIdx.x * NT + threadIdx.x, n2, gridDim.x * NT, [&](unsigned k) { return XItem{p[k], x[k]}; },
+        [&](unsigned k, const XItem& it) {
+            x[k] = make_double2(__fma_rn(alpha, it.p.x, it.x.x), __fma_rn(alpha, it.p.y, it.x.y));
+        });
 }
 
 // rz = r.z (and z.Ap for the flexible beta); beta (src/pcg3d_gpu.cu:239-247,
@@ -307,9 +345,12 @@ struct PItem {
 };
 template <class T>
 __global__ void __launch_bounds__(NT)
-    k_update_p64(unsigned n2, const T* __restrict__ z, double2* __restrict__ p, const Ctl* ctl,
+    k_update_p64(unsigned n2, const T* __restrict__ z, double2* __restrict__ p, Ctl* ctl,
                  Cond cond) {
     pdl_enter();
+    // the pending x update (k_update_x64) has run by now: none pending after
+    // this point, also when the loop has ended
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha_x = 0.0;
     if (loop_done(ctl, cond)) return;
     const double beta = ctl->beta;
     const Range br = block_range<2 * kPU>(n2);
@@ -422,21 +463,37 @@ void launch_residual64(cudaStream_t st, MgType mt, const OpView& o, unsigned n, 
 }
 
 void launch_update64(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap, double* x,
-                     double* r, void* b0, Ctl* ctl, const Red& red, Cond cond) {
+                     double* r, void* b0, Ctl* ctl, const Red& red, Cond cond, bool write_x) {
     const unsigned n2 = n / 2;
     const auto* p2 = reinterpret_cast<const double2*>(p);
     const auto* a2 = reinterpret_cast<const double2*>(Ap);
     auto* x2 = reinterpret_cast<double2*>(x);
     auto* r2 = reinterpret_cast<double2*>(r);
+    // (wave_blocks once per kernel: the four have their own occupancies)
+    auto go = [&](auto kern, int wb, auto* b) {
+        launch_pdl(kern, std::min(red.blocks, wb), NT, 0, st, n2, p2, a2, x2, r2, b, ctl, red.part, red.maxb,
+                   cond);
+    };
     if (mt == MG_F64) {
-        static const int wb = wave_blocks(k_update64<double>, 1 << 30);
-        launch_pdl(k_update64<double>, std::min(red.blocks, wb), NT, 0, st, n2, p2, a2, x2, r2, (double*)b0, ctl,
-                   red.part, red.maxb, cond);
+        static const int wb1 = wave_blocks(k_update64<double, true>, 1 << 30);
+        static const int wb0 = wave_blocks(k_update64<double, false>, 1 << 30);
+        if (write_x) go(k_update64<double, true>, wb1, (double*)b0);
+        else go(k_update64<double, false>, wb0, (double*)b0);
     } else {
-        static const int wb = wave_blocks(k_update64<float>, 1 << 30);
-        launch_pdl(k_update64<float>, std::min(red.blocks, wb), NT, 0, st, n2, p2, a2, x2, r2, (float*)b0, ctl,
-                   red.part, red.maxb, cond);
+        static const int wb1 = wave_blocks(k_update64<float, true>, 1 << 30);
+        static const int wb0 = wave_blocks(k_update64<float, false>, 1 << 30);
+        if (write_x) go(k_update64<float, true>, wb1, (float*)b0);
+        else go(k_update64<float, false>, wb0, (float*)b0);
     }
+}
+
+void launch_update_x(cudaStream_t st, unsigned n, const double* p, double* x, const Ctl* ctl, int blocks) {
+    static const int wb = wave_blocks(k_update_x64, 1 << 30);
+    const unsigned n2 = n / 2;
+    unsigned want = std::max(1u, (n2 + NT * 4 - 1) / (NT * 4));
+    if (blocks > 0) want = std::min(want, (unsigned)blocks);
+    k_update_x64<<<(int)std::min(want, (unsigned)wb), NT, 0, st>>>(n2, reinterpret_cast<const double2*>(p),
+                                                                    reinterpret_cast<double2*>(x), ctl);
 }
 
 void launch_dot64(cudaStream_t st, MgType mt, bool flexible, unsigned n, const double* r, const void* z,

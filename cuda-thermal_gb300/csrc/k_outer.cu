@@ -453,9 +453,9 @@ void launch_apply(cudaStream_t st, const OpView& o, const double* diag, const do
 }
 
 void launch_update(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap,
-                   double* x, double* r, void* b0, Ctl* ctl, const Red& red, Cond cond) {
+                   double* x, double* r, void* b0, Ctl* ctl, const Red& red, Cond cond, bool write_x) {
     if (mt != MG_NONE) {
-        launch_update64(st, mt, n, p, Ap, x, r, b0, ctl, red, cond);
+        launch_update64(st, mt, n, p, Ap, x, r, b0, ctl, red, cond, write_x);
         return;
     }
     static const int wb = wave_blocks(k_update, 1 << 30);

@@ -93,9 +93,10 @@ void launch_residual(cudaStream_t st, MgType mt, const OpView& o, const double* 
 // Ap = (A + C/dt) p; p.Ap; alpha = rz / p.Ap.
 void launch_apply(cudaStream_t st, const OpView& o, const double* diag, const double* p,
                   double* Ap, Ctl* ctl, const Red& red, Cond cond);
-// x += alpha p, r -= alpha Ap, b0 = r; rr; convergence test.
+// x += alpha p, r -= alpha Ap, b0 = r; rr; convergence test (write_x =
+// false, FP64 outer loop only: x left to launch_update_x).
 void launch_update(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap,
-                   double* x, double* r, void* b0, Ctl* ctl, const Red& red, Cond cond);
+                   double* x, double* r, void* b0, Ctl* ctl, const Red& red, Cond cond, bool write_x = true);
 // rz = r.z (and z.Ap for the flexible beta); beta. z = V-cycle result
 // (mt = MG_F32 / MG_F64) or r * invd (mt = MG_NONE, Jacobi).
 void launch_dot(cudaStream_t st, MgType mt, bool flexible, unsigned n, const double* r,
@@ -114,8 +115,13 @@ void launch_residual64(cudaStream_t st, MgType mt, const OpView& o, unsigned n, 
                        Cond cond);
 void launch_apply64(cudaStream_t st, const OpView& o, const double* diag, const double* p,
                     double* Ap, Ctl* ctl, const Red& red, Cond cond);
+// write_x = false: r only; alpha left in ctl->alpha_x for launch_update_x.
 void launch_update64(cudaStream_t st, MgType mt, unsigned n, const double* p, const double* Ap, double* x,
-                     double* r, void* b0, Ctl* ctl, const Red& red, Cond cond);
+                     double* r, void* b0, Ctl* ctl, const Red& red, Cond cond, bool write_x = true);
+// x += ctl->alpha_x p where an update is pending (a plain launch: it runs
+// beside other work and is ordered by events, not by programmatic launch), on
+// at most `blocks` blocks (0: as many as the vector wants, up to one wave).
+void launch_update_x(cudaStream_t st, unsigned n, const double* p, double* x, const Ctl* ctl, int blocks);
 void launch_dot64(cudaStream_t st, MgType mt, bool flexible, unsigned n, const double* r, const void* z,
                   const double* Ap, Ctl* ctl, const Red& red, Cond cond);
 void launch_update_p64(cudaStream_t st, MgType mt, unsigned n, const void* z, double* p, Ctl* ctl,

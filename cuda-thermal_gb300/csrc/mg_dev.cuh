@@ -492,7 +492,7 @@ constexpr int kSmallDone = 0, kSmallTimeout = 1, kSmallClosed = 2;
 
 template <class T, int MZ, class Wait, class Go>
 __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double* inv_dt_src,
-                                           unsigned char* smem, Wait wait, Go go) {
+                                           unsigned char* smem, Wait wait, Go go, bool col_sweeps = false) {
     __shared__ Geo sg[kMaxTail];      // level geometry
     __shared__ unsigned soff[kMaxTail];  // byte offset of each level in smem
     __shared__ uint64_t bar, barb;    // operator and factors; level k0's b
@@ -598,6 +598,20 @@ __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double
             for (unsigned w = tid; w < work; w += nth) {
                 const int l = (int)(w / ccols);
                 restrict_cell<T, false>(L, C, inv_dt, w - (unsigned)l * ccols, l);
+            }
+        } else if (sizeof(T) == 4 && MZ > 0 && kind != 0 && col_sweeps) {
+            // One thread per column gathers every plane's right-hand side
+            // (branch-free, all loads in flight at once) and runs the
+            // recurrence: one block barrier a sweep instead of two (FP32
+            // only: the FP64 columns' registers would spill).
+            if constexpr (sizeof(T) == 4 && MZ > 0) {
+                for (unsigned q = tid; q < ncol; q += nth) {
+                    if (kind == 1)
+                        sweep_column<T, MZ, false, false, false, true>(L, L, color, q);
+                    else
+                        sweep_column<T, MZ, false, true, false, true>(
+                            L, small_view<T>(smem + soff[k + 1], sg[k + 1]), 1, q);
+                }
             }
         } else if constexpr (MZ > 0) {
             // A sweep in two steps: one task per column and plane gathers

@@ -113,7 +113,12 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
         own_stream = false;  // a batch's stream
     else
         CT_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    if (!skip_graphs) CT_CK(cudaStreamCreateWithFlags(&st_body, cudaStreamNonBlocking));
+    if (!skip_graphs) {
+        CT_CK(cudaStreamCreateWithFlags(&st_body, cudaStreamNonBlocking));
+        CT_CK(cudaStreamCreateWithFlags(&st_side, cudaStreamNonBlocking));
+        CT_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        CT_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    }
     cs = st;
     CT_CK(cudaMallocHost(&h_ctl, sizeof(Ctl)));
     std::memset(h_ctl, 0, sizeof(Ctl));
@@ -230,6 +235,18 @@ ct_status Solver::create(const ct_model* m_in, ct_precond pc_, ct_precision prec
     // three operand streams faster than the tile ring (800 x 800 x 10 FLEX
     // solve 6.52 -> 6.46 ms). CT_SWEEP0_GRID=0 stages them too.
     if (const char* e = std::getenv("CT_SWEEP0_GRID")) sweep0_grid = e[0] != '0';
+    // x += alpha p leaves the update (which then moves 24 B a cell fewer on
+    // the iteration's critical path) for a launch of a few blocks beside the
+    // next V-cycle, forked after the restriction out of level 1: it streams x
+    // and p while the coarse levels, latency-bound, leave the memory system
+    // idle (800 x 800 FLEX solve 155.3 -> 157.8 solves/s at 64 blocks; 16 /
+    // 32 / 128 / 192 blocks: 145.7 / 155.4 / 157.6 / 156.8; forked after
+    // level 0's restriction: 156.3; the whole grid at once: 154.3).
+    // CT_XLAG = k forks after level k's restriction instead, -1 keeps x in
+    // the update; CT_XLAG_BLOCKS sets the blocks.
+    if (const char* e = std::getenv("CT_XLAG")) xlag = std::atoi(e);
+    xlag_blocks = std::max(1, sms * 64 / 152);
+    if (const char* e = std::getenv("CT_XLAG_BLOCKS")) xlag_blocks = std::max(1, std::atoi(e));
     // Tensor maps of the levels whose sweeps are staged by bulk tensor copies
     // (FP32 levels with at least one full tile row, above the shared-memory
     // levels); CT_SWEEP_TMA=0 keeps every level on the grid kernels. Levels of
@@ -401,6 +418,7 @@ void Solver::vcycle(size_t k, Cond cond, bool first_sweep_done) {
             [&] { launch_restrict_sweep0<T>(cs, L, C, ctl, cond); });
     else
         enq(("mg_restrict" + lvl).c_str(), b_restrict, [&] { launch_restrict<T>(cs, L, C, ctl, cond); });
+    if (lag_now && (int)k == fork_level()) fork_x();
     vcycle<T>(k + 1, cond, fuse);
     enq(("mg_sweep" + lvl).c_str(), b_sweep + cells / 4 * t,
         [&] { sweep<T>(k, L, 1, false, &C, cond); });
@@ -447,6 +465,10 @@ void Solver::enqueue_body(Cond cond) {
         });
         return;
     }
+    // x += alpha p of the previous iteration beside this V-cycle (x_lag())
+    lag_now = x_lag();
+    forked = false;
+    if (lag_now && fork_level() >= (int)lv.size()) fork_x();
     if (mt == MG_F32) {
         vcycle<float>(0, cond);
         z = base + lv[0].o_x;
@@ -454,14 +476,30 @@ void Solver::enqueue_body(Cond cond) {
         vcycle<double>(0, cond);
         z = base + lv[0].o_x;
     }
+    if (lag_now && !forked) fork_x();
     const double zb = mt == MG_NONE ? 16.0 : (double)tsize;
     enq("pcg_dot", N * (8 + zb + (flex ? 8 : 0)),
         [&] { launch_dot(cs, mt, flex, n, r, z, invd, Ap, ctl, red_vec(SL_DOT), cond); });
+    // the p update overwrites the p that the x update reads: join first
+    if (lag_now && !prof) cudaStreamWaitEvent(cs, ev_join, 0);
     enq("pcg_update_p", N * (zb + 16), [&] { launch_update_p(cs, mt, n, z, r, invd, p, ctl, cond); });
     enq("pcg_apply", N * 36, [&] { launch_apply(cs, op(), diag, p, Ap, ctl, red_cols(SL_APPLY), cond); });
     void* b0 = mt == MG_NONE ? nullptr : (void*)(base + lv[0].o_b);
-    enq("pcg_update_xr", N * (48 + (mt == MG_NONE ? 0 : tsize)),
-        [&] { launch_update(cs, mt, n, p, Ap, x, r, b0, ctl, red_vec(SL_UPDATE), cond); });
+    enq("pcg_update_xr", N * ((lag_now ? 24 : 48) + (mt == MG_NONE ? 0 : tsize)),
+        [&] { launch_update(cs, mt, n, p, Ap, x, r, b0, ctl, red_vec(SL_UPDATE), cond, !lag_now); });
+    lag_now = false;
+}
+
+void Solver::fork_x() {
+    forked = true;
+    if (prof) {  // timed in line, on as many blocks as it wants
+        enq("pcg_update_x", (double)ncells * 24, [&] { launch_update_x(cs, n, p, x, ctl, 0); });
+        return;
+    }
+    cudaEventRecord(ev_fork, cs);
+    cudaStreamWaitEvent(st_side, ev_fork, 0);
+    launch_update_x(st_side, n, p, x, ctl, xlag_blocks);
+    cudaEventRecord(ev_join, st_side);
 }
 
 ct_status Solver::record_graphs() {
@@ -512,6 +550,7 @@ ct_status Solver::record_graphs() {
             cs = st;
             enqueue_init(Cond{h1, 1});
             ok = add_while(h1);
+            if (ok && x_lag()) launch_update_x(st, n, p, x, ctl, 0);  // the last iteration's x update
             if (ok && dw) {
                 enqueue_replace(Cond{h2, 1});
                 ok = add_while(h2);
@@ -606,6 +645,7 @@ ct_status Solver::solve(double tol, int maxit, ct_stats* out) {
             launched += k;
             if (graphs) k = std::min(k * 2, 8);
         }
+        if (x_lag()) launch_update_x(st, n, p, x, ctl, 0);  // the last iteration's x update
     }
     CT_CK(cudaGetLastError());
     return finish_solve(out);

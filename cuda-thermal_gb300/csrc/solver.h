@@ -85,6 +85,21 @@ class Solver {
     size_t small_k0 = 0;   // levels from small_k0 down run in one block from shared memory
     bool fuse_sweep0 = true;  // a level's first (x = 0) sweep rides with the restriction into it
     bool sweep0_grid = true;  // x = 0 sweeps of the staged levels on the grid kernel
+    // x += alpha p beside the next V-cycle (FP64 outer loop, multigrid): a
+    // launch of xlag_blocks blocks on st_side, forked after the restriction
+    // out of level fork_level() (xlag < 0: x stays in the update)
+    int xlag = 1;
+    int xlag_blocks = 64;
+    cudaStream_t st_side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool lag_now = false, forked = false;  // while a body is enqueued
+    bool x_lag() const { return xlag >= 0 && !dw && mt != MG_NONE && st_side; }
+    // the last level with a restriction out of it, at most xlag (a V-cycle
+    // all in the shared-memory bottom: lv.size(), the start of the body)
+    int fork_level() const {
+        return small_k0 == 0 ? (int)lv.size() : std::min(xlag, (int)small_k0 - 1);
+    }
+    void fork_x();
     cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
     ct_setup_times times{};
     // per-kernel timing (ct_profile_solve)
@@ -101,6 +116,9 @@ class Solver {
         if (base) cudaFree(base);
         if (h_ctl) cudaFreeHost(h_ctl);
         if (st_body) cudaStreamDestroy(st_body);
+        if (st_side) cudaStreamDestroy(st_side);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
         if (st && own_stream) cudaStreamDestroy(st);
     }
 

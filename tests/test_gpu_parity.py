@@ -358,6 +358,36 @@ def test_staged_sweeps_bitwise_single_and_batch(ct, n, prec, tmp_path):
     assert np.array_equal(out[0], out[1])
 
 
+@pytest.mark.parametrize("mode", ["graph", "parts", "direct"])
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32", "MG_FP64", "MG_FP32_FLEX_DW"])
+@pytest.mark.parametrize("n,lag", [(130, "0"), (130, "1"), (130, "99"), (37, "1"), (9, "1")])
+def test_lagged_x_update_bitwise(ct, prec, n, lag, mode):
+    """x += alpha p run beside the next V-cycle (forked after the restriction
+    out of level `lag`, the last restricted level for 99, or at the start of
+    the iteration when the whole V-cycle is the shared-memory bottom, n = 9)
+    and once after the loop gives the fused update's fields and iteration
+    counts bit for bit: steady solve, two backward-Euler steps, and a solve
+    stopped by maxit (its last update still pending when the loop ends); one
+    conditional graph, part graphs polled by the host, or direct launches."""
+    import workloads
+    m = workloads.steady_hotspot(n, seed=23)
+    ct.gpu_use_graphs(mode != "direct")
+    try:
+        out = []
+        for flag in ("-1", lag):
+            with env_vars(CT_XLAG=flag, CT_COND_GRAPHS="0" if mode == "parts" else None):
+                res = steady_then_steps(ct, m, prec)
+                with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
+                    s.set_x_zero()
+                    s.set_rhs_steady()
+                    st = s.solve(1e-10, 3)
+                    res += [(st.iters, st.converged), s.get_x()]
+                out.append(res)
+    finally:
+        ct.gpu_use_graphs(True)
+    assert_same_results(out[0], out[1])
+
+
 @pytest.mark.parametrize("prec", ["MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
 @pytest.mark.parametrize("n", [203, 130, 37])
 def test_fused_first_sweep_bitwise(ct, n, prec):
@@ -453,18 +483,20 @@ def test_small_level_split_sweeps_bitwise_deep(ct, cu_planes):
 @pytest.mark.parametrize("prec", ["MG_FP32_FLEX_DW", "MG_FP32", "MG_FP64"])
 @pytest.mark.parametrize("n", [203, 64, 9])
 def test_shared_memory_bottom_bitwise(ct, n, prec):
-    """The bottom levels run by one block out of shared memory (its sweeps
-    gather every plane's right-hand side with one task per column and plane
-    before the recurrences) give the grid-wide launches' results
-    (CT_SMALL_BYTES=0: no shared-memory bottom) bit for bit: steady solve,
-    then two backward-Euler steps."""
+    """The bottom levels run by one block out of shared memory give the
+    grid-wide launches' results (CT_SMALL_BYTES=0: no shared-memory bottom)
+    bit for bit, with its FP32 sweeps one thread per column (the default) or
+    gathering every plane's right-hand side with one task per column and
+    plane before the recurrences (CT_SMALL_COL_SWEEPS=0, the FP64 form):
+    steady solve, then two backward-Euler steps."""
     import workloads
     m = workloads.steady_hotspot(n, seed=17)
     out = []
-    for flag in ("0", None):
-        with env_vars(CT_SMALL_BYTES=flag):
+    for flags in ({"CT_SMALL_BYTES": "0"}, {}, {"CT_SMALL_COL_SWEEPS": "0"}):
+        with env_vars(**flags):
             out.append(steady_then_steps(ct, m, prec))
     assert_same_results(out[0], out[1])
+    assert_same_results(out[0], out[2])
 
 
 def test_bounded_wait_runs_out_and_context_survives(ct):
