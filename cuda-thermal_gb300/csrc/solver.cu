@@ -690,6 +690,65 @@ ct_status Solver::solve_wait(ct_stats* out) {
     return finish_solve(out);
 }
 
+ct_status Solver::ensure_copy_queues() {
+    if (st_h2d) return CT_OK;
+    CT_CK(cudaStreamCreateWithFlags(&st_h2d, cudaStreamNonBlocking));
+    CT_CK(cudaStreamCreateWithFlags(&st_d2h, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+        CT_CK(cudaMalloc(&nat_in[i], ncells * 8));
+        CT_CK(cudaMalloc(&nat_out[i], ncells * 8));
+        for (cudaEvent_t* e : {&ev_in_copied[i], &ev_in_used[i], &ev_out_ready[i], &ev_out_copied[i]})
+            CT_CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    return CT_OK;
+}
+
+ct_status Solver::set_power_async(const double* P_host) {
+    const ct_status s0 = ensure_copy_queues();
+    if (s0 != CT_OK) return s0;
+    const int i = (int)(n_in & 1u);
+    // The copy waits for the conversion of the previous copy in (in stream
+    // order after the one that last used this buffer), not for the solves
+    // queued since: it overlaps them. The first waits for the solver's stream
+    // as it stands.
+    if (n_in == 0) CT_CK(cudaEventRecord(ev_in_used[1], st));
+    CT_CK(cudaStreamWaitEvent(st_h2d, ev_in_used[1 - i], 0));
+    CT_CK(cudaMemcpyAsync(nat_in[i], P_host, ncells * 8, cudaMemcpyHostToDevice, st_h2d));
+    CT_CK(cudaEventRecord(ev_in_copied[i], st_h2d));
+    CT_CK(cudaStreamWaitEvent(st, ev_in_copied[i], 0));
+    launch_to_split_d(st, g0, nat_in[i], P);
+    CT_CK(cudaGetLastError());
+    CT_CK(cudaEventRecord(ev_in_used[i], st));
+    ++n_in;
+    return CT_OK;
+}
+
+ct_status Solver::get_x_async(double* T_host) {
+    const ct_status s0 = ensure_copy_queues();
+    if (s0 != CT_OK) return s0;
+    const int j = (int)(n_out & 1u);
+    // refill this buffer only once its previous copy out is done
+    if (n_out >= 2) CT_CK(cudaStreamWaitEvent(st, ev_out_copied[j], 0));
+    launch_to_natural_d(st, g0, x_as_double(nullptr), nat_out[j]);
+    CT_CK(cudaGetLastError());
+    CT_CK(cudaEventRecord(ev_out_ready[j], st));
+    CT_CK(cudaStreamWaitEvent(st_d2h, ev_out_ready[j], 0));
+    CT_CK(cudaMemcpyAsync(T_host, nat_out[j], ncells * 8, cudaMemcpyDeviceToHost, st_d2h));
+    CT_CK(cudaEventRecord(ev_out_copied[j], st_d2h));
+    ++n_out;
+    return CT_OK;
+}
+
+ct_status Solver::copies_wait() {
+    if (!st_h2d) return CT_OK;
+    // the solver's stream then orders after every copy queued so far
+    if (n_out > 0) CT_CK(cudaStreamWaitEvent(st, ev_out_copied[(n_out - 1) & 1u], 0));
+    CT_CK(cudaStreamSynchronize(st_h2d));
+    CT_CK(cudaStreamSynchronize(st_d2h));
+    CT_CK(cudaStreamSynchronize(st));
+    return CT_OK;
+}
+
 ct_status Solver::finish_solve(ct_stats* out) {
     CT_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     CT_CK(cudaStreamSynchronize(st));
@@ -938,6 +997,23 @@ ct_status ct_solve_async(ct_solver* s, double tol, int maxit) {
 ct_status ct_solve_wait(ct_solver* s, ct_stats* st) {
     CT_SOLVER_OK(s);
     return s->impl.solve_wait(st);
+}
+
+ct_status ct_set_power_async(ct_solver* s, const double* P) {
+    CT_SOLVER_OK(s);
+    if (!P) return fail(CT_BAD_ARG, "ct_set_power_async: null");
+    return s->impl.set_power_async(P);
+}
+
+ct_status ct_get_x_async(ct_solver* s, double* T) {
+    CT_SOLVER_OK(s);
+    if (!T) return fail(CT_BAD_ARG, "ct_get_x_async: null");
+    return s->impl.get_x_async(T);
+}
+
+ct_status ct_copies_wait(ct_solver* s) {
+    CT_SOLVER_OK(s);
+    return s->impl.copies_wait();
 }
 
 ct_status ct_get_x(ct_solver* s, double* T) {

@@ -100,6 +100,18 @@ class Solver {
         return small_k0 == 0 ? (int)lv.size() : std::min(xlag, (int)small_k0 - 1);
     }
     void fork_x();
+    // queued host copies (ct_set_power_async, ct_get_x_async): two staging
+    // buffers each way, a copy stream each way, events that keep a buffer
+    // from being refilled before it is consumed
+    cudaStream_t st_h2d = nullptr, st_d2h = nullptr;
+    double* nat_in[2] = {nullptr, nullptr};
+    double* nat_out[2] = {nullptr, nullptr};
+    cudaEvent_t ev_in_copied[2] = {}, ev_in_used[2] = {}, ev_out_ready[2] = {}, ev_out_copied[2] = {};
+    unsigned long long n_in = 0, n_out = 0;
+    ct_status ensure_copy_queues();
+    ct_status set_power_async(const double* P_host);
+    ct_status get_x_async(double* T_host);
+    ct_status copies_wait();
     cudaGraphExec_t gx_solve = nullptr, gx_init = nullptr, gx_body = nullptr, gx_replace = nullptr;
     ct_setup_times times{};
     // per-kernel timing (ct_profile_solve)
@@ -110,13 +122,20 @@ class Solver {
     bool skip_graphs = false; // batch members record no graphs of their own
 
     ~Solver() {
-        if (st) cudaStreamSynchronize(st);
+        for (cudaStream_t q : {st, st_side, st_h2d, st_d2h})
+            if (q) cudaStreamSynchronize(q);
         for (cudaGraphExec_t g : {gx_solve, gx_init, gx_body, gx_replace})
             if (g) cudaGraphExecDestroy(g);
         if (base) cudaFree(base);
         if (h_ctl) cudaFreeHost(h_ctl);
-        if (st_body) cudaStreamDestroy(st_body);
-        if (st_side) cudaStreamDestroy(st_side);
+        for (int i = 0; i < 2; ++i) {
+            for (cudaEvent_t e : {ev_in_copied[i], ev_in_used[i], ev_out_ready[i], ev_out_copied[i]})
+                if (e) cudaEventDestroy(e);
+            if (nat_in[i]) cudaFree(nat_in[i]);
+            if (nat_out[i]) cudaFree(nat_out[i]);
+        }
+        for (cudaStream_t q : {st_body, st_side, st_h2d, st_d2h})
+            if (q) cudaStreamDestroy(q);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
         if (st && own_stream) cudaStreamDestroy(st);

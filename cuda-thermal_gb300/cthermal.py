@@ -102,6 +102,9 @@ def _signatures():
         "ct_solve_async": (i, [vp, d, i]),
         "ct_solve_wait": (i, [vp, C.POINTER(CtStats)]),
         "ct_get_x": (i, [vp, vp]),
+        "ct_set_power_async": (i, [vp, vp]),
+        "ct_get_x_async": (i, [vp, vp]),
+        "ct_copies_wait": (i, [vp]),
         "ct_device_x": (i, [vp, C.POINTER(vp)]),
         "ct_solver_setup_times": (i, [vp, C.POINTER(CtSetupTimes)]),
         "ct_solver_stream": (i, [vp, C.POINTER(vp)]),
@@ -739,6 +742,26 @@ class GpuPcg:
         T = out if out is not None else np.empty(self.n)
         _check(lib().ct_get_x(self._h, _ptr(T)))
         return T
+
+    def set_power_async(self, P: np.ndarray) -> None:
+        """Queues the copy of P (float64, contiguous; pinned host memory for
+        the copy to overlap the solves) and its conversion
+        (ct_set_power_async). P must stay unchanged until copies_wait()."""
+        assert P.dtype == np.float64 and P.flags.c_contiguous and P.size == self.n
+        self.__dict__.setdefault("_pending", []).append(P)
+        _check(lib().ct_set_power_async(self._h, _ptr(P)))
+
+    def get_x_async(self, out: np.ndarray) -> None:
+        """Queues x's copy into `out` after the solves queued so far
+        (ct_get_x_async); `out` holds it once copies_wait() returns."""
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.n
+        self.__dict__.setdefault("_pending", []).append(out)
+        _check(lib().ct_get_x_async(self._h, _ptr(out)))
+
+    def copies_wait(self) -> None:
+        """Blocks until every queued copy and the solver's stream are done."""
+        _check(lib().ct_copies_wait(self._h))
+        self._pending = []
 
     def device_x(self) -> int:
         p = C.c_void_p()

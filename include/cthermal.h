@@ -192,6 +192,19 @@ ct_status ct_solve(ct_solver* s, double tol, int maxit, ct_stats* st);
  * returns and ct_solve_wait reports it. */
 ct_status ct_solve_async(ct_solver* s, double tol, int maxit);
 ct_status ct_solve_wait(ct_solver* s, ct_stats* st);
+/* No counterpart in the reference. The host copies of a power-map sweep,
+ * queued beside the solves: ct_set_power_async copies P (host memory, pinned
+ * for the copy to overlap) into one of two device staging buffers on a copy
+ * stream of its own, and the solver's stream converts it into the solver's P
+ * once it has landed; ct_get_x_async converts x on the solver's stream (after
+ * the solves queued so far) into one of two staging buffers and copies it to
+ * T on a second copy stream. So the copy in of the next step and the copy
+ * out of the previous one run while the current step solves. The caller
+ * keeps P unchanged and reads T only after ct_copies_wait, which blocks until
+ * every queued copy (and the solver's stream) is done. */
+ct_status ct_set_power_async(ct_solver* s, const double* P);
+ct_status ct_get_x_async(ct_solver* s, double* T);
+ct_status ct_copies_wait(ct_solver* s);
 /* GpuPcg::get_x (src/pcg3d_gpu.cu:548-552): x to host memory. */
 ct_status ct_get_x(ct_solver* s, double* T);
 /* GpuPcg::device_x (src/pcg3d.h:130): device pointer to x in the natural
