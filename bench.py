@@ -650,7 +650,8 @@ def bench_transient_800(ct, np, solvers, m, steps):
     with the power on at t = 0 (run_transient, src/transient3d.h:48-90), dt
     10 us growing 10 % per step up to 50 ms, tol 1e-9, each step warm-started
     from the last; per step set_dt, b = P + C/dt T, the solve and the step
-    record (T_max, heat out, heat stored reduced on the device). The FP32
+    record (T_max, heat out, heat stored reduced on the device), all queued
+    on the solver's stream with one wait at the end. The FP32
     V-cycle in FP64 flexible PCG (and the double-word form) against the plain
     FP64 MG-PCG on the same steps; the solvers already hold the operator and
     hierarchy."""
@@ -658,20 +659,41 @@ def bench_transient_800(ct, np, solvers, m, steps):
     res = {}
     for name, s in solvers.items():
         s.set_x_zero()
-        dt, last, its, eb = TR_DT0, -1.0, 0, 0.0
+        dt, last = TR_DT0, -1.0
+        # every step queued on the solver's stream (ct_solve_async and the
+        # step record into the device table), one wait at the end
         t0 = time.perf_counter()
         for k in range(steps):
             if dt != last:
                 s.set_dt(dt)
                 last = dt
             s.set_rhs_transient()
-            its += s.solve(TR_TOL, MAXIT).iters
-            rec = s.step_record(dt)
-            eb = max(eb, abs(rec.q_out + rec.q_stored - ptot) / ptot)
+            s.solve_async(TR_TOL, MAXIT)
+            s.step_record_async(dt, k)
             dt = min(dt * TR_GROWTH, TR_DT_MAX)
+        recs, sts = s.step_records(0, steps)
         sec = time.perf_counter() - t0
-        res[name] = dict(sec=sec, iters=its, eb=eb, T=s.get_x(), T_max=rec.T_max)
+        its = sum(st.iters for st in sts)
+        eb = max(abs(r.q_out + r.q_stored - ptot) / ptot for r in recs)
+        assert all(st.converged for st in sts)
+        res[name] = dict(sec=sec, iters=its, eb=eb, T=s.get_x(), T_max=recs[-1].T_max)
         s.set_dt(0.0)
+    # the same FLEX steps with blocking calls (ct_solve, ct_solver_step_record)
+    s = solvers["flex"]
+    s.set_x_zero()
+    dt, last, its_b = TR_DT0, -1.0, 0
+    t0 = time.perf_counter()
+    for k in range(steps):
+        if dt != last:
+            s.set_dt(dt)
+            last = dt
+        s.set_rhs_transient()
+        its_b += s.solve(TR_TOL, MAXIT).iters
+        s.step_record(dt)
+        dt = min(dt * TR_GROWTH, TR_DT_MAX)
+    sec_b = time.perf_counter() - t0
+    same_b = bool(np.array_equal(s.get_x(), res["flex"]["T"])) and its_b == res["flex"]["iters"]
+    s.set_dt(0.0)
     fx, f64 = res["flex"], res["fp64"]
     out = {
         "value": steps / fx["sec"], "unit": "steps/s", "precision": "CT_MG_FP32_FLEX",
@@ -684,6 +706,8 @@ def bench_transient_800(ct, np, solvers, m, steps):
                         "energy_balance_err_max": f64["eb"]},
         "speedup_vs_fp64": f64["sec"] / fx["sec"],
         "max_dT_K_vs_fp64": float(np.abs(fx["T"] - f64["T"]).max()),
+        "blocking": {"value": steps / sec_b, "unit": "steps/s", "same_bits": same_b,
+                     "calls": "ct_solve and ct_solver_step_record per step (the host waits twice a step)"},
     }
     if "dw" in res:
         dw = res["dw"]

@@ -548,4 +548,23 @@ void launch_step_record(cudaStream_t st, const OpView& o, const double* x, const
     k_step_record<<<red.blocks, NT, 0, st>>>(o, x, xold, ctl, red.part, red.maxb);
 }
 
+// A step's record (the step-record sums and the last solve's statistics) into
+// entry `slot` of the device table.
+__global__ void k_record_keep(const Ctl* ctl, double dt, StepEntry* table, int slot) {
+    StepEntry e;
+    e.T_max = ctl->aux0;
+    e.q_out = ctl->aux1;
+    e.q_stored = ctl->aux2 / dt;  // IEEE division, as ct_solver_step_record divides on the host
+    e.relres = ctl->relres;
+    e.iters = ctl->iter;
+    e.converged = ctl->converged;
+    e.breakdown = ctl->breakdown;
+    e.err = ctl->err;
+    table[slot] = e;
+}
+
+void launch_record_keep(cudaStream_t st, const Ctl* ctl, double dt, StepEntry* table, int slot) {
+    k_record_keep<<<1, 1, 0, st>>>(ctl, dt, table, slot);
+}
+
 }  // namespace ct

@@ -167,6 +167,12 @@ void launch_true_residual(cudaStream_t st, const OpView& o, const double* P, con
 // ctl->aux0 = T_max, aux1 = heat out, aux2 = sum cap (x - xold).
 void launch_step_record(cudaStream_t st, const OpView& o, const double* x, const double* xold,
                         Ctl* ctl, const Red& red);
+// One entry of the device table of queued step records.
+struct StepEntry {
+    double T_max, q_out, q_stored, relres;
+    int iters, converged, breakdown, err;
+};
+void launch_record_keep(cudaStream_t st, const Ctl* ctl, double dt, StepEntry* table, int slot);
 
 // ---- double-word outer PCG (FP32 pipes), k_dw.cu -----------------------------
 // r = b - A x in FP64 from the double-word x; start of a solve, or the residual

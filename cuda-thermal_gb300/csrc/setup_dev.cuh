@@ -43,22 +43,28 @@ __device__ __forceinline__ T diag_rn(const LevelView<T>& L, int i, int j, int l,
     return RN<T>::add(d, RN<T>::mul((T)L.cap[id], inv_dt));
 }
 
-// Thomas factors of natural column q = j nx + i of a level.
+// Thomas factors of natural column q = j nx + i of a level. The factors are
+// written through restrict pointers, so the operand loads of the next planes
+// may be issued before this plane's stores.
 template <class T>
 __device__ __forceinline__ void factor_column(const LevelView<T>& L, T inv_dt, unsigned q) {
     const Geo& g = L.g;
     const int j = (int)(q / (unsigned)g.nx), i = (int)(q - (unsigned)j * g.nx);
     const unsigned s = scol(g, i, j);
+    T* __restrict__ finv = L.finv;
+    T* __restrict__ fcp = L.fcp;
+    const float* __restrict__ gU = L.gU;
     T cp_prev = 0;
+#pragma unroll 4
     for (int l = 0; l < g.nz; ++l) {
         const unsigned id = (unsigned)l * g.plane + s;
         const T d = diag_rn(L, i, j, l, inv_dt);
-        const T lower = l > 0 ? -(T)L.gU[id - g.plane] : T(0);
-        const T upper = l < g.nz - 1 ? -(T)L.gU[id] : T(0);
+        const T lower = l > 0 ? -(T)gU[id - g.plane] : T(0);
+        const T upper = l < g.nz - 1 ? -(T)gU[id] : T(0);
         const T inv = RN<T>::div(T(1), RN<T>::sub(d, RN<T>::mul(lower, cp_prev)));
-        L.finv[id] = inv;
+        finv[id] = inv;
         cp_prev = RN<T>::mul(upper, inv);
-        L.fcp[id] = cp_prev;
+        fcp[id] = cp_prev;
     }
 }
 
@@ -69,6 +75,7 @@ __device__ __forceinline__ void faces_column(const OpView& o, unsigned q, double
     const Geo& g = o.g;
     const int j = (int)(q / (unsigned)g.nx), i = (int)(q - (unsigned)j * g.nx);
     const unsigned s = scol(g, i, j);
+#pragma unroll 4
     for (int l = 0; l < g.nz; ++l) {
         const unsigned base = (unsigned)l * g.plane, id = base + s;
         double d = 0.0;
@@ -92,9 +99,11 @@ __device__ __forceinline__ void diag_column(const OpView& o, const double* __res
     const Geo& g = o.g;
     const int j = (int)(q / (unsigned)g.nx), i = (int)(q - (unsigned)j * g.nx);
     const unsigned s = scol(g, i, j);
+    const float* __restrict__ cap = o.cap;
+#pragma unroll 4
     for (int l = 0; l < g.nz; ++l) {
         const unsigned id = (unsigned)l * g.plane + s;
-        const double d = __dadd_rn(dface[id], __dmul_rn((double)o.cap[id], inv_dt));
+        const double d = __dadd_rn(dface[id], __dmul_rn((double)cap[id], inv_dt));
         diag[id] = d;
         if (invd) invd[id] = __drcp_rn(d);
         if (dgw) {

@@ -1078,6 +1078,60 @@ ct_status ct_solver_step_record(ct_solver* s, double dt, ct_step_record* out) {
     return CT_OK;
 }
 
+ct_status ct_solver_step_record_async(ct_solver* s, double dt, int slot) {
+    CT_SOLVER_OK(s);
+    if (!(dt > 0) || slot < 0) return fail(CT_BAD_ARG, "ct_solver_step_record_async: dt <= 0 or slot < 0");
+    ct::Solver& v = s->impl;
+    if (slot >= v.rec_cap) {  // grow the table (doubling), keeping the entries so far
+        int cap = std::max(64, v.rec_cap);
+        while (cap <= slot) cap *= 2;
+        ct::StepEntry* t = nullptr;
+        CT_CUDA(cudaMalloc(&t, (size_t)cap * sizeof(ct::StepEntry)));
+        if (v.rec_table) {
+            CT_CUDA(cudaMemcpyAsync(t, v.rec_table, (size_t)v.rec_cap * sizeof(ct::StepEntry),
+                                    cudaMemcpyDeviceToDevice, v.st));
+            CT_CUDA(cudaStreamSynchronize(v.st));
+            CT_CUDA(cudaFree(v.rec_table));
+        }
+        v.rec_table = t;
+        v.rec_cap = cap;
+    }
+    ct::launch_step_record(v.st, v.op(), v.x_as_double(nullptr), v.xold, v.ctl, v.red_cols(ct::SL_AUX));
+    ct::launch_record_keep(v.st, v.ctl, dt, v.rec_table, slot);
+    CT_CUDA(cudaGetLastError());
+    return CT_OK;
+}
+
+ct_status ct_solver_step_records(ct_solver* s, int first, int count, ct_step_record* out, ct_stats* stats) {
+    CT_SOLVER_OK(s);
+    ct::Solver& v = s->impl;
+    if (first < 0 || count < 0 || first + count > v.rec_cap || (count > 0 && !out))
+        return fail(CT_BAD_ARG, "ct_solver_step_records: entries %d..%d outside the table", first, first + count);
+    // a queued solve's statistics are in the table; the wait is this one
+    v.async_pending = 0;
+    std::vector<ct::StepEntry> h((size_t)count);
+    if (count > 0)
+        CT_CUDA(cudaMemcpyAsync(h.data(), v.rec_table + first, (size_t)count * sizeof(ct::StepEntry),
+                                cudaMemcpyDeviceToHost, v.st));
+    CT_CUDA(cudaStreamSynchronize(v.st));
+    bool err = false;
+    for (int k = 0; k < count; ++k) {
+        const ct::StepEntry& e = h[(size_t)k];
+        out[k].T_max = e.T_max;
+        out[k].q_out = e.q_out;
+        out[k].q_stored = e.q_stored;
+        if (stats) {
+            stats[k].iters = e.iters;
+            stats[k].relres = e.relres;
+            stats[k].converged = e.converged;
+            stats[k].breakdown = e.breakdown;
+        }
+        err = err || e.err;
+    }
+    if (err) return fail(CT_TIMEOUT, "a bounded wait for staged level data ran out in a queued step");
+    return CT_OK;
+}
+
 ct_status ct_num_levels(const ct_solver* s, int* nlev) {
     CT_SOLVER_OK(s);
     if (!nlev) return fail(CT_BAD_ARG, "ct_num_levels: null");

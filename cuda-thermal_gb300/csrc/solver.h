@@ -108,6 +108,9 @@ class Solver {
     double* nat_out[2] = {nullptr, nullptr};
     cudaEvent_t ev_in_copied[2] = {}, ev_in_used[2] = {}, ev_out_ready[2] = {}, ev_out_copied[2] = {};
     unsigned long long n_in = 0, n_out = 0;
+    // device table of queued step records (ct_solver_step_record_async)
+    StepEntry* rec_table = nullptr;
+    int rec_cap = 0;
     ct_status ensure_copy_queues();
     ct_status set_power_async(const double* P_host);
     ct_status get_x_async(double* T_host);
@@ -127,6 +130,7 @@ class Solver {
         for (cudaGraphExec_t g : {gx_solve, gx_init, gx_body, gx_replace})
             if (g) cudaGraphExecDestroy(g);
         if (base) cudaFree(base);
+        if (rec_table) cudaFree(rec_table);
         if (h_ctl) cudaFreeHost(h_ctl);
         for (int i = 0; i < 2; ++i) {
             for (cudaEvent_t e : {ev_in_copied[i], ev_in_used[i], ev_out_ready[i], ev_out_copied[i]})

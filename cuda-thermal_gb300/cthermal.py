@@ -110,6 +110,8 @@ def _signatures():
         "ct_solver_stream": (i, [vp, C.POINTER(vp)]),
         "ct_true_relres": (i, [vp, dp]),
         "ct_solver_step_record": (i, [vp, d, C.POINTER(CtStepRecord)]),
+        "ct_solver_step_record_async": (i, [vp, d, i]),
+        "ct_solver_step_records": (i, [vp, i, i, C.POINTER(CtStepRecord), C.POINTER(CtStats)]),
         "ct_num_levels": (i, [vp, ip]),
         "ct_level_dims": (i, [vp, i, ip, ip, ip]),
         "ct_level_operator": (i, [vp, i, vp, vp, vp, vp, vp]),
@@ -788,6 +790,21 @@ class GpuPcg:
         _check(lib().ct_solver_step_record(self._h, float(dt), C.byref(r)))
         return r
 
+    def step_record_async(self, dt, slot: int) -> None:
+        """Queues the step record, with the last queued solve's statistics,
+        into entry `slot` of the device table (ct_solver_step_record_async)."""
+        _check(lib().ct_solver_step_record_async(self._h, float(dt), int(slot)))
+
+    def step_records(self, first: int, count: int):
+        """Waits for the solver's stream and returns entries first ..
+        first + count - 1 of the table: (records, solve statistics)."""
+        recs = (CtStepRecord * max(1, count))()
+        sts = (CtStats * max(1, count))()
+        _check(lib().ct_solver_step_records(self._h, int(first), int(count), recs, sts))
+        return ([recs[k] for k in range(count)],
+                [PcgStats(sts[k].iters, sts[k].relres, bool(sts[k].converged), bool(sts[k].breakdown))
+                 for k in range(count)])
+
     def num_levels(self) -> int:
         v = C.c_int()
         _check(lib().ct_num_levels(self._h, C.byref(v)))
@@ -1095,8 +1112,10 @@ def run_transient(m: Model3D, o: TransientOptions = TransientOptions(),
                   device_records: bool = True) -> TransientResult:
     """run_transient (src/transient3d.h:48-90): backward Euler from T = 0 with
     geometric dt growth. With device_records the per-step T_max, heat out and
-    heat stored are reduced on the GPU and the field stays there until the
-    end; otherwise T is copied to the host every step, as the reference does."""
+    heat stored are reduced on the GPU and every step is queued on the
+    solver's stream (ct_solve_async, ct_solver_step_record_async) with one
+    wait at the end, the field staying on the device; otherwise T is copied
+    to the host every step, as the reference does."""
     t0 = time.perf_counter()
     res = TransientResult()
     s = GpuPcg(m, o.precond, o.precision)
@@ -1104,6 +1123,31 @@ def run_transient(m: Model3D, o: TransientOptions = TransientOptions(),
     T_old = np.zeros(m.ncells())
     t, dt, last_dt = 0.0, o.dt0, -1.0
     k = 0
+    if device_records:
+        steps = []
+        while (k < o.nsteps) if o.nsteps > 0 else (t < o.t_end * (1 - 1e-12)):
+            if o.nsteps <= 0:
+                dt = min(dt, o.t_end - t)
+            if dt != last_dt:
+                s.set_dt(dt)
+                last_dt = dt
+            s.set_rhs_transient()
+            s.solve_async(o.tol, o.maxit)
+            s.step_record_async(dt, k)
+            t += dt
+            steps.append((t, dt))
+            dt = min(dt * o.growth, o.dt_max)
+            k += 1
+        recs, sts = s.step_records(0, k)
+        for (tk, dtk), r, st in zip(steps, recs, sts):
+            res.steps.append(StepRecord(tk, dtk, st.iters, r.T_max, r.q_out, r.q_stored))
+            res.total_iters += st.iters
+            res.converged = res.converged and st.converged
+        res.solve_ms = (time.perf_counter() - t0) * 1e3
+        res.T = s.get_x()
+        s.close()
+        res.ms = (time.perf_counter() - t0) * 1e3
+        return res
     while (k < o.nsteps) if o.nsteps > 0 else (t < o.t_end * (1 - 1e-12)):
         if o.nsteps <= 0:
             dt = min(dt, o.t_end - t)
@@ -1115,14 +1159,10 @@ def run_transient(m: Model3D, o: TransientOptions = TransientOptions(),
         st = s.solve(o.tol, o.maxit)
         res.solve_ms += (time.perf_counter() - ts) * 1e3
         t += dt
-        if device_records:
-            r = s.step_record(dt)
-            rec = StepRecord(t, dt, st.iters, r.T_max, r.q_out, r.q_stored)
-        else:
-            T_new = s.get_x()
-            rec = StepRecord(t, dt, st.iters, float(T_new.max()), heat_out(m, T_new),
-                             heat_stored(m, T_old, T_new, dt))
-            T_old = T_new
+        T_new = s.get_x()
+        rec = StepRecord(t, dt, st.iters, float(T_new.max()), heat_out(m, T_new),
+                         heat_stored(m, T_old, T_new, dt))
+        T_old = T_new
         res.steps.append(rec)
         res.total_iters += st.iters
         res.converged = res.converged and st.converged

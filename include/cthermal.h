@@ -222,6 +222,15 @@ ct_status ct_true_relres(ct_solver* s, double* out);
  * run_transient, src/transient3d.h:72-80) on the device, for the step of
  * length dt that the last ct_set_rhs_transient started. */
 ct_status ct_solver_step_record(ct_solver* s, double dt, ct_step_record* out);
+/* No counterpart in the reference. The same record queued on the solver's
+ * stream, with the statistics of the solve queued before it, into entry
+ * `slot` (>= 0) of a table on the device, so that a transient run of
+ * ct_set_dt, ct_set_rhs_transient, ct_solve_async and this call per step
+ * never waits on the host; ct_solver_step_records waits for the solver's
+ * stream and copies entries first .. first + count - 1 out (stats may be
+ * NULL). Growing the table past its largest slot so far synchronises. */
+ct_status ct_solver_step_record_async(ct_solver* s, double dt, int slot);
+ct_status ct_solver_step_records(ct_solver* s, int first, int count, ct_step_record* out, ct_stats* stats);
 /* Multigrid hierarchy: number of levels, and level k's size. */
 ct_status ct_num_levels(const ct_solver* s, int* n);
 ct_status ct_level_dims(const ct_solver* s, int k, int* nx, int* ny, int* nz);

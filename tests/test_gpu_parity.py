@@ -358,6 +358,43 @@ def test_staged_sweeps_bitwise_single_and_batch(ct, n, prec, tmp_path):
     assert np.array_equal(out[0], out[1])
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+@pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
+def test_queued_transient_steps_match_blocking(ct, prec, graphs):
+    """Backward-Euler steps queued on the solver's stream (ct_solve_async and
+    ct_solver_step_record_async into the device table, 70 steps so the table
+    grows past its first 64 entries) give the blocking steps' records,
+    iteration counts and field bit for bit."""
+    import workloads
+    m = workloads.steady_hotspot(48, seed=11)
+    ct.gpu_use_graphs(graphs)
+    try:
+        out = []
+        for queued in (False, True):
+            with ct.GpuPcg(m, ct.Precond.Multigrid, getattr(ct.Precision, prec)) as s:
+                s.set_x_zero()
+                dt, recs, sts = 1e-5, [], []
+                for k in range(70):
+                    s.set_dt(dt)
+                    s.set_rhs_transient()
+                    if queued:
+                        s.solve_async(1e-9, 200)
+                        s.step_record_async(dt, k)
+                    else:
+                        sts.append(s.solve(1e-9, 200))
+                        recs.append(s.step_record(dt))
+                    dt = min(dt * 1.1, 0.05)
+                if queued:
+                    recs, sts = s.step_records(0, 70)
+                out.append(([(r.T_max, r.q_out, r.q_stored) for r in recs],
+                            [(st.iters, st.converged, st.relres) for st in sts], s.get_x()))
+    finally:
+        ct.gpu_use_graphs(True)
+    assert out[0][0] == out[1][0]
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])
+
+
 @pytest.mark.parametrize("pinned", [True, False])
 @pytest.mark.parametrize("prec", ["MG_FP32_FLEX", "MG_FP32_FLEX_DW", "MG_FP64"])
 def test_queued_copies_match_blocking_calls(ct, prec, pinned):
