@@ -281,7 +281,8 @@ struct TailLevels {
 };
 // The smallest levels (those whose arrays together fit kSmallSmemMax bytes),
 // run by one block out of shared memory.
-constexpr int kSmallThreads = 512;
+constexpr int kSmallThreads = 512;        // the bottom kernel's launch bound (and the batch's blocks)
+constexpr int kSmallThreadsSolver = 256;  // the single solver's bottom block
 constexpr int kSmallSmemMax = 200 * 1024;
 // Bytes one level takes there: gE, gN, gU, cap (float), gB (one plane of
 // float), fcp, finv, x, b (elem bytes each), every array rounded up to 16

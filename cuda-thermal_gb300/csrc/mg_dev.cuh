@@ -537,7 +537,7 @@ __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double
     for (int k = 0; k < nl; ++k) {
         const LevelView<T> S = small_view<T>(smem + soff[k], sg[k]);
         const unsigned ln = sg[k].plane * (unsigned)sg[k].nz;
-        for (unsigned i = threadIdx.x; i < ln; i += kSmallThreads) {
+        for (unsigned i = threadIdx.x; i < ln; i += blockDim.x) {
             S.x[i] = T(0);
             if (k > 0) S.b[i] = T(0);
         }
@@ -564,7 +564,7 @@ __device__ __forceinline__ int vsmall_body(const TailLevels<T>& tl, const double
         }
         return kSmallTimeout;
     }
-    const unsigned tid = threadIdx.x, nth = kSmallThreads;
+    const unsigned tid = threadIdx.x, nth = blockDim.x;
     const int last = nl - 1;
     // The phases in V-cycle order, driven by one loop so that each kind of
     // phase (x = 0 sweep, sweep, restriction, prolongating sweep) is one
