@@ -56,6 +56,20 @@ def test_status_strings_and_errors_without_gpu(ctlib, ct):
     assert ctlib.ct_solve(None, 1e-6, 10, None) == 5
 
 
+def test_queued_calls_refuse_a_null_solver_without_gpu(ctlib, ct):
+    """The queued copies and queued step records check their solver before
+    any device call."""
+    import ctypes as C
+    buf = (C.c_double * 4)()
+    assert ctlib.ct_set_power_async(None, buf) == 5
+    assert ctlib.ct_get_x_async(None, buf) == 5
+    assert ctlib.ct_copies_wait(None) == 5
+    assert ctlib.ct_solver_step_record_async(None, 1e-3, 0) == 5
+    assert ctlib.ct_solver_step_records(None, 0, 1, None, None) == 5
+    assert ctlib.ct_solve_async(None, 1e-6, 10) == 5
+    assert ctlib.ct_solve_wait(None, None) == 5
+
+
 def test_unfinalized_model_rejected(ctlib, ct):
     m = ct.default_model(8, 8)
     with pytest.raises(ct.CtError) as e:
