@@ -156,17 +156,22 @@ __device__ __forceinline__ bool sweep_tiles_ws(const SweepMaps* m, const LevelVi
             float v[MZ], fcr[MZ];
             float prev = 0.0f, gu_prev = 0.0f;
             bool ok = true;
+            // the neighbours' coarse corrections (PRO) one plane ahead: plane
+            // l + 1's loads are in flight while plane l waits and computes
+            float nw = 0.0f, ne = 0.0f, nso = 0.0f, nno = 0.0f;
+            auto load_corr = [&](int l) {
+                const float* cx = C.x + (unsigned)l * C.g.plane;
+                nw = hw ? cx[pw] : 0.0f;
+                ne = he ? cx[pe] : 0.0f;
+                nso = hs ? cx[ps] : 0.0f;
+                nno = hn ? cx[pn] : 0.0f;
+            };
+            if (PRO && act) load_corr(0);
 #pragma unroll
             for (int l = 0; l < MZ; ++l) {
                 if (l < nz && ok) {
-                    float cw = 0.0f, ce = 0.0f, cs = 0.0f, cn = 0.0f;
-                    if (PRO && act) {
-                        const float* cx = C.x + (unsigned)l * C.g.plane;
-                        if (hw) cw = cx[pw];
-                        if (he) ce = cx[pe];
-                        if (hs) cs = cx[ps];
-                        if (hn) cn = cx[pn];
-                    }
+                    const float cw = nw, ce = ne, cs = nso, cn = nno;
+                    if (PRO && act && l + 1 < nz) load_corr(l + 1);
                     const int s = w % NS;
                     ok = mbar_wait_or_abort(&full[s], (unsigned)(w / NS) & 1u, abort);
                     ok = __all_sync(0xffffffffu, ok);
