@@ -876,7 +876,10 @@ def main():
     achieved = top["bytes"] / top["launches"] / (top["total_ms"] / top["launches"] / 1e3) / 1e9
     traffic = traffic_from_profiles(top["name"])
     alg_bytes_solve = sum(r["bytes"] for r in rows)
-    launches_per_solve = sum(r["launches"] for r in rows)
+    # the profiled solve's launches, plus those a queued solve adds around its
+    # graph: the control-block set and the no-heat check (ct_solve_async) and
+    # the last iteration's x update after the loop
+    launches_per_solve = sum(r["launches"] for r in rows) + 3
     rows_dw = profile_rows(sdw)
 
     batched = None
