@@ -487,7 +487,9 @@ __device__ __forceinline__ LevelView<T> small_view(unsigned char* base, const Ge
 // issued, so the two latencies overlap) says whether to run the phases at
 // all. Returns kSmallDone, kSmallClosed (go() said no: nothing written once
 // the copies have landed) or kSmallTimeout (a bounded wait for the copies ran
-// out: nothing written).
+// out: nothing written). col_sweeps (FP32): each sweep one thread per column
+// over every plane; otherwise one task per column and plane gathers the
+// right-hand sides first. Same bits either way; any block size.
 constexpr int kSmallDone = 0, kSmallTimeout = 1, kSmallClosed = 2;
 
 template <class T, int MZ, class Wait, class Go>
