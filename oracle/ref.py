@@ -1,6 +1,6 @@
 """ctypes bindings to the UNMODIFIED reference solvers (oracle/_ref/).
 
-TEST AND BASELINE INFRASTRUCTURE ONLY: used to generate tests/golden/
+TEST AND COMPARISON INFRASTRUCTURE ONLY: used to generate tests/golden/
 fixtures (tests/golden/make_golden.py), to pin the C oracle against the
 reference directly, and as the timed reference arm of bench.py (the
 reference CPU solver, and the reference GPU solver on the same inputs).

@@ -1,6 +1,6 @@
 """Timed runs of the UNMODIFIED reference solvers on the benchmark workload.
 
-BASELINE INFRASTRUCTURE ONLY: bench.py's reference arm (the reference CPU
+COMPARISON INFRASTRUCTURE ONLY: bench.py's reference arm (the reference CPU
 solver on every host core) and its reference-GPU leg (the reference GPU
 solver, src/pcg3d_gpu.cu compiled for sm_103a, on the same model) run
 through here. Models are built by the reference's own stack3d.h functions

@@ -1,7 +1,7 @@
 // ref_gpu_harness.cu - C entry points around the UNMODIFIED reference GPU
 // solver (GpuPcg, src/pcg3d.h:115-163, src/pcg3d_gpu.cu:346-682), compiled
 // for sm_103a from the reference's own sources (oracle/Makefile, target
-// `ref-gpu`). BASELINE AND TEST INFRASTRUCTURE ONLY: it times the reference's
+// `ref-gpu`). COMPARISON AND TEST INFRASTRUCTURE ONLY: it times the reference's
 // GPU MG-PCG on the same inputs as this library's solver. Models come from
 // ref_model_new (ref_harness.cpp, the reference's own stack3d.h builder),
 // linked into the same library.

@@ -1,6 +1,6 @@
 // ref_harness.cpp - C entry points around the UNMODIFIED reference CPU solver,
 // compiled from an unmodified copy of the reference's own sources
-// (oracle/Makefile, targets `stage` and `ref`). TEST AND BASELINE
+// (oracle/Makefile, targets `stage` and `ref`). TEST AND COMPARISON
 // INFRASTRUCTURE ONLY: it pins the C oracle, generates the golden fixtures
 // under tests/golden/ (make_golden.py) and is the timed reference CPU solver
 // of the benchmark's reference arm. Nothing in the product loads it, and it is
