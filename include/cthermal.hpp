@@ -263,6 +263,29 @@ class GpuPcg {
         check(ct_true_relres(s_, &v));
         return v;
     }
+    // Extensions: queued work (no host wait until the matching wait call).
+    void solve_async(double tol, int maxit) { check(ct_solve_async(s_, tol, maxit)); }
+    PcgStats solve_wait() {
+        ct_stats st{};
+        const ct_status r = ct_solve_wait(s_, &st);
+        if (r != CT_OK && r != CT_NOT_CONVERGED && r != CT_BREAKDOWN) check(r);
+        PcgStats out;
+        out.iters = st.iters;
+        out.relres = st.relres;
+        out.converged = st.converged != 0;
+        return out;
+    }
+    // P and T: host memory that stays valid (P unchanged) until copies_wait.
+    void set_power_async(const double* P) { check(ct_set_power_async(s_, P)); }
+    void get_x_async(double* T) { check(ct_get_x_async(s_, T)); }
+    void copies_wait() { check(ct_copies_wait(s_)); }
+    void step_record_async(double dt, int slot) { check(ct_solver_step_record_async(s_, dt, slot)); }
+    std::vector<ct_step_record> step_records(int first, int count, std::vector<ct_stats>* stats = nullptr) {
+        std::vector<ct_step_record> r((size_t)count);
+        if (stats) stats->resize((size_t)count);
+        check(ct_solver_step_records(s_, first, count, r.data(), stats ? stats->data() : nullptr));
+        return r;
+    }
     ct_solver* handle() const { return s_; }
 
   private:
