@@ -1087,6 +1087,8 @@ ct_status ct_solver_step_record_async(ct_solver* s, double dt, int slot) {
         while (cap <= slot) cap *= 2;
         ct::StepEntry* t = nullptr;
         CT_CUDA(cudaMalloc(&t, (size_t)cap * sizeof(ct::StepEntry)));
+        // entries never recorded read back as zeros
+        CT_CUDA(cudaMemsetAsync(t, 0, (size_t)cap * sizeof(ct::StepEntry), v.st));
         if (v.rec_table) {
             CT_CUDA(cudaMemcpyAsync(t, v.rec_table, (size_t)v.rec_cap * sizeof(ct::StepEntry),
                                     cudaMemcpyDeviceToDevice, v.st));
