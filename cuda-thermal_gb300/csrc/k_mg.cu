@@ -291,9 +291,11 @@ __global__ void __launch_bounds__(32 * MZ)
         if (k < nz) C.x[(unsigned)k * cg.plane + cs] = v[k];
 }
 
-// The bottom of the V-cycle in one block from shared memory (mgdev::vsmall_body).
+// The bottom of the V-cycle in one block from shared memory (mgdev::vsmall_body),
+// bounded at the 256 threads it is launched with, so a thread may hold up to
+// 255 registers (12 planes: 167, 16 planes: 219, no spills).
 template <class T, int MZ>
-__global__ void __launch_bounds__(kSmallThreads, 1)
+__global__ void __launch_bounds__(kSmallThreadsSolver, 1)
     k_vsmall(TailLevels<T> tl, Ctl* ctl, Cond cond, bool col_sweeps) {
     extern __shared__ __align__(16) unsigned char smem[];
     const auto wait = [] { pdl_enter(); };
